@@ -1,0 +1,208 @@
+/*
+ * gbns.h — C ABI of libgbns.so, the GB300-native (sm_103a) explicit
+ * right-hand side of SPADE's compressible Navier–Stokes solver.
+ *
+ * Every entry point takes plain pointers and sizes.  Array pointers are
+ * DEVICE pointers owned by the caller, laid out exactly like SPADE's
+ * grid_array with the default linear memory map (core/mem_map.h:465-497,
+ * 654-676): for local block lb and cell (i,j,k) with ng ghost layers,
+ *
+ *     offset = v + 5*((i+ng) + ni*((j+ng) + nj*((k+ng) + nk*lb)))
+ *     ni = nx+2ng, nj = ny+2ng, nk = nz+2ng,
+ *
+ * variables fastest ("AoS5").  Primitive arrays hold (p, T, u, v, w)
+ * (navier-stokes/fluid_state.h:60-82); residual arrays hold flux_t order
+ * (continuity, energy, x-, y-, z-momentum) (fluid_state.h:106-126).
+ *
+ * Return codes: 0 = success, negative = error; the message of the last
+ * error on the calling thread is available from gbns_last_error().
+ * Calls are stream-ordered on the given stream (NULL = legacy default
+ * stream) and do not synchronise unless stated.  The library allocates no
+ * device memory on the flux_div / ghost-fill / RK-stage paths; the batched
+ * and serving entry points own their work-lists.
+ */
+#ifndef GBNS_H
+#define GBNS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBNS_ABI_VERSION 1
+
+/* ---- error codes ---------------------------------------------------- */
+#define GBNS_OK               0
+#define GBNS_ERR_INVALID    (-1)   /* bad descriptor or argument */
+#define GBNS_ERR_UNSUPPORTED (-2)  /* scheme/combination not built */
+#define GBNS_ERR_CUDA       (-3)   /* CUDA runtime error */
+#define GBNS_ERR_NONFINITE  (-4)   /* state check found NaN/Inf or p,T <= 0 */
+#define GBNS_ERR_CAPACITY   (-5)   /* batch/serving capacity or budget exceeded */
+#define GBNS_ERR_TIMEOUT    (-6)   /* a bounded device wait ran out */
+
+/* ---- grid ------------------------------------------------------------
+ * Replaces the geometry the reference kernels read from
+ * grid::cartesian_grid_t / grid_geometry_t (grid/cartesian_grid.h:48-384,
+ * grid/grid_geometry.h:16-100) and cartesian_blocks_t
+ * (grid/cartesian_blocks.h:23-117).  Blocks are numbered with x fastest:
+ * lb = bx + nbx*(by + nby*bz) (cartesian_blocks.h:54-105 with
+ * ctrs::collapse_index, core/ctrs.h:341-353).  Block boxes and spacings are
+ * derived exactly as the reference does (block min = bounds.min +
+ * b*bsize, max = min + bsize, dx = (max-min)/n, inv_dx = 1/dx).
+ */
+#define GBNS_COORDS_IDENTITY        0  /* coords::identity (core/coord_system.h:51-56) */
+#define GBNS_COORDS_TANH_Y          1  /* y = tanh(beta*eta)/tanh(beta), eta in the y bounds; x,z identity */
+#define GBNS_COORDS_INTEGRATED_TANH_Y 2 /* coords::integrated_tanh_1D in y (coord_system.h:103-140); x,z identity */
+
+typedef struct gbns_grid_desc
+{
+    int32_t nblk[3];       /* blocks per direction */
+    int32_t ncell[3];      /* cells per block per direction (nx, ny, nz) */
+    int32_t ng;            /* ghost layers (same in every direction) */
+    int32_t coords;        /* GBNS_COORDS_* */
+    double  bounds[6];     /* computational domain xmin,xmax,ymin,ymax,zmin,zmax */
+    double  coord_param[4];/* TANH_Y: beta; INTEGRATED_TANH_Y: y0,y1,inflation,rate */
+} gbns_grid_desc;
+
+/* ---- gas ------------------------------------------------------------- */
+typedef struct gbns_gas_desc
+{
+    double gamma;          /* fluid_state::ideal_gas_t::gamma (navier-stokes/gas.h:35-49) */
+    double R;              /* fluid_state::ideal_gas_t::R */
+} gbns_gas_desc;
+
+/* ---- flux scheme ------------------------------------------------------
+ * A lowered omni::compose(convective, dissipation, viscous) functor
+ * (omni/compose.h:7-45): the face flux is conv + (diss + visc) with absent
+ * terms dropped, summed in that nesting like composite_kernel_t.
+ */
+#define GBNS_CONV_NONE        0
+#define GBNS_CONV_CENT_KEEP   1   /* convective::cent_keep_scheme_t<gas,order> (navier-stokes/convective.h:96-192) */
+#define GBNS_CONV_TOTANI      2   /* convective::totani_lr (convective.h:54-94) */
+#define GBNS_CONV_FWENO       3   /* convective::fweno_t (convective.h:335-497), 3rd order, 4-point */
+#define GBNS_CONV_WENO5       4   /* 5th-order WENO-JS on fweno_t's Rusanov split (no reference counterpart) */
+
+#define GBNS_DISS_NONE        0
+#define GBNS_DISS_PRESSURE    1   /* convective::pressure_diss_lr (convective.h:194-246) */
+
+#define GBNS_SENSOR_CONST     0   /* state_sensor::const_sensor_t (navier-stokes/state_sensor.h:46-60) */
+
+#define GBNS_VISC_NONE        0
+#define GBNS_VISC_LR          1   /* viscous::visc_lr (navier-stokes/viscous.h:13-113) */
+
+#define GBNS_LAW_CONSTANT     0   /* viscous_laws::constant_viscosity_t (viscous_laws.h:62-100) */
+#define GBNS_LAW_POWER        1   /* viscous_laws::power_law_t (viscous_laws.h:102-135) */
+#define GBNS_LAW_SUTHERLAND   2   /* Sutherland's law (no reference counterpart) */
+
+#define GBNS_PREC_FP64        0   /* all arithmetic in FP64 */
+#define GBNS_PREC_FP32_FLUX   1   /* face reconstruction + flux in FP32; divergence accumulation FP64 */
+
+typedef struct gbns_scheme_desc
+{
+    int32_t convective;    /* GBNS_CONV_* */
+    int32_t order;         /* cent_keep nominal order: 2, 4, 6, 8 */
+    int32_t weno_smooth;   /* fweno_t/weno5: 1 = smoothness weights, 0 = linear weights */
+    int32_t dissipation;   /* GBNS_DISS_* */
+    int32_t sensor;        /* GBNS_SENSOR_* */
+    int32_t viscous;       /* GBNS_VISC_* */
+    int32_t visc_law;      /* GBNS_LAW_* */
+    int32_t precision;     /* GBNS_PREC_* */
+    double  eps_p, eps_T;  /* pressure_diss_lr coefficients */
+    double  sensor_alpha;  /* const_sensor_t::alpha */
+    double  mu;            /* constant: mu; power/sutherland: mu_ref */
+    double  prandtl;
+    double  T_ref;         /* power/sutherland reference temperature */
+    double  power;         /* power-law exponent */
+    double  S;             /* Sutherland constant */
+    gbns_gas_desc gas;
+} gbns_scheme_desc;
+
+/* ---- boundary conditions -------------------------------------------- */
+#define GBNS_BC_PERIODIC           0  /* block exchange wraps (grid/exchange_config.h:321-350) */
+#define GBNS_BC_NONE               1  /* ghosts left untouched */
+#define GBNS_BC_ISOTHERMAL_NOSLIP  2  /* mirror fill: p_g=p, T_g=2Tw-T, u_g=-u (grid/boundary_fill.h:106-129) */
+#define GBNS_BC_SLIP_ADIABATIC     3  /* mirror fill: p_g=p, T_g=T, u_n reflected */
+
+typedef struct gbns_bc_desc
+{
+    int32_t kind[6];       /* GBNS_BC_* per face xmin,xmax,ymin,ymax,zmin,zmax; periodic must pair */
+    double  t_wall[6];     /* wall temperature for isothermal faces */
+} gbns_bc_desc;
+
+/* ---- reductions ----------------------------------------------------- */
+#define GBNS_RED_MAX_WAVESPEED 0  /* max over interior of sqrt(gamma R T) + |u| (CFL; development/cuda-tgv/main.cc:152-172) */
+#define GBNS_RED_KINETIC       1  /* volume average of 0.5 rho |u|^2 (Jacobian-weighted) */
+#define GBNS_RED_CONSERVED     2  /* 5 Jacobian-weighted sums of (rho, rhoE, rhou, rhov, rhow) */
+#define GBNS_RED_HEALTH        3  /* count of interior cells with NaN/Inf or p<=0 or T<=0 */
+
+/* ---- entry points ---------------------------------------------------- */
+
+/* Library / ABI version; no CUDA call. */
+int gbns_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated). */
+int gbns_last_error(char* buf, size_t len);
+
+/* Validates a grid descriptor and returns the number of doubles in one AoS5
+ * array (ghosts included) in *count.  No CUDA call.  Replaces the size the
+ * reference computes in grid_array's constructor (grid/grid_array.h:244-260). */
+int gbns_array_size(const gbns_grid_desc* grid, size_t* count);
+
+/* rhs (+)= flux divergence of prims.
+ * Replaces spade::pde_algs::flux_div(prims, rhs, flux_func[, traits])
+ * (pde-algs/flux-div/flux_div.h:16-56) with the basic algorithm
+ * (flux_div_basic.h:17-76): for every interior cell,
+ *   rhs += sum_d jac*[F(i-1/2) - F(i+1/2)]*inv_dx[d].
+ * increment = 1 is the reference default (pde_algs::increment,
+ * pde_traits.h:13-20); increment = 0 is pde_algs::overwrite (interior of rhs
+ * overwritten; its ghost layers are not touched).  prims must have valid
+ * ghost layers.  Asynchronous on `stream`. */
+int gbns_flux_div(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                  const double* prims, double* rhs, int increment, void* stream);
+
+/* Ghost fill: periodic / inter-block exchange of interior donor cells into
+ * ghost layers, then wall mirror fill on non-periodic faces.
+ * Replaces arr_exchange_t::exchange (grid/make_exchange.h:111-410, single
+ * level injection) followed by algs::boundary_fill (grid/boundary_fill.h:31-133).
+ * Asynchronous on `stream`. */
+int gbns_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc,
+                     double* prims, void* stream);
+
+/* One fused explicit-RK stage update on the primitive state, in place:
+ * per interior cell  cons = prim2cons(q);  cons += coeff[j]*R_j (j < nres);
+ * q = cons2prim(cons).  coeff[j] already includes dt.
+ * Replaces time_integration::detail::transform_advance_to
+ * (time-integration/advance.h:56-102) with fluid_state::convert_state
+ * (navier-stokes/fluid_state.h:102-135).  nres <= 4.  Asynchronous. */
+int gbns_rk_stage(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
+                  double* prims, const double* const* residuals,
+                  const double* coeffs, int nres, void* stream);
+
+/* Reduction over interior cells (GBNS_RED_*); writes 1 double (5 for
+ * GBNS_RED_CONSERVED) to the HOST buffer `out` and synchronises the stream.
+ * Replaces algs::transform_reduce (algs/transform_reduce.h:53-191) for the
+ * reductions the reference drivers use. */
+int gbns_reduce(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
+                const double* prims, int kind, double* out, void* stream);
+
+/* One full SSPRK3 step with the reference's structure
+ * (integrate_advance with state_transform_t, time-integration/advance.h:234-280;
+ * ssprk3_t, time-integration/explicit.h:80-88):
+ *   R0 = L(q); q <- q + dt R0;             fill ghosts
+ *   R1 = L(q); q <- q - 3/4 dt R0 + 1/4 dt R1; fill ghosts
+ *   R2 = L(q); q <- q - 1/12 dt R0 - 1/12 dt R1 + 2/3 dt R2; fill ghosts
+ * (updates in conservative variables, state kept primitive).  `work` is a
+ * caller-owned device buffer of 3 AoS5 arrays (3*gbns_array_size doubles)
+ * holding R0..R2 (the reference's integrator_data_t residuals).  prims must
+ * have valid ghosts on entry.  Asynchronous. */
+int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                     const gbns_bc_desc* bc, double* prims, double* work,
+                     double dt, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBNS_H */

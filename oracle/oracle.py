@@ -1,0 +1,152 @@
+"""Python access to the CPU oracle.  TEST INFRASTRUCTURE ONLY.
+
+Two back ends:
+  * ``port`` — oracle/_build/libgbns_oracle.so, the plain-C restatement of
+    the reference's algorithm (oracle/gbns_oracle.c).  Built by
+    ``make -C oracle`` (and by ``__graft_entry__.build()``).
+  * ``ref``  — oracle/_ref/libspade_ref.so, the reference's own CPU path
+    (oracle/ref_harness.cc compiled against the reference headers).  Only
+    available where the reference sources exist; used to pin the port and
+    to generate tests/golden/.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+import this module.  Arrays are numpy float64 in the AoS5 layout with ghosts,
+shape (nblocks, nz+2ng, ny+2ng, nx+2ng, 5).
+"""
+import ctypes
+import os
+import numpy as np
+
+from spade_gb300 import _abi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_PATH = os.path.join(_HERE, "_build", "libgbns_oracle.so")
+REF_PATH = os.path.join(_HERE, "_ref", "libspade_ref.so")
+
+_port = None
+_ref = None
+
+
+def _ptr(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def port():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_PATH):
+            raise RuntimeError("oracle port not built: run `make -C oracle` (missing %s)" % PORT_PATH)
+        lib = ctypes.CDLL(PORT_PATH)
+        P = ctypes.POINTER
+        lib.oracle_flux_div.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        lib.oracle_fill_ghosts.argtypes = [P(_abi.GridDesc), P(_abi.BcDesc), ctypes.c_void_p]
+        lib.oracle_rk_stage.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.oracle_reduce.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        lib.oracle_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        lib.oracle_max_threads.restype = ctypes.c_int
+        _port = lib
+    return _port
+
+
+def ref_available():
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not ref_available():
+            raise RuntimeError("reference harness not built (missing %s)" % REF_PATH)
+        lib = ctypes.CDLL(REF_PATH)
+        lib.spade_ref_flux_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.spade_ref_fill_ghosts.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        lib.spade_ref_ssprk3.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        _ref = lib
+    return _ref
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("%s failed with code %d" % (what, rc))
+
+
+# ---------------------------------------------------------------- port API
+
+def flux_div(grid, scheme, prims, rhs, increment=True, nthreads=0):
+    _check(port().oracle_flux_div(ctypes.byref(grid), ctypes.byref(scheme), _ptr(prims), _ptr(rhs), int(increment), int(nthreads)), "oracle_flux_div")
+
+
+def fill_ghosts(grid, bc, prims):
+    _check(port().oracle_fill_ghosts(ctypes.byref(grid), ctypes.byref(bc), _ptr(prims)), "oracle_fill_ghosts")
+
+
+def rk_stage(grid, gas, prims, residuals, coeffs):
+    ptrs = (ctypes.c_void_p * len(residuals))(*[r.ctypes.data for r in residuals])
+    c = np.ascontiguousarray(coeffs, dtype=np.float64)
+    _check(port().oracle_rk_stage(ctypes.byref(grid), ctypes.byref(gas), _ptr(prims), ptrs, _ptr(c), len(residuals)), "oracle_rk_stage")
+
+
+def reduce(grid, gas, prims, kind):
+    out = np.zeros(5)
+    _check(port().oracle_reduce(ctypes.byref(grid), ctypes.byref(gas), _ptr(prims), int(kind), _ptr(out)), "oracle_reduce")
+    return out if kind == _abi.RED_CONSERVED else float(out[0])
+
+
+def ssprk3_step(grid, scheme, bc, prims, work, dt, nthreads=0):
+    _check(port().oracle_ssprk3_step(ctypes.byref(grid), ctypes.byref(scheme), ctypes.byref(bc), _ptr(prims), _ptr(work), float(dt), int(nthreads)), "oracle_ssprk3_step")
+
+
+def max_threads():
+    return int(port().oracle_max_threads())
+
+
+# ---------------------------------------------------------- reference API
+
+# Scheme ids understood by oracle/ref_harness.cc
+REF_CK2_VISC = 0
+REF_TOTANI_VISC = 1
+REF_CK4_VISC = 2
+REF_CK2 = 3
+REF_VISC = 4
+REF_FWENO_DISS_VISC = 5
+REF_FWENO = 6
+REF_DISS = 7
+REF_TOTANI = 8
+REF_CK6 = 9
+REF_CK8 = 10
+REF_FWENO_NOSMOOTH = 11
+REF_CK2_DISS_VISC = 12
+
+
+def _ref_problem(grid, scheme, bc=None):
+    """Flat int/real arrays for ref_harness.cc:make_problem."""
+    periodic = [1, 1, 1]
+    wall_y = 0
+    t_wall = 0.0
+    if bc is not None:
+        periodic = [int(bc.kind[2 * d] == _abi.BC_PERIODIC) for d in range(3)]
+        if bc.kind[2] == _abi.BC_ISOTHERMAL_NOSLIP:
+            wall_y = 1
+            t_wall = bc.t_wall[2]
+    ints = np.array(list(grid.nblk) + list(grid.ncell) + [grid.ng] + periodic + [wall_y], dtype=np.int32)
+    reals = np.array(list(grid.bounds) + [scheme.gas.gamma, scheme.gas.R, scheme.mu, scheme.prandtl,
+                                          scheme.eps_p, scheme.eps_T, scheme.sensor_alpha, t_wall], dtype=np.float64)
+    return ints, reals
+
+
+def ref_flux_div(ref_scheme, grid, scheme, prims, rhs, increment=True):
+    ints, reals = _ref_problem(grid, scheme)
+    _check(ref().spade_ref_flux_div(int(ref_scheme), ints.ctypes.data, reals.ctypes.data, int(not increment), _ptr(prims), _ptr(rhs)), "spade_ref_flux_div")
+
+
+def ref_fill_ghosts(grid, scheme, bc, prims):
+    ints, reals = _ref_problem(grid, scheme, bc)
+    _check(ref().spade_ref_fill_ghosts(ints.ctypes.data, reals.ctypes.data, _ptr(prims)), "spade_ref_fill_ghosts")
+
+
+def ref_ssprk3(ref_scheme, grid, scheme, bc, prims, dt, nsteps):
+    ints, reals = _ref_problem(grid, scheme, bc)
+    ke = np.zeros(nsteps + 1)
+    _check(ref().spade_ref_ssprk3(int(ref_scheme), ints.ctypes.data, reals.ctypes.data, float(dt), int(nsteps), _ptr(prims), _ptr(ke)), "spade_ref_ssprk3")
+    return ke
