@@ -1,0 +1,391 @@
+"""Benchmark: SSPRK3 cell-steps/s of the explicit Navier–Stokes RHS path on
+the plain-FP64 channel at scale (8x8x8 blocks of 32^3 = 16.8M cells, 3 ghost
+layers, tanh-stretched y (beta = 2), 5th-order WENO + pressure dissipation +
+visc_lr with Sutherland viscosity, isothermal walls, periodic x/z).
+
+One step = one SSPRK3 step over the whole grid: 3 flux_div launches, 3 fused
+RK-stage updates, 3 ghost fills.  Inputs (1.1 GB per array) are larger than
+the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+`--impl reference` times the CPU restatement of the reference's algorithm
+(oracle/, the reference's CPU path cannot be built on the GPU host) on all
+host cores over a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s"
+UNIT = "cell-steps/s"
+ALG_BYTES_FLUX = 80          # read 5 + write 5 FP64 per cell per flux_div (overwrite)
+ALG_BYTES_STEP = 720         # 3 x 80 + 120 + 160 + 200 per cell per SSPRK3 step
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gbns", choices=["gbns", "reference"])
+    p.add_argument("--precision", default="fp64", choices=["fp64", "fp32_flux"])
+    p.add_argument("--nblk", type=int, nargs=3, default=[8, 8, 8])
+    p.add_argument("--ncell", type=int, nargs=3, default=[32, 32, 32])
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp32", action="store_true", help="skip the FP32-flux side measurement")
+    return p.parse_args()
+
+
+def config(args):
+    return {"workload": "channel_fp64_weno5_sutherland_tanh",
+            "blocks": list(args.nblk), "cells_per_block": list(args.ncell), "ghosts": 3,
+            "cells": int(math.prod(args.nblk) * math.prod(args.ncell)),
+            "scheme": "compose(weno5_t, pressure_diss_lr(const_sensor), visc_lr(sutherland_t))",
+            "coords": "diagonal_coords(identity, tanh_stretch(beta=2), identity)",
+            "bc": "periodic x/z, isothermal no-slip walls y=+-1",
+            "time_integration": "ssprk3_t with state_transform_t",
+            "l2": "inputs larger than L2 (1.1 GB per array)"}
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1"):
+                        reasons.add(n)
+            except Exception:
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, world):
+    import torch
+    from spade_gb300 import _abi, _native, workloads
+    from spade_gb300 import build as _b
+    if not _b.up_to_date():
+        raise SystemExit("libgbns.so is stale or missing: run __graft_entry__.build() first")
+    lib = _native.lib()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.current_stream()
+    st = int(stream.cuda_stream)
+
+    prob = workloads.channel(nblk=tuple(args.nblk), ncell=tuple(args.ncell), ng=3, rng="torch", seed=rank)
+    q = prob.q
+    g = q.desc()
+    prec = _abi.PREC_FP64 if args.precision == "fp64" else _abi.PREC_FP32_FLUX
+    s = prob.scheme_desc(prec)
+    bc = prob.bc_desc()
+    dt = prob.dt
+    cells = prob.grid.get_grid_size()
+    n = q.data.numel()
+    R = [torch.zeros(n, dtype=torch.float64, device="cuda") for _ in range(3)]
+    rptr = [r.data_ptr() for r in R]
+    res = (ctypes.c_void_p * 3)(*rptr)
+    c1 = (ctypes.c_double * 1)((1.0 / 1.0) * dt)
+    c2 = (ctypes.c_double * 2)((-3.0 / 4.0) * dt, (1.0 / 4.0) * dt)
+    c3 = (ctypes.c_double * 3)((-1.0 / 12.0) * dt, (-1.0 / 12.0) * dt, (2.0 / 3.0) * dt)
+    gas = prob.gas.desc()
+    qp = q.ptr()
+    chk = _native.check
+
+    def step(events=None):
+        # SSPRK3 (advance.h:234-280): the same launches gbns_ssprk3_step makes,
+        # issued one by one so the flux_div launches can be bracketed by events.
+        for i, (cf, nr) in enumerate(((c1, 1), (c2, 2), (c3, 3))):
+            if events is not None:
+                events[i][0].record(stream)
+            chk(lib.gbns_flux_div(g, s, qp, rptr[i], 0, st))
+            if events is not None:
+                events[i][1].record(stream)
+            chk(lib.gbns_rk_stage(g, gas, qp, res, cf, nr, st))
+            chk(lib.gbns_fill_ghosts(g, bc, qp, st))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    evs = [[[torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)] for _ in range(3)]
+           for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    clocks = Clocks(dev)
+    time.sleep(0.3)
+    barrier()
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = t0.elapsed_time(t1)
+    flux_ms = [e[0].elapsed_time(e[1]) for ev in evs for e in ev]
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+
+    health = ctypes.c_double(0.0)
+    chk(lib.gbns_reduce(g, gas, qp, _abi.RED_HEALTH, ctypes.byref(health), st))
+    launches = 9 * args.steps
+
+    # ---- end to end through the public C-ABI call, host buffers ---------------
+    host_q = torch.empty(q.data.shape, dtype=torch.float64, pin_memory=True)
+    host_q.copy_(q.data)
+    work = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    ke = max(1, args.e2e_steps)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(ke):
+        q.data.copy_(host_q, non_blocking=True)
+        chk(lib.gbns_ssprk3_step(g, s, bc, qp, work.data_ptr(), ctypes.c_double(dt), st))
+        host_q.copy_(q.data, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / ke
+
+    # ---- FP32-flux form on the same workload (side measurement) ----------------
+    fp32 = None
+    if not args.no_fp32 and prec == _abi.PREC_FP64:
+        s32 = prob.scheme_desc(_abi.PREC_FP32_FLUX)
+        w = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            chk(lib.gbns_ssprk3_step(g, s32, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        kk = max(3, args.steps)
+        f0.record(stream)
+        for _ in range(kk):
+            chk(lib.gbns_ssprk3_step(g, s32, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
+        f1.record(stream)
+        torch.cuda.synchronize()
+        fms = f0.elapsed_time(f1) / kk
+        fp32 = {"value": cells / (fms * 1e-3), "unit": UNIT, "ms_per_step": fms, "dtype": "f32-flux/f64-state",
+                "speedup_vs_fp64": (ms / args.steps) / fms}
+
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "measured"
+    if not hbm_peak:
+        hbm_peak, peak_src = 6800.0, "fallback"
+    fp64_rate = ctypes.c_double(0.0)
+    fp32_rate = ctypes.c_double(0.0)
+    chk(lib.gbns_measure_fma_rate(1, ctypes.byref(fp64_rate), st))
+    chk(lib.gbns_measure_fma_rate(0, ctypes.byref(fp32_rate), st))
+
+    flux_avg_ms = sum(flux_ms) / len(flux_ms)
+    achieved = ALG_BYTES_FLUX * cells / (flux_avg_ms * 1e-3) / 1e9
+    traffic = _read_traffic(cells)
+    return {
+        "ms": ms, "cells": cells, "launches": launches, "flux_avg_ms": flux_avg_ms,
+        "flux_share": sum(flux_ms) / ms, "achieved": achieved, "hbm_peak": hbm_peak, "peak_src": peak_src,
+        "clocks": clk, "health_bad_cells": health.value, "e2e_ms": e2e_ms,
+        "h2d": host_q.numel() * 8, "d2h": host_q.numel() * 8, "fp32": fp32,
+        "fp64_fma_flops": fp64_rate.value, "fp32_fma_flops": fp32_rate.value, "traffic": traffic,
+    }
+
+
+def _read_traffic(cells):
+    """DRAM bytes per flux_div launch from the committed ncu summary, scaled
+    to this workload's cell count (traffic grows with the cells processed)."""
+    path = os.path.join(ROOT, "profiles", "flux_div_channel_fp64.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_cell:"):
+                return float(line.split(":")[1]) * cells
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle restatement on the host cores, bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample(steps=1, nblk=(2, 2, 2), ncell=(32, 32, 32), threads=0):
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import oracle as O
+    from spade_gb300 import _abi
+    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    beta = 2.0
+    bounds = (0.0, 4 * math.pi * nblk[0] / 8, -1.0, 1.0, 0.0, 4 * math.pi / 3 * nblk[2] / 8)
+    grid = _abi.grid_desc(nblk, ncell, 3, bounds, _abi.COORDS_TANH_Y, (beta, 0, 0, 0))
+    gamma, R, Tw = 1.4, 287.0, 300.0
+    c_w = math.sqrt(gamma * R * Tw)
+    U_b = 0.5 * c_w
+    shape = (nblk[0] * nblk[1] * nblk[2], ncell[2] + 6, ncell[1] + 6, ncell[0] + 6, 5)
+    r = np.random.Generator(np.random.PCG64(0))
+    q = np.empty(shape)
+    q[..., 0] = R * Tw
+    q[..., 1] = Tw
+    q[..., 2] = U_b * (1.0 + 0.05 * r.standard_normal(shape[:-1]))
+    q[..., 3] = 0.05 * U_b * r.standard_normal(shape[:-1])
+    q[..., 4] = 0.05 * U_b * r.standard_normal(shape[:-1])
+    s = _abi.SchemeDesc()
+    s.convective = _abi.CONV_WENO5
+    s.order = 2
+    s.weno_smooth = 1
+    s.dissipation = 1
+    s.sensor_alpha = 1.0
+    s.eps_p = s.eps_T = 0.01 * c_w
+    s.viscous = 1
+    s.visc_law = _abi.LAW_SUTHERLAND
+    s.mu = U_b / 3000.0
+    s.prandtl = 0.72
+    s.T_ref = Tw
+    s.S = 110.4
+    s.gas.gamma = gamma
+    s.gas.R = R
+    bc = _abi.bc_desc([0, 0, 2, 2, 0, 0], [0, 0, Tw, Tw, 0, 0])
+    O.fill_ghosts(grid, bc, q)
+    work = np.zeros((3,) + shape)
+    cells = math.prod(nblk) * math.prod(ncell)
+    dt = 1e-7
+    t = time.perf_counter()
+    for _ in range(steps):
+        O.ssprk3_step(grid, s, bc, q, work, dt, threads)
+    el = time.perf_counter() - t
+    cores = O.max_threads() if threads == 0 else threads
+    return {"value": cells * steps / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%d SSPRK3 step(s) of the channel scheme on a %dx%dx%d-block sub-box of %d^3 cells (%d cells), "
+                      "oracle/gbns_oracle.c (face-twice like flux_div_basic), OpenMP over blocks, %.1f s"
+                      % (steps, nblk[0], nblk[1], nblk[2], ncell[0], cells, el)}
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    cfg = config(args)
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_sample(steps=1, nblk=(4, 4, 2))
+        warm = max(0, min(args.warmup, 1))
+        for _ in range(warm):
+            cpu_sample(steps=1, nblk=(2, 2, 2))
+        vals = []
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps)):
+            vals.append(cpu_sample(steps=1, nblk=(2, 2, 2))["value"])
+            if time.perf_counter() - t0 > 120:
+                break
+        v = statistics.median(vals)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": len(vals), "warmup": warm, "ms_per_step": cfg["cells"] / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": cfg,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
+                                 "sample": "per step: 1 SSPRK3 step on a 2x2x2-block sub-box of 32^3 cells "
+                                           "(262144 cells) of the channel workload; the reference's CPU path cannot "
+                                           "be built on the GPU host (its sources are absent there), so the oracle "
+                                           "restatement oracle/gbns_oracle.c (bit-exact to the reference on the "
+                                           "pinned schemes) runs on all host cores"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    r = run_gpu(args, rank, world)
+    cells_all = r["cells"] * world
+    value = cells_all * args.steps / (r["ms"] * 1e-3)
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_sample(steps=1, nblk=(4, 4, 2))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32-flux/f64-state", "data": "synthetic", "config": cfg,
+        "roofline": {"bound": "hbm", "kernel": "flux_div", "achieved": r["achieved"], "peak": r["hbm_peak"],
+                     "unit": "GB/s", "frac": r["achieved"] / r["hbm_peak"],
+                     "traffic": r["traffic"], "peak_source": r["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "alg_bytes_per_cell": ALG_BYTES_FLUX, "avg_launch_ms": r["flux_avg_ms"],
+                     "share_of_step": r["flux_share"]},
+        "fp64_roof": {"fma_rate_tflops": r["fp64_fma_flops"] / 1e12, "fp32_fma_rate_tflops": r["fp32_fma_flops"] / 1e12,
+                      "note": "measured DFMA/FFMA chains on this GPU"},
+        "step_bytes": {"alg_bytes_per_cell_step": ALG_BYTES_STEP,
+                       "achieved_gbs": ALG_BYTES_STEP * cells_all * args.steps / (r["ms"] * 1e-3) / 1e9},
+        "clocks": r["clocks"],
+        "e2e": {"value": r["cells"] * world / (r["e2e_ms"] * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"],
+                "path": "gbns_ssprk3_step (C ABI) with the state copied from pinned host memory and back every step"},
+        "gpu_launches": r["launches"],
+        "health_bad_cells": r["health_bad_cells"],
+        "fp32_flux": r["fp32"],
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

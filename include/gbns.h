@@ -96,8 +96,9 @@ typedef struct gbns_gas_desc
 #define GBNS_LAW_POWER        1   /* viscous_laws::power_law_t (viscous_laws.h:102-135) */
 #define GBNS_LAW_SUTHERLAND   2   /* Sutherland's law (no reference counterpart) */
 
-#define GBNS_PREC_FP64        0   /* all arithmetic in FP64 */
+#define GBNS_PREC_FP64        0   /* FP64, every operation rounded as the reference's CPU code rounds it (no FMA contraction) */
 #define GBNS_PREC_FP32_FLUX   1   /* face reconstruction + flux in FP32; divergence accumulation FP64 */
+#define GBNS_PREC_FP64_FMA    2   /* FP64 with fused multiply-adds (faster; differs from the reference in the last bits) */
 
 typedef struct gbns_scheme_desc
 {
@@ -116,6 +117,8 @@ typedef struct gbns_scheme_desc
     double  T_ref;         /* power/sutherland reference temperature */
     double  power;         /* power-law exponent */
     double  S;             /* Sutherland constant */
+    double  prandtl_inv;   /* 1/Pr as the caller's law stores it; 0 = use 1.0/prandtl
+                              (constant_viscosity_t keeps only 1/Pr, viscous_laws.h:190-192) */
     gbns_gas_desc gas;
 } gbns_scheme_desc;
 

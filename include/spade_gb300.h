@@ -1,0 +1,299 @@
+/*
+ * spade_gb300.h — drop-in GB300 path for spade::pde_algs::flux_div.
+ *
+ * Include after "spade.h".  Passing the `gb300` algorithm trait selects the
+ * GB300 kernels through overload resolution; nothing else in the caller
+ * changes:
+ *
+ *     #include "spade.h"
+ *     #include "spade_gb300.h"
+ *     ...
+ *     spade::pde_algs::flux_div(prims, rhs, spade::omni::compose(tscheme, vscheme),
+ *                               spade::algs::make_traits(spade::pde_algs::gb300));
+ *
+ * The overload below replaces flux_div (pde-algs/flux-div/flux_div.h:16-56):
+ * it carries the reference's constraints plus "the traits select gb300", so
+ * it is the more constrained candidate.  It lowers the composed functor type
+ * at compile time into a gbns_scheme_desc (static_assert on anything the
+ * kernels do not implement: there is no CPU fallback), the grid_array into a
+ * gbns_grid_desc, calls gbns_flux_div on the arrays' device storage, and then
+ * synchronises and throws except::sp_exception on failure, like the
+ * reference's dispatch (dispatch/execute.h:84-96).
+ *
+ * Lowered functors: convective::cent_keep_scheme_t<gas, 2|4|6|8>,
+ * convective::totani_lr, convective::fweno_t<gas, smooth>,
+ * convective::pressure_diss_lr<gas, state_sensor::const_sensor_t>,
+ * viscous::visc_lr<viscous_laws::constant_viscosity_t | power_law_t, gas>,
+ * and omni::compose of one of each (convective, dissipation, viscous).
+ * Coordinates: coords::identity.
+ *
+ * Define GBNS_DROPIN_HOOK before including to route the lowered call to a
+ * user function `int GBNS_DROPIN_HOOK(const gbns_grid_desc*, const
+ * gbns_scheme_desc*, const double*, double*, int)` instead of the library
+ * (used by the host-only tests of the lowering).
+ */
+#pragma once
+
+#include <string>
+#include <type_traits>
+#include <cuda_runtime_api.h>
+
+#include "gbns.h"
+
+namespace spade::pde_algs
+{
+    // flux_div algorithm tag (pde-algs/flux-div/tags.h:5-33)
+    static struct tgb300_t : public fdiv_alg_base_t {} gb300;
+}
+
+namespace spade::gb300
+{
+    // flux arithmetic precision trait
+    struct flux_precision_base_t
+    {
+        constexpr static auto trait_label() { using namespace sym::literals; return "flux_precision"_sym; }
+    };
+    static struct tfp64_t      : public flux_precision_base_t { static constexpr int value = GBNS_PREC_FP64; }      fp64;
+    static struct tfp64_fma_t  : public flux_precision_base_t { static constexpr int value = GBNS_PREC_FP64_FMA; }  fp64_fma;
+    static struct tfp32_flux_t : public flux_precision_base_t { static constexpr int value = GBNS_PREC_FP32_FLUX; } fp32_flux;
+
+    namespace detail
+    {
+        template <typename T> struct always_false : std::false_type {};
+
+        template <typename gas_t>
+        inline void set_gas(gbns_scheme_desc& s, const gas_t& gas, bool& have_gas)
+        {
+            static_assert(std::is_same_v<gas_t, fluid_state::ideal_gas_t<double>>, "the GB300 path lowers ideal_gas_t<double>");
+            if (have_gas && (s.gas.gamma != gas.gamma || s.gas.R != gas.R))
+                throw except::sp_exception("gb300 flux_div: all functors of a composite must share one gas");
+            s.gas.gamma = gas.gamma;
+            s.gas.R = gas.R;
+            have_gas = true;
+        }
+
+        // slot: 0 convective, 1 dissipation, 2 viscous
+        template <typename T> struct lower
+        {
+            static_assert(always_false<T>::value, "gb300 flux_div: this flux functor has no GB300 kernel");
+        };
+
+        template <typename gas_t, const int order>
+        struct lower<convective::cent_keep_scheme_t<gas_t, order>>
+        {
+            static constexpr int slot = 0;
+            static void apply(gbns_scheme_desc& s, const convective::cent_keep_scheme_t<gas_t, order>& f, bool& g)
+            {
+                static_assert(order == 2 || order == 4 || order == 6 || order == 8, "cent_keep order 2, 4, 6 or 8");
+                s.convective = GBNS_CONV_CENT_KEEP;
+                s.order = order;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename gas_t>
+        struct lower<convective::totani_lr<gas_t>>
+        {
+            static constexpr int slot = 0;
+            static void apply(gbns_scheme_desc& s, const convective::totani_lr<gas_t>& f, bool& g)
+            {
+                s.convective = GBNS_CONV_TOTANI;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename gas_t, const convective::weno_smooth_indicator sm>
+        struct lower<convective::fweno_t<gas_t, sm>>
+        {
+            static constexpr int slot = 0;
+            static void apply(gbns_scheme_desc& s, const convective::fweno_t<gas_t, sm>& f, bool& g)
+            {
+                s.convective = GBNS_CONV_FWENO;
+                s.weno_smooth = (sm == convective::enable_smooth) ? 1 : 0;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename gas_t, typename ft>
+        struct lower<convective::pressure_diss_lr<gas_t, state_sensor::const_sensor_t<ft>>>
+        {
+            static constexpr int slot = 1;
+            static void apply(gbns_scheme_desc& s, const convective::pressure_diss_lr<gas_t, state_sensor::const_sensor_t<ft>>& f, bool& g)
+            {
+                s.dissipation = GBNS_DISS_PRESSURE;
+                s.sensor = GBNS_SENSOR_CONST;
+                s.sensor_alpha = f.scale.alpha;
+                s.eps_p = f.eps_p;
+                s.eps_T = f.eps_T;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename dt, typename gas_t>
+        struct lower<viscous::visc_lr<viscous_laws::constant_viscosity_t<dt>, gas_t>>
+        {
+            static constexpr int slot = 2;
+            static void apply(gbns_scheme_desc& s, const viscous::visc_lr<viscous_laws::constant_viscosity_t<dt>, gas_t>& f, bool& g)
+            {
+                s.viscous = GBNS_VISC_LR;
+                s.visc_law = GBNS_LAW_CONSTANT;
+                s.mu = f.vlaw.visc;
+                s.prandtl = 1.0/f.vlaw.prandtl_inv;
+                s.prandtl_inv = f.vlaw.prandtl_inv;   // the law stores 1/Pr (viscous_laws.h:190-192)
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename dt, typename gas_t>
+        struct lower<viscous::visc_lr<viscous_laws::power_law_t<dt>, gas_t>>
+        {
+            static constexpr int slot = 2;
+            static void apply(gbns_scheme_desc& s, const viscous::visc_lr<viscous_laws::power_law_t<dt>, gas_t>& f, bool& g)
+            {
+                s.viscous = GBNS_VISC_LR;
+                s.visc_law = GBNS_LAW_POWER;
+                s.mu = f.vlaw.mu_ref;
+                s.T_ref = f.vlaw.T_ref;
+                s.power = f.vlaw.power;
+                s.prandtl = f.vlaw.prandtl;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename k0_t, typename... ks_t>
+        struct lower<omni::composite_kernel_t<k0_t, ks_t...>>
+        {
+            static constexpr int slot = -1;
+            static void apply(gbns_scheme_desc& s, const omni::composite_kernel_t<k0_t, ks_t...>& f, bool& g, int* used)
+            {
+                static_assert(lower<k0_t>::slot >= 0, "nested composites are not lowered");
+                if (used[lower<k0_t>::slot]) throw except::sp_exception("gb300 flux_div: two functors of the same kind in one composite");
+                used[lower<k0_t>::slot] = 1;
+                lower<k0_t>::apply(s, f.kern, g);
+                if constexpr (sizeof...(ks_t) > 0)
+                {
+                    // compose(a, b, c) sums a + (b + c) (omni/compose.h:19-24); the
+                    // kernels sum conv + (diss + visc): a three-term composite must
+                    // come in that order, a two-term sum commutes exactly.
+                    static_assert(sizeof...(ks_t) < 2 || lower<k0_t>::slot == 0,
+                                  "three-term composites must be compose(convective, dissipation, viscous)");
+                    lower<omni::composite_kernel_t<ks_t...>>::apply(s, f.next, g, used);
+                }
+            }
+        };
+
+        template <typename kern_t>
+        struct lower<omni::composite_kernel_t<kern_t>>
+        {
+            static constexpr int slot = -1;
+            static void apply(gbns_scheme_desc& s, const omni::composite_kernel_t<kern_t>& f, bool& g, int* used)
+            {
+                if (used[lower<kern_t>::slot]) throw except::sp_exception("gb300 flux_div: two functors of the same kind in one composite");
+                used[lower<kern_t>::slot] = 1;
+                lower<kern_t>::apply(s, f.kern, g);
+            }
+        };
+
+        template <typename traits_t>
+        using fdiv_tag_of = typename utils::remove_all<decltype(algs::get_trait(std::declval<const traits_t&>(),
+                                                                                 std::declval<decltype(pde_algs::fdiv_alg_base_t::trait_label())>()))>::type;
+    }
+
+    // omni functor -> gbns_scheme_desc
+    template <typename flux_func_t>
+    gbns_scheme_desc lower_scheme(const flux_func_t& f, int precision = GBNS_PREC_FP64)
+    {
+        gbns_scheme_desc s{};
+        s.order = 2;
+        s.weno_smooth = 1;
+        s.prandtl = 1.0;
+        s.T_ref = 1.0;
+        s.precision = precision;
+        bool have_gas = false;
+        int used[3] = {0, 0, 0};
+        if constexpr (detail::lower<flux_func_t>::slot < 0) detail::lower<flux_func_t>::apply(s, f, have_gas, used);
+        else detail::lower<flux_func_t>::apply(s, f, have_gas);
+        return s;
+    }
+
+    // grid_array -> gbns_grid_desc (grid/grid_array.h:175-260, cartesian_grid.h:48-384)
+    template <typename arr_t>
+    gbns_grid_desc lower_grid(const arr_t& arr)
+    {
+        const auto& grid = arr.get_grid();
+        using coord_t = typename utils::remove_all<decltype(grid.get_coord_sys())>::type;
+        static_assert(std::is_same_v<coord_t, coords::identity<double>>, "the GB300 drop-in lowers coords::identity grids");
+        static_assert(std::is_same_v<typename arr_t::value_type, double>, "the GB300 path works on double arrays");
+        gbns_grid_desc g{};
+        const auto& blocks = grid.get_blocks();
+        const auto bnd = grid.get_bounds();
+        for (int d = 0; d < 3; ++d)
+        {
+            g.nblk[d] = blocks.num_blocks[d];
+            g.ncell[d] = grid.get_num_cells(d);
+            g.bounds[2*d] = bnd.min(d);
+            g.bounds[2*d + 1] = bnd.max(d);
+        }
+        if (grid.get_num_local_blocks() != grid.get_num_global_blocks())
+            throw except::sp_exception("gb300 flux_div: the grid must hold every block on this device");
+        const int ng = arr.get_num_exchange(0);
+        if (arr.get_num_exchange(1) != ng || arr.get_num_exchange(2) != ng)
+            throw except::sp_exception("gb300 flux_div: equal ghost depth in every direction required");
+        g.ng = ng;
+        g.coords = GBNS_COORDS_IDENTITY;
+        return g;
+    }
+
+    template <typename traits_t>
+    concept selects_gb300 = requires { typename detail::fdiv_tag_of<traits_t>; } &&
+                            std::same_as<detail::fdiv_tag_of<traits_t>, pde_algs::tgb300_t>;
+
+    template <typename traits_t>
+    constexpr int precision_of()
+    {
+        using namespace sym::literals;
+        using tr_t = typename utils::remove_all<decltype(algs::get_trait(std::declval<const traits_t&>(), "flux_precision"_sym, fp64))>::type;
+        return tr_t::value;
+    }
+}
+
+namespace spade::pde_algs
+{
+    template <
+        grid::multiblock_array sol_arr_t,
+        grid::multiblock_array rhs_arr_t,
+        typename flux_func_t,
+        typename alg_traits_t>
+    requires
+        grid::has_centering_type<sol_arr_t, grid::cell_centered> && gb300::selects_gb300<alg_traits_t>
+    static void flux_div(
+        const sol_arr_t& prims,
+        rhs_arr_t& rhs,
+        const flux_func_t& flux_func,
+        const alg_traits_t& traits)
+    {
+        using namespace sym::literals;
+        const auto& incr = algs::get_trait(traits, "pde_increment"_sym, increment);
+        using incr_mode_t = typename utils::remove_all<decltype(incr)>::type;
+        const gbns_grid_desc g = gb300::lower_grid(prims);
+        const gbns_scheme_desc s = gb300::lower_scheme(flux_func, gb300::precision_of<alg_traits_t>());
+        const double* q = prims.image().base;
+        double* r = rhs.image().base;
+#ifdef GBNS_DROPIN_HOOK
+        const int rc = GBNS_DROPIN_HOOK(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0);
+#else
+        static_assert(device::is_gpu<typename sol_arr_t::device_type> && device::is_gpu<typename rhs_arr_t::device_type>,
+                      "the gb300 flux_div runs on device::gpu arrays");
+        int rc = gbns_flux_div(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0, nullptr);
+        if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+#endif
+        if (rc != GBNS_OK)
+        {
+            char msg[512] = "drop-in hook failed";
+#ifndef GBNS_DROPIN_HOOK
+            gbns_last_error(msg, sizeof(msg));
+#endif
+            throw except::sp_exception(std::string("gb300 flux_div failed: ") + msg);
+        }
+    }
+}

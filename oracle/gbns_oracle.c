@@ -416,12 +416,12 @@ static void visc_law(const gbns_scheme_desc* S, double T, double* mu, double* be
         const double m = S->mu*(x*sqrt(x))*((S->T_ref + S->S)/(T + S->S));
         *mu = m;
         *beta = -2.0*m/3.0;
-        *alpha = m*(1.0/S->prandtl);
+        *alpha = m*(S->prandtl_inv > 0.0 ? S->prandtl_inv : 1.0/S->prandtl);
         return;
     }
     *mu = S->mu;
     *beta = -2.0*S->mu/3.0;
-    *alpha = S->mu*(1.0/S->prandtl);
+    *alpha = S->mu*(S->prandtl_inv > 0.0 ? S->prandtl_inv : 1.0/S->prandtl);
 }
 
 /* visc_lr::operator() (viscous.h:39-79) with the face value and gradient

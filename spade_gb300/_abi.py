@@ -39,6 +39,7 @@ LAW_SUTHERLAND = 2
 
 PREC_FP64 = 0
 PREC_FP32_FLUX = 1
+PREC_FP64_FMA = 2
 
 BC_PERIODIC = 0
 BC_NONE = 1
@@ -84,6 +85,7 @@ class SchemeDesc(ctypes.Structure):
         ("T_ref", ctypes.c_double),
         ("power", ctypes.c_double),
         ("S", ctypes.c_double),
+        ("prandtl_inv", ctypes.c_double),
         ("gas", GasDesc),
     ]
 

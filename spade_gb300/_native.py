@@ -1,0 +1,59 @@
+"""Loader for libgbns.so (the CUDA library).  No fallback: if the library is
+missing or fails to load, every entry point raises."""
+import ctypes
+import os
+
+from . import _abi
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libgbns.so")
+
+
+class SpadeError(RuntimeError):
+    """Raised for any nonzero libgbns return code (the reference raises
+    except::sp_exception, core/except.h:12-15)."""
+
+    def __init__(self, code, msg):
+        super().__init__("gbns error %d: %s" % (code, msg))
+        self.code = code
+
+
+def lib():
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise SpadeError(_abi.ERR_UNSUPPORTED,
+                         "libgbns.so is not built (%s); run `python -c \"import __graft_entry__ as g; g.build()\"`" % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    L.gbns_version.restype = ctypes.c_int
+    L.gbns_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.gbns_array_size.argtypes = [P(_abi.GridDesc), P(ctypes.c_size_t)]
+    L.gbns_flux_div.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, vp]
+    L.gbns_flux_div_variant.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, ctypes.c_int, vp]
+    L.gbns_flux_variant_count.argtypes = [P(_abi.SchemeDesc)]
+    L.gbns_fill_ghosts.argtypes = [P(_abi.GridDesc), P(_abi.BcDesc), vp, vp]
+    L.gbns_rk_stage.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, vp, vp, ctypes.c_int, vp]
+    L.gbns_reduce.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, vp]
+    L.gbns_reduce_scratch_size.argtypes = [P(_abi.GridDesc), P(ctypes.c_size_t), P(ctypes.c_size_t)]
+    L.gbns_reduce_async.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, ctypes.c_size_t, vp]
+    L.gbns_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double, vp]
+    L.gbns_device_status.argtypes = [P(ctypes.c_int), ctypes.c_int, vp]
+    if L.gbns_version() != _abi.ABI_VERSION:
+        raise SpadeError(_abi.ERR_UNSUPPORTED, "libgbns ABI version mismatch")
+    _LIB = L
+    return L
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    lib().gbns_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(rc):
+    if rc != 0:
+        raise SpadeError(rc, last_error())
+    return rc

@@ -1,0 +1,50 @@
+// Routes a lowered scheme to the translation unit holding its kernels.
+#include <cstdlib>
+#include "gbns_internal.cuh"
+#include "flux_launch.cuh"
+
+namespace gbns
+{
+    bool tma_disabled()
+    {
+        const char* e = std::getenv("GBNS_NO_TMA");
+        return e && e[0] == '1';
+    }
+
+    int flux_variant_count(const gbns_scheme_desc* s)
+    {
+        if (!s) return 0;
+        switch (s->convective)
+        {
+            case GBNS_CONV_CENT_KEEP: return s->order == 2 ? 4 : 1;
+            case GBNS_CONV_TOTANI:    return 2;
+            case GBNS_CONV_FWENO:     return 3;
+            case GBNS_CONV_WENO5:     return 2;
+            default:                  return 1;
+        }
+    }
+
+    int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
+                        const gbns_scheme_desc* desc, const double* prims, double* rhs,
+                        int increment, cudaStream_t stream, int variant)
+    {
+        if (variant < 0 || variant >= flux_variant_count(desc))
+            return set_error(GBNS_ERR_INVALID, "flux_div tile variant out of range");
+        FluxCall c{g, &G, Y, &S, prims, rhs, increment, stream, variant};
+        const bool stretch = g->coords != GBNS_COORDS_IDENTITY;
+        const bool upwind = desc->convective == GBNS_CONV_FWENO || desc->convective == GBNS_CONV_WENO5;
+        const int conv = desc->convective, order = desc->order;
+        if (desc->precision == GBNS_PREC_FP64)
+        {
+            if (!stretch) return upwind ? flux_f64x_identity_b(c, conv, order) : flux_f64x_identity_a(c, conv, order);
+            return upwind ? flux_f64x_stretch_b(c, conv, order) : flux_f64x_stretch_a(c, conv, order);
+        }
+        if (desc->precision == GBNS_PREC_FP64_FMA)
+        {
+            if (!stretch) return upwind ? flux_f64_identity_b(c, conv, order) : flux_f64_identity_a(c, conv, order);
+            return upwind ? flux_f64_stretch_b(c, conv, order) : flux_f64_stretch_a(c, conv, order);
+        }
+        if (!stretch) return upwind ? flux_f32_identity_b(c, conv, order) : flux_f32_identity_a(c, conv, order);
+        return upwind ? flux_f32_stretch_b(c, conv, order) : flux_f32_stretch_a(c, conv, order);
+    }
+}

@@ -1,0 +1,7 @@
+// Flux-divergence kernels: FP32 flux arithmetic, FP64 accumulation; identity coordinates; convective group a.
+#define GBNS_REAL float
+#define GBNS_STRETCH false
+#define GBNS_GROUP 0
+#define GBNS_TAG 8
+#define GBNS_FN flux_f32_identity_a
+#include "flux_inst.cuh"

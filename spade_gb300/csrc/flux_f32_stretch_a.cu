@@ -1,0 +1,7 @@
+// Flux-divergence kernels: FP32 flux arithmetic, FP64 accumulation; stretch coordinates; convective group a.
+#define GBNS_REAL float
+#define GBNS_STRETCH true
+#define GBNS_GROUP 0
+#define GBNS_TAG 10
+#define GBNS_FN flux_f32_stretch_a
+#include "flux_inst.cuh"

@@ -1,0 +1,7 @@
+// Flux-divergence kernels: FP64 with FMA contraction; stretch coordinates; convective group a.
+#define GBNS_REAL double
+#define GBNS_STRETCH true
+#define GBNS_GROUP 0
+#define GBNS_TAG 6
+#define GBNS_FN flux_f64_stretch_a
+#include "flux_inst.cuh"

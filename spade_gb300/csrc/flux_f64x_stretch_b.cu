@@ -1,0 +1,7 @@
+// Flux-divergence kernels: FP64, no FMA contraction (bit-compatible with the reference's CPU arithmetic; built with -fmad=false); stretch coordinates; convective group b.
+#define GBNS_REAL double
+#define GBNS_STRETCH true
+#define GBNS_GROUP 1
+#define GBNS_TAG 3
+#define GBNS_FN flux_f64x_stretch_b
+#include "flux_inst.cuh"

@@ -1,0 +1,94 @@
+// Instantiation helper for the flux-divergence translation units.  Each TU
+// defines GBNS_REAL, GBNS_STRETCH, GBNS_GROUP, GBNS_TAG and GBNS_FN and includes this.
+#pragma once
+
+#include <cstring>
+#include "flux_kernel.cuh"
+#include "flux_launch.cuh"
+
+namespace gbns
+{
+    namespace { status_registrar tu_status_registrar; }
+
+    namespace {
+    template <class Cfg>
+    int run_flux_cfg(const FluxCall& c)
+    {
+        const GeomK& G = *c.G;
+        FluxArgs A;
+        A.prims = c.prims;
+        A.rhs = c.rhs;
+        A.increment = c.increment;
+        A.ntile[0] = (G.n[0] + Cfg::TX - 1)/Cfg::TX;
+        A.ntile[1] = (G.n[1] + Cfg::TY - 1)/Cfg::TY;
+        A.ntile[2] = (G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
+        const long long ntiles = (long long)A.ntile[0]*A.ntile[1]*A.ntile[2];
+        if (ntiles > 2147483647ll || G.nblk > 65535)
+            return set_error(GBNS_ERR_UNSUPPORTED, "grid too large for one flux_div launch (blocks > 65535)");
+        CUtensorMap tmap;
+        std::memset(&tmap, 0, sizeof(tmap));
+        A.use_tma = 0;
+        const bool aligned = (G.ni % 2 == 0) && ((reinterpret_cast<uintptr_t>(c.prims) & 15) == 0);
+        if (aligned && !tma_disabled())
+        {
+            int rc = encode_prims_tmap(&tmap, c.prims, G, Cfg::BXE, Cfg::BY, Cfg::BZ);
+            if (rc) return rc;
+            A.use_tma = 1;
+        }
+        auto kern = flux_div_kernel<Cfg>;
+        int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM_BYTES)),
+                            "flux_div smem attribute");
+        if (rc) return rc;
+        const dim3 grid(unsigned(ntiles), unsigned(G.nblk));
+        YTabT<Cfg::STRETCH> Y;
+        if constexpr (Cfg::STRETCH) Y = *c.Y;
+        kern<<<grid, Cfg::NT, Cfg::SMEM_BYTES, c.stream>>>(tmap, G, Y, *c.S, A);
+        return check_cuda(cudaGetLastError(), "flux_div launch");
+    }
+    }
+}
+
+#define GBNS_RUN(CONV, ORDER, TX, TY, TZ, NT) \
+    return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG>>(c)
+
+namespace gbns
+{
+    int GBNS_FN(const FluxCall& c, int conv, int order)
+    {
+        const int v = c.variant;
+#if GBNS_GROUP == 0
+        if (conv == GBNS_CONV_NONE) { GBNS_RUN(GBNS_CONV_NONE, 2, 8, 8, 8, 256); }
+        if (conv == GBNS_CONV_CENT_KEEP)
+        {
+            if (order == 2)
+            {
+                if (v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 16, 8, 4, 256);
+                if (v == 2) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 4, 128);
+                if (v == 3) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 16, 8, 8, 256);
+                GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 256);
+            }
+            if (order == 4) { GBNS_RUN(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 256); }
+            if (order == 6) { GBNS_RUN(GBNS_CONV_CENT_KEEP, 6, 8, 8, 4, 256); }
+            if (order == 8) { GBNS_RUN(GBNS_CONV_CENT_KEEP, 8, 8, 8, 4, 256); }
+        }
+        if (conv == GBNS_CONV_TOTANI)
+        {
+            if (v == 1) GBNS_RUN(GBNS_CONV_TOTANI, 2, 16, 8, 4, 256);
+            GBNS_RUN(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
+        }
+#else
+        if (conv == GBNS_CONV_FWENO)
+        {
+            if (v == 1) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 4, 128);
+            if (v == 2) GBNS_RUN(GBNS_CONV_FWENO, 2, 16, 8, 4, 256);
+            GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
+        }
+        if (conv == GBNS_CONV_WENO5)
+        {
+            if (v == 1) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 8, 256);
+            GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
+        }
+#endif
+        return set_error(GBNS_ERR_UNSUPPORTED, "flux scheme not instantiated");
+    }
+}

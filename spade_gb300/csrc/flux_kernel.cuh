@@ -1,0 +1,729 @@
+// Fused flux-divergence kernel (sm_103a).
+//
+// One CTA owns one TX*TY*TZ tile of one grid block.  It stages the tile plus
+// an H-cell halo (AoS5 doubles, straight from the grid_array layout) into
+// shared memory with one 4-D TMA copy (or coalesced loads when the row pitch
+// is not 16-byte aligned), derives the per-cell quantities every face of the
+// stencil shares (rho, e or the Rusanov split) once per cell, evaluates each
+// face flux ONCE (the reference's flux_div_basic, flux_div_basic.h:47-76,
+// evaluates every face twice) into a shared face buffer, and accumulates
+//     rhs(cell) += jac*F(i-1/2)*inv_dx - jac*F(i+1/2)*inv_dx
+// per direction in FP64 registers in the reference's order
+// (flux_div_basic.h:109-129), then writes the AoS5 residual.
+//
+// Real = double: every operation in FP64 (the drop-in).
+// Real = float : per-cell derivation and face fluxes in FP32, state read and
+//                divergence accumulated and written in FP64.
+#pragma once
+
+#include <type_traits>
+#include "gbns_internal.cuh"
+
+namespace gbns
+{
+    template <int CONV, int ORDER>
+    struct ConvTraits
+    {
+        static constexpr int HC =
+            (CONV == GBNS_CONV_CENT_KEEP) ? ORDER/2 :
+            (CONV == GBNS_CONV_TOTANI)    ? 1 :
+            (CONV == GBNS_CONV_FWENO)     ? 2 :
+            (CONV == GBNS_CONV_WENO5)     ? 3 : 0;
+        static constexpr int NDER =
+            (CONV == GBNS_CONV_FWENO || CONV == GBNS_CONV_WENO5) ? 3 :
+            (CONV == GBNS_CONV_CENT_KEEP || CONV == GBNS_CONV_TOTANI) ? 2 : 0;
+    };
+
+    template <bool S> using YTabT = typename std::conditional<S, YTabK, YTabNone>::type;
+
+    constexpr int cmax3(int a, int b, int c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
+    constexpr size_t align128(size_t x) { return (x + 127) & ~size_t(127); }
+
+    // TAG_ distinguishes translation units that instantiate the same
+    // arithmetic with different compiler settings (FMA contraction on/off),
+    // so their kernels and launchers never share a symbol.
+    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_>
+    struct FluxCfg
+    {
+        using Real = Real_;
+        static constexpr int CONV = CONV_, ORDER = ORDER_;
+        static constexpr bool STRETCH = STRETCH_;
+        static constexpr int TX = TX_, TY = TY_, TZ = TZ_, NT = NT_;
+        static constexpr bool FP64 = std::is_same<Real, double>::value;
+        static constexpr int HC = ConvTraits<CONV, ORDER>::HC;
+        static constexpr int H = HC > 1 ? HC : 1;
+        static constexpr int NDER = ConvTraits<CONV, ORDER>::NDER;
+        // x start is rounded down to an even padded cell (TMA 16-byte rule),
+        // so the box is one cell wider and its width is kept even.
+        static constexpr int BXE = ((TX + 2*H + 1) + 1) & ~1;
+        static constexpr int BY = TY + 2*H, BZ = TZ + 2*H;
+        static constexpr int BOXN = BXE*BY*BZ;
+        static constexpr int SX = 1, SY = BXE, SZ = BXE*BY;
+        static constexpr int NCELL = TX*TY*TZ;
+        static constexpr int NF0 = (TX + 1)*TY*TZ, NF1 = TX*(TY + 1)*TZ, NF2 = TX*TY*(TZ + 1);
+        static constexpr int NFMAX = cmax3(NF0, NF1, NF2);
+        static constexpr int CPT = (NCELL + NT - 1)/NT;
+        static constexpr size_t STAGE_BYTES = align128(size_t(BOXN)*5*sizeof(double));
+        static constexpr size_t SOA_BYTES   = FP64 ? 0 : align128(size_t(BOXN)*5*sizeof(float));
+        static constexpr size_t DER_BYTES   = align128(size_t(NDER > 0 ? NDER : 1)*BOXN*sizeof(Real));
+        static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFMAX*sizeof(Real));
+        // FP32: the staging buffer is dead once converted, so derived values
+        // and face fluxes reuse it when they fit.
+        static constexpr bool REUSE = !FP64 && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
+        static constexpr size_t SMEM_BYTES = 128 /*mbarrier*/ + STAGE_BYTES + SOA_BYTES +
+                                             (REUSE ? 0 : DER_BYTES + FLX_BYTES);
+        static_assert(SMEM_BYTES <= 227*1024, "tile does not fit in shared memory");
+        static_assert(5*BXE <= 256, "TMA box inner extent exceeds 256 elements");
+    };
+
+    // Shared-memory view of the staged box.
+    template <class Cfg>
+    struct BoxView
+    {
+        using Real = typename Cfg::Real;
+        const double* stage;   // AoS doubles (FP64 compute)
+        const float*  soa;     // SoA floats (FP32 compute)
+        const Real*   der;     // derived per-cell values, SoA
+        __device__ __forceinline__ Real q(int v, int c) const
+        {
+            if constexpr (Cfg::FP64) return stage[c*5 + v];
+            else return soa[v*Cfg::BOXN + c];
+        }
+        __device__ __forceinline__ Real d(int k, int c) const { return der[k*Cfg::BOXN + c]; }
+    };
+
+    template <class Real>
+    struct SchemeR
+    {
+        Real gamma, R, gm1, spec_heat, inv_gamma_avg, R_avg, eps_p, eps_T, sens;
+        Real mu, beta_c, alpha_c, T_ref, power, inv_pr, prandtl, tref_plus_s, S;
+        Real ck_a[4];
+        int diss, visc, law, smooth;
+        __device__ __forceinline__ void load(const SchemeK& s)
+        {
+            gamma = Real(s.gamma); R = Real(s.R); gm1 = Real(s.gm1); spec_heat = Real(s.spec_heat);
+            inv_gamma_avg = Real(s.inv_gamma_avg); R_avg = Real(s.R_avg);
+            eps_p = Real(s.eps_p); eps_T = Real(s.eps_T); sens = Real(s.sens);
+            mu = Real(s.mu); beta_c = Real(s.beta_c); alpha_c = Real(s.alpha_c);
+            T_ref = Real(s.T_ref); power = Real(s.power); inv_pr = Real(s.inv_pr); prandtl = Real(s.prandtl);
+            tref_plus_s = Real(s.tref_plus_s); S = Real(s.S);
+            for (int i = 0; i < 4; ++i) ck_a[i] = Real(s.ck_a[i]);
+            diss = s.diss; visc = s.visc; law = s.law; smooth = s.smooth;
+        }
+    };
+
+    __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
+    __device__ __forceinline__ float  dev_sqrt(float x)  { return sqrtf(x); }
+    __device__ __forceinline__ double dev_pow(double x, double y) { return pow(x, y); }
+    __device__ __forceinline__ float  dev_pow(float x, float y)   { return powf(x, y); }
+
+    // ------------------------------------------------------------------
+    // per-cell derived quantities (computed once per staged cell)
+    // ------------------------------------------------------------------
+    template <class Cfg>
+    __device__ __forceinline__ void derive_cell(const BoxView<Cfg>& V, typename Cfg::Real* der,
+                                                const SchemeR<typename Cfg::Real>& S, int c)
+    {
+        using Real = typename Cfg::Real;
+        const Real p = V.q(0, c), T = V.q(1, c), u = V.q(2, c), v = V.q(3, c), w = V.q(4, c);
+        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP || Cfg::CONV == GBNS_CONV_TOTANI)
+        {
+            // convective.h:130-131 / 80-84
+            const Real rho = p/(S.R*T);
+            der[0*Cfg::BOXN + c] = rho;
+            der[1*Cfg::BOXN + c] = p/(rho*S.gm1);
+        }
+        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5)
+        {
+            // fweno_t per-point split (convective.h:360-376, 458-467)
+            Real r = S.R*T;
+            Real h = u*u;
+            h += v*v;
+            h += w*w;
+            h = dev_sqrt(h);
+            h += dev_sqrt(r*S.gamma);
+            const Real rho = p/r;
+            h *= rho;
+            h *= Real(0.5);
+            Real e = u*u;
+            e += v*v;
+            e += w*w;
+            e *= Real(0.5);
+            e += (S.R*T)/S.gm1;
+            der[0*Cfg::BOXN + c] = rho;
+            der[1*Cfg::BOXN + c] = h;
+            der[2*Cfg::BOXN + c] = e;
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // face fluxes.  D = face direction, rc = box index of the right cell,
+    // nD = normal component along D (1 for identity coordinates).
+    // ------------------------------------------------------------------
+    template <class Cfg, int D> struct DirStride
+    {
+        static constexpr int S  = D == 0 ? Cfg::SX : (D == 1 ? Cfg::SY : Cfg::SZ);
+        static constexpr int S1 = (D + 1) % 3 == 0 ? Cfg::SX : ((D + 1) % 3 == 1 ? Cfg::SY : Cfg::SZ);
+        static constexpr int S2 = (D + 2) % 3 == 0 ? Cfg::SX : ((D + 2) % 3 == 1 ? Cfg::SY : Cfg::SZ);
+    };
+
+    // cent_keep_scheme_t::operator() (convective.h:117-184)
+    template <class Cfg, int D>
+    __device__ __forceinline__ void conv_cent_keep(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                   int rc, typename Cfg::Real nD, typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int W = Cfg::ORDER, hw = Cfg::ORDER/2, SD = DirStride<Cfg, D>::S;
+        Real un[W], rho[W], eng[W];
+        #pragma unroll
+        for (int m = 0; m < W; ++m)
+        {
+            const int c = rc + (m - hw)*SD;
+            un[m]  = V.q(2 + D, c)*nD;
+            rho[m] = V.d(0, c);
+            eng[m] = V.d(1, c);
+        }
+        Real cc = 0, mx = 0, my = 0, mz = 0, g = 0, k = 0, ie = 0, pp = 0;
+        #pragma unroll
+        for (int ii = 1; ii < hw + 1; ++ii)
+        {
+            const Real a = S.ck_a[ii - 1];
+            #pragma unroll
+            for (int jj = 0; jj < ii; ++jj)
+            {
+                const int i0 = hw - 1 - jj, i1 = i0 + ii;
+                const int c0 = rc + (i0 - hw)*SD, c1 = rc + (i1 - hw)*SD;
+                const Real u0 = V.q(2, c0), v0 = V.q(3, c0), w0 = V.q(4, c0), p0 = V.q(0, c0);
+                const Real u1 = V.q(2, c1), v1 = V.q(3, c1), w1 = V.q(4, c1), p1 = V.q(0, c1);
+                const Real c_loc = a*(Real(0.25)*(rho[i0] + rho[i1])*(un[i1] + un[i0]));
+                cc += c_loc;
+                mx += c_loc*(Real(0.5)*(u0 + u1));
+                my += c_loc*(Real(0.5)*(v0 + v1));
+                mz += c_loc*(Real(0.5)*(w0 + w1));
+                g  += a*(Real(0.5)*(p0 + p1));
+                k  += Real(0.5)*c_loc*(u0*u1 + v0*v1 + w0*w1);
+                ie += c_loc*(Real(0.5)*(eng[i0] + eng[i1]));
+                pp += a*(Real(0.5)*(un[i0]*p1 + un[i1]*p0));
+            }
+        }
+        out[0] = Real(2.0)*cc;
+        out[1] = Real(2.0)*(k + ie + pp);
+        out[2] = Real(2.0)*(D == 0 ? mx + g*nD : mx);
+        out[3] = Real(2.0)*(D == 1 ? my + g*nD : my);
+        out[4] = Real(2.0)*(D == 2 ? mz + g*nD : mz);
+    }
+
+    // totani_lr::operator() (convective.h:68-93)
+    template <class Cfg, int D>
+    __device__ __forceinline__ void conv_totani(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                int rc, typename Cfg::Real nD, typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int SD = DirStride<Cfg, D>::S;
+        const int cl = rc - SD, cr = rc;
+        const Real pl = V.q(0, cl), ul = V.q(2, cl), vl = V.q(3, cl), wl = V.q(4, cl);
+        const Real pr = V.q(0, cr), ur = V.q(2, cr), vr = V.q(3, cr), wr = V.q(4, cr);
+        const Real un_l = V.q(2 + D, cl)*nD, un_r = V.q(2 + D, cr)*nD;
+        const Real rho_l = V.d(0, cl), rho_r = V.d(0, cr);
+        const Real e_l = V.d(1, cl), e_r = V.d(1, cr);
+        const Real c = Real(0.25)*(rho_l + rho_r)*(un_l + un_r);
+        out[0] = c;
+        out[1] = Real(0.5)*c*(e_l + e_r + ul*ur + vl*vr + wl*wr) + Real(0.5)*(un_l*pr + un_r*pl);
+        const Real pn = Real(0.5)*(nD*pl + nD*pr);
+        out[2] = Real(0.5)*c*(ul + ur) + (D == 0 ? pn : Real(0));
+        out[3] = Real(0.5)*c*(vl + vr) + (D == 1 ? pn : Real(0));
+        out[4] = Real(0.5)*c*(wl + wr) + (D == 2 ? pn : Real(0));
+    }
+
+    // fweno_t flux/dissipation of equation `eq` at one stencil point
+    // (convective.h:442-493).
+    template <class Cfg, int D>
+    __device__ __forceinline__ void fweno_point(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                int c, int eq, typename Cfg::Real nD,
+                                                typename Cfg::Real& fl, typename Cfg::Real& ds)
+    {
+        using Real = typename Cfg::Real;
+        const Real rho = V.d(0, c), hsr = V.d(1, c);
+        const Real un = V.q(2 + D, c)*nD;
+        if (eq == 0)
+        {
+            fl = un*(Real(0.5)*rho);
+            ds = hsr;
+        }
+        else if (eq == 1)
+        {
+            const Real engy = V.d(2, c);
+            fl = (un*(Real(0.5)*rho))*(engy + S.R*V.q(1, c));
+            ds = hsr*engy;
+        }
+        else
+        {
+            const int dr = eq - 2;
+            const Real ud = V.q(2 + dr, c);
+            Real m = un*rho;
+            m *= ud;
+            if (dr == D) m += V.q(0, c)*nD;
+            m *= Real(0.5);
+            fl = m;
+            ds = hsr*ud;
+        }
+    }
+
+    // apply_weno of fweno_t (convective.h:378-427)
+    template <class Real>
+    __device__ __forceinline__ Real fweno_apply(const Real fl[4], const Real ds[4], int smooth)
+    {
+        const Real f0uk = fl[0] + ds[0], f0dk = fl[0] - ds[0];
+        const Real f1uk = fl[1] + ds[1], f1dk = fl[1] - ds[1];
+        const Real f2uk = fl[2] + ds[2], f2dk = fl[2] - ds[2];
+        const Real f3uk = fl[3] + ds[3], f3dk = fl[3] - ds[3];
+        const Real r0 = Real(-0.5)*(f0uk) + Real(1.5)*(f1uk);
+        const Real r1 = Real( 0.5)*(f1uk) + Real(0.5)*(f2uk);
+        const Real r2 = Real( 0.5)*(f1dk) + Real(0.5)*(f2dk);
+        const Real r3 = Real( 1.5)*(f2dk) - Real(0.5)*(f3dk);
+        if (!smooth)
+            return Real(1.0/3.0)*r0 + Real(2.0/3.0)*r1 + Real(2.0/3.0)*r2 + Real(1.0/3.0)*r3;
+        const Real eps = Real(1e-16);
+        Real a0 = (f0uk) - (f1uk), a1 = (f1uk) - (f2uk), a2 = (f1dk) - (f2dk), a3 = (f2dk) - (f3dk);
+        a0 *= a0; a0 += eps; a0 *= a0;
+        a1 *= a1; a1 += eps; a1 *= a1;
+        a2 *= a2; a2 += eps; a2 *= a2;
+        a3 *= a3; a3 += eps; a3 *= a3;
+        a0 += a0; a0 += a1; a0 = a1/a0;
+        a3 += a3; a3 += a2; a3 = a2/a3;
+        a1 = Real(1.0) - a0;
+        a2 = Real(1.0) - a3;
+        return a0*r0 + a1*r1 + a2*r2 + a3*r3;
+    }
+
+    template <class Cfg, int D>
+    __device__ __forceinline__ void conv_fweno(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                               int rc, typename Cfg::Real nD, typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int SD = DirStride<Cfg, D>::S;
+        #pragma unroll 1
+        for (int eq = 0; eq < 5; ++eq)
+        {
+            Real fl[4], ds[4];
+            #pragma unroll
+            for (int m = 0; m < 4; ++m) fweno_point<Cfg, D>(V, S, rc + (m - 2)*SD, eq, nD, fl[m], ds[m]);
+            out[eq] = fweno_apply<Real>(fl, ds, S.smooth);
+        }
+    }
+
+    // 5th-order WENO-JS side reconstruction (Jiang & Shu 1996); cells a..e
+    // upwind to downwind.  No reference counterpart.
+    template <class Real>
+    __device__ __forceinline__ Real weno5_side(Real a, Real b, Real c, Real d, Real e, int smooth)
+    {
+        const Real sixth = Real(1.0/6.0);
+        const Real p0 = (Real(2.0)*a - Real(7.0)*b + Real(11.0)*c)*sixth;
+        const Real p1 = (-b + Real(5.0)*c + Real(2.0)*d)*sixth;
+        const Real p2 = (Real(2.0)*c + Real(5.0)*d - e)*sixth;
+        if (!smooth) return Real(0.1)*p0 + Real(0.6)*p1 + Real(0.3)*p2;
+        const Real t0 = a - Real(2.0)*b + c, s0 = a - Real(4.0)*b + Real(3.0)*c;
+        const Real t1 = b - Real(2.0)*c + d, s1 = b - d;
+        const Real t2 = c - Real(2.0)*d + e, s2 = Real(3.0)*c - Real(4.0)*d + e;
+        const Real k13 = Real(13.0/12.0);
+        const Real b0 = k13*t0*t0 + Real(0.25)*s0*s0;
+        const Real b1 = k13*t1*t1 + Real(0.25)*s1*s1;
+        const Real b2 = k13*t2*t2 + Real(0.25)*s2*s2;
+        const Real eps = Real(1e-16);
+        const Real a0 = Real(0.1)/((b0 + eps)*(b0 + eps));
+        const Real a1 = Real(0.6)/((b1 + eps)*(b1 + eps));
+        const Real a2 = Real(0.3)/((b2 + eps)*(b2 + eps));
+        const Real inv = Real(1.0)/(a0 + a1 + a2);
+        return (a0*p0 + a1*p1 + a2*p2)*inv;
+    }
+
+    template <class Cfg, int D>
+    __device__ __forceinline__ void conv_weno5(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                               int rc, typename Cfg::Real nD, typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int SD = DirStride<Cfg, D>::S;
+        #pragma unroll 1
+        for (int eq = 0; eq < 5; ++eq)
+        {
+            Real up[6], dn[6];
+            #pragma unroll
+            for (int m = 0; m < 6; ++m)
+            {
+                Real fl, ds;
+                fweno_point<Cfg, D>(V, S, rc + (m - 3)*SD, eq, nD, fl, ds);
+                up[m] = fl + ds;
+                dn[m] = fl - ds;
+            }
+            out[eq] = weno5_side<Real>(up[0], up[1], up[2], up[3], up[4], S.smooth)
+                    + weno5_side<Real>(dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
+        }
+    }
+
+    // pressure_diss_lr<gas, const_sensor_t>::operator() (convective.h:212-245)
+    template <class Cfg, int D>
+    __device__ __forceinline__ void diss_pressure(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                  int rc, typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int SD = DirStride<Cfg, D>::S;
+        const int cl = rc - SD, cr = rc;
+        const Real pl = V.q(0, cl), Tl = V.q(1, cl), ul = V.q(2, cl), vl = V.q(3, cl), wl = V.q(4, cl);
+        const Real pr = V.q(0, cr), Tr = V.q(1, cr), ur = V.q(2, cr), vr = V.q(3, cr), wr = V.q(4, cr);
+        const Real delta_p = pl - pr;
+        const Real delta_T = Tl - Tr;
+        const Real pavg = Real(0.5)*(pl + pr);
+        const Real Tavg = Real(0.5)*(Tl + Tr);
+        const Real inv_RT = Real(1.0)/(S.R_avg*Tavg);
+        const Real p_inv_rt2 = pavg*inv_RT/Tavg;
+        const Real k = Real(0.5)*(ul*ur + vl*vr + wl*wr);
+        const Real u = Real(0.5)*(ul + ur);
+        const Real v = Real(0.5)*(vl + vr);
+        const Real w = Real(0.5)*(wl + wr);
+        const Real ap = S.sens*S.eps_p*delta_p;
+        const Real aT = S.sens*S.eps_T*delta_T*p_inv_rt2;
+        out[0] = ap*inv_RT;
+        out[1] = ap*(k*inv_RT + S.inv_gamma_avg);
+        out[2] = ap*u*inv_RT;
+        out[3] = ap*v*inv_RT;
+        out[4] = ap*w*inv_RT;
+        out[0] -= aT;
+        out[1] -= aT*(Real(0.5)*k);
+        out[2] -= aT*u;
+        out[3] -= aT*v;
+        out[4] -= aT*w;
+    }
+
+    // visc_lr::operator() (viscous.h:39-79) with info::value / info::gradient
+    // at the face (info_value.h:28-40, info_gradient.h:61-123).
+    template <class Cfg, int D>
+    __device__ __forceinline__ void visc_lr(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                            int rc, typename Cfg::Real nD,
+                                            const typename Cfg::Real inv[3], typename Cfg::Real im,
+                                            typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int SD = DirStride<Cfg, D>::S, S1 = DirStride<Cfg, D>::S1, S2 = DirStride<Cfg, D>::S2;
+        constexpr int D1 = (D + 1) % 3, D2 = (D + 2) % 3;
+        const int cl = rc - SD, cr = rc;
+        // grad[a][t]: a = direction, t = 0:T 1:u 2:v 3:w
+        Real grad[3][4];
+        #pragma unroll
+        for (int t = 0; t < 4; ++t)
+        {
+            const int v = t + 1;
+            grad[D][t]  = (Real(-1.0)*V.q(v, cl))*inv[D];
+            grad[D1][t] = (Real(0.25)*V.q(v, cl + S1))*inv[D1];
+            grad[D1][t] += (Real(-0.25)*V.q(v, cl - S1))*inv[D1];
+            grad[D2][t] = (Real(0.25)*V.q(v, cl + S2))*inv[D2];
+            grad[D2][t] += (Real(-0.25)*V.q(v, cl - S2))*inv[D2];
+            grad[D][t]  += (Real(1.0)*V.q(v, cr))*inv[D];
+            grad[D1][t] += (Real(0.25)*V.q(v, cr + S1))*inv[D1];
+            grad[D1][t] += (Real(-0.25)*V.q(v, cr - S1))*inv[D1];
+            grad[D2][t] += (Real(0.25)*V.q(v, cr + S2))*inv[D2];
+            grad[D2][t] += (Real(-0.25)*V.q(v, cr - S2))*inv[D2];
+            if constexpr (Cfg::STRETCH) grad[1][t] *= im;
+        }
+        Real qf[5];
+        #pragma unroll
+        for (int v = 0; v < 5; ++v) { qf[v] = V.q(v, cl); qf[v] += V.q(v, cr); qf[v] *= Real(0.5); }
+        Real visc, visc2, dfs;
+        if (S.law == GBNS_LAW_CONSTANT)
+        {
+            visc = S.mu; visc2 = S.beta_c; dfs = S.alpha_c;
+        }
+        else if (S.law == GBNS_LAW_POWER)
+        {
+            visc = S.mu*dev_pow(qf[1]/S.T_ref, S.power);
+            visc2 = Real(-0.66666666667)*visc;
+            dfs = visc/S.prandtl;
+        }
+        else
+        {
+            const Real x = qf[1]/S.T_ref;
+            visc = S.mu*(x*dev_sqrt(x))*(S.tref_plus_s/(qf[1] + S.S));
+            visc2 = Real(-2.0)*visc/Real(3.0);
+            dfs = visc*S.inv_pr;
+        }
+        const Real div = grad[0][1] + grad[1][2] + grad[2][3];
+        const Real t00 = visc*(grad[0][1] + grad[0][1]) + visc2*div;
+        const Real t01 = visc*(grad[0][2] + grad[1][1]);
+        const Real t02 = visc*(grad[0][3] + grad[2][1]);
+        const Real t12 = visc*(grad[1][3] + grad[2][2]);
+        const Real t11 = visc*(grad[1][2] + grad[1][2]) + visc2*div;
+        const Real t22 = visc*(grad[2][3] + grad[2][3]) + visc2*div;
+        const Real cond = S.spec_heat*dfs;
+        // only row D of tau and component D of the heat flux survive n = nD e_D
+        Real tr0, tr1, tr2;
+        if constexpr (D == 0) { tr0 = t00; tr1 = t01; tr2 = t02; }
+        else if constexpr (D == 1) { tr0 = t01; tr1 = t11; tr2 = t12; }
+        else { tr0 = t02; tr1 = t12; tr2 = t22; }
+        const Real ht = qf[2]*tr0 + qf[3]*tr1 + qf[4]*tr2 + cond*grad[D][0];
+        out[0] = Real(0.0);
+        out[1] = -(nD*ht);
+        out[2] = -(nD*tr0);
+        out[3] = -(nD*tr1);
+        out[4] = -(nD*tr2);
+    }
+
+    // Composite face flux conv + (diss + visc)  (omni/compose.h:19-24)
+    template <class Cfg, int D>
+    __device__ __forceinline__ void face_flux(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                              int rc, typename Cfg::Real nD,
+                                              const typename Cfg::Real inv[3], typename Cfg::Real im,
+                                              typename Cfg::Real* F)
+    {
+        using Real = typename Cfg::Real;
+        Real t0[5], t1[5], t2[5];
+        int nterm = 0;
+        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP) { conv_cent_keep<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
+        else if constexpr (Cfg::CONV == GBNS_CONV_TOTANI) { conv_totani<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
+        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) { conv_fweno<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
+        else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) { conv_weno5<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
+        Real* nxt = nterm == 0 ? t0 : t1;
+        int extra = 0;
+        if (S.diss) { diss_pressure<Cfg, D>(V, S, rc, nxt); ++extra; }
+        if (S.visc)
+        {
+            Real* dst = (extra == 0) ? nxt : t2;
+            visc_lr<Cfg, D>(V, S, rc, nD, inv, im, dst);
+            ++extra;
+        }
+        if constexpr (Cfg::CONV == GBNS_CONV_NONE)
+        {
+            // diss + visc, diss, or visc
+            if (extra == 2) { for (int v = 0; v < 5; ++v) F[v] = t0[v] + t2[v]; }
+            else if (extra == 1) { for (int v = 0; v < 5; ++v) F[v] = t0[v]; }
+            else { for (int v = 0; v < 5; ++v) F[v] = Real(0); }
+        }
+        else
+        {
+            if (extra == 2) { for (int v = 0; v < 5; ++v) F[v] = t0[v] + (t1[v] + t2[v]); }
+            else if (extra == 1) { for (int v = 0; v < 5; ++v) F[v] = t0[v] + t1[v]; }
+            else { for (int v = 0; v < 5; ++v) F[v] = t0[v]; }
+        }
+    }
+
+    // ------------------------------------------------------------------
+    // the kernel
+    // ------------------------------------------------------------------
+    struct FluxArgs
+    {
+        const double* prims;
+        double* rhs;
+        int increment;
+        int ntile[3];       // tiles per block per direction
+        int use_tma;
+    };
+
+    template <class Cfg, int D>
+    __device__ __forceinline__ void face_pass(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                              typename Cfg::Real* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
+                                              int lb, const int b[3], int i0, int j0, int k0, int shift,
+                                              const typename Cfg::Real inv[3],
+                                              double (&relem)[Cfg::CPT][5], const double invd[3])
+    {
+        using Real = typename Cfg::Real;
+        constexpr int TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ, H = Cfg::H;
+        constexpr int NF = D == 0 ? Cfg::NF0 : (D == 1 ? Cfg::NF1 : Cfg::NF2);
+        constexpr int EX = TX + (D == 0), EY = TY + (D == 1);
+        const int tid = threadIdx.x;
+        const int ny = G.n[1];
+        for (int f = tid; f < NF; f += Cfg::NT)
+        {
+            const int fx = f % EX;
+            const int r = f / EX;
+            const int fy = r % EY;
+            const int fz = r / EY;
+            const int gi = i0 + fx, gj = j0 + fy, gk = k0 + fz;
+            const bool valid = (D == 0 ? gi <= G.n[0] : gi < G.n[0]) &&
+                               (D == 1 ? gj <= G.n[1] : gj < G.n[1]) &&
+                               (D == 2 ? gk <= G.n[2] : gk < G.n[2]);
+            Real F[5] = {Real(0), Real(0), Real(0), Real(0), Real(0)};
+            if (valid)
+            {
+                const int rc = (fz + H)*Cfg::SZ + (fy + H)*Cfg::SY + (fx + H + shift);
+                Real nD = Real(1.0), im = Real(1.0);
+                if constexpr (Cfg::STRETCH)
+                {
+                    if constexpr (D == 1) im = Real(Y.im_face[b[1]*(ny + 1) + gj]);
+                    else
+                    {
+                        nD = Real(Y.m_cell[b[1]*ny + gj]);
+                        im = Real(Y.im_cell[b[1]*ny + gj]);
+                    }
+                }
+                face_flux<Cfg, D>(V, S, rc, nD, inv, im, F);
+            }
+            #pragma unroll
+            for (int v = 0; v < 5; ++v) sF[v*Cfg::NFMAX + f] = F[v];
+        }
+        __syncthreads();
+        #pragma unroll
+        for (int s = 0; s < Cfg::CPT; ++s)
+        {
+            const int c = tid + s*Cfg::NT;
+            if (c >= Cfg::NCELL) break;
+            const int cx = c % TX, cy = (c / TX) % TY, cz = c / (TX*TY);
+            if (i0 + cx >= G.n[0] || j0 + cy >= G.n[1] || k0 + cz >= G.n[2]) continue;
+            int fL, fR;
+            if constexpr (D == 0) { fL = cx + (TX + 1)*(cy + TY*cz); fR = fL + 1; }
+            else if constexpr (D == 1) { fL = cx + TX*(cy + (TY + 1)*cz); fR = fL + TX; }
+            else { fL = cx + TX*(cy + TY*cz); fR = fL + TX*TY; }
+            double jac = 1.0;
+            if constexpr (Cfg::STRETCH) jac = Y.im_cell[b[1]*ny + j0 + cy];
+            const double multL = (jac*1.0)*invd[D];
+            const double multR = (jac*(-1.0))*invd[D];
+            #pragma unroll
+            for (int v = 0; v < 5; ++v)
+            {
+                relem[s][v] += double(sF[v*Cfg::NFMAX + fL])*multL;
+                relem[s][v] += double(sF[v*Cfg::NFMAX + fR])*multR;
+            }
+        }
+        __syncthreads();
+    }
+
+    template <class Cfg>
+    __global__ void __launch_bounds__(Cfg::NT)
+    flux_div_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ GeomK G,
+                    const __grid_constant__ YTabT<Cfg::STRETCH> Y, const __grid_constant__ SchemeK SK, const FluxArgs A)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ, H = Cfg::H;
+        extern __shared__ __align__(128) unsigned char smem_raw[];
+        uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
+        double* stage = reinterpret_cast<double*>(smem_raw + 128);
+        float* soa = reinterpret_cast<float*>(smem_raw + 128 + Cfg::STAGE_BYTES);
+        unsigned char* tail = smem_raw + 128 + Cfg::STAGE_BYTES + Cfg::SOA_BYTES;
+        Real* der = Cfg::REUSE ? reinterpret_cast<Real*>(stage) : reinterpret_cast<Real*>(tail);
+        Real* sF  = Cfg::REUSE ? reinterpret_cast<Real*>(reinterpret_cast<unsigned char*>(stage) + Cfg::DER_BYTES)
+                               : reinterpret_cast<Real*>(tail + Cfg::DER_BYTES);
+
+        const int tid = threadIdx.x;
+        const int lb = blockIdx.y;
+        const int tile = blockIdx.x;
+        const int tx = tile % A.ntile[0];
+        const int ty = (tile / A.ntile[0]) % A.ntile[1];
+        const int tz = tile / (A.ntile[0]*A.ntile[1]);
+        const int i0 = tx*TX, j0 = ty*TY, k0 = tz*TZ;
+        const int b[3] = {lb % G.nb[0], (lb / G.nb[0]) % G.nb[1], lb / (G.nb[0]*G.nb[1])};
+        const int px = i0 - H + G.ng;
+        const int xs = px & ~1;
+        const int shift = px - xs;
+        const int ys = j0 - H + G.ng, zs = k0 - H + G.ng;
+
+        // ---- stage the tile + halo --------------------------------------
+        if (A.use_tma)
+        {
+            if (tid == 0) mbar_init(bar, 1);
+            __syncthreads();
+            if (tid == 0)
+            {
+                mbar_expect_tx(bar, uint32_t(Cfg::BOXN)*5u*8u);
+                tma_load_4d(stage, &tmap, bar, xs*5, ys, zs, lb);
+            }
+            const bool ok = mbar_wait(bar, 0, MBAR_POLL_LIMIT);
+            if (__syncthreads_or(!ok))
+            {
+                if (tid == 0) atomicExch(&g_device_status, DEV_TMA_TIMEOUT);
+                return;
+            }
+        }
+        else
+        {
+            const double* base = A.prims + (long long)lb*G.bstride;
+            const int rowlen = Cfg::BXE*5;
+            for (int e = tid; e < Cfg::BOXN*5; e += Cfg::NT)
+            {
+                const int row = e / rowlen, col = e - row*rowlen;
+                const int yy = row % Cfg::BY, zz = row / Cfg::BY;
+                const int X = xs + col/5, Y_ = ys + yy, Z = zs + zz;
+                double val = 0.0;
+                if (X < G.ni && Y_ < G.nj && Z < G.nk)
+                    val = __ldg(base + ((long long)(Z*G.nj + Y_)*G.ni + xs)*5 + col);
+                stage[e] = val;
+            }
+        }
+        // initial residual (increment mode reads it)
+        double relem[Cfg::CPT][5];
+        #pragma unroll
+        for (int s = 0; s < Cfg::CPT; ++s)
+        {
+            #pragma unroll
+            for (int v = 0; v < 5; ++v) relem[s][v] = 0.0;
+            const int c = tid + s*Cfg::NT;
+            if (A.increment && c < Cfg::NCELL)
+            {
+                const int cx = c % TX, cy = (c / TX) % TY, cz = c / (TX*TY);
+                if (i0 + cx < G.n[0] && j0 + cy < G.n[1] && k0 + cz < G.n[2])
+                {
+                    const double* r = A.rhs + (long long)lb*G.bstride +
+                        ((long long)((k0 + cz + G.ng)*G.nj + (j0 + cy + G.ng))*G.ni + (i0 + cx + G.ng))*5;
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) relem[s][v] = r[v];
+                }
+            }
+        }
+        __syncthreads();
+
+        // ---- FP32: convert the staged box to SoA floats -------------------
+        if constexpr (!Cfg::FP64)
+        {
+            for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
+            {
+                #pragma unroll
+                for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = float(stage[c*5 + v]);
+            }
+            __syncthreads();
+        }
+
+        BoxView<Cfg> V;
+        V.stage = stage;
+        V.soa = soa;
+        V.der = der;
+        SchemeR<Real> S;
+        S.load(SK);
+
+        // ---- per-cell derived values on the stencil cross -------------------
+        if constexpr (Cfg::NDER > 0)
+        {
+            constexpr int HC = Cfg::HC;
+            for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
+            {
+                const int bx = c % Cfg::BXE, by = (c / Cfg::BXE) % Cfg::BY, bz = c / (Cfg::BXE*Cfg::BY);
+                const int rx = bx - shift - H, ry = by - H, rz = bz - H;
+                const bool inx = rx >= 0 && rx < TX, iny = ry >= 0 && ry < TY, inz = rz >= 0 && rz < TZ;
+                const bool need = (iny && inz && rx >= -HC && rx < TX + HC) ||
+                                  (inx && inz && ry >= -HC && ry < TY + HC) ||
+                                  (inx && iny && rz >= -HC && rz < TZ + HC);
+                if (need) derive_cell<Cfg>(V, der, S, c);
+            }
+            __syncthreads();
+        }
+
+        double invd[3];
+        Real inv[3];
+        #pragma unroll
+        for (int d = 0; d < 3; ++d) { invd[d] = G.inv_dx[d][b[d]]; inv[d] = Real(invd[d]); }
+
+        face_pass<Cfg, 0>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
+        face_pass<Cfg, 1>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
+        face_pass<Cfg, 2>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
+
+        // ---- write the residual ------------------------------------------------
+        #pragma unroll
+        for (int s = 0; s < Cfg::CPT; ++s)
+        {
+            const int c = tid + s*Cfg::NT;
+            if (c >= Cfg::NCELL) break;
+            const int cx = c % TX, cy = (c / TX) % TY, cz = c / (TX*TY);
+            if (i0 + cx >= G.n[0] || j0 + cy >= G.n[1] || k0 + cz >= G.n[2]) continue;
+            double* r = A.rhs + (long long)lb*G.bstride +
+                ((long long)((k0 + cz + G.ng)*G.nj + (j0 + cy + G.ng))*G.ni + (i0 + cx + G.ng))*5;
+            #pragma unroll
+            for (int v = 0; v < 5; ++v) r[v] = relem[s][v];
+        }
+        if (A.use_tma && tid == 0) mbar_inval(bar);
+    }
+}

@@ -1,0 +1,182 @@
+// Internal definitions shared by the libgbns.so translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda.h>
+#include <cstdint>
+#include <cstddef>
+#include <string>
+
+#include "gbns.h"
+
+namespace gbns
+{
+    // ------------------------------------------------------------------
+    // limits of the kernel-parameter geometry
+    // ------------------------------------------------------------------
+    constexpr int MAX_BLK_PER_DIM = 64;     // blocks per direction
+    constexpr int MAX_YTAB        = 1024;   // doubles per stretched-metric table
+
+    // ------------------------------------------------------------------
+    // error reporting (per host thread)
+    // ------------------------------------------------------------------
+    int set_error(int code, const std::string& msg);
+    int check_cuda(cudaError_t e, const char* what);
+
+    // Device-side status words: kernels that give up on a bounded wait or
+    // find an inconsistent launch set a nonzero code in their translation
+    // unit's status word and return.  Each TU registers a reader at load.
+    typedef int (*status_reader_fn)(int* status, int reset, cudaStream_t stream);
+    void register_status_reader(status_reader_fn fn);
+    int read_device_status(int* status, int reset, cudaStream_t stream);
+
+    // ------------------------------------------------------------------
+    // geometry passed by value to kernels
+    // ------------------------------------------------------------------
+    struct GeomK
+    {
+        int nb[3];          // blocks per direction
+        int n[3];           // interior cells per block
+        int ng;             // ghost layers
+        int ni, nj, nk;     // padded extents
+        int nblk;           // total blocks
+        long long bstride;  // doubles per block (5*ni*nj*nk)
+        double inv_dx[3][MAX_BLK_PER_DIM];   // 1/dx per direction per block index (grid_geometry.h:91-99)
+    };
+
+    // Stretched-y metric tables, per block row by:
+    //   m_cell[by*ny + j]      dy/deta at interior cell centres
+    //   im_cell[by*ny + j]     1/(dy/deta) at interior cell centres (= Jacobian)
+    //   im_face[by*(ny+1) + j] 1/(dy/deta) at y-faces j = 0..ny
+    struct YTabK
+    {
+        double m_cell[MAX_YTAB];
+        double im_cell[MAX_YTAB];
+        double im_face[MAX_YTAB];
+    };
+    struct YTabNone { };
+
+    // Runtime scheme constants (host-derived with the reference's formulas).
+    struct SchemeK
+    {
+        int diss, visc, law, smooth;
+        double gamma, R, gm1;          // gm1 = gamma - 1.0
+        double spec_heat;              // gamma*R/(gamma - 1.0)        (viscous.h:67)
+        double inv_gamma_avg;          // 1.0/(0.5*(gamma + gamma))    (convective.h:226,233)
+        double R_avg;                  // 0.5*(R + R)                   (convective.h:224)
+        double eps_p, eps_T, sens;     // pressure_diss_lr
+        double mu, beta_c, alpha_c;    // constant law: mu, -2.0*mu/3.0, mu*(1.0/Pr)
+        double T_ref, power, inv_pr, prandtl, tref_plus_s, S;
+        double ck_a[4];                // cent_keep centred coefficients a(1..order/2)
+    };
+
+    // Host helpers ------------------------------------------------------
+    int make_geom(const gbns_grid_desc* g, GeomK& G);
+    int make_ytab(const gbns_grid_desc* g, const GeomK& G, YTabK& Y);
+    int make_scheme(const gbns_scheme_desc* s, SchemeK& S);
+    int scheme_halo(const gbns_scheme_desc* s);
+    double y_deriv(const gbns_grid_desc* g, double eta);
+
+    // Tensor-map creation through the driver entry point (no -lcuda link).
+    int encode_prims_tmap(CUtensorMap* map, const double* base, const GeomK& G,
+                          int box_cells_x, int box_y, int box_z);
+
+    // Launchers (defined in the kernel translation units) -----------------
+    int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
+                        const gbns_scheme_desc* desc, const double* prims, double* rhs,
+                        int increment, cudaStream_t stream, int variant);
+    int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream);
+    int launch_rk_stage(const GeomK& G, double gamma, double R, double* prims,
+                        const double* const* res, const double* coeffs, int nres, cudaStream_t stream);
+    int launch_reduce(const gbns_grid_desc* g, const GeomK& G, double gamma, double R, const double* prims,
+                      int kind, double* partials, int npart, cudaStream_t stream);
+
+    // ------------------------------------------------------------------
+    // device helpers
+    // ------------------------------------------------------------------
+    namespace
+    {
+        __device__ int g_device_status = 0;   // one per translation unit
+
+        int read_tu_status(int* status, int reset, cudaStream_t stream)
+        {
+            int v = 0;
+            cudaError_t e = cudaMemcpyFromSymbolAsync(&v, g_device_status, sizeof(int), 0, cudaMemcpyDeviceToHost, stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+            if (e != cudaSuccess) return check_cuda(e, "read device status");
+            if (v && !*status) *status = v;
+            if (reset && v)
+            {
+                const int zero = 0;
+                e = cudaMemcpyToSymbolAsync(g_device_status, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, stream);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+                if (e != cudaSuccess) return check_cuda(e, "reset device status");
+            }
+            return GBNS_OK;
+        }
+
+        struct status_registrar
+        {
+            status_registrar() { register_status_reader(read_tu_status); }
+        };
+    }
+
+    // Bounded mbarrier wait: returns false if the phase did not complete
+    // within `limit` polls (then the caller flags an error and returns).
+    __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit)
+    {
+        const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+        for (long long it = 0; it < limit; ++it)
+        {
+            uint32_t done;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "selp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+            if (done) return true;
+        }
+        return false;
+    }
+
+    __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+    {
+        const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" :: "r"(addr), "r"(count) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+
+    __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+    {
+        const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" :: "r"(addr), "r"(bytes) : "memory");
+    }
+
+    __device__ __forceinline__ void mbar_inval(uint64_t* bar)
+    {
+        const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" :: "r"(addr) : "memory");
+    }
+
+    // 4-D tiled TMA load global -> shared, completion on `bar`.
+    __device__ __forceinline__ void tma_load_4d(void* smem_dst, const CUtensorMap* map, uint64_t* bar,
+                                                int c0, int c1, int c2, int c3)
+    {
+        const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+        const uint32_t mb  = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+        asm volatile(
+            "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+            " [%0], [%1, {%2, %3, %4, %5}], [%6];"
+            :: "r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(mb)
+            : "memory");
+    }
+
+    constexpr long long MBAR_POLL_LIMIT = 1ll << 24;   // ~tens of ms of polling
+
+    enum device_status_code
+    {
+        DEV_OK = 0,
+        DEV_TMA_TIMEOUT = 1,
+        DEV_BAD_LAUNCH = 2
+    };
+}

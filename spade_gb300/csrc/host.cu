@@ -1,0 +1,401 @@
+// Host side of libgbns.so: descriptor validation and lowering, geometry
+// tables, TMA tensor maps, error reporting and the C-ABI entry points.
+#include <cstdio>
+#include <cstring>
+#include <cmath>
+#include <string>
+#include <mutex>
+#include <vector>
+
+#include "gbns_internal.cuh"
+#include "flux_launch.cuh"
+
+namespace gbns
+{
+    static thread_local std::string t_last_error;
+
+    static std::mutex& readers_mu() { static std::mutex m; return m; }
+    static std::vector<status_reader_fn>& readers() { static std::vector<status_reader_fn> v; return v; }
+
+    void register_status_reader(status_reader_fn fn)
+    {
+        std::lock_guard<std::mutex> lk(readers_mu());
+        readers().push_back(fn);
+    }
+
+    int read_device_status(int* status, int reset, cudaStream_t stream)
+    {
+        *status = 0;
+        std::vector<status_reader_fn> fns;
+        {
+            std::lock_guard<std::mutex> lk(readers_mu());
+            fns = readers();
+        }
+        for (auto fn : fns)
+        {
+            int rc = fn(status, reset, stream);
+            if (rc) return rc;
+        }
+        return GBNS_OK;
+    }
+
+    int set_error(int code, const std::string& msg)
+    {
+        t_last_error = msg;
+        return code;
+    }
+
+    int check_cuda(cudaError_t e, const char* what)
+    {
+        if (e == cudaSuccess) return GBNS_OK;
+        return set_error(GBNS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+
+    // Block geometry exactly as the reference derives it:
+    // cartesian_blocks.h:49 (bsize), :69-70 (box), cartesian_grid.h:134-135
+    // (dx = box.size/n, inv_dx = 1/dx).
+    static void block_dx(const gbns_grid_desc* g, int d, int b, double* bmin, double* dx)
+    {
+        const double bsize = (g->bounds[2*d+1] - g->bounds[2*d]) / g->nblk[d];
+        const double mn = g->bounds[2*d] + b*bsize;
+        const double mx = mn + bsize;
+        *bmin = mn;
+        *dx = (mx - mn) / g->ncell[d];
+    }
+
+    double y_deriv(const gbns_grid_desc* g, double eta)
+    {
+        if (g->coords == GBNS_COORDS_TANH_Y)
+        {
+            const double beta = g->coord_param[0];
+            const double y0 = g->bounds[2], y1 = g->bounds[3];
+            const double s = (2.0*eta - (y0 + y1)) / (y1 - y0);
+            const double th = tanh(beta*s);
+            return beta*(1.0 - th*th)/tanh(beta);
+        }
+        if (g->coords == GBNS_COORDS_INTEGRATED_TANH_Y)
+        {
+            // coords::integrated_tanh_1D::coord_deriv (core/coord_system.h:103-140)
+            const double eta1 = g->coord_param[0], eta0 = g->coord_param[1];
+            const double deta = eta1 - eta0;
+            const double k = g->coord_param[3], strch = g->coord_param[2];
+            const double alpha0 = k/deta, alpha1 = -k/deta;
+            const double beta0 = alpha0*(strch*deta - eta0);
+            const double beta1 = alpha0*(eta1 + strch*deta);
+            auto f = [&](double e) { return log(fabs(cosh(alpha0*e + beta0)))/alpha0 + log(fabs(cosh(alpha1*e + beta1)))/alpha1 - e; };
+            const double f0 = f(eta0);
+            const double normInv = 1.0/(f(eta1) - f0);
+            return (deta*(tanh(alpha0*eta + beta0) + tanh(alpha1*eta + beta1) - 1.0))*normInv;
+        }
+        return 1.0;
+    }
+
+    static int validate_grid(const gbns_grid_desc* g)
+    {
+        if (!g) return set_error(GBNS_ERR_INVALID, "grid descriptor is NULL");
+        for (int d = 0; d < 3; ++d)
+        {
+            if (g->nblk[d] < 1 || g->nblk[d] > MAX_BLK_PER_DIM)
+                return set_error(GBNS_ERR_INVALID, "blocks per direction must be in [1, 64]");
+            if (g->ncell[d] < 1) return set_error(GBNS_ERR_INVALID, "cells per block must be >= 1");
+            if (!(g->bounds[2*d+1] > g->bounds[2*d])) return set_error(GBNS_ERR_INVALID, "domain bounds must satisfy min < max");
+        }
+        if (g->ng < 1 || g->ng > 8) return set_error(GBNS_ERR_INVALID, "ghost layers must be in [1, 8]");
+        if (g->coords < GBNS_COORDS_IDENTITY || g->coords > GBNS_COORDS_INTEGRATED_TANH_Y)
+            return set_error(GBNS_ERR_INVALID, "unknown coordinate system");
+        const double cells = double(g->nblk[0])*g->nblk[1]*g->nblk[2]*
+                             (g->ncell[0] + 2.0*g->ng)*(g->ncell[1] + 2.0*g->ng)*(g->ncell[2] + 2.0*g->ng);
+        if (cells*5 > 9.0e18) return set_error(GBNS_ERR_INVALID, "grid too large");
+        return GBNS_OK;
+    }
+
+    int make_geom(const gbns_grid_desc* g, GeomK& G)
+    {
+        int rc = validate_grid(g);
+        if (rc) return rc;
+        std::memset(&G, 0, sizeof(G));
+        for (int d = 0; d < 3; ++d) { G.nb[d] = g->nblk[d]; G.n[d] = g->ncell[d]; }
+        G.ng = g->ng;
+        G.ni = G.n[0] + 2*G.ng;
+        G.nj = G.n[1] + 2*G.ng;
+        G.nk = G.n[2] + 2*G.ng;
+        G.nblk = G.nb[0]*G.nb[1]*G.nb[2];
+        G.bstride = 5ll*G.ni*G.nj*G.nk;
+        for (int d = 0; d < 3; ++d)
+            for (int b = 0; b < G.nb[d]; ++b)
+            {
+                double mn, dx;
+                block_dx(g, d, b, &mn, &dx);
+                G.inv_dx[d][b] = 1.0/dx;
+            }
+        return GBNS_OK;
+    }
+
+    int make_ytab(const gbns_grid_desc* g, const GeomK& G, YTabK& Y)
+    {
+        const int ny = G.n[1];
+        if (G.nb[1]*(ny + 1) > MAX_YTAB)
+            return set_error(GBNS_ERR_UNSUPPORTED, "stretched-y metric table exceeds 1024 entries (blocks_y*(ny+1))");
+        for (int by = 0; by < G.nb[1]; ++by)
+        {
+            double bmin, dy;
+            block_dx(g, 1, by, &bmin, &dy);
+            for (int j = 0; j < ny; ++j)
+            {
+                const double m = y_deriv(g, bmin + ((double)j + 0.5)*dy);
+                Y.m_cell[by*ny + j] = m;
+                Y.im_cell[by*ny + j] = 1.0/m;
+            }
+            for (int j = 0; j <= ny; ++j)
+                Y.im_face[by*(ny + 1) + j] = 1.0/y_deriv(g, bmin + (double)j*dy);
+        }
+        return GBNS_OK;
+    }
+
+    static double cfd_coeff(int idx, int order)
+    {
+        // centered_finite_diff_t<idx, order>::value (core/finite_diff.h:25-34)
+        const int h = order/2;
+        double fh = 1, fhp = 1, fhm = 1;
+        for (int i = 2; i <= h; ++i) fh *= i;
+        for (int i = 2; i <= h + idx; ++i) fhp *= i;
+        for (int i = 2; i <= h - idx; ++i) fhm *= i;
+        const double d0 = fh/fhp;
+        const double d1 = fh/fhm;
+        const double sgn = ((1 + idx) % 2 == 0) ? 1.0 : -1.0;
+        return d0*d1*sgn/(double)idx;
+    }
+
+    int scheme_halo(const gbns_scheme_desc* s)
+    {
+        int h = 0;
+        if (s->convective == GBNS_CONV_CENT_KEEP) h = s->order/2;
+        else if (s->convective == GBNS_CONV_TOTANI) h = 1;
+        else if (s->convective == GBNS_CONV_FWENO) h = 2;
+        else if (s->convective == GBNS_CONV_WENO5) h = 3;
+        if ((s->dissipation || s->viscous) && h < 1) h = 1;
+        return h;
+    }
+
+    int make_scheme(const gbns_scheme_desc* s, SchemeK& S)
+    {
+        if (!s) return set_error(GBNS_ERR_INVALID, "scheme descriptor is NULL");
+        if (s->convective < GBNS_CONV_NONE || s->convective > GBNS_CONV_WENO5)
+            return set_error(GBNS_ERR_INVALID, "unknown convective scheme");
+        if (s->convective == GBNS_CONV_CENT_KEEP && !(s->order == 2 || s->order == 4 || s->order == 6 || s->order == 8))
+            return set_error(GBNS_ERR_UNSUPPORTED, "cent_keep order must be 2, 4, 6 or 8");
+        if (s->dissipation < 0 || s->dissipation > GBNS_DISS_PRESSURE) return set_error(GBNS_ERR_INVALID, "unknown dissipation");
+        if (s->dissipation && s->sensor != GBNS_SENSOR_CONST) return set_error(GBNS_ERR_UNSUPPORTED, "only const_sensor_t is lowered");
+        if (s->viscous < 0 || s->viscous > GBNS_VISC_LR) return set_error(GBNS_ERR_INVALID, "unknown viscous scheme");
+        if (s->viscous && (s->visc_law < GBNS_LAW_CONSTANT || s->visc_law > GBNS_LAW_SUTHERLAND))
+            return set_error(GBNS_ERR_INVALID, "unknown viscosity law");
+        if (s->precision != GBNS_PREC_FP64 && s->precision != GBNS_PREC_FP32_FLUX && s->precision != GBNS_PREC_FP64_FMA)
+            return set_error(GBNS_ERR_INVALID, "unknown precision");
+        if (!(s->gas.gamma > 1.0) || !(s->gas.R > 0.0)) return set_error(GBNS_ERR_INVALID, "gas requires gamma > 1 and R > 0");
+        if (s->viscous && !(s->prandtl > 0.0)) return set_error(GBNS_ERR_INVALID, "viscous scheme requires prandtl > 0");
+        std::memset(&S, 0, sizeof(S));
+        S.diss = s->dissipation;
+        S.visc = s->viscous;
+        S.law = s->visc_law;
+        S.smooth = s->weno_smooth;
+        const double gam = s->gas.gamma, R = s->gas.R;
+        S.gamma = gam; S.R = R;
+        S.gm1 = gam - 1.0;
+        S.spec_heat = gam*R/(gam - 1.0);
+        S.inv_gamma_avg = 1.0/(0.5*(gam + gam));
+        S.R_avg = 0.5*(R + R);
+        S.eps_p = s->eps_p; S.eps_T = s->eps_T; S.sens = s->sensor_alpha;
+        S.mu = s->mu;
+        S.beta_c = -2.0*s->mu/3.0;
+        S.inv_pr = s->prandtl_inv > 0.0 ? s->prandtl_inv : 1.0/s->prandtl;
+        S.alpha_c = s->mu*S.inv_pr;
+        S.T_ref = s->T_ref; S.power = s->power; S.prandtl = s->prandtl;
+        S.tref_plus_s = s->T_ref + s->S;
+        S.S = s->S;
+        if (s->convective == GBNS_CONV_CENT_KEEP)
+            for (int ii = 1; ii <= s->order/2; ++ii) S.ck_a[ii - 1] = cfd_coeff(ii, s->order);
+        return GBNS_OK;
+    }
+
+    // cuTensorMapEncodeTiled fetched through the runtime's driver entry point.
+    typedef CUresult (*encode_tiled_fn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                        const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                        CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+    static encode_tiled_fn get_encode_fn()
+    {
+        static encode_tiled_fn fn = nullptr;
+        static std::once_flag once;
+        std::call_once(once, []()
+        {
+            void* p = nullptr;
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+                q == cudaDriverEntryPointSuccess)
+                fn = reinterpret_cast<encode_tiled_fn>(p);
+        });
+        return fn;
+    }
+
+    int encode_prims_tmap(CUtensorMap* map, const double* base, const GeomK& G, int box_cells_x, int box_y, int box_z)
+    {
+        encode_tiled_fn fn = get_encode_fn();
+        if (!fn) return set_error(GBNS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        const cuuint64_t dims[4] = {cuuint64_t(G.ni)*5, cuuint64_t(G.nj), cuuint64_t(G.nk), cuuint64_t(G.nblk)};
+        const cuuint64_t strides[3] = {cuuint64_t(G.ni)*5*8, cuuint64_t(G.ni)*G.nj*5*8, cuuint64_t(G.ni)*G.nj*G.nk*5*8};
+        const cuuint32_t box[4] = {cuuint32_t(box_cells_x*5), cuuint32_t(box_y), cuuint32_t(box_z), 1};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<double*>(base), dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return set_error(GBNS_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string(int(r)) + ")");
+        return GBNS_OK;
+    }
+
+    static int validate_bc(const gbns_bc_desc* bc)
+    {
+        if (!bc) return set_error(GBNS_ERR_INVALID, "bc descriptor is NULL");
+        for (int d = 0; d < 3; ++d)
+        {
+            for (int s = 0; s < 2; ++s)
+                if (bc->kind[2*d+s] < GBNS_BC_PERIODIC || bc->kind[2*d+s] > GBNS_BC_SLIP_ADIABATIC)
+                    return set_error(GBNS_ERR_INVALID, "unknown boundary kind");
+            if ((bc->kind[2*d] == GBNS_BC_PERIODIC) != (bc->kind[2*d+1] == GBNS_BC_PERIODIC))
+                return set_error(GBNS_ERR_INVALID, "periodic boundaries must be paired");
+        }
+        return GBNS_OK;
+    }
+}
+
+using namespace gbns;
+
+extern "C"
+{
+    int gbns_version(void) { return GBNS_ABI_VERSION; }
+
+    int gbns_last_error(char* buf, size_t len)
+    {
+        if (!buf || len == 0) return GBNS_ERR_INVALID;
+        std::snprintf(buf, len, "%s", t_last_error.c_str());
+        return GBNS_OK;
+    }
+
+    int gbns_array_size(const gbns_grid_desc* grid, size_t* count)
+    {
+        GeomK G;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        if (!count) return set_error(GBNS_ERR_INVALID, "count is NULL");
+        *count = size_t(G.bstride)*G.nblk;
+        return GBNS_OK;
+    }
+
+    int gbns_flux_div(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                      const double* prims, double* rhs, int increment, void* stream)
+    {
+        GeomK G;
+        SchemeK S;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        rc = make_scheme(scheme, S);
+        if (rc) return rc;
+        if (!prims || !rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
+        if (prims == rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
+        if (scheme_halo(scheme) > G.ng)
+            return set_error(GBNS_ERR_INVALID, "scheme stencil needs " + std::to_string(scheme_halo(scheme)) +
+                             " ghost layers, grid has " + std::to_string(G.ng));
+        YTabK* Y = nullptr;
+        static thread_local YTabK ytab;
+        if (grid->coords != GBNS_COORDS_IDENTITY)
+        {
+            rc = make_ytab(grid, G, ytab);
+            if (rc) return rc;
+            Y = &ytab;
+        }
+        return launch_flux_div(grid, G, Y, S, scheme, prims, rhs, increment, static_cast<cudaStream_t>(stream), 0);
+    }
+
+    int gbns_flux_div_variant(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                              const double* prims, double* rhs, int increment, int variant, void* stream)
+    {
+        GeomK G;
+        SchemeK S;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        rc = make_scheme(scheme, S);
+        if (rc) return rc;
+        if (!prims || !rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
+        if (scheme_halo(scheme) > G.ng) return set_error(GBNS_ERR_INVALID, "scheme stencil needs more ghost layers");
+        YTabK* Y = nullptr;
+        static thread_local YTabK ytab;
+        if (grid->coords != GBNS_COORDS_IDENTITY)
+        {
+            rc = make_ytab(grid, G, ytab);
+            if (rc) return rc;
+            Y = &ytab;
+        }
+        return launch_flux_div(grid, G, Y, S, scheme, prims, rhs, increment, static_cast<cudaStream_t>(stream), variant);
+    }
+
+    int gbns_flux_variant_count(const gbns_scheme_desc* scheme)
+    {
+        return flux_variant_count(scheme);
+    }
+
+    int gbns_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc, double* prims, void* stream)
+    {
+        GeomK G;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        rc = validate_bc(bc);
+        if (rc) return rc;
+        if (!prims) return set_error(GBNS_ERR_INVALID, "prims pointer is NULL");
+        return launch_fill_ghosts(G, bc, prims, static_cast<cudaStream_t>(stream));
+    }
+
+    int gbns_rk_stage(const gbns_grid_desc* grid, const gbns_gas_desc* gas, double* prims,
+                      const double* const* residuals, const double* coeffs, int nres, void* stream)
+    {
+        GeomK G;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        if (!gas || !(gas->gamma > 1.0) || !(gas->R > 0.0)) return set_error(GBNS_ERR_INVALID, "invalid gas");
+        if (nres < 0 || nres > 4) return set_error(GBNS_ERR_INVALID, "nres must be in [0, 4]");
+        if (!prims || (nres > 0 && (!residuals || !coeffs))) return set_error(GBNS_ERR_INVALID, "NULL pointer");
+        for (int j = 0; j < nres; ++j) if (!residuals[j]) return set_error(GBNS_ERR_INVALID, "NULL residual pointer");
+        return launch_rk_stage(G, gas->gamma, gas->R, prims, residuals, coeffs, nres, static_cast<cudaStream_t>(stream));
+    }
+
+    int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                         const gbns_bc_desc* bc, double* prims, double* work, double dt, void* stream)
+    {
+        GeomK G;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        if (!work) return set_error(GBNS_ERR_INVALID, "work pointer is NULL");
+        const size_t n = size_t(G.bstride)*G.nblk;
+        double* R0 = work;
+        double* R1 = work + n;
+        double* R2 = work + 2*n;
+        const double* res[3] = {R0, R1, R2};
+        // ratio_diff_t of consecutive ssprk3_t rows (explicit.h:80-88, advance.h:80-95)
+        const double c1[1] = {(1.0/1.0)*dt};
+        const double c2[2] = {(-3.0/4.0)*dt, (1.0/4.0)*dt};
+        const double c3[3] = {(-1.0/12.0)*dt, (-1.0/12.0)*dt, (2.0/3.0)*dt};
+        if ((rc = gbns_flux_div(grid, scheme, prims, R0, 0, stream))) return rc;
+        if ((rc = gbns_rk_stage(grid, &scheme->gas, prims, res, c1, 1, stream))) return rc;
+        if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
+        if ((rc = gbns_flux_div(grid, scheme, prims, R1, 0, stream))) return rc;
+        if ((rc = gbns_rk_stage(grid, &scheme->gas, prims, res, c2, 2, stream))) return rc;
+        if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
+        if ((rc = gbns_flux_div(grid, scheme, prims, R2, 0, stream))) return rc;
+        if ((rc = gbns_rk_stage(grid, &scheme->gas, prims, res, c3, 3, stream))) return rc;
+        return gbns_fill_ghosts(grid, bc, prims, stream);
+    }
+
+    int gbns_device_status(int* status, int reset, void* stream)
+    {
+        if (!status) return set_error(GBNS_ERR_INVALID, "status is NULL");
+        return read_device_status(status, reset, static_cast<cudaStream_t>(stream));
+    }
+}

@@ -1,0 +1,171 @@
+"""Block-structured grid and the AoS5 grid_array (grid/cartesian_blocks.h,
+grid/cartesian_grid.h, grid/grid_array.h, core/mem_map.h:465-497).
+
+A grid_array owns one torch float64 tensor on the GPU of shape
+(nblocks, nz+2ng, ny+2ng, nx+2ng, 5), which is byte-for-byte SPADE's
+linear_t<5> map: variables fastest, then i, j, k, block.  torch is used only
+for device memory and streams.
+"""
+import numpy as np
+import torch
+
+from . import _abi, _native
+from . import coords as _coords
+
+
+class cartesian_blocks_t:
+    """grid::cartesian_blocks_t(num_blocks, bounds) (cartesian_blocks.h:23-117).
+    `bounds` = (xmin, xmax, ymin, ymax, zmin, zmax)."""
+
+    def __init__(self, num_blocks, bounds):
+        self.num_blocks = tuple(int(n) for n in num_blocks)
+        if len(self.num_blocks) != 3:
+            raise ValueError("num_blocks must have 3 entries")
+        self.bounds = tuple(float(b) for b in bounds)
+        if len(self.bounds) != 6:
+            raise ValueError("bounds must be (xmin, xmax, ymin, ymax, zmin, zmax)")
+
+    def total_num_blocks(self):
+        n = self.num_blocks
+        return n[0] * n[1] * n[2]
+
+
+class cartesian_grid_t:
+    """grid::cartesian_grid_t(cells_in_block, blocks, coords) (cartesian_grid.h:48-384)."""
+
+    def __init__(self, cells_in_block, blocks, coord_sys=None):
+        self.cells = tuple(int(n) for n in cells_in_block)
+        self.blocks = blocks
+        self.coord_sys = coord_sys if coord_sys is not None else _coords.identity()
+
+    def get_num_cells(self, i=None):
+        return self.cells if i is None else self.cells[i]
+
+    def get_num_global_blocks(self):
+        return self.blocks.total_num_blocks()
+
+    get_num_local_blocks = get_num_global_blocks
+
+    def get_grid_size(self):
+        c = self.cells
+        return c[0] * c[1] * c[2] * self.get_num_global_blocks()
+
+    def desc(self, ng):
+        return _abi.grid_desc(self.blocks.num_blocks, self.cells, ng, self.blocks.bounds,
+                              self.coord_sys.kind, self.coord_sys.params)
+
+    def get_dx(self, i, lb=0):
+        """Block spacing exactly as the reference computes it."""
+        nb = self.blocks.num_blocks[i]
+        b = [lb % self.blocks.num_blocks[0], (lb // self.blocks.num_blocks[0]) % self.blocks.num_blocks[1],
+             lb // (self.blocks.num_blocks[0] * self.blocks.num_blocks[1])][i]
+        lo, hi = self.blocks.bounds[2 * i], self.blocks.bounds[2 * i + 1]
+        bsize = (hi - lo) / nb
+        mn = lo + b * bsize
+        return ((mn + bsize) - mn) / self.cells[i]
+
+
+class grid_array:
+    """grid::grid_array(grid, fill, num_exch, device) (grid_array.h:175-422)."""
+
+    def __init__(self, grid, fill=0.0, num_exch=2, device="cuda", data=None):
+        self.grid = grid
+        ng = num_exch if np.isscalar(num_exch) else num_exch[0]
+        if not np.isscalar(num_exch) and len(set(num_exch)) != 1:
+            raise ValueError("the GB300 path uses the same ghost depth in every direction")
+        self.ng = int(ng)
+        c = grid.cells
+        self.shape = (grid.get_num_global_blocks(), c[2] + 2 * self.ng, c[1] + 2 * self.ng, c[0] + 2 * self.ng, 5)
+        if data is not None:
+            if tuple(data.shape) != self.shape or data.dtype != torch.float64:
+                raise ValueError("data must be float64 with shape %s" % (self.shape,))
+            self.data = data
+        else:
+            self.data = torch.empty(self.shape, dtype=torch.float64, device=device)
+            self.fill_(fill)
+        self._desc = grid.desc(self.ng)
+        self.periodic = None
+
+    def fill_(self, fill):
+        if np.isscalar(fill):
+            self.data.fill_(float(fill))
+        else:
+            self.data.copy_(torch.as_tensor(np.asarray(fill, dtype=np.float64), device=self.data.device).expand(self.shape))
+        return self
+
+    def desc(self):
+        return self._desc
+
+    def ptr(self):
+        return self.data.data_ptr()
+
+    def interior(self):
+        g = self.ng
+        return self.data[:, g:-g, g:-g, g:-g, :]
+
+    def numpy(self):
+        return self.data.detach().cpu().numpy()
+
+    def copy_from_numpy(self, arr):
+        self.data.copy_(torch.from_numpy(np.ascontiguousarray(arr, dtype=np.float64)))
+        return self
+
+    def device(self):
+        return self.data.device
+
+    def __iadd__(self, other):
+        self.data += other.data if isinstance(other, grid_array) else other
+        return self
+
+    def assign(self, value):
+        """rhs = value (grid_array::operator=, grid_array.h:383-392)."""
+        if isinstance(value, grid_array):
+            self.data.copy_(value.data)
+        else:
+            self.data.fill_(float(value))
+        return self
+
+
+def _stream(stream):
+    if stream is None:
+        return ctypes_stream(torch.cuda.current_stream())
+    if isinstance(stream, int):
+        return stream
+    return ctypes_stream(stream)
+
+
+def ctypes_stream(s):
+    return int(s.cuda_stream)
+
+
+class arr_exchange_t:
+    """Handle returned by make_exchange (make_exchange.h:98-421).
+    exchange(q) fills every ghost that has a donor block (periodic wrap where
+    periodic[d]); ghosts across non-periodic faces are left for boundary_fill."""
+
+    def __init__(self, periodic):
+        self.periodic = tuple(bool(p) for p in periodic)
+
+    def bc_desc(self, walls=None):
+        kinds = []
+        t_wall = []
+        for d in range(3):
+            for s in range(2):
+                face = 2 * d + s
+                if walls and face in walls:
+                    kinds.append(walls[face].kind)
+                    t_wall.append(walls[face].t_wall)
+                else:
+                    kinds.append(_abi.BC_PERIODIC if self.periodic[d] else _abi.BC_NONE)
+                    t_wall.append(0.0)
+        return _abi.bc_desc(kinds, t_wall)
+
+    def exchange(self, q, group=None, stream=None):
+        bc = self.bc_desc()
+        _native.check(_native.lib().gbns_fill_ghosts(q.desc(), bc, q.ptr(), _stream(stream)))
+
+
+def make_exchange(q, periodic):
+    h = arr_exchange_t(periodic)
+    q.periodic = h.periodic
+    return h

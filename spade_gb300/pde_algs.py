@@ -1,0 +1,112 @@
+"""pde_algs::flux_div and its traits (pde-algs/flux-div/flux_div.h:16-56,
+pde-algs/pde_traits.h:5-20, pde-algs/flux-div/tags.h:5-33), lowered onto
+libgbns.so."""
+from . import _abi, _native, convective, viscous, omni
+from .grid import _stream
+
+
+class _trait:
+    def __init__(self, label, name, **kw):
+        self.trait_label = label
+        self.name = name
+        self.__dict__.update(kw)
+
+    def __repr__(self):
+        return "pde_algs.%s" % self.name
+
+
+# pde_increment trait (pde_traits.h:13-20)
+overwrite = _trait("pde_increment", "overwrite", increment_mode=False)
+increment = _trait("pde_increment", "increment", increment_mode=True)
+# flux_div algorithm tag: the GB300 fused tile kernel
+gb300 = _trait("flux_div", "gb300")
+basic = gb300   # the reference's default tag maps to the same kernel here
+# flux arithmetic precision
+fp64 = _trait("flux_precision", "fp64", precision=_abi.PREC_FP64)
+fp32_flux = _trait("flux_precision", "fp32_flux", precision=_abi.PREC_FP32_FLUX)
+fp64_fma = _trait("flux_precision", "fp64_fma", precision=_abi.PREC_FP64_FMA)
+
+
+def lower(flux_func, precision=_abi.PREC_FP64):
+    """Lowers a flux functor (or omni.compose of functors) to the C ABI's
+    gbns_scheme_desc.  Raises for anything the GB300 kernels do not
+    implement (there is no CPU fallback)."""
+    kernels = flux_func.kernels if isinstance(flux_func, omni.composite_kernel_t) else (flux_func,)
+    s = _abi.SchemeDesc()
+    s.order = 2
+    s.weno_smooth = 1
+    s.precision = int(precision)
+    s.prandtl = 1.0
+    s.T_ref = 1.0
+    gas = None
+    order = []   # canonical order: convective, dissipation, viscous
+    for k in kernels:
+        if isinstance(k, (convective.cent_keep_scheme_t, convective.totani_lr, convective.fweno_t, convective.weno5_t)):
+            if s.convective != _abi.CONV_NONE:
+                raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "at most one convective functor per composite")
+            s.convective = k.kind
+            s.order = k.order
+            s.weno_smooth = getattr(k, "smooth", 1)
+            order.append(0)
+        elif isinstance(k, convective.pressure_diss_lr):
+            if s.dissipation:
+                raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "at most one pressure_diss_lr per composite")
+            s.dissipation = _abi.DISS_PRESSURE
+            s.sensor = k.sensor.kind
+            s.sensor_alpha = k.sensor.alpha
+            s.eps_p = k.eps_p
+            s.eps_T = k.eps_T
+            order.append(1)
+        elif isinstance(k, viscous.visc_lr):
+            if s.viscous:
+                raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "at most one visc_lr per composite")
+            s.viscous = _abi.VISC_LR
+            law = k.vlaw
+            s.visc_law = law.law
+            s.mu = law.mu
+            s.prandtl = law.prandtl
+            s.T_ref = law.T_ref
+            s.power = law.power
+            s.S = law.S
+            order.append(2)
+        else:
+            raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "flux functor %r cannot be lowered to the GB300 kernels" % (k,))
+        g = k.gas
+        if gas is not None and (g.gamma != gas.gamma or g.R != gas.R):
+            raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "all functors of a composite must share one gas")
+        gas = g
+    # compose(a, b, c) = a + (b + c); a two-term sum commutes exactly, a
+    # three-term sum is lowered only in the canonical order.
+    if len(order) == 3 and order != [0, 1, 2]:
+        raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "three-term composites must be compose(convective, dissipation, viscous)")
+    s.gas.gamma = gas.gamma
+    s.gas.R = gas.R
+    return s
+
+
+def flux_div(prims, rhs, flux_func, traits=None, stream=None, variant=0):
+    """rhs (+)= div F(prims): pde_algs::flux_div(prims, rhs, flux_func[, traits]).
+    Default increment mode like the reference; pass
+    make_traits(pde_algs.overwrite) to overwrite.  Asynchronous on the
+    current torch stream."""
+    traits = traits or ()
+    inc = True
+    prec = _abi.PREC_FP64
+    for t in traits:
+        lab = getattr(t, "trait_label", None)
+        if lab == "pde_increment":
+            inc = t.increment_mode
+        elif lab == "flux_precision":
+            prec = t.precision
+        elif lab == "flux_div":
+            pass
+        else:
+            raise ValueError("unknown trait %r" % (t,))
+    if prims.shape != rhs.shape or prims.grid is not rhs.grid and prims.shape != rhs.shape:
+        raise ValueError("prims and rhs must live on the same grid")
+    scheme = flux_func if isinstance(flux_func, _abi.SchemeDesc) else lower(flux_func, prec)
+    if variant:
+        rc = _native.lib().gbns_flux_div_variant(prims.desc(), scheme, prims.ptr(), rhs.ptr(), int(inc), int(variant), _stream(stream))
+    else:
+        rc = _native.lib().gbns_flux_div(prims.desc(), scheme, prims.ptr(), rhs.ptr(), int(inc), _stream(stream))
+    _native.check(rc)

@@ -1,0 +1,167 @@
+"""Explicit Runge–Kutta integration (time-integration/explicit.h,
+integrator.h, advance.h).
+
+`integrator_t` mirrors the reference's driver structure: the user supplies
+calc_rhs(rhs, q, t) and bc(q, t); the state is kept primitive and every stage
+update runs in conservative variables through the fused native RK-stage
+kernel (integrate_advance with state_transform_t, advance.h:234-280).
+`ssprk3_stepper` is the fused native SSPRK3 step (one C-ABI call per step,
+optionally replayed from a captured CUDA graph).
+"""
+import ctypes
+from fractions import Fraction as F
+
+import torch
+
+from . import _abi, _native
+from .grid import grid_array, _stream
+
+
+class rk_t:
+    """Butcher table (A, b, c) as exact fractions (explicit.h:25-35)."""
+
+    def __init__(self, A, b, c):
+        self.A = [[F(x) for x in row] for row in A]
+        self.b = [F(x) for x in b]
+        self.c = [F(x) for x in c]
+        self.stages = len(self.b)
+
+    def diff_coeffs(self, prev, curr):
+        """ratio_diff_t of two rows (advance.h:48-54, 85-95): the nonzero
+        (index, value) pairs of curr - prev, value = num/den in FP64."""
+        out = []
+        for j in range(len(curr)):
+            d = curr[j] - prev[j]
+            if d != 0:
+                out.append((j, float(d.numerator) / float(d.denominator)))
+        return out
+
+
+# explicit.h:36-116
+rk2_t = rk_t([[0, 0], [F(1, 2), 0]], [0, 1], [0, F(1, 2)])
+rk4_t = rk_t([[0, 0, 0, 0], [F(1, 2), 0, 0, 0], [0, F(1, 2), 0, 0], [0, 0, 1, 0]],
+             [F(1, 6), F(1, 3), F(1, 3), F(1, 6)], [0, F(1, 2), F(1, 2), 1])
+ssprk34_t = rk_t([[0, 0, 0, 0], [F(1, 2), 0, 0, 0], [F(1, 2), F(1, 2), 0, 0], [F(1, 6), F(1, 6), F(1, 6), 0]],
+                 [F(1, 6), F(1, 6), F(1, 6), F(1, 2)], [0, F(1, 2), 1, F(1, 2)])
+ssprk3_t = rk_t([[0, 0, 0], [1, 0, 0], [F(1, 4), F(1, 4), 0]],
+                [F(1, 6), F(1, 6), F(2, 3)], [0, 1, F(1, 2)])
+rk38r_t = rk_t([[0, 0, 0, 0], [F(1, 3), 0, 0, 0], [F(-1, 3), 1, 0, 0], [1, -1, 1, 0]],
+               [F(1, 8), F(3, 8), F(3, 8), F(1, 8)], [0, F(1, 3), F(2, 3), 1])
+
+
+class time_axis_t:
+    """time_integration::time_axis_t(t0, dt)."""
+
+    def __init__(self, t0, dt):
+        self.t = float(t0)
+        self.dt = float(dt)
+
+    def time(self):
+        return self.t
+
+    def timestep(self):
+        return self.dt
+
+
+class integrator_data_t:
+    """time_integration::integrator_data_t(q, rhs, scheme): the solution and
+    one residual array per stage."""
+
+    def __init__(self, q, rhs, scheme):
+        self.q = q
+        self.residuals = [rhs] + [grid_array(rhs.grid, 0.0, rhs.ng) for _ in range(scheme.stages - 1)]
+
+    def solution(self):
+        return self.q
+
+    def residual(self, i):
+        return self.residuals[i]
+
+
+def rk_stage(q, gas, residuals, coeffs, stream=None):
+    """One fused stage update q <- prim(cons(q) + sum_j coeffs[j] R_j)."""
+    n = len(residuals)
+    ptrs = (ctypes.c_void_p * max(n, 1))(*[r.ptr() for r in residuals])
+    cf = (ctypes.c_double * max(n, 1))(*coeffs)
+    _native.check(_native.lib().gbns_rk_stage(q.desc(), gas.desc(), q.ptr(), ptrs, cf, n, _stream(stream)))
+
+
+class integrator_t:
+    """time_integration::integrator_t(axis, scheme, data, calc_rhs, bc, trans)
+    (integrator.h:18-59); advance() follows integrate_advance with the
+    state transform (advance.h:234-280)."""
+
+    def __init__(self, axis, scheme, data, calc_rhs, bc, trans):
+        self.axis = axis
+        self.scheme = scheme
+        self.data = data
+        self.calc_rhs = calc_rhs
+        self.bc = bc
+        self.trans = trans
+
+    def solution(self):
+        return self.data.q
+
+    def time(self):
+        return self.axis.t
+
+    def advance(self):
+        sch = self.scheme
+        q = self.data.q
+        dt = self.axis.dt
+        gas = self.trans.gas
+        t0 = self.axis.t
+        self.calc_rhs(self.data.residual(0), q, t0 + float(sch.c[0]) * dt)
+        for i in range(1, sch.stages):
+            pairs = sch.diff_coeffs(sch.A[i - 1], sch.A[i])
+            rk_stage(q, gas, [self.data.residual(j) for j, _ in pairs], [v * dt for _, v in pairs])
+            ti = t0 + float(sch.c[i]) * dt
+            self.bc(q, ti)
+            self.calc_rhs(self.data.residual(i), q, ti)
+        pairs = sch.diff_coeffs(sch.A[sch.stages - 1], sch.b)
+        rk_stage(q, gas, [self.data.residual(j) for j, _ in pairs], [v * dt for _, v in pairs])
+        self.axis.t = t0 + dt
+        self.bc(q, self.axis.t)
+
+
+class ssprk3_stepper:
+    """Fused native SSPRK3 step of `q` (gbns_ssprk3_step): three flux_div
+    launches, three fused stage updates and three ghost fills per step with
+    the reference's arithmetic.  With use_graph=True the first call captures
+    the nine launches of one step in a CUDA graph on a side stream and later
+    calls replay it (dt is fixed at capture)."""
+
+    def __init__(self, q, scheme_desc, bc_desc, dt, use_graph=False):
+        self.q = q
+        self.scheme = scheme_desc
+        self.bc = bc_desc
+        self.dt = float(dt)
+        n = 1
+        for s in q.shape:
+            n *= s
+        self.work = torch.zeros(3 * n, dtype=torch.float64, device=q.data.device)
+        self.use_graph = use_graph
+        self.graph = None
+
+    def _launch(self, stream):
+        _native.check(_native.lib().gbns_ssprk3_step(self.q.desc(), self.scheme, self.bc, self.q.ptr(),
+                                                     self.work.data_ptr(), ctypes.c_double(self.dt), stream))
+
+    def step(self, nsteps=1):
+        if not self.use_graph:
+            st = _stream(None)
+            for _ in range(nsteps):
+                self._launch(st)
+            return
+        if self.graph is None:
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side):
+                    self._launch(int(side.cuda_stream))
+            torch.cuda.current_stream().wait_stream(side)
+            self.graph = g
+            # capture does not execute; run the first step by replay
+        for _ in range(nsteps):
+            self.graph.replay()

@@ -1,0 +1,61 @@
+// Host-only check of include/spade_gb300.h against the reference's headers:
+// the gb300 trait must select the drop-in flux_div overload, which lowers the
+// composed functor and the grid_array into the C-ABI descriptors.  The GPU
+// call is replaced by a hook (GBNS_DROPIN_HOOK) that prints the descriptors.
+#include <cstdio>
+#include "gbns.h"
+
+static int g_calls = 0;
+static int record(const gbns_grid_desc* g, const gbns_scheme_desc* s, const double* q, double* r, int incr)
+{
+    ++g_calls;
+    std::printf("grid %d %d %d %d %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g\n",
+                g->nblk[0], g->nblk[1], g->nblk[2], g->ncell[0], g->ncell[1], g->ncell[2], g->ng,
+                g->bounds[0], g->bounds[1], g->bounds[2], g->bounds[3], g->bounds[4], g->bounds[5]);
+    std::printf("scheme %d %d %d %d %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g incr %d ptrs %d\n",
+                s->convective, s->order, s->weno_smooth, s->dissipation, s->viscous, s->visc_law, s->precision,
+                s->eps_p, s->eps_T, s->sensor_alpha, s->mu, s->prandtl_inv, s->gas.gamma, s->gas.R, s->T_ref,
+                incr, int(q != nullptr && r != nullptr));
+    return 0;
+}
+#define GBNS_DROPIN_HOOK record
+
+#include "spade.h"
+#include "spade_gb300.h"
+
+int main(int argc, char** argv)
+{
+    using real_t = double;
+    spade::parallel::compute_env_t env(&argc, &argv, {0});
+    env.exec([&](spade::parallel::pool_t& group)
+    {
+        spade::ctrs::array<int, 3> num_blocks(2, 3, 1);
+        spade::ctrs::array<int, 3> cells(8, 6, 4);
+        spade::bound_box_t<real_t, 3> bounds;
+        bounds.min(0) = 0.0; bounds.max(0) = 2.0;
+        bounds.min(1) = -1.0; bounds.max(1) = 1.0;
+        bounds.min(2) = 0.0; bounds.max(2) = 0.5;
+        spade::coords::identity<real_t> coords;
+        spade::grid::cartesian_blocks_t blocks(num_blocks, bounds);
+        spade::grid::cartesian_grid_t grid(cells, blocks, coords, group);
+        spade::ctrs::array<int, 3> nexch(3, 3, 3);
+        spade::grid::grid_array q  (grid, spade::fluid_state::prim_t<real_t>(0.0), nexch, spade::device::cpu);
+        spade::grid::grid_array rhs(grid, spade::fluid_state::flux_t<real_t>(0.0), nexch, spade::device::cpu);
+        spade::fluid_state::ideal_gas_t<real_t> air(1.4, 287.0);
+        spade::viscous_laws::constant_viscosity_t<real_t> law(1.5e-5, 0.72);
+        spade::viscous::visc_lr visc(law, air);
+        spade::state_sensor::const_sensor_t<real_t> sens(0.25);
+        spade::convective::pressure_diss_lr diss(air, sens, 0.1, 0.2);
+        // 1: the C1 composite, default (increment) mode
+        spade::pde_algs::flux_div(q, rhs, spade::omni::compose(spade::convective::cent_keep<2>(air), visc),
+                                  spade::algs::make_traits(spade::pde_algs::gb300));
+        // 2: the channel composite, overwrite mode, FP32 flux
+        spade::pde_algs::flux_div(q, rhs, spade::omni::compose(spade::convective::fweno_t<decltype(air)>(air), diss, visc),
+                                  spade::algs::make_traits(spade::pde_algs::gb300, spade::pde_algs::overwrite, spade::gb300::fp32_flux));
+        // 3: a single functor
+        spade::pde_algs::flux_div(q, rhs, spade::convective::totani_lr(air),
+                                  spade::algs::make_traits(spade::pde_algs::gb300, spade::pde_algs::overwrite));
+    });
+    std::printf("calls %d\n", g_calls);
+    return g_calls == 3 ? 0 : 1;
+}

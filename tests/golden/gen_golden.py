@@ -1,0 +1,155 @@
+"""Generates the golden fixtures in tests/golden/ from the REFERENCE's own CPU
+path (oracle/_ref/libspade_ref.so, built by `make -C oracle ref` where the
+reference sources exist).  Run from the repository root:
+
+    python tests/golden/gen_golden.py
+
+Fixtures hold inputs (or the 1-D tables and seeds that rebuild them
+bit-exactly, tests/problems.py) and the reference's outputs.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+from spade_gb300 import _abi  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+import problems as P  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+# (reference harness scheme id, scheme kwargs for tests/problems.scheme)
+FLUX_CASES = {
+    "ck2_visc": (O.REF_CK2_VISC, dict(conv=_abi.CONV_CENT_KEEP, order=2, visc=1)),
+    "totani_visc": (O.REF_TOTANI_VISC, dict(conv=_abi.CONV_TOTANI, visc=1)),
+    "ck4_visc": (O.REF_CK4_VISC, dict(conv=_abi.CONV_CENT_KEEP, order=4, visc=1)),
+    "ck2": (O.REF_CK2, dict(conv=_abi.CONV_CENT_KEEP, order=2)),
+    "visc": (O.REF_VISC, dict(conv=_abi.CONV_NONE, visc=1)),
+    "fweno_diss_visc": (O.REF_FWENO_DISS_VISC, dict(conv=_abi.CONV_FWENO, diss=1, visc=1)),
+    "fweno": (O.REF_FWENO, dict(conv=_abi.CONV_FWENO)),
+    "diss": (O.REF_DISS, dict(conv=_abi.CONV_NONE, diss=1)),
+    "totani": (O.REF_TOTANI, dict(conv=_abi.CONV_TOTANI)),
+    "ck6": (O.REF_CK6, dict(conv=_abi.CONV_CENT_KEEP, order=6)),
+    "ck8": (O.REF_CK8, dict(conv=_abi.CONV_CENT_KEEP, order=8)),
+    "fweno_nosmooth": (O.REF_FWENO_NOSMOOTH, dict(conv=_abi.CONV_FWENO, smooth=0)),
+    "ck2_diss_visc": (O.REF_CK2_DISS_VISC, dict(conv=_abi.CONV_CENT_KEEP, order=2, diss=1, visc=1)),
+}
+
+FLUX_GRID = dict(nblk=(2, 1, 1), ncell=(6, 5, 4), ng=4, bounds=(0.0, 1.3, 0.0, 0.9, 0.0, 0.7))
+GHOST_GRID = dict(nblk=(2, 3, 2), ncell=(4, 3, 5), ng=2, bounds=(0.0, 1.0, -1.0, 1.0, 0.0, 2.0))
+
+
+def interior(a, ng):
+    return a[:, ng:-ng, ng:-ng, ng:-ng, :]
+
+
+def gen_flux():
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    q = P.random_state(fg["nblk"], fg["ncell"], fg["ng"], seed=11)
+    out = {"q": q}
+    for name, (rid, kw) in FLUX_CASES.items():
+        s = P.scheme(**kw)
+        r = np.zeros_like(q)
+        O.ref_flux_div(rid, grid, s, q, r, increment=False)
+        out["rhs_" + name] = interior(r, fg["ng"]).copy()
+    # increment mode on a nonzero residual
+    r0 = P.random_state(fg["nblk"], fg["ncell"], fg["ng"], seed=12, p0=1.0, T0=1.0, u0=1.0)
+    r = r0.copy()
+    O.ref_flux_div(O.REF_CK2_VISC, grid, P.scheme(conv=_abi.CONV_CENT_KEEP, order=2, visc=1), q, r, increment=True)
+    out["rhs0_increment"] = r0
+    out["rhs_increment_ck2_visc"] = interior(r, fg["ng"]).copy()
+    np.savez_compressed(os.path.join(OUT, "flux_div_ref.npz"), **out)
+
+
+def gen_ghosts():
+    gg = GHOST_GRID
+    grid = _abi.grid_desc(gg["nblk"], gg["ncell"], gg["ng"], gg["bounds"])
+    q = P.random_state(gg["nblk"], gg["ncell"], gg["ng"], seed=21)
+    s = P.scheme()
+    a = q.copy()
+    O.ref_fill_ghosts(grid, s, P.periodic_bc(), a)
+    b = q.copy()
+    O.ref_fill_ghosts(grid, s, P.channel_bc(290.0), b)
+    np.savez_compressed(os.path.join(OUT, "ghosts_ref.npz"), q=q, periodic=a, walls=b)
+
+
+def gen_tgv():
+    # C1: 2x2x2 blocks of 16^3, ng = 2, cent_keep<2> + visc_lr(constant), 20 SSPRK3 steps
+    nblk, ncell, ng = (2, 2, 2), (16, 16, 16), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    tables = P.tgv_tables(nblk, ncell, ng)
+    q = P.tgv_state(nblk, ncell, ng, tables, seed=0)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    dt = P.tgv_dt(q, grid, ng)
+    s = P.tgv_scheme()
+    r = np.zeros_like(q)
+    O.ref_flux_div(O.REF_CK2_VISC, grid, s, q, r, increment=False)
+    rin = interior(r, ng)
+    qf = q.copy()
+    ke = O.ref_ssprk3(O.REF_CK2_VISC, grid, s, P.periodic_bc(), qf, dt, 20)
+    qi = interior(qf, ng)
+    np.savez_compressed(os.path.join(OUT, "tgv_ref.npz"), dt=dt, ke=ke,
+                        rhs_sum=rin.reshape(-1, 5).sum(axis=0), rhs_abs=np.abs(rin).reshape(-1, 5).sum(axis=0),
+                        rhs_probe=rin[:, ::5, ::5, ::5, :].copy(),
+                        q_sum=qi.reshape(-1, 5).sum(axis=0), q_probe=qi[:, ::3, ::3, ::3, :].copy(),
+                        **{"tab_" + k: v for k, v in tables.items()})
+    # a smaller TGV whose whole final state is stored
+    nblk, ncell, ng = (2, 2, 2), (8, 8, 8), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    tables = P.tgv_tables(nblk, ncell, ng)
+    q = P.tgv_state(nblk, ncell, ng, tables, seed=3)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    dt = P.tgv_dt(q, grid, ng)
+    qf = q.copy()
+    ke = O.ref_ssprk3(O.REF_CK2_VISC, grid, s, P.periodic_bc(), qf, dt, 10)
+    np.savez_compressed(os.path.join(OUT, "tgv_small_ref.npz"), dt=dt, ke=ke, q_final=interior(qf, ng).copy(),
+                        **{"tab_" + k: v for k, v in tables.items()})
+
+
+def gen_channel():
+    # uniform-grid channel subset the reference can run: fweno_t +
+    # pressure_diss_lr(const_sensor) + visc_lr(constant), isothermal walls
+    nblk, ncell, ng = (2, 2, 2), (8, 8, 8), 3
+    bounds = (0.0, 4 * math.pi, -1.0, 1.0, 0.0, 4 * math.pi / 3)
+    grid = _abi.grid_desc(nblk, ncell, ng, bounds)
+    c_w = math.sqrt(P.GAMMA * P.RGAS * 300.0)
+    U_b = 0.5 * c_w
+    y = P.cell_centres(nblk, ncell, ng, bounds, 1)[:, None, :, None]
+    q = np.empty(P.padded_shape(nblk, ncell, ng))
+    q[..., 0] = P.RGAS * 300.0
+    q[..., 1] = 300.0
+    q[..., 2] = 1.5 * U_b * (1.0 - y * y)
+    q[..., 3] = 0.0
+    q[..., 4] = 0.0
+    r = np.random.Generator(np.random.PCG64(5))
+    inner = q[:, ng:-ng, ng:-ng, ng:-ng, 2:5]
+    inner += r.standard_normal(inner.shape) * (0.05 * U_b)
+    bc = P.channel_bc(300.0)
+    O.fill_ghosts(grid, bc, q)
+    s = P.scheme(conv=_abi.CONV_FWENO, diss=1, visc=1, mu=U_b / 3000.0, eps_p=0.01 * c_w, eps_T=0.01 * c_w, alpha=1.0)
+    a = q[:, ng:-ng, ng:-ng, ng:-ng, :]
+    amax = float((np.sqrt(P.GAMMA * P.RGAS * a[..., 1]) + np.sqrt((a[..., 2:] ** 2).sum(-1))).max())
+    dt = 0.5 * min(4 * math.pi / 16, 2.0 / 16, (4 * math.pi / 3) / 16) / amax
+    qf = q.copy()
+    ke = O.ref_ssprk3(O.REF_FWENO_DISS_VISC, grid, s, bc, qf, dt, 5)
+    assert np.all(np.isfinite(qf)) and np.all(np.isfinite(ke))
+    np.savez_compressed(os.path.join(OUT, "channel_ref.npz"), q0=q, dt=dt, ke=ke, q_final=interior(qf, ng).copy(),
+                        mu=U_b / 3000.0, eps=0.01 * c_w)
+
+
+if __name__ == "__main__":
+    if not O.ref_available():
+        sys.exit("reference harness not built: make -C oracle ref")
+    gen_flux()
+    gen_ghosts()
+    gen_tgv()
+    gen_channel()
+    for f in sorted(os.listdir(OUT)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(OUT, f)))

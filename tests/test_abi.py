@@ -1,0 +1,150 @@
+"""C-ABI checks that need no GPU: libgbns.so loads, exports every entry point
+include/*.h declares, the ctypes descriptor layouts match the C structs, and
+descriptor validation fails loudly before any CUDA call."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+from spade_gb300 import _abi, _native, pde_algs, convective, viscous, viscous_laws, omni, fluid_state, state_sensor
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(INCLUDE):
+        if f.endswith(".h"):
+            src = open(os.path.join(INCLUDE, f)).read()
+            names |= set(re.findall(r"^\s*int\s+(gbns_\w+)\s*\(", src, re.M))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ctypes.CDLL(_native.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 8
+    for name in syms:
+        assert hasattr(lib, name), name
+
+
+def test_library_version_without_gpu():
+    assert _native.lib().gbns_version() == _abi.ABI_VERSION
+
+
+def test_struct_layouts_match_c():
+    src = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "gbns.h"
+int main(void){
+  printf("%zu %zu %zu %zu\n", sizeof(gbns_grid_desc), sizeof(gbns_scheme_desc), sizeof(gbns_bc_desc), sizeof(gbns_gas_desc));
+  printf("%zu %zu %zu\n", offsetof(gbns_grid_desc, bounds), offsetof(gbns_scheme_desc, eps_p), offsetof(gbns_scheme_desc, gas));
+  printf("%zu\n", offsetof(gbns_bc_desc, t_wall));
+  return 0;}
+"""
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(c, "w").write(src)
+        subprocess.run(["gcc", "-I" + INCLUDE, c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    got = [int(x) for x in out]
+    want = [ctypes.sizeof(_abi.GridDesc), ctypes.sizeof(_abi.SchemeDesc), ctypes.sizeof(_abi.BcDesc), ctypes.sizeof(_abi.GasDesc),
+            _abi.GridDesc.bounds.offset, _abi.SchemeDesc.eps_p.offset, _abi.SchemeDesc.gas.offset, _abi.BcDesc.t_wall.offset]
+    assert got == want
+
+
+def test_array_size_matches_grid_array_layout():
+    g = _abi.grid_desc((2, 3, 4), (5, 6, 7), 2, (0, 1, 0, 1, 0, 1))
+    n = ctypes.c_size_t(0)
+    _native.check(_native.lib().gbns_array_size(g, ctypes.byref(n)))
+    assert n.value == 2 * 3 * 4 * 9 * 10 * 11 * 5
+
+
+@pytest.mark.parametrize("bad", ["nblk", "ng", "bounds", "coords"])
+def test_invalid_grid_rejected_before_cuda(bad):
+    g = _abi.grid_desc((2, 2, 2), (8, 8, 8), 2, (0, 1, 0, 1, 0, 1))
+    if bad == "nblk":
+        g.nblk[1] = 0
+    elif bad == "ng":
+        g.ng = 0
+    elif bad == "bounds":
+        g.bounds[3] = g.bounds[2]
+    else:
+        g.coords = 9
+    n = ctypes.c_size_t(0)
+    rc = _native.lib().gbns_array_size(g, ctypes.byref(n))
+    assert rc == _abi.ERR_INVALID
+    assert len(_native.last_error()) > 0
+
+
+def test_flux_div_rejects_insufficient_ghosts_before_cuda():
+    import problems as P
+    g = _abi.grid_desc((1, 1, 1), (8, 8, 8), 2, (0, 1, 0, 1, 0, 1))
+    s = P.scheme(conv=_abi.CONV_WENO5)
+    rc = _native.lib().gbns_flux_div(g, s, ctypes.c_void_p(16), ctypes.c_void_p(32), 0, None)
+    assert rc == _abi.ERR_INVALID
+    assert "ghost" in _native.last_error()
+
+
+def test_flux_div_rejects_bad_scheme_before_cuda():
+    import problems as P
+    g = _abi.grid_desc((1, 1, 1), (8, 8, 8), 4, (0, 1, 0, 1, 0, 1))
+    s = P.scheme(conv=_abi.CONV_CENT_KEEP, order=3)
+    assert _native.lib().gbns_flux_div(g, s, ctypes.c_void_p(16), ctypes.c_void_p(32), 0, None) == _abi.ERR_UNSUPPORTED
+    s = P.scheme(gamma=1.0)
+    assert _native.lib().gbns_flux_div(g, s, ctypes.c_void_p(16), ctypes.c_void_p(32), 0, None) == _abi.ERR_INVALID
+
+
+def test_fill_ghosts_rejects_unpaired_periodic():
+    g = _abi.grid_desc((1, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    bc = _abi.bc_desc([_abi.BC_PERIODIC, _abi.BC_NONE, 0, 0, 0, 0])
+    assert _native.lib().gbns_fill_ghosts(g, bc, ctypes.c_void_p(16), None) == _abi.ERR_INVALID
+
+
+# ---------------------------------------------------------- host lowering
+
+def air():
+    return fluid_state.ideal_gas_t(1.4, 287.0)
+
+
+def test_lower_compose_cent_keep_visc():
+    f = omni.compose(convective.cent_keep(2, air()), viscous.visc_lr(viscous_laws.constant_viscosity_t(1e-3, 0.72), air()))
+    s = pde_algs.lower(f)
+    assert (s.convective, s.order, s.viscous, s.visc_law, s.dissipation) == (_abi.CONV_CENT_KEEP, 2, 1, _abi.LAW_CONSTANT, 0)
+    assert s.mu == 1e-3 and s.prandtl == 0.72 and s.gas.gamma == 1.4
+
+
+def test_lower_channel_composite_and_precision_trait():
+    f = omni.compose(convective.weno5_t(air()),
+                     convective.pressure_diss_lr(air(), state_sensor.const_sensor_t(0.5), 2.0, 3.0),
+                     viscous.visc_lr(viscous_laws.sutherland_t(1e-3, 300.0, 110.4, 0.72), air()))
+    s = pde_algs.lower(f, _abi.PREC_FP32_FLUX)
+    assert (s.convective, s.dissipation, s.viscous, s.visc_law, s.precision) == (_abi.CONV_WENO5, 1, 1, _abi.LAW_SUTHERLAND, 1)
+    assert (s.eps_p, s.eps_T, s.sensor_alpha, s.S) == (2.0, 3.0, 0.5, 110.4)
+
+
+def test_lower_rejects_noncanonical_three_term_composite():
+    f = omni.compose(viscous.visc_lr(viscous_laws.constant_viscosity_t(1e-3, 0.72), air()),
+                     convective.cent_keep(2, air()),
+                     convective.pressure_diss_lr(air(), state_sensor.const_sensor_t(1.0), 1.0))
+    with pytest.raises(_native.SpadeError):
+        pde_algs.lower(f)
+
+
+def test_lower_rejects_mixed_gases():
+    f = omni.compose(convective.cent_keep(2, air()), viscous.visc_lr(viscous_laws.constant_viscosity_t(1e-3, 0.72),
+                                                                     fluid_state.ideal_gas_t(1.3, 287.0)))
+    with pytest.raises(_native.SpadeError):
+        pde_algs.lower(f)
+
+
+def test_cent_keep_rejects_odd_order():
+    with pytest.raises(ValueError):
+        convective.cent_keep(3, air())

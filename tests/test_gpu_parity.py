@@ -1,0 +1,366 @@
+"""GPU parity: the CUDA path through the C ABI of libgbns.so against the
+reference's outputs (tests/golden/) and the CPU oracle on identical inputs.
+
+GBNS_PREC_FP64 (the drop-in) performs every FP64 operation in the
+reference's order without FMA contraction, so its results must equal the
+reference's BIT FOR BIT (pinned schemes) and the oracle's bit for bit
+(features the reference lacks).  GBNS_PREC_FP64_FMA contracts multiply-adds:
+tolerance 1e-12 normwise per variable (max|gpu-ref| <= 1e-12 max|ref|).
+FP32-flux: 2e-4 normwise.  Ghost fills are copies: bit for bit.
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from spade_gb300 import _abi, _native
+from oracle import oracle as O
+import problems as P
+from golden.gen_golden import FLUX_CASES, FLUX_GRID, GHOST_GRID
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+TOL64 = 1e-12
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+def interior(a, ng):
+    return a[:, ng:-ng, ng:-ng, ng:-ng, :]
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def lib():
+    return _native.lib()
+
+
+def stream():
+    return int(torch.cuda.current_stream().cuda_stream)
+
+
+def gpu_flux(grid, scheme, q, rhs0=None, increment=False, variant=0):
+    qd = dev(q)
+    rd = dev(rhs0 if rhs0 is not None else np.zeros_like(q))
+    if variant:
+        rc = lib().gbns_flux_div_variant(grid, scheme, qd.data_ptr(), rd.data_ptr(), int(increment), variant, stream())
+    else:
+        rc = lib().gbns_flux_div(grid, scheme, qd.data_ptr(), rd.data_ptr(), int(increment), stream())
+    _native.check(rc)
+    return host(rd)
+
+
+def gpu_fill(grid, bc, q):
+    qd = dev(q)
+    _native.check(lib().gbns_fill_ghosts(grid, bc, qd.data_ptr(), stream()))
+    return host(qd)
+
+
+def gpu_status_ok():
+    st = ctypes.c_int(0)
+    _native.check(lib().gbns_device_status(ctypes.byref(st), 1, stream()))
+    return st.value == 0
+
+
+@pytest.fixture(autouse=True)
+def _device_status_clean():
+    yield
+    assert gpu_status_ok(), "a kernel reported a device-side error"
+
+
+# ---------------------------------------------------------------- flux_div
+
+def normwise(a, b):
+    a = np.asarray(a).reshape(-1, 5)
+    b = np.asarray(b).reshape(-1, 5)
+    return (np.abs(a - b).max(axis=0) / np.maximum(np.abs(b).max(axis=0), 1e-300)).max()
+
+
+@pytest.mark.parametrize("name", sorted(FLUX_CASES))
+def test_flux_div_fp64_bitwise_equals_reference(name):
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    r = gpu_flux(grid, P.scheme(**FLUX_CASES[name][1]), g["q"])
+    assert np.array_equal(interior(r, fg["ng"]), g["rhs_" + name])
+
+
+@pytest.mark.parametrize("name", sorted(FLUX_CASES))
+def test_flux_div_fp64_fma_within_tolerance(name):
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    r = gpu_flux(grid, P.scheme(precision=_abi.PREC_FP64_FMA, **FLUX_CASES[name][1]), g["q"])
+    assert normwise(interior(r, fg["ng"]), g["rhs_" + name]) <= TOL64
+
+
+def test_flux_div_overwrite_leaves_ghost_layers():
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    sentinel = np.full_like(g["q"], 7.25)
+    r = gpu_flux(grid, P.scheme(conv=_abi.CONV_CENT_KEEP, order=2, visc=1), g["q"], rhs0=sentinel, increment=False)
+    mask = np.ones(r.shape[:-1], bool)
+    n = fg["ng"]
+    mask[:, n:-n, n:-n, n:-n] = False
+    assert np.all(r[mask] == 7.25)
+
+
+def test_flux_div_increment_mode():
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    r = gpu_flux(grid, P.scheme(conv=_abi.CONV_CENT_KEEP, order=2, visc=1), g["q"], rhs0=g["rhs0_increment"], increment=True)
+    assert np.array_equal(interior(r, fg["ng"]), g["rhs_increment_ck2_visc"])
+
+
+@pytest.mark.parametrize("name", ["ck2_visc", "totani_visc", "fweno_diss_visc", "ck6"])
+def test_flux_div_tma_and_plain_staging_identical(name, monkeypatch):
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    s = P.scheme(**FLUX_CASES[name][1])
+    a = gpu_flux(grid, s, g["q"])
+    monkeypatch.setenv("GBNS_NO_TMA", "1")
+    b = gpu_flux(grid, s, g["q"])
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("conv,order", [(_abi.CONV_CENT_KEEP, 2), (_abi.CONV_TOTANI, 2), (_abi.CONV_FWENO, 2), (_abi.CONV_WENO5, 2)])
+def test_flux_div_tile_variants_identical(conv, order):
+    nblk, ncell, ng = (2, 2, 1), (20, 12, 10), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 2.0, 0.0, 1.0, 0.0, 1.5))
+    q = P.random_state(nblk, ncell, ng, seed=31)
+    s = P.scheme(conv=conv, order=order, diss=1, visc=1)
+    base = gpu_flux(grid, s, q)
+    nvar = lib().gbns_flux_variant_count(s)
+    assert nvar >= 2
+    for v in range(1, nvar):
+        assert np.array_equal(gpu_flux(grid, s, q, variant=v), base), v
+
+
+@pytest.mark.parametrize("coords", [_abi.COORDS_IDENTITY, _abi.COORDS_TANH_Y, _abi.COORDS_INTEGRATED_TANH_Y])
+@pytest.mark.parametrize("case", ["weno5_diss_suth", "weno5_nosmooth", "fweno_power", "ck4_suth", "ck8"])
+def test_flux_div_fp64_matches_oracle_unpinned_features(coords, case):
+    """WENO5, Sutherland, power law with visc_lr and stretched-y metrics have
+    no reference implementation: checked against the CPU restatement."""
+    kw = {
+        "weno5_diss_suth": dict(conv=_abi.CONV_WENO5, diss=1, visc=1, law=_abi.LAW_SUTHERLAND),
+        "weno5_nosmooth": dict(conv=_abi.CONV_WENO5, smooth=0),
+        "fweno_power": dict(conv=_abi.CONV_FWENO, visc=1, law=_abi.LAW_POWER),
+        "ck4_suth": dict(conv=_abi.CONV_CENT_KEEP, order=4, visc=1, law=_abi.LAW_SUTHERLAND),
+        "ck8": dict(conv=_abi.CONV_CENT_KEEP, order=8, visc=1),
+    }[case]
+    ng = 4 if case == "ck8" else 3
+    nblk, ncell = (2, 3, 1), (9, 7, 5)
+    cp = (2.0, 0, 0, 0) if coords == _abi.COORDS_TANH_Y else ((1.0, -1.0, 0.3, 2.5) if coords == _abi.COORDS_INTEGRATED_TANH_Y else (0, 0, 0, 0))
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 2.0, -1.0, 1.0, 0.0, 1.0), coords, cp)
+    q = P.random_state(nblk, ncell, ng, seed=41)
+    s = P.scheme(**kw)
+    ref = np.zeros_like(q)
+    O.flux_div(grid, s, q, ref, increment=False)
+    r = gpu_flux(grid, s, q)
+    if kw.get("law") == _abi.LAW_POWER:
+        # pow() of the GPU math library and of the host libm may differ in the last bit
+        assert normwise(interior(r, ng), interior(ref, ng)) <= 1e-14
+    else:
+        assert np.array_equal(interior(r, ng), interior(ref, ng))
+
+
+@pytest.mark.parametrize("name", ["ck2_visc", "fweno_diss_visc", "totani_visc"])
+def test_flux_div_fp32_flux_error_bounded(name):
+    """FP32 face arithmetic, FP64 accumulation: normwise error vs the FP64
+    reference stays at single-precision level."""
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    s = P.scheme(precision=_abi.PREC_FP32_FLUX, **FLUX_CASES[name][1])
+    r = interior(gpu_flux(grid, s, g["q"]), fg["ng"])
+    ref = g["rhs_" + name]
+    err = np.abs(r - ref).reshape(-1, 5).max(axis=0) / np.abs(ref).reshape(-1, 5).max(axis=0)
+    assert np.all(err < 2e-4), err
+
+
+def test_flux_div_conservation_periodic_tgv():
+    """Telescoping: the sum of the residual over a periodic box is round-off."""
+    nblk, ncell, ng = (2, 2, 2), (16, 16, 16), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    q = P.tgv_state(nblk, ncell, ng, P.tgv_tables(nblk, ncell, ng), seed=0)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    for prec in (_abi.PREC_FP64, _abi.PREC_FP32_FLUX):
+        r = interior(gpu_flux(grid, P.tgv_scheme(precision=prec), q), ng).reshape(-1, 5)
+        tot = np.abs(r.sum(axis=0))
+        scale = np.abs(r).sum(axis=0)
+        assert np.all(tot <= 1e-12 * scale), (prec, tot / scale)
+
+
+# ------------------------------------------------------------- ghost fill
+
+def test_fill_ghosts_matches_reference_bitwise():
+    g = load("ghosts_ref.npz")
+    gg = GHOST_GRID
+    grid = _abi.grid_desc(gg["nblk"], gg["ncell"], gg["ng"], gg["bounds"])
+    assert np.array_equal(gpu_fill(grid, P.periodic_bc(), g["q"]), g["periodic"])
+    assert np.array_equal(gpu_fill(grid, P.channel_bc(290.0), g["q"]), g["walls"])
+
+
+def test_fill_ghosts_slip_and_none_match_oracle():
+    nblk, ncell, ng = (3, 2, 2), (5, 4, 3), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    q = P.random_state(nblk, ncell, ng, seed=51)
+    bc = _abi.bc_desc([_abi.BC_SLIP_ADIABATIC, _abi.BC_ISOTHERMAL_NOSLIP, _abi.BC_PERIODIC, _abi.BC_PERIODIC,
+                       _abi.BC_NONE, _abi.BC_SLIP_ADIABATIC], [0, 310.0, 0, 0, 0, 0])
+    a = q.copy()
+    O.fill_ghosts(grid, bc, a)
+    assert np.array_equal(gpu_fill(grid, bc, q), a)
+
+
+# -------------------------------------------------------------- RK stage
+
+def test_rk_stage_matches_oracle():
+    nblk, ncell, ng = (2, 1, 2), (6, 7, 5), 2
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    q = P.random_state(nblk, ncell, ng, seed=61)
+    res = [P.random_state(nblk, ncell, ng, seed=62 + j, p0=1e3, T0=1e2, u0=10.0) for j in range(3)]
+    coeffs = [-1.0 / 12.0 * 1e-4, -1.0 / 12.0 * 1e-4, 2.0 / 3.0 * 1e-4]
+    a = q.copy()
+    O.rk_stage(grid, P.gas_desc(), a, res, coeffs)
+    qd = dev(q)
+    rd = [dev(r) for r in res]
+    ptrs = (ctypes.c_void_p * 3)(*[t.data_ptr() for t in rd])
+    cf = (ctypes.c_double * 3)(*coeffs)
+    _native.check(lib().gbns_rk_stage(grid, P.gas_desc(), qd.data_ptr(), ptrs, cf, 3, stream()))
+    b = host(qd)
+    assert np.array_equal(interior(b, ng), interior(a, ng))
+    ghost = np.ones(q.shape[:-1], bool)
+    ghost[:, ng:-ng, ng:-ng, ng:-ng] = False
+    assert np.array_equal(b[ghost], q[ghost])
+
+
+# ---------------------------------------------------------- time stepping
+
+def gpu_ssprk3(grid, scheme, bc, q, dt, nsteps, ke_every=True):
+    qd = dev(q)
+    n = qd.numel()
+    work = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    ke = []
+    out = np.zeros(5)
+
+    def red():
+        _native.check(lib().gbns_reduce(grid, scheme.gas, qd.data_ptr(), _abi.RED_KINETIC,
+                                        out.ctypes.data_as(ctypes.c_void_p), stream()))
+        return float(out[0])
+
+    ke.append(red())
+    for _ in range(nsteps):
+        _native.check(lib().gbns_ssprk3_step(grid, scheme, bc, qd.data_ptr(), work.data_ptr(), ctypes.c_double(dt), stream()))
+        if ke_every:
+            ke.append(red())
+    return host(qd), np.array(ke)
+
+
+def test_tgv_c1_flux_div_and_ke_history():
+    """C1: 2x2x2 blocks of 16^3, ng=2, cent_keep<2> + visc_lr(constant):
+    one flux_div and the 20-step SSPRK3 kinetic-energy history of the
+    reference."""
+    g = load("tgv_ref.npz")
+    nblk, ncell, ng = (2, 2, 2), (16, 16, 16), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    tables = {k[4:]: g[k] for k in g.files if k.startswith("tab_")}
+    q = P.tgv_state(nblk, ncell, ng, tables, seed=0)
+    q = gpu_fill(grid, P.periodic_bc(), q)
+    r = interior(gpu_flux(grid, P.tgv_scheme(), q), ng)
+    assert np.array_equal(r[:, ::5, ::5, ::5, :], g["rhs_probe"])
+    qf, ke = gpu_ssprk3(grid, P.tgv_scheme(), P.periodic_bc(), q, float(g["dt"]), 20)
+    # the state is bit-identical; the KE reduction sums in another order
+    np.testing.assert_allclose(ke, g["ke"], rtol=1e-13, atol=0)
+    qi = interior(qf, ng)
+    assert np.array_equal(qi[:, ::3, ::3, ::3, :], g["q_probe"])
+
+
+def test_tgv_c1_fp64_fma_and_fp32_flux_ke_error():
+    """The faster forms against the reference's 20-step KE history."""
+    g = load("tgv_ref.npz")
+    nblk, ncell, ng = (2, 2, 2), (16, 16, 16), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    tables = {k[4:]: g[k] for k in g.files if k.startswith("tab_")}
+    q = gpu_fill(grid, P.periodic_bc(), P.tgv_state(nblk, ncell, ng, tables, seed=0))
+    _, ke = gpu_ssprk3(grid, P.tgv_scheme(precision=_abi.PREC_FP64_FMA), P.periodic_bc(), q, float(g["dt"]), 20)
+    np.testing.assert_allclose(ke, g["ke"], rtol=1e-12, atol=0)
+    _, ke32 = gpu_ssprk3(grid, P.tgv_scheme(precision=_abi.PREC_FP32_FLUX), P.periodic_bc(), q, float(g["dt"]), 20)
+    assert np.abs(ke32 / g["ke"] - 1.0).max() < 1e-5
+
+
+def test_tgv_small_final_state():
+    g = load("tgv_small_ref.npz")
+    nblk, ncell, ng = (2, 2, 2), (8, 8, 8), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    tables = {k[4:]: g[k] for k in g.files if k.startswith("tab_")}
+    q = P.tgv_state(nblk, ncell, ng, tables, seed=3)
+    q = gpu_fill(grid, P.periodic_bc(), q)
+    qf, ke = gpu_ssprk3(grid, P.tgv_scheme(), P.periodic_bc(), q, float(g["dt"]), 10)
+    assert np.array_equal(interior(qf, ng), g["q_final"])
+    np.testing.assert_allclose(ke, g["ke"], rtol=1e-13)
+
+
+def test_channel_fweno_walls_5_steps():
+    g = load("channel_ref.npz")
+    nblk, ncell, ng = (2, 2, 2), (8, 8, 8), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 4 * math.pi, -1.0, 1.0, 0.0, 4 * math.pi / 3))
+    s = P.scheme(conv=_abi.CONV_FWENO, diss=1, visc=1, mu=float(g["mu"]), eps_p=float(g["eps"]), eps_T=float(g["eps"]), alpha=1.0)
+    qf, ke = gpu_ssprk3(grid, s, P.channel_bc(300.0), g["q0"], float(g["dt"]), 5)
+    assert np.array_equal(interior(qf, ng), g["q_final"])
+    np.testing.assert_allclose(ke, g["ke"], rtol=1e-13)
+
+
+def test_stretched_channel_weno5_sutherland_matches_oracle_3_steps():
+    nblk, ncell, ng = (2, 2, 1), (8, 8, 8), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 2.0, -1.0, 1.0, 0.0, 1.0), _abi.COORDS_TANH_Y, (2.0, 0, 0, 0))
+    q = P.random_state(nblk, ncell, ng, seed=71, rel=0.01, u0=5.0)
+    bc = P.channel_bc(300.0)
+    O.fill_ghosts(grid, bc, q)
+    s = P.scheme(conv=_abi.CONV_WENO5, diss=1, visc=1, law=_abi.LAW_SUTHERLAND, mu=0.05, eps_p=3.0, eps_T=3.0, alpha=1.0)
+    dt = 2e-6
+    a = q.copy()
+    work = np.zeros((3,) + q.shape)
+    for _ in range(3):
+        O.ssprk3_step(grid, s, bc, a, work, dt)
+    b, _ = gpu_ssprk3(grid, s, bc, q, dt, 3, ke_every=False)
+    assert np.array_equal(interior(b, ng), interior(a, ng))
+
+
+# ------------------------------------------------------------- reductions
+
+@pytest.mark.parametrize("kind", [_abi.RED_MAX_WAVESPEED, _abi.RED_KINETIC, _abi.RED_CONSERVED, _abi.RED_HEALTH])
+@pytest.mark.parametrize("coords", [_abi.COORDS_IDENTITY, _abi.COORDS_TANH_Y])
+def test_reductions_match_oracle(kind, coords):
+    nblk, ncell, ng = (3, 2, 2), (7, 6, 5), 2
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, -1.0, 1.0, 0.0, 2.0), coords, (2.0, 0, 0, 0))
+    q = P.random_state(nblk, ncell, ng, seed=81)
+    q[0, ng + 1, ng + 1, ng + 1, 0] = -1.0      # one non-physical cell
+    q[1, ng + 2, ng, ng + 3, 4] = np.nan        # and one NaN
+    if kind != _abi.RED_HEALTH:
+        q = np.nan_to_num(np.abs(q))
+    want = O.reduce(grid, P.gas_desc(), q, kind)
+    qd = dev(q)
+    out = np.zeros(5)
+    _native.check(lib().gbns_reduce(grid, P.gas_desc(), qd.data_ptr(), kind, out.ctypes.data_as(ctypes.c_void_p), stream()))
+    got = out if kind == _abi.RED_CONSERVED else out[0]
+    if kind == _abi.RED_HEALTH:
+        assert got == want == 2.0
+    else:
+        np.testing.assert_allclose(got, want, rtol=1e-13)
