@@ -190,6 +190,35 @@ int gbns_rk_stage(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
 int gbns_reduce(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
                 const double* prims, int kind, double* out, void* stream);
 
+/* flux_div with an explicit tile-shape variant (0 .. gbns_flux_variant_count-1);
+ * every variant computes bit-identical results.  The autotuner's search
+ * space; replaces the reference's choice among flux_div_{basic,bfoct,fldbc,
+ * ldbal,shfus,longf} by trait (flux_div.h:30-40). */
+int gbns_flux_div_variant(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                          const double* prims, double* rhs, int increment, int variant, void* stream);
+
+/* Number of tile variants built for a scheme (>= 1); no CUDA call. */
+int gbns_flux_variant_count(const gbns_scheme_desc* scheme);
+
+/* Scratch size (doubles) and result offset for gbns_reduce_async; no CUDA call. */
+int gbns_reduce_scratch_size(const gbns_grid_desc* grid, size_t* ndouble, size_t* result_offset);
+
+/* gbns_reduce with caller-owned device scratch; the result stays in device
+ * memory at scratch + result_offset.  Asynchronous.  Replaces
+ * algs::transform_reduce (algs/transform_reduce.h:53-191). */
+int gbns_reduce_async(const gbns_grid_desc* grid, const gbns_gas_desc* gas, const double* prims,
+                      int kind, double* scratch, size_t scratch_len, void* stream);
+
+/* Device-side status: nonzero after a kernel gave up on a bounded wait
+ * (GBNS_ERR_TIMEOUT class events).  reset != 0 clears it.  Synchronises
+ * `stream`.  Replaces the reference's post-launch error check
+ * (dispatch/execute.h:86-96). */
+int gbns_device_status(int* status, int reset, void* stream);
+
+/* Measured FMA throughput of this GPU (FLOP/s) with dependent FMA chains:
+ * fp64 != 0 -> double, else float.  Benchmark aid (no reference counterpart). */
+int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);
+
 /* One full SSPRK3 step with the reference's structure
  * (integrate_advance with state_transform_t, time-integration/advance.h:234-280;
  * ssprk3_t, time-integration/explicit.h:80-88):

@@ -361,8 +361,10 @@ static st5 flux_fweno(const ctx_t* C, const double* cells[4], const double ncell
 /* 5th-order WENO-JS (Jiang & Shu 1996) on the same per-point Rusanov split
  * as fweno_t.  cells[m], m = 0..5, at face offsets -5,-3,-1,1,3,5.  The
  * upwind part reconstructs f+ = fl+ds from cells 0..4, the downwind part
- * f- = fl-ds from cells 5..1 (mirrored); F = f+ + f-.  No reference
- * counterpart: parity unpinned. */
+ * f- = fl-ds from cells 5..1 (mirrored); F = f+ + f-.  The nonlinear
+ * weights g_k/D_k, D_k = (eps + beta_k)^2, are normalised with one
+ * division as g_k prod_{j!=k} D_j / sum.  No reference counterpart:
+ * parity unpinned. */
 static double weno5_side(double a, double b, double c, double d, double e, int smooth)
 {
     const double p0 = (2.0*a - 7.0*b + 11.0*c)*(1.0/6.0);
@@ -376,11 +378,13 @@ static double weno5_side(double a, double b, double c, double d, double e, int s
     const double b1 = (13.0/12.0)*t1*t1 + 0.25*s1*s1;
     const double b2 = (13.0/12.0)*t2*t2 + 0.25*s2*s2;
     const double eps = 1e-16;
-    const double a0 = 0.1/((b0 + eps)*(b0 + eps));
-    const double a1 = 0.6/((b1 + eps)*(b1 + eps));
-    const double a2 = 0.3/((b2 + eps)*(b2 + eps));
-    const double inv = 1.0/(a0 + a1 + a2);
-    return (a0*p0 + a1*p1 + a2*p2)*inv;
+    const double d0 = (b0 + eps)*(b0 + eps);
+    const double d1 = (b1 + eps)*(b1 + eps);
+    const double d2 = (b2 + eps)*(b2 + eps);
+    const double a0 = 0.1*(d1*d2);
+    const double a1 = 0.6*(d0*d2);
+    const double a2 = 0.3*(d0*d1);
+    return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
 }
 
 static st5 flux_weno5(const ctx_t* C, const double* cells[6], const double ncell[6][3])

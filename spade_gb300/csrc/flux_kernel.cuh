@@ -313,7 +313,10 @@ namespace gbns
     }
 
     // 5th-order WENO-JS side reconstruction (Jiang & Shu 1996); cells a..e
-    // upwind to downwind.  No reference counterpart.
+    // upwind to downwind.  No reference counterpart.  In FP64 the nonlinear
+    // weights share one division: w_k = g_k prod_{j!=k} D_j / sum, with
+    // D_j = (eps + beta_j)^2 (the same weights as g_k/D_k normalised); FP32
+    // keeps the per-weight divisions because the products can overflow.
     template <class Real>
     __device__ __forceinline__ Real weno5_side(Real a, Real b, Real c, Real d, Real e, int smooth)
     {
@@ -330,11 +333,24 @@ namespace gbns
         const Real b1 = k13*t1*t1 + Real(0.25)*s1*s1;
         const Real b2 = k13*t2*t2 + Real(0.25)*s2*s2;
         const Real eps = Real(1e-16);
-        const Real a0 = Real(0.1)/((b0 + eps)*(b0 + eps));
-        const Real a1 = Real(0.6)/((b1 + eps)*(b1 + eps));
-        const Real a2 = Real(0.3)/((b2 + eps)*(b2 + eps));
-        const Real inv = Real(1.0)/(a0 + a1 + a2);
-        return (a0*p0 + a1*p1 + a2*p2)*inv;
+        const Real d0 = (b0 + eps)*(b0 + eps);
+        const Real d1 = (b1 + eps)*(b1 + eps);
+        const Real d2 = (b2 + eps)*(b2 + eps);
+        if constexpr (sizeof(Real) == 8)
+        {
+            const Real a0 = Real(0.1)*(d1*d2);
+            const Real a1 = Real(0.6)*(d0*d2);
+            const Real a2 = Real(0.3)*(d0*d1);
+            return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
+        }
+        else
+        {
+            const Real a0 = Real(0.1)/d0;
+            const Real a1 = Real(0.6)/d1;
+            const Real a2 = Real(0.3)/d2;
+            const Real inv = Real(1.0)/(a0 + a1 + a2);
+            return (a0*p0 + a1*p1 + a2*p2)*inv;
+        }
     }
 
     template <class Cfg, int D>
