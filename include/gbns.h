@@ -219,6 +219,25 @@ int gbns_device_status(int* status, int reset, void* stream);
  * fp64 != 0 -> double, else float.  Benchmark aid (no reference counterpart). */
 int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);
 
+/* Reduction that allocates nothing.  For callers that cannot let the
+ * library call cudaMalloc: work recorded into a CUDA graph while a stream is
+ * being captured (allocation is not allowed during capture) and applications
+ * whose device memory all belongs to their own pool allocator.  Same
+ * reductions and results as gbns_reduce; the result (1 double, 5 for
+ * GBNS_RED_CONSERVED) goes to the caller's DEVICE buffer out_dev,
+ * asynchronously on `stream`.  Its partial sums live in a fixed file-scope
+ * device array of 6,152 doubles (about 48 KB, held by every GPU that loads
+ * the library until exit); a grid whose reduction would need more scratch is
+ * rejected with GBNS_ERR_CAPACITY (the current partitioning never needs more
+ * than 1024 partial records).  The first call on a device looks up the
+ * array's device address with that device current: make that first call
+ * before any stream capture.  All calls share the one array and leave their
+ * partial sums in it: calls that overlap on the GPU (several streams, or
+ * several host threads on one device) race and must be serialised by the
+ * caller.  No counterpart in the reference. */
+int gbns_reduce_noalloc(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
+                        const double* prims, int kind, double* out_dev, void* stream);
+
 /* One full SSPRK3 step with the reference's structure
  * (integrate_advance with state_transform_t, time-integration/advance.h:234-280;
  * ssprk3_t, time-integration/explicit.h:80-88):

@@ -39,6 +39,7 @@ def lib():
     L.gbns_reduce.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, vp]
     L.gbns_reduce_scratch_size.argtypes = [P(_abi.GridDesc), P(ctypes.c_size_t), P(ctypes.c_size_t)]
     L.gbns_reduce_async.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, ctypes.c_size_t, vp]
+    L.gbns_reduce_noalloc.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, vp]
     L.gbns_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double, vp]
     L.gbns_device_status.argtypes = [P(ctypes.c_int), ctypes.c_int, vp]
     if L.gbns_version() != _abi.ABI_VERSION:

@@ -1,0 +1,53 @@
+"""gbns_reduce_noalloc: the reduction entry point that allocates nothing (its
+partial sums live in a fixed device array inside the library), for callers
+that cannot let the library call cudaMalloc — work recorded into a CUDA graph
+while a stream is being captured, or applications whose device memory all
+belongs to their own pool allocator.
+
+The test calls it through the C ABI twice in a row for every reduction kind
+and checks each result against gbns_reduce (which uses library-allocated
+scratch) on the same state, within the tolerance the other reduction tests
+use.  It must pass alone in a fresh process and after the other tests."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from spade_gb300 import _abi, _native
+import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("coords", [_abi.COORDS_IDENTITY, _abi.COORDS_TANH_Y])
+def test_reduce_noalloc_matches_reduce_twice_in_a_row(coords):
+    lib = _native.lib()
+    st = int(torch.cuda.current_stream().cuda_stream)
+    nblk, ncell, ng = (3, 2, 2), (9, 7, 6), 2
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, -1.0, 1.0, 0.0, 2.0), coords, (2.0, 0, 0, 0))
+    gas = P.gas_desc()
+    q = np.abs(P.random_state(nblk, ncell, ng, seed=91))
+    q[0, ng + 2, ng + 1, ng + 3, 1] = -5.0          # one cell the health count must see
+    qd = torch.from_numpy(q).cuda()
+    out_dev = torch.full((5,), -1.0, dtype=torch.float64, device="cuda")
+    for kind in (_abi.RED_MAX_WAVESPEED, _abi.RED_KINETIC, _abi.RED_CONSERVED, _abi.RED_HEALTH):
+        want = np.zeros(5)
+        _native.check(lib.gbns_reduce(grid, gas, qd.data_ptr(), kind, want.ctypes.data_as(ctypes.c_void_p), st))
+        n = 5 if kind == _abi.RED_CONSERVED else 1
+        for _ in range(2):
+            out_dev.fill_(-1.0)
+            _native.check(lib.gbns_reduce_noalloc(grid, gas, qd.data_ptr(), kind, out_dev.data_ptr(), st))
+            torch.cuda.synchronize()
+            got = out_dev.cpu().numpy()[:n]
+            np.testing.assert_allclose(got, want[:n], rtol=1e-13, atol=0)
+
+
+def test_reduce_noalloc_rejects_bad_arguments():
+    lib = _native.lib()
+    grid = _abi.grid_desc((1, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    rc = lib.gbns_reduce_noalloc(grid, P.gas_desc(), ctypes.c_void_p(16), 99, ctypes.c_void_p(32), None)
+    assert rc == _abi.ERR_INVALID
+    rc = lib.gbns_reduce_noalloc(grid, P.gas_desc(), ctypes.c_void_p(16), _abi.RED_KINETIC, None, None)
+    assert rc == _abi.ERR_INVALID
