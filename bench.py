@@ -137,6 +137,11 @@ def run_gpu(args, rank, world):
     qp = q.ptr()
     chk = _native.check
 
+    from spade_gb300 import autotune
+    tuned = {}
+    best, times = autotune.tune(g, s, qp, rptr[0], reps=2, use_cache=False)
+    tuned[args.precision] = {"variant": best, "ms_per_variant": times}
+
     def step(events=None):
         # SSPRK3 (advance.h:234-280): the same launches gbns_ssprk3_step makes,
         # issued one by one so the flux_div launches can be bracketed by events.
@@ -206,6 +211,8 @@ def run_gpu(args, rank, world):
     fp32 = None
     if not args.no_fp32 and prec == _abi.PREC_FP64:
         s32 = prob.scheme_desc(_abi.PREC_FP32_FLUX)
+        b32, t32 = autotune.tune(g, s32, qp, rptr[0], reps=3, use_cache=False)
+        tuned["fp32_flux"] = {"variant": b32, "ms_per_variant": t32}
         w = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
         for _ in range(2):
             chk(lib.gbns_ssprk3_step(g, s32, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
@@ -246,6 +253,7 @@ def run_gpu(args, rank, world):
         "clocks": clk, "health_bad_cells": health.value, "e2e_ms": e2e_ms,
         "h2d": host_q.numel() * 8, "d2h": host_q.numel() * 8, "fp32": fp32,
         "fp64_fma_flops": fp64_rate.value, "fp32_fma_flops": fp32_rate.value, "traffic": traffic,
+        "tuned": tuned,
     }
 
 
@@ -381,6 +389,7 @@ def main():
         "gpu_launches": r["launches"],
         "health_bad_cells": r["health_bad_cells"],
         "fp32_flux": r["fp32"],
+        "autotune": r["tuned"],
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu

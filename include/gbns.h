@@ -110,6 +110,9 @@ typedef struct gbns_scheme_desc
     int32_t viscous;       /* GBNS_VISC_* */
     int32_t visc_law;      /* GBNS_LAW_* */
     int32_t precision;     /* GBNS_PREC_* */
+    int32_t tile_variant;  /* flux_div tile shape, 0 .. gbns_flux_variant_count-1 (0 = default);
+                              every variant gives bit-identical results */
+    int32_t reserved;      /* must be 0 */
     double  eps_p, eps_T;  /* pressure_diss_lr coefficients */
     double  sensor_alpha;  /* const_sensor_t::alpha */
     double  mu;            /* constant: mu; power/sutherland: mu_ref */

@@ -77,6 +77,8 @@ class SchemeDesc(ctypes.Structure):
         ("viscous", ctypes.c_int32),
         ("visc_law", ctypes.c_int32),
         ("precision", ctypes.c_int32),
+        ("tile_variant", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("eps_p", ctypes.c_double),
         ("eps_T", ctypes.c_double),
         ("sensor_alpha", ctypes.c_double),

@@ -14,13 +14,15 @@ namespace gbns
     int flux_variant_count(const gbns_scheme_desc* s)
     {
         if (!s) return 0;
+        // FP32-flux adds one variant: the TMA-staged FP64 box.
+        const int extra = s->precision == GBNS_PREC_FP32_FLUX ? 1 : 0;
         switch (s->convective)
         {
-            case GBNS_CONV_CENT_KEEP: return s->order == 2 ? 4 : 1;
-            case GBNS_CONV_TOTANI:    return 2;
-            case GBNS_CONV_FWENO:     return 3;
-            case GBNS_CONV_WENO5:     return 2;
-            default:                  return 1;
+            case GBNS_CONV_CENT_KEEP: return (s->order == 2 ? 4 : 1) + extra;
+            case GBNS_CONV_TOTANI:    return 2 + extra;
+            case GBNS_CONV_FWENO:     return 3 + extra;
+            case GBNS_CONV_WENO5:     return 3 + extra;
+            default:                  return 1 + extra;
         }
     }
 

@@ -2,6 +2,7 @@
 #define GBNS_REAL float
 #define GBNS_STRETCH false
 #define GBNS_GROUP 0
+#define GBNS_FP32 1
 #define GBNS_TAG 8
 #define GBNS_FN flux_f32_identity_a
 #include "flux_inst.cuh"

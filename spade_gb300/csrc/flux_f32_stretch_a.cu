@@ -2,6 +2,7 @@
 #define GBNS_REAL float
 #define GBNS_STRETCH true
 #define GBNS_GROUP 0
+#define GBNS_FP32 1
 #define GBNS_TAG 10
 #define GBNS_FN flux_f32_stretch_a
 #include "flux_inst.cuh"

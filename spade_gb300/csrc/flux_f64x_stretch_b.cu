@@ -2,6 +2,7 @@
 #define GBNS_REAL double
 #define GBNS_STRETCH true
 #define GBNS_GROUP 1
+#define GBNS_FP32 0
 #define GBNS_TAG 3
 #define GBNS_FN flux_f64x_stretch_b
 #include "flux_inst.cuh"

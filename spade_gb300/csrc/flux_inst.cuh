@@ -29,7 +29,7 @@ namespace gbns
         std::memset(&tmap, 0, sizeof(tmap));
         A.use_tma = 0;
         const bool aligned = (G.ni % 2 == 0) && ((reinterpret_cast<uintptr_t>(c.prims) & 15) == 0);
-        if (aligned && !tma_disabled())
+        if (!Cfg::DIRECT && aligned && !tma_disabled())
         {
             int rc = encode_prims_tmap(&tmap, c.prims, G, Cfg::BXE, Cfg::BY, Cfg::BZ);
             if (rc) return rc;
@@ -49,44 +49,77 @@ namespace gbns
 }
 
 #define GBNS_RUN(CONV, ORDER, TX, TY, TZ, NT) \
-    return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG>>(c)
+    return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG, 0>>(c)
+// FP32 only: stencil cells loaded straight into FP32 shared memory
+#define GBNS_RUN_DIRECT(CONV, ORDER, TX, TY, TZ, NT) \
+    return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG, 1>>(c)
+#if GBNS_FP32
+#define GBNS_RUN_D GBNS_RUN_DIRECT
+#else
+#define GBNS_RUN_D GBNS_RUN
+#endif
 
 namespace gbns
 {
+    // Tile variants.  Variant 0 is the default; every variant computes
+    // bit-identical results.  In FP32 TUs the GBNS_RUN_D variants load the
+    // stencil straight into FP32 shared memory and the last variant stages
+    // the FP64 box through TMA.
     int GBNS_FN(const FluxCall& c, int conv, int order)
     {
         const int v = c.variant;
 #if GBNS_GROUP == 0
-        if (conv == GBNS_CONV_NONE) { GBNS_RUN(GBNS_CONV_NONE, 2, 8, 8, 8, 256); }
+        if (conv == GBNS_CONV_NONE)
+        {
+            if (GBNS_FP32 && v == 1) GBNS_RUN(GBNS_CONV_NONE, 2, 8, 8, 8, 256);
+            GBNS_RUN_D(GBNS_CONV_NONE, 2, 8, 8, 8, 256);
+        }
         if (conv == GBNS_CONV_CENT_KEEP)
         {
             if (order == 2)
             {
-                if (v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 16, 8, 4, 256);
-                if (v == 2) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 4, 128);
-                if (v == 3) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 16, 8, 8, 256);
-                GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 256);
+                if (v == 1) GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 16, 8, 4, 256);
+                if (v == 2) GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 8, 8, 4, 128);
+                if (v == 3) GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 16, 8, 8, 256);
+                if (GBNS_FP32 && v == 4) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 256);
+                GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 256);
             }
-            if (order == 4) { GBNS_RUN(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 256); }
-            if (order == 6) { GBNS_RUN(GBNS_CONV_CENT_KEEP, 6, 8, 8, 4, 256); }
-            if (order == 8) { GBNS_RUN(GBNS_CONV_CENT_KEEP, 8, 8, 8, 4, 256); }
+            if (order == 4)
+            {
+                if (GBNS_FP32 && v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 256);
+                GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 256);
+            }
+            if (order == 6)
+            {
+                if (GBNS_FP32 && v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 6, 8, 8, 4, 256);
+                GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 6, 8, 8, 4, 256);
+            }
+            if (order == 8)
+            {
+                if (GBNS_FP32 && v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 8, 8, 8, 4, 256);
+                GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 8, 8, 8, 4, 256);
+            }
         }
         if (conv == GBNS_CONV_TOTANI)
         {
-            if (v == 1) GBNS_RUN(GBNS_CONV_TOTANI, 2, 16, 8, 4, 256);
-            GBNS_RUN(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
+            if (v == 1) GBNS_RUN_D(GBNS_CONV_TOTANI, 2, 16, 8, 4, 256);
+            if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
+            GBNS_RUN_D(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
         }
 #else
         if (conv == GBNS_CONV_FWENO)
         {
-            if (v == 1) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 4, 128);
-            if (v == 2) GBNS_RUN(GBNS_CONV_FWENO, 2, 16, 8, 4, 256);
-            GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
+            if (v == 1) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 4, 128);
+            if (v == 2) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 16, 8, 4, 256);
+            if (GBNS_FP32 && v == 3) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
+            GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
         }
         if (conv == GBNS_CONV_WENO5)
         {
-            if (v == 1) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 8, 256);
-            GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
+            if (v == 1) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 8, 256);
+            if (v == 2) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 4, 4, 128);
+            if (GBNS_FP32 && v == 3) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
+            GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
         }
 #endif
         return set_error(GBNS_ERR_UNSUPPORTED, "flux scheme not instantiated");

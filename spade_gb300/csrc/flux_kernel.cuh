@@ -42,7 +42,10 @@ namespace gbns
     // TAG_ distinguishes translation units that instantiate the same
     // arithmetic with different compiler settings (FMA contraction on/off),
     // so their kernels and launchers never share a symbol.
-    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_>
+    // STG_ (FP32 only): 0 = stage the FP64 box (TMA or coalesced loads) and
+    // convert it; 1 = load the stencil cells straight into FP32 shared
+    // memory (no FP64 staging buffer, more CTAs per SM).
+    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_, int STG_ = 0>
     struct FluxCfg
     {
         using Real = Real_;
@@ -50,6 +53,7 @@ namespace gbns
         static constexpr bool STRETCH = STRETCH_;
         static constexpr int TX = TX_, TY = TY_, TZ = TZ_, NT = NT_;
         static constexpr bool FP64 = std::is_same<Real, double>::value;
+        static constexpr bool DIRECT = !FP64 && STG_ == 1;
         static constexpr int HC = ConvTraits<CONV, ORDER>::HC;
         static constexpr int H = HC > 1 ? HC : 1;
         static constexpr int NDER = ConvTraits<CONV, ORDER>::NDER;
@@ -63,16 +67,20 @@ namespace gbns
         static constexpr int NF0 = (TX + 1)*TY*TZ, NF1 = TX*(TY + 1)*TZ, NF2 = TX*TY*(TZ + 1);
         static constexpr int NFMAX = cmax3(NF0, NF1, NF2);
         static constexpr int CPT = (NCELL + NT - 1)/NT;
-        static constexpr size_t STAGE_BYTES = align128(size_t(BOXN)*5*sizeof(double));
+        static constexpr size_t STAGE_BYTES = DIRECT ? 0 : align128(size_t(BOXN)*5*sizeof(double));
         static constexpr size_t SOA_BYTES   = FP64 ? 0 : align128(size_t(BOXN)*5*sizeof(float));
         static constexpr size_t DER_BYTES   = align128(size_t(NDER > 0 ? NDER : 1)*BOXN*sizeof(Real));
-        static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFMAX*sizeof(Real));
-        // FP32: the staging buffer is dead once converted, so derived values
-        // and face fluxes reuse it when they fit.
-        static constexpr bool REUSE = !FP64 && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
+        // face fluxes are kept in FP64 (converted once per face)
+        static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFMAX*sizeof(double));
+        // FP32 staged: the staging buffer is dead once converted, so derived
+        // values and face fluxes reuse it when they fit.
+        static constexpr bool REUSE = !FP64 && !DIRECT && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
         static constexpr size_t SMEM_BYTES = 128 /*mbarrier*/ + STAGE_BYTES + SOA_BYTES +
                                              (REUSE ? 0 : DER_BYTES + FLX_BYTES);
         static_assert(SMEM_BYTES <= 227*1024, "tile does not fit in shared memory");
+        // CTAs per SM that shared memory allows (the register budget follows)
+        static constexpr int MINB_RAW = int((227*1024) / (SMEM_BYTES + 1024));
+        static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
         static_assert(5*BXE <= 256, "TMA box inner extent exceeds 256 elements");
     };
 
@@ -302,7 +310,7 @@ namespace gbns
     {
         using Real = typename Cfg::Real;
         constexpr int SD = DirStride<Cfg, D>::S;
-        #pragma unroll 1
+        #pragma unroll
         for (int eq = 0; eq < 5; ++eq)
         {
             Real fl[4], ds[4];
@@ -359,7 +367,7 @@ namespace gbns
     {
         using Real = typename Cfg::Real;
         constexpr int SD = DirStride<Cfg, D>::S;
-        #pragma unroll 1
+        #pragma unroll
         for (int eq = 0; eq < 5; ++eq)
         {
             Real up[6], dn[6];
@@ -490,33 +498,23 @@ namespace gbns
                                               typename Cfg::Real* F)
     {
         using Real = typename Cfg::Real;
+        // terms in fixed registers (no pointer selection: keeps them out of
+        // local memory); summed conv + (diss + visc) like compose
         Real t0[5], t1[5], t2[5];
-        int nterm = 0;
-        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP) { conv_cent_keep<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
-        else if constexpr (Cfg::CONV == GBNS_CONV_TOTANI) { conv_totani<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
-        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) { conv_fweno<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
-        else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) { conv_weno5<Cfg, D>(V, S, rc, nD, t0); nterm = 1; }
-        Real* nxt = nterm == 0 ? t0 : t1;
-        int extra = 0;
-        if (S.diss) { diss_pressure<Cfg, D>(V, S, rc, nxt); ++extra; }
-        if (S.visc)
+        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP) conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
+        else if constexpr (Cfg::CONV == GBNS_CONV_TOTANI) conv_totani<Cfg, D>(V, S, rc, nD, t0);
+        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) conv_fweno<Cfg, D>(V, S, rc, nD, t0);
+        else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) conv_weno5<Cfg, D>(V, S, rc, nD, t0);
+        const bool hd = S.diss != 0, hv = S.visc != 0;
+        if (hd) diss_pressure<Cfg, D>(V, S, rc, t1);
+        if (hv) visc_lr<Cfg, D>(V, S, rc, nD, inv, im, t2);
+        #pragma unroll
+        for (int v = 0; v < 5; ++v)
         {
-            Real* dst = (extra == 0) ? nxt : t2;
-            visc_lr<Cfg, D>(V, S, rc, nD, inv, im, dst);
-            ++extra;
-        }
-        if constexpr (Cfg::CONV == GBNS_CONV_NONE)
-        {
-            // diss + visc, diss, or visc
-            if (extra == 2) { for (int v = 0; v < 5; ++v) F[v] = t0[v] + t2[v]; }
-            else if (extra == 1) { for (int v = 0; v < 5; ++v) F[v] = t0[v]; }
-            else { for (int v = 0; v < 5; ++v) F[v] = Real(0); }
-        }
-        else
-        {
-            if (extra == 2) { for (int v = 0; v < 5; ++v) F[v] = t0[v] + (t1[v] + t2[v]); }
-            else if (extra == 1) { for (int v = 0; v < 5; ++v) F[v] = t0[v] + t1[v]; }
-            else { for (int v = 0; v < 5; ++v) F[v] = t0[v]; }
+            if constexpr (Cfg::CONV == GBNS_CONV_NONE)
+                F[v] = (hd && hv) ? t1[v] + t2[v] : (hd ? t1[v] : (hv ? t2[v] : Real(0)));
+            else
+                F[v] = (hd && hv) ? t0[v] + (t1[v] + t2[v]) : (hd ? t0[v] + t1[v] : (hv ? t0[v] + t2[v] : t0[v]));
         }
     }
 
@@ -534,7 +532,7 @@ namespace gbns
 
     template <class Cfg, int D>
     __device__ __forceinline__ void face_pass(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                              typename Cfg::Real* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
+                                              double* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
                                               int lb, const int b[3], int i0, int j0, int k0, int shift,
                                               const typename Cfg::Real inv[3],
                                               double (&relem)[Cfg::CPT][5], const double invd[3])
@@ -572,7 +570,7 @@ namespace gbns
                 face_flux<Cfg, D>(V, S, rc, nD, inv, im, F);
             }
             #pragma unroll
-            for (int v = 0; v < 5; ++v) sF[v*Cfg::NFMAX + f] = F[v];
+            for (int v = 0; v < 5; ++v) sF[v*Cfg::NFMAX + f] = double(F[v]);
         }
         __syncthreads();
         #pragma unroll
@@ -593,15 +591,15 @@ namespace gbns
             #pragma unroll
             for (int v = 0; v < 5; ++v)
             {
-                relem[s][v] += double(sF[v*Cfg::NFMAX + fL])*multL;
-                relem[s][v] += double(sF[v*Cfg::NFMAX + fR])*multR;
+                relem[s][v] += sF[v*Cfg::NFMAX + fL]*multL;
+                relem[s][v] += sF[v*Cfg::NFMAX + fR]*multR;
             }
         }
         __syncthreads();
     }
 
     template <class Cfg>
-    __global__ void __launch_bounds__(Cfg::NT)
+    __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
     flux_div_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ GeomK G,
                     const __grid_constant__ YTabT<Cfg::STRETCH> Y, const __grid_constant__ SchemeK SK, const FluxArgs A)
     {
@@ -613,8 +611,8 @@ namespace gbns
         float* soa = reinterpret_cast<float*>(smem_raw + 128 + Cfg::STAGE_BYTES);
         unsigned char* tail = smem_raw + 128 + Cfg::STAGE_BYTES + Cfg::SOA_BYTES;
         Real* der = Cfg::REUSE ? reinterpret_cast<Real*>(stage) : reinterpret_cast<Real*>(tail);
-        Real* sF  = Cfg::REUSE ? reinterpret_cast<Real*>(reinterpret_cast<unsigned char*>(stage) + Cfg::DER_BYTES)
-                               : reinterpret_cast<Real*>(tail + Cfg::DER_BYTES);
+        double* sF = Cfg::REUSE ? reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(stage) + Cfg::DER_BYTES)
+                                : reinterpret_cast<double*>(tail + Cfg::DER_BYTES);
 
         const int tid = threadIdx.x;
         const int lb = blockIdx.y;
@@ -630,7 +628,39 @@ namespace gbns
         const int ys = j0 - H + G.ng, zs = k0 - H + G.ng;
 
         // ---- stage the tile + halo --------------------------------------
-        if (A.use_tma)
+        if constexpr (Cfg::DIRECT)
+        {
+            // Only the cells some face reads: the tile, the stencil cross of
+            // radius max(HC, 1), and the edge cells one step out in two
+            // directions (transverse neighbours of the viscous gradient).
+            constexpr int R1 = Cfg::HC > 1 ? Cfg::HC : 1;
+            const double* base = A.prims + (long long)lb*G.bstride;
+            for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
+            {
+                const int bx = c % Cfg::BXE, by = (c / Cfg::BXE) % Cfg::BY, bz = c / (Cfg::BXE*Cfg::BY);
+                const int rx = bx - shift - H, ry = by - H, rz = bz - H;
+                const int ox = rx < 0 ? -rx : (rx >= TX ? rx - TX + 1 : 0);
+                const int oy = ry < 0 ? -ry : (ry >= TY ? ry - TY + 1 : 0);
+                const int oz = rz < 0 ? -rz : (rz >= TZ ? rz - TZ + 1 : 0);
+                const int nout = (ox > 0) + (oy > 0) + (oz > 0);
+                const int omax = ox > oy ? (ox > oz ? ox : oz) : (oy > oz ? oy : oz);
+                const bool need = nout == 0 || (nout == 1 && omax <= R1) || (nout == 2 && omax == 1);
+                if (!need) continue;
+                const int X = xs + bx, Y_ = ys + by, Z = zs + bz;
+                if (X < G.ni && Y_ < G.nj && Z < G.nk)
+                {
+                    const double* src = base + ((long long)(Z*G.nj + Y_)*G.ni + X)*5;
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = float(__ldg(src + v));
+                }
+                else
+                {
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = 0.0f;
+                }
+            }
+        }
+        else if (A.use_tma)
         {
             if (tid == 0) mbar_init(bar, 1);
             __syncthreads();
@@ -683,8 +713,8 @@ namespace gbns
         }
         __syncthreads();
 
-        // ---- FP32: convert the staged box to SoA floats -------------------
-        if constexpr (!Cfg::FP64)
+        // ---- FP32 staged: convert the box to SoA floats -------------------
+        if constexpr (!Cfg::FP64 && !Cfg::DIRECT)
         {
             for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
             {
@@ -740,6 +770,6 @@ namespace gbns
             #pragma unroll
             for (int v = 0; v < 5; ++v) r[v] = relem[s][v];
         }
-        if (A.use_tma && tid == 0) mbar_inval(bar);
+        if (!Cfg::DIRECT && A.use_tma && tid == 0) mbar_inval(bar);
     }
 }

@@ -312,7 +312,8 @@ extern "C"
             if (rc) return rc;
             Y = &ytab;
         }
-        return launch_flux_div(grid, G, Y, S, scheme, prims, rhs, increment, static_cast<cudaStream_t>(stream), 0);
+        return launch_flux_div(grid, G, Y, S, scheme, prims, rhs, increment, static_cast<cudaStream_t>(stream),
+                               scheme->tile_variant);
     }
 
     int gbns_flux_div_variant(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
