@@ -45,6 +45,10 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=3)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp32", action="store_true", help="skip the FP32-flux side measurement")
+    p.add_argument("--no-forms", action="store_true", help="skip the batched and serving measurements")
+    p.add_argument("--batch-instances", type=int, default=96)
+    p.add_argument("--batch-steps", type=int, default=10)
+    p.add_argument("--serve-requests", type=int, default=24)
     return p.parse_args()
 
 
@@ -271,6 +275,94 @@ def _read_traffic(cells):
 
 
 # ---------------------------------------------------------------------------
+# batched form: 96 Taylor-Green instances of uneven size in one batch
+# ---------------------------------------------------------------------------
+BLOCK_ARRANGEMENTS = {1: (1, 1, 1), 2: (2, 1, 1), 4: (2, 2, 1), 8: (2, 2, 2), 16: (4, 2, 2), 32: (4, 4, 2), 64: (4, 4, 4)}
+
+
+def batch_instances(n, seed=0):
+    """Seeded instance mix: blocks of 16^3 in {1,...,64}, Re log-uniform in
+    [100, 3000], Mach uniform in [0.05, 0.4]."""
+    import numpy as np
+    r = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        nb = int(r.choice(list(BLOCK_ARRANGEMENTS)))
+        re = float(math.exp(r.uniform(math.log(100.0), math.log(3000.0))))
+        ma = float(r.uniform(0.05, 0.4))
+        out.append((BLOCK_ARRANGEMENTS[nb], re, ma))
+    return out
+
+
+def run_batch_form(args):
+    import torch
+    from spade_gb300 import _abi, _native, workloads
+    from spade_gb300.batch import batch_t
+    lib = _native.lib()
+    st = int(torch.cuda.current_stream().cuda_stream)
+    mix = batch_instances(args.batch_instances, seed=1)
+    probs = []
+    for i, (nb, re, ma) in enumerate(mix):
+        probs.append(workloads.taylor_green(nblk=nb, ncell=(16, 16, 16), ng=2, mach=ma, reynolds=re, seed=i, rng="torch"))
+    cells = sum(p.grid.get_grid_size() for p in probs)
+    out = {"workload": "96 Taylor-Green instances, 16^3 blocks, blocks per instance from {1,...,64}, Re log-uniform "
+                       "[100,3000], Mach uniform [0.05,0.4]", "instances": len(probs), "cells": cells,
+           "steps": args.batch_steps}
+    for name, prec in (("fp64", _abi.PREC_FP64), ("fp32_flux", _abi.PREC_FP32_FLUX)):
+        budget = sum(batch_t.instance_bytes(p.q.desc()) for p in probs) + (256 << 20)
+        b = batch_t(budget, prec, True)
+        for p in probs:
+            b.add(p.q.desc(), p.scheme_desc(prec), p.bc_desc(), p.dt, p.q.ptr())
+        b.step(2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.step(args.batch_steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.batch_steps
+        out[name] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms,
+                     "launches_per_step": 9, "graph": True}
+        b.close()
+    # the same instances one grid at a time (one gbns_ssprk3_step per instance)
+    works = [torch.zeros(3 * p.q.data.numel(), dtype=torch.float64, device="cuda") for p in probs]
+    descs = [(p.q.desc(), p.scheme_desc(_abi.PREC_FP64), p.bc_desc(), p.q.ptr(), w.data_ptr(), ctypes.c_double(p.dt))
+             for p, w in zip(probs, works)]
+    def one_step():
+        for g, sc, bc, qp, wp, dt in descs:
+            _native.check(lib.gbns_ssprk3_step(g, sc, bc, qp, wp, dt, st))
+    one_step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(max(1, args.batch_steps // 2)):
+        one_step()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.batch_steps // 2)
+    out["fp64_one_grid_at_a_time"] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms,
+                                      "launches_per_step": 9 * len(probs)}
+    out["fp32_batched_vs_fp64_plain"] = out["fp32_flux"]["cell_steps_per_s"] / out["fp64_one_grid_at_a_time"]["cell_steps_per_s"]
+    del probs, works
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_serve_form(args):
+    import torch
+    from spade_gb300 import _abi, serve
+    reqs = serve.poisson_requests(args.serve_requests, rate=40.0, seed=3)
+    srv = serve.server_t(_abi.PREC_FP32_FLUX, hbm_budget=150 << 30, chunk=32, health_every=8)
+    stats = srv.run(reqs)
+    srv.close()
+    torch.cuda.empty_cache()
+    stats["workload"] = ("%d requests, Poisson arrivals 40/s, 70%% Taylor-Green / 30%% channel, edges {16,32,64,128}, "
+                         "steps U[100,2000], Re log-U[100,3000], Mach U[0.05,0.4], 150 GB HBM budget" % len(reqs))
+    stats["precision"] = "fp32_flux"
+    return stats
+
+
+# ---------------------------------------------------------------------------
 # CPU baseline: the oracle restatement on the host cores, bounded sample
 # ---------------------------------------------------------------------------
 def cpu_sample(steps=1, nblk=(2, 2, 2), ncell=(32, 32, 32), threads=0):
@@ -332,14 +424,15 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_sample(steps=1, nblk=(4, 4, 2))
         warm = max(0, min(args.warmup, 1))
         for _ in range(warm):
-            cpu_sample(steps=1, nblk=(2, 2, 2))
+            cpu_sample(steps=1, nblk=(4, 4, 2))
         vals = []
+        cb = None
         t0 = time.perf_counter()
         for _ in range(max(1, args.steps)):
-            vals.append(cpu_sample(steps=1, nblk=(2, 2, 2))["value"])
+            cb = cpu_sample(steps=1, nblk=(4, 4, 2))
+            vals.append(cb["value"])
             if time.perf_counter() - t0 > 120:
                 break
         v = statistics.median(vals)
@@ -348,8 +441,8 @@ def main():
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": cfg,
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
-                                 "sample": "per step: 1 SSPRK3 step on a 2x2x2-block sub-box of 32^3 cells "
-                                           "(262144 cells) of the channel workload; the reference's CPU path cannot "
+                                 "sample": "per step: 1 SSPRK3 step on a 4x4x2-block sub-box of 32^3 cells "
+                                           "(1048576 cells) of the channel workload; the reference's CPU path cannot "
                                            "be built on the GPU host (its sources are absent there), so the oracle "
                                            "restatement oracle/gbns_oracle.c (bit-exact to the reference on the "
                                            "pinned schemes) runs on all host cores"},
@@ -366,6 +459,10 @@ def main():
     value = cells_all * args.steps / (r["ms"] * 1e-3)
     if rank != 0:
         return
+    forms = {}
+    if not args.no_forms:
+        forms["batch_form"] = run_batch_form(args)
+        forms["serve_form"] = run_serve_form(args)
     cpu = None
     if world == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(steps=1, nblk=(4, 4, 2))
@@ -391,6 +488,7 @@ def main():
         "fp32_flux": r["fp32"],
         "autotune": r["tuned"],
     }
+    line.update(forms)
     if cpu is not None:
         line["cpu_baseline"] = cpu
     print(json.dumps(line))

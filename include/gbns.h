@@ -255,6 +255,43 @@ int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                      const gbns_bc_desc* bc, double* prims, double* work,
                      double dt, void* stream);
 
+/* ---- batched form ----------------------------------------------------
+ * Many independent grids ("instances") of uneven size advanced together:
+ * each SSPRK3 stage is one persistent flux launch per kernel class (walking a
+ * device work-list of tiles of every instance), one batched RK-stage launch
+ * and one batched ghost fill; with use_graph the nine-launch step is captured
+ * once in a CUDA graph and replayed.  Instance state stays resident in an
+ * arena of hbm_budget_bytes allocated at creation; adding an instance that
+ * does not fit returns GBNS_ERR_CAPACITY.  Every instance's result is
+ * bit-identical to advancing it alone (gbns_ssprk3_step).  Supported kernel
+ * classes: cent_keep<2>, totani_lr, fweno_t and WENO5 on identity grids,
+ * WENO5 on stretched-y grids; precision GBNS_PREC_FP64 or GBNS_PREC_FP32_FLUX
+ * (one per batch).  All calls are ordered on the batch's stream.
+ * No counterpart in the reference (its integrator advances one grid,
+ * time-integration/integrator.h:52-55). */
+typedef struct gbns_batch gbns_batch;
+
+int gbns_batch_create(gbns_batch** batch, size_t hbm_budget_bytes, int precision, int use_graph, void* stream);
+int gbns_batch_destroy(gbns_batch* batch);
+
+/* Adds an instance; `prims` (device or pinned host pointer) holds its AoS5
+ * initial state, copied in; ghosts are refilled.  dt is its fixed step. */
+int gbns_batch_add(gbns_batch* batch, const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                   const gbns_bc_desc* bc, double dt, const double* prims, int* slot);
+int gbns_batch_remove(gbns_batch* batch, int slot);
+
+/* Advances every active instance by nsteps SSPRK3 steps (asynchronous). */
+int gbns_batch_step(gbns_batch* batch, int nsteps);
+
+/* Device pointer to an instance's AoS5 state (owned by the batch) and its step count. */
+int gbns_batch_state(gbns_batch* batch, int slot, double** prims, long long* steps_done);
+
+/* Arena bytes in use / budget, active instances, interior cells. */
+int gbns_batch_usage(gbns_batch* batch, size_t* bytes_used, size_t* bytes_budget, int* active, long long* cells);
+
+/* Arena bytes one instance of this grid occupies (state + 3 residuals); 0 if invalid. */
+size_t gbns_batch_instance_bytes(const gbns_grid_desc* grid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,6 +42,15 @@ def lib():
     L.gbns_reduce_noalloc.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, vp]
     L.gbns_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double, vp]
     L.gbns_device_status.argtypes = [P(ctypes.c_int), ctypes.c_int, vp]
+    L.gbns_batch_create.argtypes = [P(vp), ctypes.c_size_t, ctypes.c_int, ctypes.c_int, vp]
+    L.gbns_batch_destroy.argtypes = [vp]
+    L.gbns_batch_add.argtypes = [vp, P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), ctypes.c_double, vp, P(ctypes.c_int)]
+    L.gbns_batch_remove.argtypes = [vp, ctypes.c_int]
+    L.gbns_batch_step.argtypes = [vp, ctypes.c_int]
+    L.gbns_batch_state.argtypes = [vp, ctypes.c_int, P(vp), P(ctypes.c_longlong)]
+    L.gbns_batch_usage.argtypes = [vp, P(ctypes.c_size_t), P(ctypes.c_size_t), P(ctypes.c_int), P(ctypes.c_longlong)]
+    L.gbns_batch_instance_bytes.argtypes = [P(_abi.GridDesc)]
+    L.gbns_batch_instance_bytes.restype = ctypes.c_size_t
     if L.gbns_version() != _abi.ABI_VERSION:
         raise SpadeError(_abi.ERR_UNSUPPORTED, "libgbns ABI version mismatch")
     _LIB = L

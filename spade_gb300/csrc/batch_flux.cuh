@@ -1,0 +1,78 @@
+// Persistent flux-divergence kernels of the batched form.  Each TU defines
+// GBNS_REAL, GBNS_TAG, GBNS_FP32 and GBNS_BATCH_FN and includes this.
+#pragma once
+
+#include "flux_kernel.cuh"
+#include "batch_internal.cuh"
+
+namespace gbns
+{
+    namespace
+    {
+        status_registrar tu_status_registrar;
+
+        // CTAs loop over their class's range of the tile list; the arrays
+        // are read through the instance descriptors (no TMA: the halo is
+        // staged with coalesced loads, or straight into FP32 for FP32-flux).
+        template <class Cfg>
+        __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
+        flux_batch_kernel(const TileItem* __restrict__ items, const int* __restrict__ offsets,
+                          const int* __restrict__ counts, const InstK* __restrict__ insts,
+                          const YTabK* __restrict__ ytabs, const int cls, const int stage)
+        {
+            extern __shared__ __align__(128) unsigned char smem_raw[];
+            const int base = offsets[cls];
+            const int n = counts[cls];
+            for (int it = blockIdx.x; it < n; it += gridDim.x)
+            {
+                const TileItem w = items[base + it];
+                const InstK& I = insts[w.inst];
+                FluxArgs A;
+                A.prims = I.q;
+                A.rhs = I.R[stage];
+                A.increment = 0;
+                A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
+                A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
+                A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
+                A.use_tma = 0;
+                if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, I.G, ytabs[I.ytab], I.S, A, w.lb, w.tile);
+                else flux_tile<Cfg>(smem_raw, nullptr, I.G, YTabNone{}, I.S, A, w.lb, w.tile);
+                __syncthreads();
+            }
+        }
+
+        template <class Cfg>
+        int run_batch(const TileItem* items, const int* offsets, const int* counts, const InstK* insts,
+                      const YTabK* ytabs, int cls, int stage, cudaStream_t st)
+        {
+            auto kern = flux_batch_kernel<Cfg>;
+            int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM_BYTES)),
+                                "flux_batch smem attribute");
+            if (rc) return rc;
+            kern<<<persistent_grid(Cfg::MINB), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, cls, stage);
+            return check_cuda(cudaGetLastError(), "flux_batch launch");
+        }
+    }
+
+#define GBNS_BRUN(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
+    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, cls, stage, st)
+
+    int GBNS_BATCH_FN(int cls, const TileItem* items, const int* offsets, const int* counts,
+                      const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st)
+    {
+        switch (cls)
+        {
+            case BCLASS_CK2_ID:    GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, 256);
+            case BCLASS_TOTANI_ID: GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, 256);
+            case BCLASS_FWENO_ID:  GBNS_BRUN(GBNS_CONV_FWENO, 2, false, 8, 8, 8, 256);
+#if GBNS_FP32
+            case BCLASS_WENO5_ST:  GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 4, 256);
+            case BCLASS_WENO5_ID:  GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 4, 256);
+#else
+            case BCLASS_WENO5_ST:  GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 256);
+            case BCLASS_WENO5_ID:  GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 256);
+#endif
+        }
+        return set_error(GBNS_ERR_UNSUPPORTED, "no batched kernel for this class");
+    }
+}

@@ -1,0 +1,68 @@
+// Batched form: many independent grids advanced together.
+//
+// Every active grid ("instance") has a descriptor InstK in device memory.
+// Work is described by device work-lists that the host rebuilds when the set
+// of instances changes:
+//   * tile items (instance, block, tile), grouped by kernel class (the
+//     compile-time flux configuration: convective scheme, coordinates);
+//   * block items (instance, block) for the RK stage and the ghost fill.
+// Persistent kernels (one CTA per SM slot) walk the lists; counts and
+// offsets are read from device memory, so a captured CUDA graph of one step
+// stays valid while instances come and go.
+#pragma once
+
+#include "gbns_internal.cuh"
+
+namespace gbns
+{
+    struct BcK
+    {
+        int kind[6];
+        double t_wall[6];
+    };
+
+    struct InstK
+    {
+        GeomK G;
+        SchemeK S;
+        BcK bc;
+        double* q;          // primitive state, AoS5 with ghosts
+        double* R[3];       // SSPRK3 residuals
+        double dt;
+        int ytab;           // index into the Y-metric table array, -1 for identity
+        int pad;
+    };
+
+    struct TileItem { int inst, lb, tile, pad; };
+    struct BlockItem { int inst, lb; };
+
+    // Kernel classes of the batched flux launch.
+    enum batch_class
+    {
+        BCLASS_CK2_ID = 0,     // cent_keep<2>, identity coordinates (Taylor-Green)
+        BCLASS_TOTANI_ID,      // totani_lr, identity
+        BCLASS_FWENO_ID,       // fweno_t, identity
+        BCLASS_WENO5_ST,       // WENO5, stretched y (channel)
+        BCLASS_WENO5_ID,       // WENO5, identity
+        BCLASS_COUNT
+    };
+
+    // Returns the class of a (grid, scheme) pair or -1 if it has no batched kernel.
+    int batch_class_of(const gbns_grid_desc* g, const gbns_scheme_desc* s);
+
+    // Tile shape of a class (for counting tiles per block on the host).
+    void batch_class_tile(int cls, int precision, int tile[3]);
+
+    // Persistent flux launch of one class for one SSPRK3 stage.  `offsets`
+    // and `counts` (device, BCLASS_COUNT ints) locate the class's items.
+    int launch_flux_batch_f64x(int cls, const TileItem* items, const int* offsets, const int* counts,
+                               const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
+    int launch_flux_batch_f32(int cls, const TileItem* items, const int* offsets, const int* counts,
+                              const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
+
+    // Batched RK stage (stage 0, 1, 2 of ssprk3_t) and ghost fill.
+    int launch_rk_batch(const BlockItem* items, const int* count, const InstK* insts, int stage, cudaStream_t st);
+    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, cudaStream_t st);
+
+    int persistent_grid(int ctas_per_sm);
+}

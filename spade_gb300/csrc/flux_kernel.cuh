@@ -598,14 +598,16 @@ namespace gbns
         __syncthreads();
     }
 
+    // One tile of one block: the whole per-CTA algorithm.  Called by the
+    // per-grid kernel (one CTA per tile) and by the persistent batch kernel
+    // (CTAs loop over a work-list of tiles of many grids).
     template <class Cfg>
-    __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
-    flux_div_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ GeomK G,
-                    const __grid_constant__ YTabT<Cfg::STRETCH> Y, const __grid_constant__ SchemeK SK, const FluxArgs A)
+    __device__ __forceinline__ void flux_tile(unsigned char* smem_raw, const CUtensorMap* tmap, const GeomK& G,
+                                              const YTabT<Cfg::STRETCH>& Y, const SchemeK& SK, const FluxArgs& A,
+                                              const int lb, const int tile)
     {
         using Real = typename Cfg::Real;
         constexpr int TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ, H = Cfg::H;
-        extern __shared__ __align__(128) unsigned char smem_raw[];
         uint64_t* bar = reinterpret_cast<uint64_t*>(smem_raw);
         double* stage = reinterpret_cast<double*>(smem_raw + 128);
         float* soa = reinterpret_cast<float*>(smem_raw + 128 + Cfg::STAGE_BYTES);
@@ -615,8 +617,6 @@ namespace gbns
                                 : reinterpret_cast<double*>(tail + Cfg::DER_BYTES);
 
         const int tid = threadIdx.x;
-        const int lb = blockIdx.y;
-        const int tile = blockIdx.x;
         const int tx = tile % A.ntile[0];
         const int ty = (tile / A.ntile[0]) % A.ntile[1];
         const int tz = tile / (A.ntile[0]*A.ntile[1]);
@@ -667,7 +667,7 @@ namespace gbns
             if (tid == 0)
             {
                 mbar_expect_tx(bar, uint32_t(Cfg::BOXN)*5u*8u);
-                tma_load_4d(stage, &tmap, bar, xs*5, ys, zs, lb);
+                tma_load_4d(stage, tmap, bar, xs*5, ys, zs, lb);
             }
             const bool ok = mbar_wait(bar, 0, MBAR_POLL_LIMIT);
             if (__syncthreads_or(!ok))
@@ -771,5 +771,14 @@ namespace gbns
             for (int v = 0; v < 5; ++v) r[v] = relem[s][v];
         }
         if (!Cfg::DIRECT && A.use_tma && tid == 0) mbar_inval(bar);
+    }
+
+    template <class Cfg>
+    __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
+    flux_div_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ GeomK G,
+                    const __grid_constant__ YTabT<Cfg::STRETCH> Y, const __grid_constant__ SchemeK SK, const FluxArgs A)
+    {
+        extern __shared__ __align__(128) unsigned char smem_raw[];
+        flux_tile<Cfg>(smem_raw, &tmap, G, Y, SK, A, int(blockIdx.y), int(blockIdx.x));
     }
 }

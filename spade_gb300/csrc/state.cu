@@ -4,23 +4,82 @@
 #include <mutex>
 #include <vector>
 #include "gbns_internal.cuh"
+#include "batch_internal.cuh"
 
 namespace gbns
 {
     // ------------------------------------------------------------------
     // ghost fill
     // ------------------------------------------------------------------
-    struct BcK
-    {
-        int kind[6];
-        double t_wall[6];
-    };
 
-    // One thread per padded cell; interior cells return at once.  Every
+    // Fills ghost cell (ii, jj, kk) (padded indices) of block lb.  Every
     // ghost value is resolved to an INTERIOR donor cell (mirror across wall
     // faces first, boundary_fill.h:113-114, then the block exchange with
     // periodic wrap, get_transaction.h:55-87 / exchange_config.h:336-344),
     // so one launch fills every ghost layer without ordering hazards.
+    // Interior cells are left alone.
+    __device__ __forceinline__ void fill_one_ghost(double* __restrict__ q, const GeomK& G, const BcK& bc,
+                                                   const int lb, const int ii, const int jj, const int kk)
+    {
+        int c[3] = {ii - G.ng, jj - G.ng, kk - G.ng};
+        if (c[0] >= 0 && c[0] < G.n[0] && c[1] >= 0 && c[1] < G.n[1] && c[2] >= 0 && c[2] < G.n[2]) return;
+        int b[3] = {lb % G.nb[0], (lb / G.nb[0]) % G.nb[1], lb / (G.nb[0]*G.nb[1])};
+        int walls[3];
+        int nwall = 0;
+        #pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+            int face = -1;
+            if (c[d] < 0 && b[d] == 0) face = 2*d;
+            if (c[d] >= G.n[d] && b[d] == G.nb[d] - 1) face = 2*d + 1;
+            if (face < 0) continue;
+            const int kind = bc.kind[face];
+            if (kind == GBNS_BC_ISOTHERMAL_NOSLIP || kind == GBNS_BC_SLIP_ADIABATIC)
+            {
+                c[d] = (face % 2 == 0) ? -1 - c[d] : 2*G.n[d] - (c[d] + 1);
+                walls[nwall++] = face;
+            }
+        }
+        #pragma unroll
+        for (int d = 0; d < 3; ++d)
+        {
+            int o = 0;
+            if (c[d] < 0) o = -1;
+            else if (c[d] >= G.n[d]) o = 1;
+            if (o == 0) continue;
+            const bool at_min = b[d] == 0, at_max = b[d] == G.nb[d] - 1;
+            if ((o < 0 && at_min && bc.kind[2*d] != GBNS_BC_PERIODIC) ||
+                (o > 0 && at_max && bc.kind[2*d + 1] != GBNS_BC_PERIODIC)) return;   // left untouched (GBNS_BC_NONE)
+            b[d] += o;
+            if (b[d] < 0) b[d] += G.nb[d];
+            if (b[d] >= G.nb[d]) b[d] -= G.nb[d];
+            c[d] -= o*G.n[d];
+        }
+        const int lbs = b[0] + G.nb[0]*(b[1] + G.nb[1]*b[2]);
+        const double* s = q + (long long)lbs*G.bstride +
+            ((long long)((c[2] + G.ng)*G.nj + (c[1] + G.ng))*G.ni + (c[0] + G.ng))*5;
+        double val[5];
+        #pragma unroll
+        for (int v = 0; v < 5; ++v) val[v] = s[v];
+        for (int w = 0; w < nwall; ++w)
+        {
+            const int face = walls[w];
+            if (bc.kind[face] == GBNS_BC_ISOTHERMAL_NOSLIP)
+            {
+                val[1] = 2.0*bc.t_wall[face] - val[1];
+                val[2] = -val[2]; val[3] = -val[3]; val[4] = -val[4];
+            }
+            else
+            {
+                val[2 + face/2] = -val[2 + face/2];
+            }
+        }
+        double* dst = q + (long long)lb*G.bstride + ((long long)(kk*G.nj + jj)*G.ni + ii)*5;
+        #pragma unroll
+        for (int v = 0; v < 5; ++v) dst[v] = val[v];
+    }
+
+    // One thread per padded cell; interior cells return at once.
     __global__ void __launch_bounds__(256)
     fill_ghosts_kernel(double* __restrict__ q, const __grid_constant__ GeomK G, const BcK bc)
     {
@@ -34,64 +93,7 @@ namespace gbns
             const int kk = int(rem / ((long long)G.ni*G.nj));
             const int jj = int((rem / G.ni) % G.nj);
             const int ii = int(rem % G.ni);
-            int c[3] = {ii - G.ng, jj - G.ng, kk - G.ng};
-            if (c[0] >= 0 && c[0] < G.n[0] && c[1] >= 0 && c[1] < G.n[1] && c[2] >= 0 && c[2] < G.n[2]) continue;
-            int b[3] = {lb % G.nb[0], (lb / G.nb[0]) % G.nb[1], lb / (G.nb[0]*G.nb[1])};
-            int walls[3];
-            int nwall = 0;
-            #pragma unroll
-            for (int d = 0; d < 3; ++d)
-            {
-                int face = -1;
-                if (c[d] < 0 && b[d] == 0) face = 2*d;
-                if (c[d] >= G.n[d] && b[d] == G.nb[d] - 1) face = 2*d + 1;
-                if (face < 0) continue;
-                const int kind = bc.kind[face];
-                if (kind == GBNS_BC_ISOTHERMAL_NOSLIP || kind == GBNS_BC_SLIP_ADIABATIC)
-                {
-                    c[d] = (face % 2 == 0) ? -1 - c[d] : 2*G.n[d] - (c[d] + 1);
-                    walls[nwall++] = face;
-                }
-            }
-            bool ok = true;
-            #pragma unroll
-            for (int d = 0; d < 3; ++d)
-            {
-                int o = 0;
-                if (c[d] < 0) o = -1;
-                else if (c[d] >= G.n[d]) o = 1;
-                if (o == 0) continue;
-                const bool at_min = b[d] == 0, at_max = b[d] == G.nb[d] - 1;
-                if ((o < 0 && at_min && bc.kind[2*d] != GBNS_BC_PERIODIC) ||
-                    (o > 0 && at_max && bc.kind[2*d + 1] != GBNS_BC_PERIODIC)) { ok = false; break; }
-                b[d] += o;
-                if (b[d] < 0) b[d] += G.nb[d];
-                if (b[d] >= G.nb[d]) b[d] -= G.nb[d];
-                c[d] -= o*G.n[d];
-            }
-            if (!ok) continue;   // ghost left untouched (GBNS_BC_NONE)
-            const int lbs = b[0] + G.nb[0]*(b[1] + G.nb[1]*b[2]);
-            const double* s = q + (long long)lbs*G.bstride +
-                ((long long)((c[2] + G.ng)*G.nj + (c[1] + G.ng))*G.ni + (c[0] + G.ng))*5;
-            double val[5];
-            #pragma unroll
-            for (int v = 0; v < 5; ++v) val[v] = s[v];
-            for (int w = 0; w < nwall; ++w)
-            {
-                const int face = walls[w];
-                if (bc.kind[face] == GBNS_BC_ISOTHERMAL_NOSLIP)
-                {
-                    val[1] = 2.0*bc.t_wall[face] - val[1];
-                    val[2] = -val[2]; val[3] = -val[3]; val[4] = -val[4];
-                }
-                else
-                {
-                    val[2 + face/2] = -val[2 + face/2];
-                }
-            }
-            double* dst = q + idx*5;
-            #pragma unroll
-            for (int v = 0; v < 5; ++v) dst[v] = val[v];
+            fill_one_ghost(q, G, bc, lb, ii, jj, kk);
         }
     }
 
@@ -130,6 +132,35 @@ namespace gbns
         double gamma, R, gm1;
     };
 
+    // transform_advance_to for one cell at offset `off` (advance.h:75-101,
+    // fluid_state.h:151-184): prim -> cons, cons += coeff_j R_j, cons -> prim.
+    template <int NRES>
+    __device__ __forceinline__ void rk_update_cell(double* __restrict__ q, const double* const* res,
+                                                   const double* coeff, const double R, const double gm1,
+                                                   const long long off)
+    {
+        double* qq = q + off;
+        const double p = qq[0], T = qq[1], u = qq[2], v = qq[3], w = qq[4];
+        const double rho = p/(R*T);
+        const double rhoU2 = rho*(u*u + v*v + w*w);
+        const double rhoE = 0.5*rhoU2 + (p/(gm1));
+        double c[5] = {rho, rhoE, rho*u, rho*v, rho*w};
+        #pragma unroll
+        for (int r = 0; r < NRES; ++r)
+        {
+            const double* rr = res[r] + off;
+            #pragma unroll
+            for (int s = 0; s < 5; ++s) c[s] += coeff[r]*rr[s];
+        }
+        const double rh = c[0];
+        const double invrho = 1.0/rh;
+        const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
+        const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
+        const double pp = gm1*(c[1] - 0.5*ru2);
+        const double TT = pp/(R*rh);
+        qq[0] = pp; qq[1] = TT; qq[2] = uu; qq[3] = vv; qq[4] = ww;
+    }
+
     template <int NRES>
     __global__ void __launch_bounds__(256)
     rk_stage_kernel(double* __restrict__ q, const __grid_constant__ GeomK G, const RkK k)
@@ -146,28 +177,7 @@ namespace gbns
             const int i_ = int(rem % G.n[0]);
             const long long off = (long long)lb*G.bstride +
                 ((long long)((k_ + G.ng)*G.nj + (j_ + G.ng))*G.ni + (i_ + G.ng))*5;
-            double* qq = q + off;
-            const double p = qq[0], T = qq[1], u = qq[2], v = qq[3], w = qq[4];
-            // prim -> cons (fluid_state.h:151-165)
-            const double rho = p/(k.R*T);
-            const double rhoU2 = rho*(u*u + v*v + w*w);
-            const double rhoE = 0.5*rhoU2 + (p/(k.gm1));
-            double c[5] = {rho, rhoE, rho*u, rho*v, rho*w};
-            #pragma unroll
-            for (int r = 0; r < NRES; ++r)
-            {
-                const double* rr = k.res[r] + off;
-                #pragma unroll
-                for (int s = 0; s < 5; ++s) c[s] += k.coeff[r]*rr[s];
-            }
-            // cons -> prim (fluid_state.h:167-184)
-            const double rh = c[0];
-            const double invrho = 1.0/rh;
-            const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
-            const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
-            const double pp = k.gm1*(c[1] - 0.5*ru2);
-            const double TT = pp/(k.R*rh);
-            qq[0] = pp; qq[1] = TT; qq[2] = uu; qq[3] = vv; qq[4] = ww;
+            rk_update_cell<NRES>(q, k.res, k.coeff, k.R, k.gm1, off);
         }
     }
 
@@ -190,6 +200,75 @@ namespace gbns
             default: rk_stage_kernel<4><<<grid, 256, 0, stream>>>(prims, G, k); break;
         }
         return check_cuda(cudaGetLastError(), "rk_stage launch");
+    }
+
+    // ------------------------------------------------------------------
+    // batched forms: one CTA per (instance, block) item of a device list
+    // ------------------------------------------------------------------
+    int persistent_grid(int ctas_per_sm)
+    {
+        return sm_count()*ctas_per_sm;
+    }
+
+    template <int NRES>
+    __global__ void __launch_bounds__(256)
+    rk_batch_kernel(const BlockItem* __restrict__ items, const int* __restrict__ count, const InstK* __restrict__ insts)
+    {
+        const int n = *count;
+        for (int it = blockIdx.x; it < n; it += gridDim.x)
+        {
+            const BlockItem w = items[it];
+            const InstK& I = insts[w.inst];
+            const GeomK& G = I.G;
+            const double dt = I.dt;
+            // ratio_diff_t of consecutive ssprk3_t rows times dt (advance.h:80-95)
+            double coeff[3];
+            if (NRES == 1) { coeff[0] = (1.0/1.0)*dt; }
+            else if (NRES == 2) { coeff[0] = (-3.0/4.0)*dt; coeff[1] = (1.0/4.0)*dt; }
+            else { coeff[0] = (-1.0/12.0)*dt; coeff[1] = (-1.0/12.0)*dt; coeff[2] = (2.0/3.0)*dt; }
+            const double* res[3] = {I.R[0], I.R[1], I.R[2]};
+            const int ncell = G.n[0]*G.n[1]*G.n[2];
+            for (int c = threadIdx.x; c < ncell; c += blockDim.x)
+            {
+                const int i_ = c % G.n[0], j_ = (c / G.n[0]) % G.n[1], k_ = c / (G.n[0]*G.n[1]);
+                const long long off = (long long)w.lb*G.bstride +
+                    ((long long)((k_ + G.ng)*G.nj + (j_ + G.ng))*G.ni + (i_ + G.ng))*5;
+                rk_update_cell<NRES>(I.q, res, coeff, I.S.R, I.S.gm1, off);
+            }
+        }
+    }
+
+    __global__ void __launch_bounds__(256)
+    ghost_batch_kernel(const BlockItem* __restrict__ items, const int* __restrict__ count, const InstK* __restrict__ insts)
+    {
+        const int n = *count;
+        for (int it = blockIdx.x; it < n; it += gridDim.x)
+        {
+            const BlockItem w = items[it];
+            const InstK& I = insts[w.inst];
+            const GeomK& G = I.G;
+            const int npad = G.ni*G.nj*G.nk;
+            for (int c = threadIdx.x; c < npad; c += blockDim.x)
+            {
+                const int ii = c % G.ni, jj = (c / G.ni) % G.nj, kk = c / (G.ni*G.nj);
+                fill_one_ghost(I.q, G, I.bc, w.lb, ii, jj, kk);
+            }
+        }
+    }
+
+    int launch_rk_batch(const BlockItem* items, const int* count, const InstK* insts, int stage, cudaStream_t st)
+    {
+        const int grid = persistent_grid(8);
+        if (stage == 0) rk_batch_kernel<1><<<grid, 256, 0, st>>>(items, count, insts);
+        else if (stage == 1) rk_batch_kernel<2><<<grid, 256, 0, st>>>(items, count, insts);
+        else rk_batch_kernel<3><<<grid, 256, 0, st>>>(items, count, insts);
+        return check_cuda(cudaGetLastError(), "rk_batch launch");
+    }
+
+    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, cudaStream_t st)
+    {
+        ghost_batch_kernel<<<persistent_grid(8), 256, 0, st>>>(items, count, insts);
+        return check_cuda(cudaGetLastError(), "ghost_batch launch");
     }
 
     // ------------------------------------------------------------------
