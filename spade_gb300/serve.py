@@ -76,7 +76,7 @@ def build_instance(req, precision, seed):
         prob = workloads.taylor_green(nblk=(nb, nb, nb), ncell=(req.block,) * 3, ng=2, mach=req.mach,
                                       reynolds=req.reynolds, seed=seed, rng="torch")
     else:
-        prob = workloads.channel(nblk=(nb, nb, nb), ncell=(req.block,) * 3, ng=3, mach_b=min(req.mach * 2.0, 0.8),
+        prob = workloads.channel(nblk=(nb, nb, nb), ncell=(req.block,) * 3, ng=3, mach_b=req.mach,
                                  re_b=req.reynolds, seed=seed, rng="torch")
     if req.corrupt:
         g = prob.ng

@@ -16,6 +16,14 @@ from . import _abi, algs, boundary, convective, coords, fluid_state, grid as _gr
 from . import omni, pde_algs, state_sensor, viscous, viscous_laws
 
 
+def stable_dt(cfl, dmin, umax, nu_max):
+    """Explicit SSPRK3 time step: the convective CFL limit cfl*dx/max(|u|+a)
+    and the 3-D diffusive limit 0.2*dx^2/nu (SSPRK3 reaches about 2.5 along
+    the negative real axis; the viscous operator's largest eigenvalue is
+    about 12 nu/dx^2), whichever is smaller."""
+    return min(cfl * dmin / umax, 0.2 * dmin * dmin / nu_max)
+
+
 class problem:
     """A grid, its primitive state, the flux functor, BCs and the time step."""
 
@@ -93,7 +101,8 @@ def taylor_green(nblk=(2, 2, 2), ncell=(16, 16, 16), ng=2, mach=0.1, reynolds=16
     flux = omni.compose(conv, viscous.visc_lr(viscous_laws.constant_viscosity_t(mu, prandtl), air))
     dx = min(g.get_dx(0), g.get_dx(1), g.get_dx(2))
     umax = algs.transform_reduce(q, air, algs.reduce_ops.max_wavespeed)
-    dt = cfl * dx / umax
+    rho_min = float((q.interior()[..., 0] / (R * q.interior()[..., 1])).min())
+    dt = stable_dt(cfl, dx, umax, mu / rho_min)
     return problem(name="taylor_green", grid=g, q=q, gas=air, flux=flux, exchange=h, walls={},
                    dt=dt, mu=mu, u0=u0, ng=ng)
 
@@ -150,6 +159,6 @@ def channel(nblk=(8, 8, 8), ncell=(32, 32, 32), ng=3, beta=2.0, mach_b=0.5, re_b
     dydeta_min = beta * (1.0 - math.tanh(beta * s_wall) ** 2) / math.tanh(beta)
     dmin = min(g.get_dx(0), g.get_dx(2), deta * dydeta_min)
     umax = algs.transform_reduce(q, air, algs.reduce_ops.max_wavespeed)
-    dt = cfl * dmin / umax
+    dt = stable_dt(cfl, dmin, umax, mu_ref / rho_b)
     return problem(name="channel", grid=g, q=q, gas=air, flux=flux, exchange=h, walls=walls,
                    dt=dt, mu=mu_ref, u0=U_b, ng=ng)
