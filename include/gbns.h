@@ -88,6 +88,7 @@ typedef struct gbns_gas_desc
 #define GBNS_DISS_PRESSURE    1   /* convective::pressure_diss_lr (convective.h:194-246) */
 
 #define GBNS_SENSOR_CONST     0   /* state_sensor::const_sensor_t (navier-stokes/state_sensor.h:46-60) */
+#define GBNS_SENSOR_DUCROS    1   /* state_sensor::ducros_t on the face gradient (state_sensor.h:21-43) */
 
 #define GBNS_VISC_NONE        0
 #define GBNS_VISC_LR          1   /* viscous::visc_lr (navier-stokes/viscous.h:13-113) */
@@ -114,7 +115,7 @@ typedef struct gbns_scheme_desc
                               every variant gives bit-identical results */
     int32_t reserved;      /* must be 0 */
     double  eps_p, eps_T;  /* pressure_diss_lr coefficients */
-    double  sensor_alpha;  /* const_sensor_t::alpha */
+    double  sensor_alpha;  /* const_sensor_t::alpha, or ducros_t::epsilon */
     double  mu;            /* constant: mu; power/sutherland: mu_ref */
     double  prandtl;
     double  T_ref;         /* power/sutherland reference temperature */
@@ -241,16 +242,35 @@ int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);
 int gbns_reduce_noalloc(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
                         const double* prims, int kind, double* out_dev, void* stream);
 
+/* flux_div (overwrite mode) fused with the RK stage update that consumes
+ * it: the launch computes R = L(prims) for each tile and, for the same
+ * cells, q_out = prim(cons(prims) + sum_j coeffs[j] R_j) with
+ * R_0..R_{nres-2} = earlier[] and R_{nres-1} = R (transform_advance_to,
+ * time-integration/advance.h:75-101, fused with flux_div_basic.h:17-76).
+ * R is stored to rhs only if write_rhs.  q_out must not alias prims (other
+ * tiles still read their halo from prims); its ghosts are not touched.
+ * Arithmetic identical to gbns_flux_div followed by gbns_rk_stage.
+ * Asynchronous. */
+int gbns_flux_div_rk(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
+                     double* rhs, int write_rhs, int nres, const double* const* earlier,
+                     const double* coeffs, double* q_out, void* stream);
+
+/* dst = src on interior cells, dst's ghost layers filled from src's interior
+ * donors (gbns_fill_ghosts of src, written into dst).  Asynchronous. */
+int gbns_copy_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc, double* dst,
+                          const double* src, void* stream);
+
 /* One full SSPRK3 step with the reference's structure
  * (integrate_advance with state_transform_t, time-integration/advance.h:234-280;
  * ssprk3_t, time-integration/explicit.h:80-88):
- *   R0 = L(q); q <- q + dt R0;             fill ghosts
- *   R1 = L(q); q <- q - 3/4 dt R0 + 1/4 dt R1; fill ghosts
- *   R2 = L(q); q <- q - 1/12 dt R0 - 1/12 dt R1 + 2/3 dt R2; fill ghosts
- * (updates in conservative variables, state kept primitive).  `work` is a
- * caller-owned device buffer of 3 AoS5 arrays (3*gbns_array_size doubles)
- * holding R0..R2 (the reference's integrator_data_t residuals).  prims must
- * have valid ghosts on entry.  Asynchronous. */
+ *   R0 = L(q);  q1 = q + dt R0;                      fill ghosts
+ *   R1 = L(q1); q2 = q1 - 3/4 dt R0 + 1/4 dt R1;     fill ghosts
+ *   R2 = L(q2); q  = q2 - 1/12 dt R0 - 1/12 dt R1 + 2/3 dt R2; fill ghosts
+ * (updates in conservative variables, state kept primitive; bit-identical to
+ * the reference in GBNS_PREC_FP64).  Each stage is one gbns_flux_div_rk
+ * launch plus a ghost fill.  `work` is a caller-owned device buffer of 3
+ * AoS5 arrays (3*gbns_array_size doubles) holding R0, R1 and the
+ * intermediate state.  prims must have valid ghosts on entry.  Asynchronous. */
 int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                      const gbns_bc_desc* bc, double* prims, double* work,
                      double dt, void* stream);

@@ -22,7 +22,7 @@
  *
  * Lowered functors: convective::cent_keep_scheme_t<gas, 2|4|6|8>,
  * convective::totani_lr, convective::fweno_t<gas, smooth>,
- * convective::pressure_diss_lr<gas, state_sensor::const_sensor_t>,
+ * convective::pressure_diss_lr<gas, state_sensor::const_sensor_t | ducros_t>,
  * viscous::visc_lr<viscous_laws::constant_viscosity_t | power_law_t, gas>,
  * and omni::compose of one of each (convective, dissipation, viscous).
  * Coordinates: coords::identity.
@@ -123,6 +123,21 @@ namespace spade::gb300
                 s.dissipation = GBNS_DISS_PRESSURE;
                 s.sensor = GBNS_SENSOR_CONST;
                 s.sensor_alpha = f.scale.alpha;
+                s.eps_p = f.eps_p;
+                s.eps_T = f.eps_T;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename gas_t, typename ft>
+        struct lower<convective::pressure_diss_lr<gas_t, state_sensor::ducros_t<ft>>>
+        {
+            static constexpr int slot = 1;
+            static void apply(gbns_scheme_desc& s, const convective::pressure_diss_lr<gas_t, state_sensor::ducros_t<ft>>& f, bool& g)
+            {
+                s.dissipation = GBNS_DISS_PRESSURE;
+                s.sensor = GBNS_SENSOR_DUCROS;
+                s.sensor_alpha = f.scale.epsilon;   // ducros_t epsilon
                 s.eps_p = f.eps_p;
                 s.eps_T = f.eps_T;
                 set_gas(s, f.gas, g);

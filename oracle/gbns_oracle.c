@@ -235,11 +235,34 @@ static st5 flux_totani(const ctx_t* C, const double* ql, const double* qr, const
     return F;
 }
 
-/* pressure_diss_lr<gas, const_sensor_t>::operator() (convective.h:212-245) */
-static st5 flux_pdiss(const ctx_t* C, const double* ql, const double* qr)
+static void face_grad(const ctx_t* C, int d, int i, int j, int k, double grad[3][5]);
+
+/* state_sensor::ducros_t::get_sensor (navier-stokes/state_sensor.h:21-43)
+ * on the face gradient. */
+static double ducros_sensor(const double grad[3][5], double epsilon)
+{
+    double theta_sq = grad[0][2] + grad[1][3] + grad[2][4];
+    theta_sq *= theta_sq;
+    const double vort0 = grad[1][4] - grad[2][3];
+    const double vort1 = grad[2][2] - grad[0][4];
+    const double vort2 = grad[0][3] - grad[1][2];
+    const double vort_sq = vort0*vort0 + vort1*vort1 + vort2*vort2;
+    return theta_sq / (theta_sq + vort_sq + epsilon);
+}
+
+/* pressure_diss_lr<gas, sensor>::operator() (convective.h:212-245) with
+ * const_sensor_t (sensor_alpha) or ducros_t (epsilon = sensor_alpha). */
+static st5 flux_pdiss(const ctx_t* C, int d, int ci, int cj, int ck, const double* ql, const double* qr)
 {
     const double gam = C->S->gas.gamma, R = C->S->gas.R;
-    const double scl = C->S->sensor_alpha, eps_p = C->S->eps_p, eps_T = C->S->eps_T;
+    const double eps_p = C->S->eps_p, eps_T = C->S->eps_T;
+    double scl = C->S->sensor_alpha;
+    if (C->S->sensor == GBNS_SENSOR_DUCROS)
+    {
+        double grad[3][5];
+        face_grad(C, d, ci, cj, ck, grad);
+        scl = ducros_sensor(grad, C->S->sensor_alpha);
+    }
     const double delta_p = ql[0] - qr[0];
     const double delta_T = ql[1] - qr[1];
     const double pavg = 0.5*(ql[0] + qr[0]);
@@ -428,15 +451,13 @@ static void visc_law(const gbns_scheme_desc* S, double T, double* mu, double* be
     *alpha = S->mu*(S->prandtl_inv > 0.0 ? S->prandtl_inv : 1.0/S->prandtl);
 }
 
-/* visc_lr::operator() (viscous.h:39-79) with the face value and gradient
- * of info_value.h:28-40 / info_gradient.h:61-123.  Face in direction d whose
- * right cell is (i,j,k). */
-static st5 flux_visc(const ctx_t* C, int d, int i, int j, int k, const double n[3])
+/* info::gradient at the face in direction d whose right cell is (i,j,k)
+ * (info_gradient.h:61-123); grad[a][v] for every primitive v. */
+static void face_grad(const ctx_t* C, int d, int i, int j, int k, double grad[3][5])
 {
     const int idir[3] = {d, (d+1)%3, (d+2)%3};
     int ic[3] = {i, j, k};
     ic[d] -= 1;                       /* left cell */
-    double grad[3][5];
     for (int a = 0; a < 3; ++a) for (int v = 0; v < 5; ++v) grad[a][v] = 0.0;
     const double* inv = C->inv_dx;
 #define GBNS_APPLY(iset, coeff) do { const double* qq = cellp(C, ic[0], ic[1], ic[2]); \
@@ -465,6 +486,14 @@ static st5 flux_visc(const ctx_t* C, int d, int i, int j, int k, const double n[
         const double im = 1.0/y_deriv(C->G, eta);
         for (int v = 0; v < 5; ++v) grad[1][v] *= im;
     }
+}
+
+/* visc_lr::operator() (viscous.h:39-79) with the face value of
+ * info_value.h:28-40 and the face gradient above. */
+static st5 flux_visc(const ctx_t* C, int d, int i, int j, int k, const double n[3])
+{
+    double grad[3][5];
+    face_grad(C, d, i, j, k, grad);
     const double* qL = cellp(C, i - (d==0), j - (d==1), k - (d==2));
     const double* qR = cellp(C, i, j, k);
     double qf[5];
@@ -544,7 +573,7 @@ static st5 face_flux(const ctx_t* C, int d, int i, int j, int k)
     }
     if (S->dissipation == GBNS_DISS_PRESSURE)
     {
-        terms[nterm++] = flux_pdiss(C, cellp(C, i - dd[0], j - dd[1], k - dd[2]), cellp(C, i, j, k));
+        terms[nterm++] = flux_pdiss(C, d, i, j, k, cellp(C, i - dd[0], j - dd[1], k - dd[2]), cellp(C, i, j, k));
     }
     if (S->viscous == GBNS_VISC_LR)
     {

@@ -117,6 +117,8 @@ REF_CK6 = 9
 REF_CK8 = 10
 REF_FWENO_NOSMOOTH = 11
 REF_CK2_DISS_VISC = 12
+REF_DUCROS_DISS = 13
+REF_FWENO_DUCROS_VISC = 14
 
 
 def _ref_problem(grid, scheme, bc=None):

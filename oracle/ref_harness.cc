@@ -53,7 +53,9 @@ namespace
         S_CK6         = 9,  // cent_keep<6>
         S_CK8         = 10, // cent_keep<8>
         S_FWENO_NOSMOOTH = 11, // fweno_t<gas, disable_smooth>
-        S_CK2_DISS_VISC  = 12  // compose(cent_keep<2>, pressure_diss_lr(const_sensor), visc_lr(constant))
+        S_CK2_DISS_VISC  = 12, // compose(cent_keep<2>, pressure_diss_lr(const_sensor), visc_lr(constant))
+        S_DUCROS_DISS    = 13, // pressure_diss_lr(ducros_t)
+        S_FWENO_DUCROS_VISC = 14 // compose(fweno_t, pressure_diss_lr(ducros_t), visc_lr(constant))
     };
 
     template <typename func_t>
@@ -64,6 +66,8 @@ namespace
         spade::viscous::visc_lr visc(law, air);
         spade::state_sensor::const_sensor_t<real_t> sens(pb.sensor);
         spade::convective::pressure_diss_lr diss(air, sens, pb.eps_p, pb.eps_T);
+        spade::state_sensor::ducros_t<real_t> ducros(pb.sensor);
+        spade::convective::pressure_diss_lr ddiss(air, ducros, pb.eps_p, pb.eps_T);
         switch (scheme)
         {
             case S_CK2_VISC:    func(spade::omni::compose(spade::convective::cent_keep<2>(air), visc)); break;
@@ -82,6 +86,9 @@ namespace
                 func(spade::convective::fweno_t<gas_t, spade::convective::disable_smooth>(air)); break;
             case S_CK2_DISS_VISC:
                 func(spade::omni::compose(spade::convective::cent_keep<2>(air), diss, visc)); break;
+            case S_DUCROS_DISS: func(ddiss); break;
+            case S_FWENO_DUCROS_VISC:
+                func(spade::omni::compose(spade::convective::fweno_t<gas_t>(air), ddiss, visc)); break;
             default: throw std::runtime_error("unknown scheme id");
         }
     }

@@ -29,6 +29,7 @@ DISS_NONE = 0
 DISS_PRESSURE = 1
 
 SENSOR_CONST = 0
+SENSOR_DUCROS = 1
 
 VISC_NONE = 0
 VISC_LR = 1

@@ -35,6 +35,8 @@ namespace gbns
                 A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
                 A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
                 A.use_tma = 0;
+                A.rk_nres = 0;
+                A.write_rhs = 1;
                 if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, I.G, ytabs[I.ytab], I.S, A, w.lb, w.tile);
                 else flux_tile<Cfg>(smem_raw, nullptr, I.G, YTabNone{}, I.S, A, w.lb, w.tile);
                 __syncthreads();

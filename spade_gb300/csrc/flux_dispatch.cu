@@ -28,11 +28,11 @@ namespace gbns
 
     int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
                         const gbns_scheme_desc* desc, const double* prims, double* rhs,
-                        int increment, cudaStream_t stream, int variant)
+                        int increment, cudaStream_t stream, int variant, const RkFuse* fuse)
     {
         if (variant < 0 || variant >= flux_variant_count(desc))
             return set_error(GBNS_ERR_INVALID, "flux_div tile variant out of range");
-        FluxCall c{g, &G, Y, &S, prims, rhs, increment, stream, variant};
+        FluxCall c{g, &G, Y, &S, prims, rhs, increment, stream, variant, fuse};
         const bool stretch = g->coords != GBNS_COORDS_IDENTITY;
         const bool upwind = desc->convective == GBNS_CONV_FWENO || desc->convective == GBNS_CONV_WENO5;
         const int conv = desc->convective, order = desc->order;

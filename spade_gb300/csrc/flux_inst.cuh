@@ -19,6 +19,20 @@ namespace gbns
         A.prims = c.prims;
         A.rhs = c.rhs;
         A.increment = c.increment;
+        A.rk_nres = 0;
+        A.write_rhs = 1;
+        A.q_out = nullptr;
+        A.rk_res[0] = A.rk_res[1] = nullptr;
+        A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
+        if (c.fuse)
+        {
+            A.rk_nres = c.fuse->nres;
+            A.write_rhs = c.fuse->write_rhs;
+            A.rk_res[0] = c.fuse->res[0];
+            A.rk_res[1] = c.fuse->res[1];
+            for (int j = 0; j < 3; ++j) A.rk_coeff[j] = c.fuse->coeff[j];
+            A.q_out = c.fuse->q_out;
+        }
         A.ntile[0] = (G.n[0] + Cfg::TX - 1)/Cfg::TX;
         A.ntile[1] = (G.n[1] + Cfg::TY - 1)/Cfg::TY;
         A.ntile[2] = (G.n[2] + Cfg::TZ - 1)/Cfg::TZ;

@@ -106,7 +106,7 @@ namespace gbns
         Real gamma, R, gm1, spec_heat, inv_gamma_avg, R_avg, eps_p, eps_T, sens;
         Real mu, beta_c, alpha_c, T_ref, power, inv_pr, prandtl, tref_plus_s, S;
         Real ck_a[4];
-        int diss, visc, law, smooth;
+        int diss, visc, law, smooth, sensor;
         __device__ __forceinline__ void load(const SchemeK& s)
         {
             gamma = Real(s.gamma); R = Real(s.R); gm1 = Real(s.gm1); spec_heat = Real(s.spec_heat);
@@ -116,7 +116,7 @@ namespace gbns
             T_ref = Real(s.T_ref); power = Real(s.power); inv_pr = Real(s.inv_pr); prandtl = Real(s.prandtl);
             tref_plus_s = Real(s.tref_plus_s); S = Real(s.S);
             for (int i = 0; i < 4; ++i) ck_a[i] = Real(s.ck_a[i]);
-            diss = s.diss; visc = s.visc; law = s.law; smooth = s.smooth;
+            diss = s.diss; visc = s.visc; law = s.law; smooth = s.smooth; sensor = s.sensor;
         }
     };
 
@@ -384,10 +384,11 @@ namespace gbns
         }
     }
 
-    // pressure_diss_lr<gas, const_sensor_t>::operator() (convective.h:212-245)
+    // pressure_diss_lr<gas, sensor>::operator() (convective.h:212-245); scl is
+    // the sensor value at the face (const_sensor_t alpha or ducros_t).
     template <class Cfg, int D>
     __device__ __forceinline__ void diss_pressure(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                                  int rc, typename Cfg::Real* out)
+                                                  int rc, typename Cfg::Real scl, typename Cfg::Real* out)
     {
         using Real = typename Cfg::Real;
         constexpr int SD = DirStride<Cfg, D>::S;
@@ -404,8 +405,8 @@ namespace gbns
         const Real u = Real(0.5)*(ul + ur);
         const Real v = Real(0.5)*(vl + vr);
         const Real w = Real(0.5)*(wl + wr);
-        const Real ap = S.sens*S.eps_p*delta_p;
-        const Real aT = S.sens*S.eps_T*delta_T*p_inv_rt2;
+        const Real ap = scl*S.eps_p*delta_p;
+        const Real aT = scl*S.eps_T*delta_T*p_inv_rt2;
         out[0] = ap*inv_RT;
         out[1] = ap*(k*inv_RT + S.inv_gamma_avg);
         out[2] = ap*u*inv_RT;
@@ -418,20 +419,17 @@ namespace gbns
         out[4] -= aT*w;
     }
 
-    // visc_lr::operator() (viscous.h:39-79) with info::value / info::gradient
-    // at the face (info_value.h:28-40, info_gradient.h:61-123).
+    // info::gradient at the face (info_gradient.h:61-123): grad[a][t],
+    // a = direction, t = 0:T 1:u 2:v 3:w (the pressure gradient is unused).
     template <class Cfg, int D>
-    __device__ __forceinline__ void visc_lr(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                            int rc, typename Cfg::Real nD,
-                                            const typename Cfg::Real inv[3], typename Cfg::Real im,
-                                            typename Cfg::Real* out)
+    __device__ __forceinline__ void face_gradient(const BoxView<Cfg>& V, int rc,
+                                                  const typename Cfg::Real inv[3], typename Cfg::Real im,
+                                                  typename Cfg::Real (&grad)[3][4])
     {
         using Real = typename Cfg::Real;
         constexpr int SD = DirStride<Cfg, D>::S, S1 = DirStride<Cfg, D>::S1, S2 = DirStride<Cfg, D>::S2;
         constexpr int D1 = (D + 1) % 3, D2 = (D + 2) % 3;
         const int cl = rc - SD, cr = rc;
-        // grad[a][t]: a = direction, t = 0:T 1:u 2:v 3:w
-        Real grad[3][4];
         #pragma unroll
         for (int t = 0; t < 4; ++t)
         {
@@ -448,6 +446,32 @@ namespace gbns
             grad[D2][t] += (Real(-0.25)*V.q(v, cr - S2))*inv[D2];
             if constexpr (Cfg::STRETCH) grad[1][t] *= im;
         }
+    }
+
+    // state_sensor::ducros_t::get_sensor (state_sensor.h:21-43)
+    template <class Real>
+    __device__ __forceinline__ Real ducros_sensor(const Real (&g)[3][4], Real epsilon)
+    {
+        Real theta_sq = g[0][1] + g[1][2] + g[2][3];
+        theta_sq *= theta_sq;
+        const Real vort0 = g[1][3] - g[2][2];
+        const Real vort1 = g[2][1] - g[0][3];
+        const Real vort2 = g[0][2] - g[1][1];
+        const Real vort_sq = vort0*vort0 + vort1*vort1 + vort2*vort2;
+        return theta_sq / (theta_sq + vort_sq + epsilon);
+    }
+
+    // visc_lr::operator() (viscous.h:39-79) with info::value / info::gradient
+    // at the face (info_value.h:28-40, info_gradient.h:61-123).
+    template <class Cfg, int D>
+    __device__ __forceinline__ void visc_lr(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                            int rc, typename Cfg::Real nD,
+                                            const typename Cfg::Real (&grad)[3][4],
+                                            typename Cfg::Real* out)
+    {
+        using Real = typename Cfg::Real;
+        constexpr int SD = DirStride<Cfg, D>::S;
+        const int cl = rc - SD, cr = rc;
         Real qf[5];
         #pragma unroll
         for (int v = 0; v < 5; ++v) { qf[v] = V.q(v, cl); qf[v] += V.q(v, cr); qf[v] *= Real(0.5); }
@@ -506,8 +530,14 @@ namespace gbns
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) conv_fweno<Cfg, D>(V, S, rc, nD, t0);
         else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) conv_weno5<Cfg, D>(V, S, rc, nD, t0);
         const bool hd = S.diss != 0, hv = S.visc != 0;
-        if (hd) diss_pressure<Cfg, D>(V, S, rc, t1);
-        if (hv) visc_lr<Cfg, D>(V, S, rc, nD, inv, im, t2);
+        const bool ducros = hd && S.sensor == GBNS_SENSOR_DUCROS;
+        // const_sensor_t dissipation runs before the gradient is formed, so
+        // the gradient is not live across it; ducros_t needs the gradient first.
+        if (hd && !ducros) diss_pressure<Cfg, D>(V, S, rc, S.sens, t1);
+        Real grad[3][4];
+        if (hv || ducros) face_gradient<Cfg, D>(V, rc, inv, im, grad);
+        if (ducros) diss_pressure<Cfg, D>(V, S, rc, ducros_sensor<Real>(grad, S.sens), t1);
+        if (hv) visc_lr<Cfg, D>(V, S, rc, nD, grad, t2);
         #pragma unroll
         for (int v = 0; v < 5; ++v)
         {
@@ -528,6 +558,14 @@ namespace gbns
         int increment;
         int ntile[3];       // tiles per block per direction
         int use_tma;
+        // Fused RK stage (0 = none): q_out = prim(cons(q) + sum_j rk_coeff[j] R_j)
+        // for the tile's cells, with R_{rk_nres-1} this launch's residual (in
+        // registers) and R_0..R_{rk_nres-2} read from rk_res.
+        int rk_nres;
+        int write_rhs;      // with a fused stage: also store this launch's residual
+        const double* rk_res[2];
+        double rk_coeff[3];
+        double* q_out;
     };
 
     template <class Cfg, int D>
@@ -757,7 +795,7 @@ namespace gbns
         face_pass<Cfg, 1>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
         face_pass<Cfg, 2>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
 
-        // ---- write the residual ------------------------------------------------
+        // ---- write the residual (and the fused stage update) -----------------
         #pragma unroll
         for (int s = 0; s < Cfg::CPT; ++s)
         {
@@ -765,10 +803,46 @@ namespace gbns
             if (c >= Cfg::NCELL) break;
             const int cx = c % TX, cy = (c / TX) % TY, cz = c / (TX*TY);
             if (i0 + cx >= G.n[0] || j0 + cy >= G.n[1] || k0 + cz >= G.n[2]) continue;
-            double* r = A.rhs + (long long)lb*G.bstride +
+            const long long off = (long long)lb*G.bstride +
                 ((long long)((k0 + cz + G.ng)*G.nj + (j0 + cy + G.ng))*G.ni + (i0 + cx + G.ng))*5;
-            #pragma unroll
-            for (int v = 0; v < 5; ++v) r[v] = relem[s][v];
+            if (A.rk_nres == 0 || A.write_rhs)
+            {
+                double* r = A.rhs + off;
+                #pragma unroll
+                for (int v = 0; v < 5; ++v) r[v] = relem[s][v];
+            }
+            if (A.rk_nres)
+            {
+                // transform_advance_to for this cell (advance.h:75-101)
+                double qv[5];
+                if constexpr (Cfg::FP64)
+                {
+                    const int bc_ = (cz + H)*Cfg::SZ + (cy + H)*Cfg::SY + (cx + H + shift);
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) qv[v] = stage[bc_*5 + v];
+                }
+                else
+                {
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) qv[v] = __ldg(A.prims + off + v);
+                }
+                double cs[5];
+                prim_to_cons(qv, SK.R, SK.gm1, cs);
+                for (int j = 0; j + 1 < A.rk_nres; ++j)
+                {
+                    const double* rr = A.rk_res[j] + off;
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) cs[v] += A.rk_coeff[j]*rr[v];
+                }
+                const double cl = A.rk_coeff[A.rk_nres - 1];
+                #pragma unroll
+                for (int v = 0; v < 5; ++v) cs[v] += cl*relem[s][v];
+                double qn[5];
+                cons_to_prim(cs, SK.R, SK.gm1, qn);
+                double* o = A.q_out + off;
+                #pragma unroll
+                for (int v = 0; v < 5; ++v) o[v] = qn[v];
+            }
         }
         if (!Cfg::DIRECT && A.use_tma && tid == 0) mbar_inval(bar);
     }

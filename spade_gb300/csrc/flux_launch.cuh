@@ -5,6 +5,16 @@
 
 namespace gbns
 {
+    // Fused RK stage riding on a flux_div launch (see FluxArgs).
+    struct RkFuse
+    {
+        int nres;
+        int write_rhs;
+        const double* res[2];
+        double coeff[3];
+        double* q_out;
+    };
+
     struct FluxCall
     {
         const gbns_grid_desc* g;
@@ -16,6 +26,7 @@ namespace gbns
         int increment;
         cudaStream_t stream;
         int variant;
+        const RkFuse* fuse;
     };
 
     // f64x: FP64 without FMA contraction (-fmad=false): the kernels follow the

@@ -59,12 +59,12 @@ namespace gbns
     // Runtime scheme constants (host-derived with the reference's formulas).
     struct SchemeK
     {
-        int diss, visc, law, smooth;
+        int diss, visc, law, smooth, sensor;
         double gamma, R, gm1;          // gm1 = gamma - 1.0
         double spec_heat;              // gamma*R/(gamma - 1.0)        (viscous.h:67)
         double inv_gamma_avg;          // 1.0/(0.5*(gamma + gamma))    (convective.h:226,233)
         double R_avg;                  // 0.5*(R + R)                   (convective.h:224)
-        double eps_p, eps_T, sens;     // pressure_diss_lr
+        double eps_p, eps_T, sens;     // pressure_diss_lr; sens = const_sensor_t alpha or ducros_t epsilon
         double mu, beta_c, alpha_c;    // constant law: mu, -2.0*mu/3.0, mu*(1.0/Pr)
         double T_ref, power, inv_pr, prandtl, tref_plus_s, S;
         double ck_a[4];                // cent_keep centred coefficients a(1..order/2)
@@ -82,9 +82,11 @@ namespace gbns
                           int box_cells_x, int box_y, int box_z);
 
     // Launchers (defined in the kernel translation units) -----------------
+    struct RkFuse;
     int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
                         const gbns_scheme_desc* desc, const double* prims, double* rhs,
-                        int increment, cudaStream_t stream, int variant);
+                        int increment, cudaStream_t stream, int variant, const RkFuse* fuse = nullptr);
+    int launch_copy_fill(const GeomK& G, const gbns_bc_desc* bc, double* dst, const double* src, cudaStream_t stream);
     int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream);
     int launch_rk_stage(const GeomK& G, double gamma, double R, double* prims,
                         const double* const* res, const double* coeffs, int nres, cudaStream_t stream);
@@ -172,6 +174,33 @@ namespace gbns
     }
 
     constexpr long long MBAR_POLL_LIMIT = 1ll << 24;   // ~tens of ms of polling
+
+    // fluid_state::convert_state prim -> cons and cons -> prim
+    // (navier-stokes/fluid_state.h:151-184), in the reference's operation order.
+    __device__ __forceinline__ void prim_to_cons(const double q[5], const double R, const double gm1, double c[5])
+    {
+        const double rho = q[0]/(R*q[1]);
+        const double rhoU2 = rho*(q[2]*q[2] + q[3]*q[3] + q[4]*q[4]);
+        c[0] = rho;
+        c[1] = 0.5*rhoU2 + (q[0]/(gm1));
+        c[2] = rho*q[2];
+        c[3] = rho*q[3];
+        c[4] = rho*q[4];
+    }
+
+    __device__ __forceinline__ void cons_to_prim(const double c[5], const double R, const double gm1, double q[5])
+    {
+        const double rh = c[0];
+        const double invrho = 1.0/rh;
+        const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
+        const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
+        const double pp = gm1*(c[1] - 0.5*ru2);
+        q[0] = pp;
+        q[1] = pp/(R*rh);
+        q[2] = uu;
+        q[3] = vv;
+        q[4] = ww;
+    }
 
     enum device_status_code
     {

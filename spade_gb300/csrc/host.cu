@@ -9,6 +9,7 @@
 
 #include "gbns_internal.cuh"
 #include "flux_launch.cuh"
+#include <cstring>
 
 namespace gbns
 {
@@ -173,7 +174,7 @@ namespace gbns
         else if (s->convective == GBNS_CONV_TOTANI) h = 1;
         else if (s->convective == GBNS_CONV_FWENO) h = 2;
         else if (s->convective == GBNS_CONV_WENO5) h = 3;
-        if ((s->dissipation || s->viscous) && h < 1) h = 1;
+        if ((s->dissipation || s->viscous) && h < 1) h = 1;   // ducros_t's face gradient needs 1 too
         return h;
     }
 
@@ -185,7 +186,8 @@ namespace gbns
         if (s->convective == GBNS_CONV_CENT_KEEP && !(s->order == 2 || s->order == 4 || s->order == 6 || s->order == 8))
             return set_error(GBNS_ERR_UNSUPPORTED, "cent_keep order must be 2, 4, 6 or 8");
         if (s->dissipation < 0 || s->dissipation > GBNS_DISS_PRESSURE) return set_error(GBNS_ERR_INVALID, "unknown dissipation");
-        if (s->dissipation && s->sensor != GBNS_SENSOR_CONST) return set_error(GBNS_ERR_UNSUPPORTED, "only const_sensor_t is lowered");
+        if (s->dissipation && s->sensor != GBNS_SENSOR_CONST && s->sensor != GBNS_SENSOR_DUCROS)
+            return set_error(GBNS_ERR_UNSUPPORTED, "unknown shock sensor");
         if (s->viscous < 0 || s->viscous > GBNS_VISC_LR) return set_error(GBNS_ERR_INVALID, "unknown viscous scheme");
         if (s->viscous && (s->visc_law < GBNS_LAW_CONSTANT || s->visc_law > GBNS_LAW_SUTHERLAND))
             return set_error(GBNS_ERR_INVALID, "unknown viscosity law");
@@ -198,6 +200,7 @@ namespace gbns
         S.visc = s->viscous;
         S.law = s->visc_law;
         S.smooth = s->weno_smooth;
+        S.sensor = s->sensor;
         const double gam = s->gas.gamma, R = s->gas.R;
         S.gamma = gam; S.R = R;
         S.gm1 = gam - 1.0;
@@ -367,6 +370,56 @@ extern "C"
         return launch_rk_stage(G, gas->gamma, gas->R, prims, residuals, coeffs, nres, static_cast<cudaStream_t>(stream));
     }
 
+    int gbns_flux_div_rk(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
+                         double* rhs, int write_rhs, int nres, const double* const* earlier,
+                         const double* coeffs, double* q_out, void* stream)
+    {
+        GeomK G;
+        SchemeK S;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        rc = make_scheme(scheme, S);
+        if (rc) return rc;
+        if (nres < 1 || nres > 3) return set_error(GBNS_ERR_INVALID, "nres must be 1, 2 or 3");
+        if (!prims || !q_out || !coeffs || (write_rhs && !rhs) || (nres > 1 && !earlier))
+            return set_error(GBNS_ERR_INVALID, "NULL pointer");
+        if (q_out == prims) return set_error(GBNS_ERR_INVALID, "q_out must not alias prims (other tiles still read it)");
+        if (scheme_halo(scheme) > G.ng) return set_error(GBNS_ERR_INVALID, "scheme stencil needs more ghost layers");
+        RkFuse f;
+        std::memset(&f, 0, sizeof(f));
+        f.nres = nres;
+        f.write_rhs = write_rhs ? 1 : 0;
+        for (int j = 0; j + 1 < nres; ++j)
+        {
+            if (!earlier[j]) return set_error(GBNS_ERR_INVALID, "NULL residual pointer");
+            f.res[j] = earlier[j];
+        }
+        for (int j = 0; j < nres; ++j) f.coeff[j] = coeffs[j];
+        f.q_out = q_out;
+        YTabK* Y = nullptr;
+        static thread_local YTabK ytab;
+        if (grid->coords != GBNS_COORDS_IDENTITY)
+        {
+            rc = make_ytab(grid, G, ytab);
+            if (rc) return rc;
+            Y = &ytab;
+        }
+        return launch_flux_div(grid, G, Y, S, scheme, prims, write_rhs ? rhs : q_out, 0,
+                               static_cast<cudaStream_t>(stream), scheme->tile_variant, &f);
+    }
+
+    int gbns_copy_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc, double* dst,
+                              const double* src, void* stream)
+    {
+        GeomK G;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        rc = validate_bc(bc);
+        if (rc) return rc;
+        if (!dst || !src || dst == src) return set_error(GBNS_ERR_INVALID, "dst/src must be distinct non-NULL arrays");
+        return launch_copy_fill(G, bc, dst, src, static_cast<cudaStream_t>(stream));
+    }
+
     int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                          const gbns_bc_desc* bc, double* prims, double* work, double dt, void* stream)
     {
@@ -374,24 +427,25 @@ extern "C"
         int rc = make_geom(grid, G);
         if (rc) return rc;
         if (!work) return set_error(GBNS_ERR_INVALID, "work pointer is NULL");
+        rc = validate_bc(bc);
+        if (rc) return rc;
         const size_t n = size_t(G.bstride)*G.nblk;
         double* R0 = work;
         double* R1 = work + n;
-        double* R2 = work + 2*n;
-        const double* res[3] = {R0, R1, R2};
+        double* B = work + 2*n;      // the state between stages
         // ratio_diff_t of consecutive ssprk3_t rows (explicit.h:80-88, advance.h:80-95)
         const double c1[1] = {(1.0/1.0)*dt};
         const double c2[2] = {(-3.0/4.0)*dt, (1.0/4.0)*dt};
         const double c3[3] = {(-1.0/12.0)*dt, (-1.0/12.0)*dt, (2.0/3.0)*dt};
-        if ((rc = gbns_flux_div(grid, scheme, prims, R0, 0, stream))) return rc;
-        if ((rc = gbns_rk_stage(grid, &scheme->gas, prims, res, c1, 1, stream))) return rc;
+        const double* e1[2] = {R0, nullptr};
+        const double* e2[2] = {R0, R1};
+        // each stage: residual and stage update in one launch, then the ghost fill
+        if ((rc = gbns_flux_div_rk(grid, scheme, prims, R0, 1, 1, e1, c1, B, stream))) return rc;
+        if ((rc = gbns_fill_ghosts(grid, bc, B, stream))) return rc;
+        if ((rc = gbns_flux_div_rk(grid, scheme, B, R1, 1, 2, e1, c2, prims, stream))) return rc;
         if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
-        if ((rc = gbns_flux_div(grid, scheme, prims, R1, 0, stream))) return rc;
-        if ((rc = gbns_rk_stage(grid, &scheme->gas, prims, res, c2, 2, stream))) return rc;
-        if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
-        if ((rc = gbns_flux_div(grid, scheme, prims, R2, 0, stream))) return rc;
-        if ((rc = gbns_rk_stage(grid, &scheme->gas, prims, res, c3, 3, stream))) return rc;
-        return gbns_fill_ghosts(grid, bc, prims, stream);
+        if ((rc = gbns_flux_div_rk(grid, scheme, prims, nullptr, 0, 3, e2, c3, B, stream))) return rc;
+        return gbns_copy_fill_ghosts(grid, bc, prims, B, stream);
     }
 
     int gbns_device_status(int* status, int reset, void* stream)

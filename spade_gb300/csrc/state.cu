@@ -18,8 +18,9 @@ namespace gbns
     // periodic wrap, get_transaction.h:55-87 / exchange_config.h:336-344),
     // so one launch fills every ghost layer without ordering hazards.
     // Interior cells are left alone.
-    __device__ __forceinline__ void fill_one_ghost(double* __restrict__ q, const GeomK& G, const BcK& bc,
-                                                   const int lb, const int ii, const int jj, const int kk)
+    __device__ __forceinline__ void fill_one_ghost_from(double* dstq, const double* q,
+                                                        const GeomK& G, const BcK& bc,
+                                                        const int lb, const int ii, const int jj, const int kk)
     {
         int c[3] = {ii - G.ng, jj - G.ng, kk - G.ng};
         if (c[0] >= 0 && c[0] < G.n[0] && c[1] >= 0 && c[1] < G.n[1] && c[2] >= 0 && c[2] < G.n[2]) return;
@@ -74,9 +75,15 @@ namespace gbns
                 val[2 + face/2] = -val[2 + face/2];
             }
         }
-        double* dst = q + (long long)lb*G.bstride + ((long long)(kk*G.nj + jj)*G.ni + ii)*5;
+        double* dst = dstq + (long long)lb*G.bstride + ((long long)(kk*G.nj + jj)*G.ni + ii)*5;
         #pragma unroll
         for (int v = 0; v < 5; ++v) dst[v] = val[v];
+    }
+
+    __device__ __forceinline__ void fill_one_ghost(double* q, const GeomK& G, const BcK& bc,
+                                                   const int lb, const int ii, const int jj, const int kk)
+    {
+        fill_one_ghost_from(q, q, G, bc, lb, ii, jj, kk);
     }
 
     // One thread per padded cell; interior cells return at once.
@@ -97,6 +104,35 @@ namespace gbns
         }
     }
 
+    // dst = src on interior cells; dst ghosts filled from src's interior
+    // donors (the ghost fill of the state that the last fused stage wrote to
+    // the scratch buffer, landing in the caller's array).
+    __global__ void __launch_bounds__(256)
+    copy_fill_kernel(double* __restrict__ dst, const double* __restrict__ src, const __grid_constant__ GeomK G, const BcK bc)
+    {
+        const long long per_block = (long long)G.ni*G.nj*G.nk;
+        const long long total = per_block*G.nblk;
+        for (long long idx = blockIdx.x*(long long)blockDim.x + threadIdx.x; idx < total;
+             idx += (long long)gridDim.x*blockDim.x)
+        {
+            const int lb = int(idx / per_block);
+            const long long rem = idx - lb*per_block;
+            const int kk = int(rem / ((long long)G.ni*G.nj));
+            const int jj = int((rem / G.ni) % G.nj);
+            const int ii = int(rem % G.ni);
+            const int i = ii - G.ng, j = jj - G.ng, k = kk - G.ng;
+            if (i >= 0 && i < G.n[0] && j >= 0 && j < G.n[1] && k >= 0 && k < G.n[2])
+            {
+                #pragma unroll
+                for (int v = 0; v < 5; ++v) dst[idx*5 + v] = src[idx*5 + v];
+            }
+            else
+            {
+                fill_one_ghost_from(dst, src, G, bc, lb, ii, jj, kk);
+            }
+        }
+    }
+
     static int sm_count()
     {
         int dev = 0, n = 0;
@@ -110,6 +146,15 @@ namespace gbns
         const long long want = (work + threads - 1)/threads;
         const long long cap = (long long)sm_count()*per_sm;
         return unsigned(want < cap ? (want > 0 ? want : 1) : cap);
+    }
+
+    int launch_copy_fill(const GeomK& G, const gbns_bc_desc* bc, double* dst, const double* src, cudaStream_t stream)
+    {
+        BcK k;
+        for (int i = 0; i < 6; ++i) { k.kind[i] = bc->kind[i]; k.t_wall[i] = bc->t_wall[i]; }
+        const long long total = (long long)G.ni*G.nj*G.nk*G.nblk;
+        copy_fill_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(dst, src, G, k);
+        return check_cuda(cudaGetLastError(), "copy_fill launch");
     }
 
     int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream)
@@ -140,11 +185,9 @@ namespace gbns
                                                    const long long off)
     {
         double* qq = q + off;
-        const double p = qq[0], T = qq[1], u = qq[2], v = qq[3], w = qq[4];
-        const double rho = p/(R*T);
-        const double rhoU2 = rho*(u*u + v*v + w*w);
-        const double rhoE = 0.5*rhoU2 + (p/(gm1));
-        double c[5] = {rho, rhoE, rho*u, rho*v, rho*w};
+        const double qv[5] = {qq[0], qq[1], qq[2], qq[3], qq[4]};
+        double c[5];
+        prim_to_cons(qv, R, gm1, c);
         #pragma unroll
         for (int r = 0; r < NRES; ++r)
         {
@@ -152,13 +195,10 @@ namespace gbns
             #pragma unroll
             for (int s = 0; s < 5; ++s) c[s] += coeff[r]*rr[s];
         }
-        const double rh = c[0];
-        const double invrho = 1.0/rh;
-        const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
-        const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
-        const double pp = gm1*(c[1] - 0.5*ru2);
-        const double TT = pp/(R*rh);
-        qq[0] = pp; qq[1] = TT; qq[2] = uu; qq[3] = vv; qq[4] = ww;
+        double out[5];
+        cons_to_prim(c, R, gm1, out);
+        #pragma unroll
+        for (int v = 0; v < 5; ++v) qq[v] = out[v];
     }
 
     template <int NRES>

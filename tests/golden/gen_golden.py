@@ -38,6 +38,9 @@ FLUX_CASES = {
     "ck8": (O.REF_CK8, dict(conv=_abi.CONV_CENT_KEEP, order=8)),
     "fweno_nosmooth": (O.REF_FWENO_NOSMOOTH, dict(conv=_abi.CONV_FWENO, smooth=0)),
     "ck2_diss_visc": (O.REF_CK2_DISS_VISC, dict(conv=_abi.CONV_CENT_KEEP, order=2, diss=1, visc=1)),
+    "ducros_diss": (O.REF_DUCROS_DISS, dict(conv=_abi.CONV_NONE, diss=1, sensor=_abi.SENSOR_DUCROS, alpha=0.7)),
+    "fweno_ducros_visc": (O.REF_FWENO_DUCROS_VISC, dict(conv=_abi.CONV_FWENO, diss=1, visc=1,
+                                                         sensor=_abi.SENSOR_DUCROS, alpha=0.7)),
 }
 
 FLUX_GRID = dict(nblk=(2, 1, 1), ncell=(6, 5, 4), ng=4, bounds=(0.0, 1.3, 0.0, 0.9, 0.0, 0.7))

@@ -30,7 +30,9 @@ def random_state(nblk, ncell, ng, seed, p0=86100.0, T0=300.0, u0=34.7, rel=0.02)
 
 def scheme(conv=_abi.CONV_CENT_KEEP, order=2, diss=0, visc=0, smooth=1, law=_abi.LAW_CONSTANT,
            mu=2.17e-2, eps_p=0.3, eps_T=0.2, alpha=0.7, T_ref=300.0, power=0.76, S=110.4,
-           precision=_abi.PREC_FP64, gamma=GAMMA, R=RGAS):
+           precision=_abi.PREC_FP64, gamma=GAMMA, R=RGAS, sensor=_abi.SENSOR_CONST):
+    """alpha is const_sensor_t's alpha, or ducros_t's epsilon when sensor is
+    SENSOR_DUCROS."""
     s = _abi.SchemeDesc()
     s.convective = conv
     s.order = order
@@ -43,6 +45,7 @@ def scheme(conv=_abi.CONV_CENT_KEEP, order=2, diss=0, visc=0, smooth=1, law=_abi
     s.prandtl = PRANDTL
     s.eps_p = eps_p
     s.eps_T = eps_T
+    s.sensor = sensor
     s.sensor_alpha = alpha
     s.T_ref = T_ref
     s.power = power

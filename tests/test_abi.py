@@ -130,6 +130,14 @@ def test_lower_channel_composite_and_precision_trait():
     assert (s.eps_p, s.eps_T, s.sensor_alpha, s.S) == (2.0, 3.0, 0.5, 110.4)
 
 
+def test_lower_ducros_sensor_carries_epsilon():
+    f = omni.compose(convective.fweno_t(air()),
+                     convective.pressure_diss_lr(air(), state_sensor.ducros_t(1e-4), 2.0, 3.0))
+    s = pde_algs.lower(f)
+    assert (s.convective, s.dissipation, s.sensor) == (_abi.CONV_FWENO, 1, _abi.SENSOR_DUCROS)
+    assert (s.eps_p, s.eps_T, s.sensor_alpha) == (2.0, 3.0, 1e-4)
+
+
 def test_lower_rejects_noncanonical_three_term_composite():
     f = omni.compose(viscous.visc_lr(viscous_laws.constant_viscosity_t(1e-3, 0.72), air()),
                      convective.cent_keep(2, air()),

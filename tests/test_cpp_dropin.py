@@ -28,7 +28,7 @@ def test_dropin_overload_and_lowering():
     lines = out.stdout.strip().splitlines()
     grids = [l.split() for l in lines if l.startswith("grid")]
     schemes = [l.split() for l in lines if l.startswith("scheme")]
-    assert len(grids) == 3 and len(schemes) == 3
+    assert len(grids) == 4 and len(schemes) == 4
     assert grids[0][1:8] == ["2", "3", "1", "8", "6", "4", "3"]
     assert [float(x) for x in grids[0][8:14]] == [0.0, 2.0, -1.0, 1.0, 0.0, 0.5]
     # cent_keep<2> + visc_lr(constant), FP64, increment
@@ -39,6 +39,12 @@ def test_dropin_overload_and_lowering():
     s = schemes[1]
     assert s[1:8] == ["3", "2", "1", "1", "1", "0", "1"] and s[s.index("incr") + 1] == "0"
     assert [float(x) for x in s[8:11]] == [0.1, 0.2, 0.25]
+    assert s[s.index("sensor") + 1] == "0"
     # totani alone
     s = schemes[2]
     assert s[1:8] == ["2", "2", "1", "0", "0", "0", "0"]
+    # fweno + pressure_diss(ducros_t(0.5), 0.1, 0.2) + visc: the sensor kind
+    # is ducros and sensor_alpha carries epsilon
+    s = schemes[3]
+    assert s[1:8] == ["3", "2", "1", "1", "1", "0", "0"] and s[s.index("sensor") + 1] == "1"
+    assert [float(x) for x in s[8:11]] == [0.1, 0.2, 0.5]

@@ -364,3 +364,37 @@ def test_reductions_match_oracle(kind, coords):
         assert got == want == 2.0
     else:
         np.testing.assert_allclose(got, want, rtol=1e-13)
+
+
+@pytest.mark.parametrize("precision", [_abi.PREC_FP64, _abi.PREC_FP32_FLUX])
+def test_flux_div_rk_equals_flux_div_then_rk_stage(precision):
+    """The fused launch (residual + stage update) against the two separate
+    launches: bit-identical in FP64; FP32-flux rounds the FP64 stage update
+    with FMA contraction, so 1e-14 normwise there."""
+    nblk, ncell, ng = (2, 2, 1), (12, 8, 8), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 2.0, -1.0, 1.0, 0.0, 1.0), _abi.COORDS_TANH_Y, (2.0, 0, 0, 0))
+    q = P.random_state(nblk, ncell, ng, seed=101, rel=0.01, u0=5.0)
+    s = P.scheme(conv=_abi.CONV_WENO5, diss=1, visc=1, law=_abi.LAW_SUTHERLAND, mu=0.05, eps_p=3.0, eps_T=3.0,
+                 alpha=1.0, precision=precision)
+    r0 = P.random_state(nblk, ncell, ng, seed=102, p0=1e3, T0=1e2, u0=10.0)
+    r1 = P.random_state(nblk, ncell, ng, seed=103, p0=1e3, T0=1e2, u0=10.0)
+    coeffs = [-1.0 / 12.0 * 1e-6, -1.0 / 12.0 * 1e-6, 2.0 / 3.0 * 1e-6]
+    qd, r0d, r1d = dev(q), dev(r0), dev(r1)
+    # separate launches
+    r2d = torch.zeros_like(qd)
+    _native.check(lib().gbns_flux_div(grid, s, qd.data_ptr(), r2d.data_ptr(), 0, stream()))
+    qa = qd.clone()
+    ptrs = (ctypes.c_void_p * 3)(r0d.data_ptr(), r1d.data_ptr(), r2d.data_ptr())
+    cf = (ctypes.c_double * 3)(*coeffs)
+    _native.check(lib().gbns_rk_stage(grid, s.gas, qa.data_ptr(), ptrs, cf, 3, stream()))
+    # fused
+    qb = torch.zeros_like(qd)
+    earlier = (ctypes.c_void_p * 2)(r0d.data_ptr(), r1d.data_ptr())
+    r2f = torch.zeros_like(qd)
+    _native.check(lib().gbns_flux_div_rk(grid, s, qd.data_ptr(), r2f.data_ptr(), 1, 3, earlier, cf, qb.data_ptr(), stream()))
+    a, b = interior(host(qa), ng), interior(host(qb), ng)
+    assert np.array_equal(host(r2f), host(r2d))
+    if precision == _abi.PREC_FP64:
+        assert np.array_equal(a, b)
+    else:
+        assert normwise(b, a) <= 1e-14
