@@ -52,6 +52,9 @@ def parse():
     p.add_argument("--batch-instances", type=int, default=96)
     p.add_argument("--batch-steps", type=int, default=10)
     p.add_argument("--serve-requests", type=int, default=24)
+    p.add_argument("--precision-report", type=int, default=0, metavar="STEPS",
+                   help="instead of the bench line: run the channel workload STEPS steps in FP64 and in the "
+                        "FP32-flux form from the same state and print their per-variable errors and drifts")
     return p.parse_args()
 
 
@@ -428,11 +431,93 @@ def cpu_sample(steps=1, nblk=(2, 2, 2), ncell=(32, 32, 32), threads=0):
                       % (steps, nblk[0], nblk[1], nblk[2], ncell[0], cells, el)}
 
 
+def run_precision_report(args):
+    """Precision form on the channel workload: STEPS SSPRK3 steps in plain
+    FP64 (bit-identical to the reference's arithmetic) and in the FP32-flux
+    form from the same initial state.  Reports, per conserved variable, the
+    max and L2 error of the FP32-flux state against the FP64 run, the drift of
+    total mass and energy in both runs, and the kinetic-energy history error."""
+    import torch
+    from spade_gb300 import _abi, _native, workloads
+    lib = _native.lib()
+    st = int(torch.cuda.current_stream().cuda_stream)
+    prob = workloads.channel(nblk=tuple(args.nblk), ncell=tuple(args.ncell), ng=3, rng="torch", seed=0)
+    g = prob.q.desc()
+    bc = prob.bc_desc()
+    gas = prob.gas.desc()
+    dt = prob.dt
+    q0 = prob.q.data.clone()
+    n = q0.numel()
+    work = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
+    every = max(1, args.precision_report // 50)
+
+    def reduce(ptr, kind):
+        out = (ctypes.c_double * 5)()
+        _native.check(lib.gbns_reduce(g, gas, ctypes.c_void_p(ptr), kind, ctypes.byref(out), st))
+        return list(out)
+
+    def run(prec):
+        s = prob.scheme_desc(prec)
+        q = prob.q
+        q.data.copy_(q0)
+        hist = {"step": [], "ke": [], "mass": [], "energy": []}
+        t0 = time.perf_counter()
+        for k in range(args.precision_report + 1):
+            if k % every == 0 or k == args.precision_report:
+                c = reduce(q.ptr(), _abi.RED_CONSERVED)
+                hist["step"].append(k)
+                hist["ke"].append(reduce(q.ptr(), _abi.RED_KINETIC)[0])
+                hist["mass"].append(c[0])
+                hist["energy"].append(c[1])
+            if k < args.precision_report:
+                _native.check(lib.gbns_ssprk3_step(g, s, bc, q.ptr(), work.data_ptr(), ctypes.c_double(dt), st))
+        torch.cuda.synchronize()
+        return q.data.clone(), hist, time.perf_counter() - t0
+
+    q64, h64, t64 = run(_abi.PREC_FP64)
+    q32, h32, t32 = run(_abi.PREC_FP32_FLUX)
+    ng = prob.ng
+    i64 = q64[:, ng:-ng, ng:-ng, ng:-ng, :].reshape(-1, 5)
+    i32 = q32[:, ng:-ng, ng:-ng, ng:-ng, :].reshape(-1, 5)
+    # conserved variables (rho, rhoE, rhou, rhov, rhow) from the primitives
+    def cons(a):
+        p, T, u = a[:, 0], a[:, 1], a[:, 2:5]
+        rho = p / (prob.gas.R * T)
+        e = p / (rho * (prob.gas.gamma - 1.0)) + 0.5 * (u * u).sum(1)
+        return torch.stack([rho, rho * e, rho * u[:, 0], rho * u[:, 1], rho * u[:, 2]], 1)
+    c64, c32 = cons(i64), cons(i32)
+    names = ["rho", "rhoE", "rhou", "rhov", "rhow"]
+    err = {}
+    for v, nm in enumerate(names):
+        d = (c32[:, v] - c64[:, v])
+        scale = c64[:, v].abs().max().item()
+        err[nm] = {"max_abs": d.abs().max().item(), "max_rel_to_field_max": d.abs().max().item() / scale,
+                   "l2_rel": (d.norm() / c64[:, v].norm()).item()}
+    ke_rel = max(abs(a - b) / abs(b) for a, b in zip(h32["ke"], h64["ke"]))
+    out = {
+        "report": "precision_form", "workload": config(args)["workload"], "cells": prob.grid.get_grid_size(),
+        "steps": args.precision_report, "dt": dt,
+        "per_variable_error_fp32_flux_vs_fp64": err,
+        "ke_history_max_rel_error": ke_rel,
+        "mass_drift_rel": {"fp64": (h64["mass"][-1] - h64["mass"][0]) / h64["mass"][0],
+                           "fp32_flux": (h32["mass"][-1] - h32["mass"][0]) / h32["mass"][0]},
+        "energy_drift_rel": {"fp64": (h64["energy"][-1] - h64["energy"][0]) / h64["energy"][0],
+                             "fp32_flux": (h32["energy"][-1] - h32["energy"][0]) / h32["energy"][0]},
+        "wall_s": {"fp64": t64, "fp32_flux": t32},
+        "history": {"step": h64["step"], "ke_fp64": h64["ke"], "ke_fp32_flux": h32["ke"],
+                    "energy_fp64": h64["energy"], "energy_fp32_flux": h32["energy"]},
+    }
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     cfg = config(args)
+    if args.precision_report:
+        run_precision_report(args)
+        return
     if args.impl == "reference":
         if rank != 0:
             return
