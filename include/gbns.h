@@ -83,6 +83,12 @@ typedef struct gbns_gas_desc
 #define GBNS_CONV_TOTANI      2   /* convective::totani_lr (convective.h:54-94) */
 #define GBNS_CONV_FWENO       3   /* convective::fweno_t (convective.h:335-497), 3rd order, 4-point */
 #define GBNS_CONV_WENO5       4   /* 5th-order WENO-JS on fweno_t's Rusanov split (no reference counterpart) */
+#define GBNS_CONV_HYBRID      5   /* convective::hybrid_scheme_t<cent_keep_scheme_t<gas,order>, fweno_t<gas,smooth>,
+                                     sensor, tag> (navier-stokes/hybrid_scheme.h:14-47): the centred flux blended
+                                     with fweno_t by a face sensor (hybrid_sensor, hybrid_param); order 2 or 4 */
+
+#define GBNS_HYBRID_FULL_FLUX 0   /* convective::full_flux: (1 - s) F_centred + s F_fweno */
+#define GBNS_HYBRID_DISS_FLUX 1   /* convective::diss_flux: F_centred + s F_fweno */
 
 #define GBNS_DISS_NONE        0
 #define GBNS_DISS_PRESSURE    1   /* convective::pressure_diss_lr (convective.h:194-246) */
@@ -113,7 +119,7 @@ typedef struct gbns_scheme_desc
     int32_t precision;     /* GBNS_PREC_* */
     int32_t tile_variant;  /* flux_div tile shape, 0 .. gbns_flux_variant_count-1 (0 = default);
                               every variant gives bit-identical results */
-    int32_t reserved;      /* must be 0 */
+    int32_t hybrid_flux;   /* GBNS_CONV_HYBRID: GBNS_HYBRID_FULL_FLUX or GBNS_HYBRID_DISS_FLUX */
     double  eps_p, eps_T;  /* pressure_diss_lr coefficients */
     double  sensor_alpha;  /* const_sensor_t::alpha, or ducros_t::epsilon */
     double  mu;            /* constant: mu; power/sutherland: mu_ref */
@@ -124,6 +130,9 @@ typedef struct gbns_scheme_desc
     double  prandtl_inv;   /* 1/Pr as the caller's law stores it; 0 = use 1.0/prandtl
                               (constant_viscosity_t keeps only 1/Pr, viscous_laws.h:190-192) */
     gbns_gas_desc gas;
+    int32_t hybrid_sensor; /* GBNS_CONV_HYBRID blender: GBNS_SENSOR_* */
+    int32_t reserved;      /* must be 0 */
+    double  hybrid_param;  /* blender const_sensor_t::alpha, or ducros_t::epsilon */
 } gbns_scheme_desc;
 
 /* ---- boundary conditions -------------------------------------------- */

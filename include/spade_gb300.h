@@ -23,6 +23,7 @@
  * Lowered functors: convective::cent_keep_scheme_t<gas, 2|4|6|8>,
  * convective::totani_lr, convective::fweno_t<gas, smooth>,
  * convective::pressure_diss_lr<gas, state_sensor::const_sensor_t | ducros_t>,
+ * convective::hybrid_scheme_t<cent_keep_scheme_t<gas, 2|4>, fweno_t, const_sensor_t | ducros_t, full_flux | diss_flux>,
  * viscous::visc_lr<viscous_laws::constant_viscosity_t | power_law_t, gas>,
  * and omni::compose of one of each (convective, dissipation, viscous).
  * Coordinates: coords::identity.
@@ -111,6 +112,43 @@ namespace spade::gb300
                 s.convective = GBNS_CONV_FWENO;
                 s.weno_smooth = (sm == convective::enable_smooth) ? 1 : 0;
                 set_gas(s, f.gas, g);
+            }
+        };
+
+        // blender of hybrid_scheme_t: kind and parameter
+        template <typename T> struct blender
+        {
+            static_assert(always_false<T>::value, "gb300 flux_div: hybrid blender must be const_sensor_t or ducros_t");
+        };
+        template <typename ft> struct blender<state_sensor::const_sensor_t<ft>>
+        {
+            static constexpr int kind = GBNS_SENSOR_CONST;
+            static double param(const state_sensor::const_sensor_t<ft>& b) { return b.alpha; }
+        };
+        template <typename ft> struct blender<state_sensor::ducros_t<ft>>
+        {
+            static constexpr int kind = GBNS_SENSOR_DUCROS;
+            static double param(const state_sensor::ducros_t<ft>& b) { return b.epsilon; }
+        };
+
+        // hybrid_scheme_t<cent_keep<2|4>, fweno_t, blender, tag> (navier-stokes/hybrid_scheme.h:14-47)
+        template <typename gas_t, const int order, const convective::weno_smooth_indicator sm, typename blend_t, typename tag_t>
+        struct lower<convective::hybrid_scheme_t<convective::cent_keep_scheme_t<gas_t, order>, convective::fweno_t<gas_t, sm>,
+                                                 blend_t, tag_t>>
+        {
+            static constexpr int slot = 0;
+            template <typename hyb_t>
+            static void apply(gbns_scheme_desc& s, const hyb_t& f, bool& g)
+            {
+                static_assert(order == 2 || order == 4, "hybrid_scheme_t is lowered with cent_keep order 2 or 4");
+                s.convective = GBNS_CONV_HYBRID;
+                s.order = order;
+                s.weno_smooth = (sm == convective::enable_smooth) ? 1 : 0;
+                s.hybrid_flux = tag_t::value ? GBNS_HYBRID_FULL_FLUX : GBNS_HYBRID_DISS_FLUX;
+                s.hybrid_sensor = blender<blend_t>::kind;
+                s.hybrid_param = blender<blend_t>::param(f.blender);
+                set_gas(s, f.scheme0.gas, g);
+                set_gas(s, f.scheme1.gas, g);
             }
         };
 

@@ -529,6 +529,53 @@ static st5 flux_visc(const ctx_t* C, int d, int i, int j, int k, const double n[
     return F;
 }
 
+/* Stencil of `width` cells centred on the face (direction d, right cell
+ * (i,j,k)) with each cell's metric normal (info_metric.h:188-197). */
+static void face_window(const ctx_t* C, int d, int i, int j, int k, int width,
+                        const double* cells[8], double ncell[8][3])
+{
+    const int dd[3] = {d == 0, d == 1, d == 2};
+    const int hw = width/2;
+    for (int m = 0; m < width; ++m)
+    {
+        const int off = m - hw;
+        const int ci = i + off*dd[0], cj = j + off*dd[1], ck = k + off*dd[2];
+        cells[m] = cellp(C, ci, cj, ck);
+        const double eta_c = C->bmin[1] + ((double)cj + 0.5)*C->dx[1];
+        face_normal(C, d, eta_c, ncell[m]);
+    }
+}
+
+/* hybrid_scheme_t<cent_keep_scheme_t, fweno_t, blender, tag>::operator()
+ * (navier-stokes/hybrid_scheme.h:30-46): s = blender at the face
+ * (const_sensor_t alpha, or ducros_t on the face gradient); F = c0 F_centred
+ * + s F_fweno with c0 = 1 - s (full_flux) or 1 (diss_flux). */
+static st5 flux_hybrid(const ctx_t* C, int d, int i, int j, int k, const double nface[3])
+{
+    const gbns_scheme_desc* S = C->S;
+    double blend = S->hybrid_param;
+    if (S->hybrid_sensor == GBNS_SENSOR_DUCROS)
+    {
+        double grad[3][5];
+        face_grad(C, d, i, j, k, grad);
+        blend = ducros_sensor(grad, S->hybrid_param);
+    }
+    const double* cells[8];
+    double ncell[8][3];
+    face_window(C, d, i, j, k, S->order, cells, ncell);
+    st5 f0 = flux_cent_keep(C, cells, S->order, (const double (*)[3])ncell, nface);
+    face_window(C, d, i, j, k, 4, cells, ncell);
+    st5 f1 = flux_fweno(C, cells, (const double (*)[3])ncell);
+    const double coeff0 = (S->hybrid_flux == GBNS_HYBRID_DISS_FLUX) ? 1.0 : (1.0 - blend);
+    for (int v = 0; v < 5; ++v)
+    {
+        f0.v[v] *= coeff0;
+        f1.v[v] *= blend;
+        f0.v[v] += f1.v[v];
+    }
+    return f0;
+}
+
 /* Face flux of the lowered composite for the face in direction d whose
  * right cell is (i,j,k): conv + (diss + visc) (compose.h:19-24). */
 static st5 face_flux(const ctx_t* C, int d, int i, int j, int k)
@@ -543,7 +590,11 @@ static st5 face_flux(const ctx_t* C, int d, int i, int j, int k)
 
     st5 terms[3];
     int nterm = 0;
-    if (S->convective != GBNS_CONV_NONE)
+    if (S->convective == GBNS_CONV_HYBRID)
+    {
+        terms[nterm++] = flux_hybrid(C, d, i, j, k, nface);
+    }
+    else if (S->convective != GBNS_CONV_NONE)
     {
         st5 F;
         int width = 2;
@@ -598,6 +649,7 @@ static int stencil_halo(const gbns_scheme_desc* S)
     else if (S->convective == GBNS_CONV_TOTANI) h = 1;
     else if (S->convective == GBNS_CONV_FWENO) h = 2;
     else if (S->convective == GBNS_CONV_WENO5) h = 3;
+    else if (S->convective == GBNS_CONV_HYBRID) h = S->order/2 > 2 ? S->order/2 : 2;
     if (S->dissipation && h < 1) h = 1;
     if (S->viscous && h < 1) h = 1;
     return h;

@@ -119,6 +119,9 @@ REF_FWENO_NOSMOOTH = 11
 REF_CK2_DISS_VISC = 12
 REF_DUCROS_DISS = 13
 REF_FWENO_DUCROS_VISC = 14
+REF_HYB_CK2_FULL = 15
+REF_HYB_CK4_DISS_VISC = 16
+REF_HYB_CK2_CONST_DISS_VISC = 17
 
 
 def _ref_problem(grid, scheme, bc=None):
@@ -133,7 +136,8 @@ def _ref_problem(grid, scheme, bc=None):
             t_wall = bc.t_wall[2]
     ints = np.array(list(grid.nblk) + list(grid.ncell) + [grid.ng] + periodic + [wall_y], dtype=np.int32)
     reals = np.array(list(grid.bounds) + [scheme.gas.gamma, scheme.gas.R, scheme.mu, scheme.prandtl,
-                                          scheme.eps_p, scheme.eps_T, scheme.sensor_alpha, t_wall], dtype=np.float64)
+                                          scheme.eps_p, scheme.eps_T, scheme.sensor_alpha, t_wall,
+                                          scheme.hybrid_param], dtype=np.float64)
     return ints, reals
 
 

@@ -33,6 +33,7 @@ namespace
         double bounds[6];
         double gamma, rgas, mu, prandtl;
         double eps_p, eps_T, sensor;
+        double hybrid_param;   // hybrid_scheme_t blender: const_sensor_t alpha or ducros_t epsilon
         int periodic[3];
         int wall_y;
         double t_wall;
@@ -55,7 +56,11 @@ namespace
         S_FWENO_NOSMOOTH = 11, // fweno_t<gas, disable_smooth>
         S_CK2_DISS_VISC  = 12, // compose(cent_keep<2>, pressure_diss_lr(const_sensor), visc_lr(constant))
         S_DUCROS_DISS    = 13, // pressure_diss_lr(ducros_t)
-        S_FWENO_DUCROS_VISC = 14 // compose(fweno_t, pressure_diss_lr(ducros_t), visc_lr(constant))
+        S_FWENO_DUCROS_VISC = 14, // compose(fweno_t, pressure_diss_lr(ducros_t), visc_lr(constant))
+        S_HYB_CK2_FULL      = 15, // hybrid_scheme_t(cent_keep<2>, fweno_t, ducros_t, full_flux)
+        S_HYB_CK4_DISS_VISC = 16, // compose(hybrid_scheme_t(cent_keep<4>, fweno_t, ducros_t, diss_flux), visc_lr(constant))
+        S_HYB_CK2_CONST_DISS_VISC = 17 // compose(hybrid_scheme_t(cent_keep<2>, fweno_t, const_sensor_t, full_flux),
+                                       //         pressure_diss_lr(ducros_t), visc_lr(constant))
     };
 
     template <typename func_t>
@@ -67,6 +72,8 @@ namespace
         spade::state_sensor::const_sensor_t<real_t> sens(pb.sensor);
         spade::convective::pressure_diss_lr diss(air, sens, pb.eps_p, pb.eps_T);
         spade::state_sensor::ducros_t<real_t> ducros(pb.sensor);
+        spade::state_sensor::const_sensor_t<real_t> hsens(pb.hybrid_param);
+        spade::state_sensor::ducros_t<real_t> hducros(pb.hybrid_param);
         spade::convective::pressure_diss_lr ddiss(air, ducros, pb.eps_p, pb.eps_T);
         switch (scheme)
         {
@@ -89,6 +96,17 @@ namespace
             case S_DUCROS_DISS: func(ddiss); break;
             case S_FWENO_DUCROS_VISC:
                 func(spade::omni::compose(spade::convective::fweno_t<gas_t>(air), ddiss, visc)); break;
+            case S_HYB_CK2_FULL:
+                func(spade::convective::hybrid_scheme_t(spade::convective::cent_keep<2>(air), spade::convective::fweno_t<gas_t>(air),
+                                                        hducros, spade::convective::full_flux)); break;
+            case S_HYB_CK4_DISS_VISC:
+                func(spade::omni::compose(spade::convective::hybrid_scheme_t(spade::convective::cent_keep<4>(air),
+                                                                             spade::convective::fweno_t<gas_t>(air),
+                                                                             hducros, spade::convective::diss_flux), visc)); break;
+            case S_HYB_CK2_CONST_DISS_VISC:
+                func(spade::omni::compose(spade::convective::hybrid_scheme_t(spade::convective::cent_keep<2>(air),
+                                                                             spade::convective::fweno_t<gas_t>(air),
+                                                                             hsens, spade::convective::full_flux), ddiss, visc)); break;
             default: throw std::runtime_error("unknown scheme id");
         }
     }
@@ -208,6 +226,7 @@ extern "C"
         for (int i = 0; i < 6; ++i) pb.bounds[i] = reals[i];
         pb.gamma = reals[6]; pb.rgas = reals[7]; pb.mu = reals[8]; pb.prandtl = reals[9];
         pb.eps_p = reals[10]; pb.eps_T = reals[11]; pb.sensor = reals[12]; pb.t_wall = reals[13];
+        pb.hybrid_param = reals[14];
         return pb;
     }
 

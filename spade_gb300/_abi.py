@@ -24,6 +24,9 @@ CONV_CENT_KEEP = 1
 CONV_TOTANI = 2
 CONV_FWENO = 3
 CONV_WENO5 = 4
+CONV_HYBRID = 5
+HYBRID_FULL_FLUX = 0
+HYBRID_DISS_FLUX = 1
 
 DISS_NONE = 0
 DISS_PRESSURE = 1
@@ -79,7 +82,7 @@ class SchemeDesc(ctypes.Structure):
         ("visc_law", ctypes.c_int32),
         ("precision", ctypes.c_int32),
         ("tile_variant", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("hybrid_flux", ctypes.c_int32),
         ("eps_p", ctypes.c_double),
         ("eps_T", ctypes.c_double),
         ("sensor_alpha", ctypes.c_double),
@@ -90,6 +93,9 @@ class SchemeDesc(ctypes.Structure):
         ("S", ctypes.c_double),
         ("prandtl_inv", ctypes.c_double),
         ("gas", GasDesc),
+        ("hybrid_sensor", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("hybrid_param", ctypes.c_double),
     ]
 
 

@@ -64,3 +64,40 @@ class pressure_diss_lr:
         self.sensor = sensor
         self.eps_p = float(eps_p)
         self.eps_T = float(eps_p if eps_T is None else eps_T)
+
+
+class hybrid_secheme_tag_t:
+    """convective::hybrid_secheme_tag_t<full> (hybrid_scheme.h:5-12)."""
+
+    def __init__(self, full):
+        self.value = bool(full)
+        self.kind = _abi.HYBRID_FULL_FLUX if full else _abi.HYBRID_DISS_FLUX
+
+
+full_flux = hybrid_secheme_tag_t(True)
+diss_flux = hybrid_secheme_tag_t(False)
+
+
+class hybrid_scheme_t:
+    """convective::hybrid_scheme_t(scheme0, scheme1, blender, tag)
+    (hybrid_scheme.h:14-47): the face flux (1 - s) F0 + s F1 (full_flux) or
+    F0 + s F1 (diss_flux), s = blender.get_sensor at the face.  Lowered for
+    scheme0 = cent_keep<2|4>, scheme1 = fweno_t and a const_sensor_t or
+    ducros_t blender."""
+
+    def __init__(self, scheme0, scheme1, blender, tag):
+        if not isinstance(scheme0, cent_keep_scheme_t) or scheme0.order not in (2, 4):
+            raise ValueError("hybrid_scheme_t is lowered with scheme0 = cent_keep<2> or cent_keep<4>")
+        if not isinstance(scheme1, fweno_t):
+            raise ValueError("hybrid_scheme_t is lowered with scheme1 = fweno_t")
+        g0, g1 = scheme0.gas, scheme1.gas
+        if g0.gamma != g1.gamma or g0.R != g1.R:
+            raise ValueError("hybrid_scheme_t schemes must share one gas")
+        self.scheme0 = scheme0
+        self.scheme1 = scheme1
+        self.blender = blender
+        self.tag = tag
+        self.gas = g0
+        self.order = scheme0.order
+        self.smooth = scheme1.smooth
+        self.kind = _abi.CONV_HYBRID

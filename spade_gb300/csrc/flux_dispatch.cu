@@ -22,6 +22,7 @@ namespace gbns
             case GBNS_CONV_TOTANI:    return 2 + extra;
             case GBNS_CONV_FWENO:     return 3 + extra;
             case GBNS_CONV_WENO5:     return 3 + extra;
+            case GBNS_CONV_HYBRID:    return 2 + extra;
             default:                  return 1 + extra;
         }
     }
@@ -36,6 +37,14 @@ namespace gbns
         const bool stretch = g->coords != GBNS_COORDS_IDENTITY;
         const bool upwind = desc->convective == GBNS_CONV_FWENO || desc->convective == GBNS_CONV_WENO5;
         const int conv = desc->convective, order = desc->order;
+        if (conv == GBNS_CONV_HYBRID)
+        {
+            if (desc->precision == GBNS_PREC_FP64)
+                return stretch ? flux_f64x_stretch_c(c, conv, order) : flux_f64x_identity_c(c, conv, order);
+            if (desc->precision == GBNS_PREC_FP64_FMA)
+                return stretch ? flux_f64_stretch_c(c, conv, order) : flux_f64_identity_c(c, conv, order);
+            return stretch ? flux_f32_stretch_c(c, conv, order) : flux_f32_identity_c(c, conv, order);
+        }
         if (desc->precision == GBNS_PREC_FP64)
         {
             if (!stretch) return upwind ? flux_f64x_identity_b(c, conv, order) : flux_f64x_identity_a(c, conv, order);

@@ -1,5 +1,6 @@
 // Instantiation helper for the flux-divergence translation units.  Each TU
 // defines GBNS_REAL, GBNS_STRETCH, GBNS_GROUP, GBNS_TAG and GBNS_FN and includes this.
+// Groups: 0 = none / cent_keep / totani, 1 = fweno / WENO5, 2 = hybrid.
 #pragma once
 
 #include <cstring>
@@ -120,7 +121,7 @@ namespace gbns
             if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
             GBNS_RUN_D(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
         }
-#else
+#elif GBNS_GROUP == 1
         if (conv == GBNS_CONV_FWENO)
         {
             if (v == 1) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 4, 128);
@@ -134,6 +135,22 @@ namespace gbns
             if (v == 2) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 4, 4, 128);
             if (GBNS_FP32 && v == 3) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
             GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
+        }
+#else
+        if (conv == GBNS_CONV_HYBRID)
+        {
+            if (order == 2)
+            {
+                if (v == 1) GBNS_RUN_D(GBNS_CONV_HYBRID, 2, 8, 8, 8, 256);
+                if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_HYBRID, 2, 8, 8, 4, 256);
+                GBNS_RUN_D(GBNS_CONV_HYBRID, 2, 8, 8, 4, 256);
+            }
+            if (order == 4)
+            {
+                if (v == 1) GBNS_RUN_D(GBNS_CONV_HYBRID, 4, 8, 8, 8, 256);
+                if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_HYBRID, 4, 8, 8, 4, 256);
+                GBNS_RUN_D(GBNS_CONV_HYBRID, 4, 8, 8, 4, 256);
+            }
         }
 #endif
         return set_error(GBNS_ERR_UNSUPPORTED, "flux scheme not instantiated");

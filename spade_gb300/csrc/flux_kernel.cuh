@@ -28,10 +28,17 @@ namespace gbns
             (CONV == GBNS_CONV_CENT_KEEP) ? ORDER/2 :
             (CONV == GBNS_CONV_TOTANI)    ? 1 :
             (CONV == GBNS_CONV_FWENO)     ? 2 :
-            (CONV == GBNS_CONV_WENO5)     ? 3 : 0;
+            (CONV == GBNS_CONV_WENO5)     ? 3 :
+            (CONV == GBNS_CONV_HYBRID)    ? (ORDER/2 > 2 ? ORDER/2 : 2) : 0;
+        // derived per-cell values: centred schemes (rho, e), fweno/WENO5
+        // (rho, Rusanov speed * rho/2, total energy); the hybrid keeps the
+        // fweno three plus the centred e (rho is the same value for both).
         static constexpr int NDER =
+            (CONV == GBNS_CONV_HYBRID) ? 4 :
             (CONV == GBNS_CONV_FWENO || CONV == GBNS_CONV_WENO5) ? 3 :
             (CONV == GBNS_CONV_CENT_KEEP || CONV == GBNS_CONV_TOTANI) ? 2 : 0;
+        // slot of the centred internal energy p/(rho (gamma-1))
+        static constexpr int CK_E = (CONV == GBNS_CONV_HYBRID) ? 3 : 1;
     };
 
     template <bool S> using YTabT = typename std::conditional<S, YTabK, YTabNone>::type;
@@ -106,7 +113,8 @@ namespace gbns
         Real gamma, R, gm1, spec_heat, inv_gamma_avg, R_avg, eps_p, eps_T, sens;
         Real mu, beta_c, alpha_c, T_ref, power, inv_pr, prandtl, tref_plus_s, S;
         Real ck_a[4];
-        int diss, visc, law, smooth, sensor;
+        int diss, visc, law, smooth, sensor, hyb_flux, hyb_sensor;
+        Real hyb_param;
         __device__ __forceinline__ void load(const SchemeK& s)
         {
             gamma = Real(s.gamma); R = Real(s.R); gm1 = Real(s.gm1); spec_heat = Real(s.spec_heat);
@@ -117,6 +125,7 @@ namespace gbns
             tref_plus_s = Real(s.tref_plus_s); S = Real(s.S);
             for (int i = 0; i < 4; ++i) ck_a[i] = Real(s.ck_a[i]);
             diss = s.diss; visc = s.visc; law = s.law; smooth = s.smooth; sensor = s.sensor;
+            hyb_flux = s.hyb_flux; hyb_sensor = s.hyb_sensor; hyb_param = Real(s.hyb_param);
         }
     };
 
@@ -141,7 +150,8 @@ namespace gbns
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = p/(rho*S.gm1);
         }
-        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5)
+        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5 ||
+                           Cfg::CONV == GBNS_CONV_HYBRID)
         {
             // fweno_t per-point split (convective.h:360-376, 458-467)
             Real r = S.R*T;
@@ -161,6 +171,9 @@ namespace gbns
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = h;
             der[2*Cfg::BOXN + c] = e;
+            // cent_keep's e (convective.h:131); its rho = p/(R*T) is the
+            // same rounding as fweno's p/r above
+            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = p/(rho*S.gm1);
         }
     }
 
@@ -189,7 +202,7 @@ namespace gbns
             const int c = rc + (m - hw)*SD;
             un[m]  = V.q(2 + D, c)*nD;
             rho[m] = V.d(0, c);
-            eng[m] = V.d(1, c);
+            eng[m] = V.d(ConvTraits<Cfg::CONV, Cfg::ORDER>::CK_E, c);
         }
         Real cc = 0, mx = 0, my = 0, mz = 0, g = 0, k = 0, ie = 0, pp = 0;
         #pragma unroll
@@ -525,17 +538,42 @@ namespace gbns
         // terms in fixed registers (no pointer selection: keeps them out of
         // local memory); summed conv + (diss + visc) like compose
         Real t0[5], t1[5], t2[5];
-        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP) conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
+        Real grad[3][4];
+        bool have_grad = false;
+        const bool hd = S.diss != 0, hv = S.visc != 0;
+        const bool ducros = hd && S.sensor == GBNS_SENSOR_DUCROS;
+        if constexpr (Cfg::CONV == GBNS_CONV_HYBRID)
+        {
+            // hybrid_scheme_t::operator() (hybrid_scheme.h:30-46): the blender
+            // at the face, then (1 - s) F_centred + s F_fweno (full_flux) or
+            // F_centred + s F_fweno (diss_flux).  The face gradient, when the
+            // blender needs it, is kept for dissipation and viscous terms.
+            Real blend = S.hyb_param;
+            if (S.hyb_sensor == GBNS_SENSOR_DUCROS)
+            {
+                face_gradient<Cfg, D>(V, rc, inv, im, grad);
+                have_grad = true;
+                blend = ducros_sensor<Real>(grad, S.hyb_param);
+            }
+            conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
+            conv_fweno<Cfg, D>(V, S, rc, nD, t1);
+            const Real c0 = S.hyb_flux == GBNS_HYBRID_DISS_FLUX ? Real(1.0) : Real(1.0) - blend;
+            #pragma unroll
+            for (int v = 0; v < 5; ++v)
+            {
+                t0[v] *= c0;
+                t1[v] *= blend;
+                t0[v] += t1[v];
+            }
+        }
+        else if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP) conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
         else if constexpr (Cfg::CONV == GBNS_CONV_TOTANI) conv_totani<Cfg, D>(V, S, rc, nD, t0);
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) conv_fweno<Cfg, D>(V, S, rc, nD, t0);
         else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) conv_weno5<Cfg, D>(V, S, rc, nD, t0);
-        const bool hd = S.diss != 0, hv = S.visc != 0;
-        const bool ducros = hd && S.sensor == GBNS_SENSOR_DUCROS;
         // const_sensor_t dissipation runs before the gradient is formed, so
         // the gradient is not live across it; ducros_t needs the gradient first.
         if (hd && !ducros) diss_pressure<Cfg, D>(V, S, rc, S.sens, t1);
-        Real grad[3][4];
-        if (hv || ducros) face_gradient<Cfg, D>(V, rc, inv, im, grad);
+        if ((hv || ducros) && !have_grad) face_gradient<Cfg, D>(V, rc, inv, im, grad);
         if (ducros) diss_pressure<Cfg, D>(V, S, rc, ducros_sensor<Real>(grad, S.sens), t1);
         if (hv) visc_lr<Cfg, D>(V, S, rc, nD, grad, t2);
         #pragma unroll

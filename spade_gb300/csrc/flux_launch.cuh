@@ -49,6 +49,12 @@ namespace gbns
     int flux_f32_identity_b(const FluxCall& c, int conv, int order);
     int flux_f32_stretch_a (const FluxCall& c, int conv, int order);
     int flux_f32_stretch_b (const FluxCall& c, int conv, int order);
+    int flux_f64x_identity_c(const FluxCall& c, int conv, int order);
+    int flux_f64x_stretch_c (const FluxCall& c, int conv, int order);
+    int flux_f64_identity_c(const FluxCall& c, int conv, int order);
+    int flux_f64_stretch_c (const FluxCall& c, int conv, int order);
+    int flux_f32_identity_c(const FluxCall& c, int conv, int order);
+    int flux_f32_stretch_c (const FluxCall& c, int conv, int order);
 
     // Number of tile variants built for a scheme (autotuner search space).
     int flux_variant_count(const gbns_scheme_desc* s);

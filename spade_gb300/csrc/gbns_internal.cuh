@@ -60,6 +60,8 @@ namespace gbns
     struct SchemeK
     {
         int diss, visc, law, smooth, sensor;
+        int hyb_flux, hyb_sensor;      // hybrid_scheme_t tag and blender kind
+        double hyb_param;              // blender const_sensor_t alpha or ducros_t epsilon
         double gamma, R, gm1;          // gm1 = gamma - 1.0
         double spec_heat;              // gamma*R/(gamma - 1.0)        (viscous.h:67)
         double inv_gamma_avg;          // 1.0/(0.5*(gamma + gamma))    (convective.h:226,233)

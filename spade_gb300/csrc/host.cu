@@ -174,6 +174,7 @@ namespace gbns
         else if (s->convective == GBNS_CONV_TOTANI) h = 1;
         else if (s->convective == GBNS_CONV_FWENO) h = 2;
         else if (s->convective == GBNS_CONV_WENO5) h = 3;
+        else if (s->convective == GBNS_CONV_HYBRID) h = s->order/2 > 2 ? s->order/2 : 2;
         if ((s->dissipation || s->viscous) && h < 1) h = 1;   // ducros_t's face gradient needs 1 too
         return h;
     }
@@ -181,10 +182,19 @@ namespace gbns
     int make_scheme(const gbns_scheme_desc* s, SchemeK& S)
     {
         if (!s) return set_error(GBNS_ERR_INVALID, "scheme descriptor is NULL");
-        if (s->convective < GBNS_CONV_NONE || s->convective > GBNS_CONV_WENO5)
+        if (s->convective < GBNS_CONV_NONE || s->convective > GBNS_CONV_HYBRID)
             return set_error(GBNS_ERR_INVALID, "unknown convective scheme");
         if (s->convective == GBNS_CONV_CENT_KEEP && !(s->order == 2 || s->order == 4 || s->order == 6 || s->order == 8))
             return set_error(GBNS_ERR_UNSUPPORTED, "cent_keep order must be 2, 4, 6 or 8");
+        if (s->convective == GBNS_CONV_HYBRID)
+        {
+            if (!(s->order == 2 || s->order == 4))
+                return set_error(GBNS_ERR_UNSUPPORTED, "hybrid_scheme_t is lowered with cent_keep order 2 or 4");
+            if (s->hybrid_flux != GBNS_HYBRID_FULL_FLUX && s->hybrid_flux != GBNS_HYBRID_DISS_FLUX)
+                return set_error(GBNS_ERR_INVALID, "unknown hybrid flux tag");
+            if (s->hybrid_sensor != GBNS_SENSOR_CONST && s->hybrid_sensor != GBNS_SENSOR_DUCROS)
+                return set_error(GBNS_ERR_UNSUPPORTED, "unknown hybrid blender");
+        }
         if (s->dissipation < 0 || s->dissipation > GBNS_DISS_PRESSURE) return set_error(GBNS_ERR_INVALID, "unknown dissipation");
         if (s->dissipation && s->sensor != GBNS_SENSOR_CONST && s->sensor != GBNS_SENSOR_DUCROS)
             return set_error(GBNS_ERR_UNSUPPORTED, "unknown shock sensor");
@@ -201,6 +211,9 @@ namespace gbns
         S.law = s->visc_law;
         S.smooth = s->weno_smooth;
         S.sensor = s->sensor;
+        S.hyb_flux = s->hybrid_flux;
+        S.hyb_sensor = s->hybrid_sensor;
+        S.hyb_param = s->hybrid_param;
         const double gam = s->gas.gamma, R = s->gas.R;
         S.gamma = gam; S.R = R;
         S.gm1 = gam - 1.0;
@@ -215,7 +228,7 @@ namespace gbns
         S.T_ref = s->T_ref; S.power = s->power; S.prandtl = s->prandtl;
         S.tref_plus_s = s->T_ref + s->S;
         S.S = s->S;
-        if (s->convective == GBNS_CONV_CENT_KEEP)
+        if (s->convective == GBNS_CONV_CENT_KEEP || s->convective == GBNS_CONV_HYBRID)
             for (int ii = 1; ii <= s->order/2; ++ii) S.ck_a[ii - 1] = cfd_coeff(ii, s->order);
         return GBNS_OK;
     }

@@ -41,12 +41,17 @@ def lower(flux_func, precision=_abi.PREC_FP64):
     gas = None
     order = []   # canonical order: convective, dissipation, viscous
     for k in kernels:
-        if isinstance(k, (convective.cent_keep_scheme_t, convective.totani_lr, convective.fweno_t, convective.weno5_t)):
+        if isinstance(k, (convective.cent_keep_scheme_t, convective.totani_lr, convective.fweno_t, convective.weno5_t,
+                          convective.hybrid_scheme_t)):
             if s.convective != _abi.CONV_NONE:
                 raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "at most one convective functor per composite")
             s.convective = k.kind
             s.order = k.order
             s.weno_smooth = getattr(k, "smooth", 1)
+            if k.kind == _abi.CONV_HYBRID:
+                s.hybrid_flux = k.tag.kind
+                s.hybrid_sensor = k.blender.kind
+                s.hybrid_param = k.blender.alpha
             order.append(0)
         elif isinstance(k, convective.pressure_diss_lr):
             if s.dissipation:

@@ -74,7 +74,7 @@ def build_instance(req, precision, seed):
     nb = req.edge // req.block
     if req.kind == "tgv":
         prob = workloads.taylor_green(nblk=(nb, nb, nb), ncell=(req.block,) * 3, ng=2, mach=req.mach,
-                                      reynolds=req.reynolds, seed=seed, rng="torch")
+                                      reynolds=req.reynolds, seed=seed, rng="torch", p_factor=1.0 / 16.0)
     else:
         prob = workloads.channel(nblk=(nb, nb, nb), ncell=(req.block,) * 3, ng=3, mach_b=req.mach,
                                  re_b=req.reynolds, seed=seed, rng="torch")

@@ -67,8 +67,14 @@ def _noise(shape, kind, scale, seed, rng, device):
 
 def taylor_green(nblk=(2, 2, 2), ncell=(16, 16, 16), ng=2, mach=0.1, reynolds=1600.0, prandtl=0.72,
                  gamma=1.4, R=287.0, T0=300.0, rho0=1.0, noise=1e-3, seed=0, cfl=0.5,
-                 rng="numpy", device="cuda", convective_scheme="cent_keep2"):
-    """Taylor–Green vortex on [0, 2 pi]^3 (identity coordinates, periodic)."""
+                 rng="numpy", device="cuda", convective_scheme="cent_keep2", p_factor=1.0):
+    """Taylor–Green vortex on [0, 2 pi]^3 (identity coordinates, periodic).
+
+    p = p0 + p_factor rho0 u0^2 (cos 2x + cos 2y)(cos 2z + 2).  p_factor = 1
+    is the reference driver's form (development/cuda-tgv/main.cc:107-116),
+    which omits the textbook 1/16 and so turns the pressure negative above
+    Mach ~0.27 (gamma M^2 * 6 > 1); p_factor = 1/16 is the textbook field,
+    positive up to Mach ~1."""
     L = 1.0
     p0 = rho0 * R * T0
     u0 = mach * math.sqrt(gamma * R * T0)
@@ -82,7 +88,7 @@ def taylor_green(nblk=(2, 2, 2), ncell=(16, 16, 16), ng=2, mach=0.1, reynolds=16
     y = torch.from_numpy(_cell_centres(g, nb, ng, 1)).to(device)[:, None, :, None]
     z = torch.from_numpy(_cell_centres(g, nb, ng, 2)).to(device)[:, :, None, None]
     d = q.data
-    d[..., 0] = p0 + rho0 * u0 * u0 * (torch.cos(2 * x / L) + torch.cos(2 * y / L)) * (torch.cos(2 * z / L) + 2.0)
+    d[..., 0] = p0 + p_factor * rho0 * u0 * u0 * (torch.cos(2 * x / L) + torch.cos(2 * y / L)) * (torch.cos(2 * z / L) + 2.0)
     d[..., 1] = T0
     d[..., 2] = u0 * torch.sin(x / L) * torch.cos(y / L) * torch.cos(z / L)
     d[..., 3] = -u0 * torch.cos(x / L) * torch.sin(y / L) * torch.cos(z / L)

@@ -12,10 +12,10 @@ static int record(const gbns_grid_desc* g, const gbns_scheme_desc* s, const doub
     std::printf("grid %d %d %d %d %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g\n",
                 g->nblk[0], g->nblk[1], g->nblk[2], g->ncell[0], g->ncell[1], g->ncell[2], g->ng,
                 g->bounds[0], g->bounds[1], g->bounds[2], g->bounds[3], g->bounds[4], g->bounds[5]);
-    std::printf("scheme %d %d %d %d %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g incr %d ptrs %d sensor %d\n",
+    std::printf("scheme %d %d %d %d %d %d %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g incr %d ptrs %d sensor %d hyb %d %d %.17g\n",
                 s->convective, s->order, s->weno_smooth, s->dissipation, s->viscous, s->visc_law, s->precision,
                 s->eps_p, s->eps_T, s->sensor_alpha, s->mu, s->prandtl_inv, s->gas.gamma, s->gas.R, s->T_ref,
-                incr, int(q != nullptr && r != nullptr), s->sensor);
+                incr, int(q != nullptr && r != nullptr), s->sensor, s->hybrid_flux, s->hybrid_sensor, s->hybrid_param);
     return 0;
 }
 #define GBNS_DROPIN_HOOK record
@@ -60,7 +60,11 @@ int main(int argc, char** argv)
         spade::convective::pressure_diss_lr ddiss(air, ducros, 0.1, 0.2);
         spade::pde_algs::flux_div(q, rhs, spade::omni::compose(spade::convective::fweno_t<decltype(air)>(air), ddiss, visc),
                                   spade::algs::make_traits(spade::pde_algs::gb300));
+        // 5: hybrid centred/WENO flux blended by the Ducros sensor, diss_flux tag
+        spade::convective::hybrid_scheme_t hyb(spade::convective::cent_keep<4>(air), spade::convective::fweno_t<decltype(air)>(air),
+                                               spade::state_sensor::ducros_t<real_t>(0.125), spade::convective::diss_flux);
+        spade::pde_algs::flux_div(q, rhs, spade::omni::compose(hyb, visc), spade::algs::make_traits(spade::pde_algs::gb300));
     });
     std::printf("calls %d\n", g_calls);
-    return g_calls == 4 ? 0 : 1;
+    return g_calls == 5 ? 0 : 1;
 }

@@ -41,6 +41,15 @@ FLUX_CASES = {
     "ducros_diss": (O.REF_DUCROS_DISS, dict(conv=_abi.CONV_NONE, diss=1, sensor=_abi.SENSOR_DUCROS, alpha=0.7)),
     "fweno_ducros_visc": (O.REF_FWENO_DUCROS_VISC, dict(conv=_abi.CONV_FWENO, diss=1, visc=1,
                                                          sensor=_abi.SENSOR_DUCROS, alpha=0.7)),
+    "hyb_ck2_full": (O.REF_HYB_CK2_FULL, dict(conv=_abi.CONV_HYBRID, order=2, hybrid_flux=_abi.HYBRID_FULL_FLUX,
+                                               hybrid_sensor=_abi.SENSOR_DUCROS, hybrid_param=0.5)),
+    "hyb_ck4_diss_visc": (O.REF_HYB_CK4_DISS_VISC, dict(conv=_abi.CONV_HYBRID, order=4, visc=1,
+                                                         hybrid_flux=_abi.HYBRID_DISS_FLUX,
+                                                         hybrid_sensor=_abi.SENSOR_DUCROS, hybrid_param=0.5)),
+    "hyb_ck2_const_ducros_diss_visc": (O.REF_HYB_CK2_CONST_DISS_VISC,
+                                       dict(conv=_abi.CONV_HYBRID, order=2, diss=1, visc=1, sensor=_abi.SENSOR_DUCROS,
+                                            alpha=0.7, hybrid_flux=_abi.HYBRID_FULL_FLUX,
+                                            hybrid_sensor=_abi.SENSOR_CONST, hybrid_param=0.3)),
 }
 
 FLUX_GRID = dict(nblk=(2, 1, 1), ncell=(6, 5, 4), ng=4, bounds=(0.0, 1.3, 0.0, 0.9, 0.0, 0.7))

@@ -30,9 +30,10 @@ def random_state(nblk, ncell, ng, seed, p0=86100.0, T0=300.0, u0=34.7, rel=0.02)
 
 def scheme(conv=_abi.CONV_CENT_KEEP, order=2, diss=0, visc=0, smooth=1, law=_abi.LAW_CONSTANT,
            mu=2.17e-2, eps_p=0.3, eps_T=0.2, alpha=0.7, T_ref=300.0, power=0.76, S=110.4,
-           precision=_abi.PREC_FP64, gamma=GAMMA, R=RGAS, sensor=_abi.SENSOR_CONST):
+           precision=_abi.PREC_FP64, gamma=GAMMA, R=RGAS, sensor=_abi.SENSOR_CONST,
+           hybrid_flux=_abi.HYBRID_FULL_FLUX, hybrid_sensor=_abi.SENSOR_DUCROS, hybrid_param=0.5):
     """alpha is const_sensor_t's alpha, or ducros_t's epsilon when sensor is
-    SENSOR_DUCROS."""
+    SENSOR_DUCROS.  hybrid_* describe the blender of a CONV_HYBRID scheme."""
     s = _abi.SchemeDesc()
     s.convective = conv
     s.order = order
@@ -47,6 +48,9 @@ def scheme(conv=_abi.CONV_CENT_KEEP, order=2, diss=0, visc=0, smooth=1, law=_abi
     s.eps_T = eps_T
     s.sensor = sensor
     s.sensor_alpha = alpha
+    s.hybrid_flux = hybrid_flux
+    s.hybrid_sensor = hybrid_sensor
+    s.hybrid_param = hybrid_param
     s.T_ref = T_ref
     s.power = power
     s.S = S

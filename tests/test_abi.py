@@ -45,7 +45,7 @@ def test_struct_layouts_match_c():
 int main(void){
   printf("%zu %zu %zu %zu\n", sizeof(gbns_grid_desc), sizeof(gbns_scheme_desc), sizeof(gbns_bc_desc), sizeof(gbns_gas_desc));
   printf("%zu %zu %zu\n", offsetof(gbns_grid_desc, bounds), offsetof(gbns_scheme_desc, eps_p), offsetof(gbns_scheme_desc, gas));
-  printf("%zu\n", offsetof(gbns_bc_desc, t_wall));
+  printf("%zu %zu\n", offsetof(gbns_bc_desc, t_wall), offsetof(gbns_scheme_desc, hybrid_param));
   return 0;}
 """
     with tempfile.TemporaryDirectory() as d:
@@ -56,7 +56,8 @@ int main(void){
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
     got = [int(x) for x in out]
     want = [ctypes.sizeof(_abi.GridDesc), ctypes.sizeof(_abi.SchemeDesc), ctypes.sizeof(_abi.BcDesc), ctypes.sizeof(_abi.GasDesc),
-            _abi.GridDesc.bounds.offset, _abi.SchemeDesc.eps_p.offset, _abi.SchemeDesc.gas.offset, _abi.BcDesc.t_wall.offset]
+            _abi.GridDesc.bounds.offset, _abi.SchemeDesc.eps_p.offset, _abi.SchemeDesc.gas.offset, _abi.BcDesc.t_wall.offset,
+            _abi.SchemeDesc.hybrid_param.offset]
     assert got == want
 
 
@@ -156,3 +157,14 @@ def test_lower_rejects_mixed_gases():
 def test_cent_keep_rejects_odd_order():
     with pytest.raises(ValueError):
         convective.cent_keep(3, air())
+
+
+def test_lower_hybrid_scheme():
+    h = convective.hybrid_scheme_t(convective.cent_keep(4, air()), convective.fweno_t(air()),
+                                   state_sensor.ducros_t(0.25), convective.diss_flux)
+    s = pde_algs.lower(omni.compose(h, viscous.visc_lr(viscous_laws.constant_viscosity_t(1e-3, 0.72), air())))
+    assert (s.convective, s.order, s.hybrid_flux, s.hybrid_sensor, s.hybrid_param, s.viscous) == \
+        (_abi.CONV_HYBRID, 4, _abi.HYBRID_DISS_FLUX, _abi.SENSOR_DUCROS, 0.25, 1)
+    with pytest.raises(ValueError):
+        convective.hybrid_scheme_t(convective.cent_keep(6, air()), convective.fweno_t(air()),
+                                   state_sensor.const_sensor_t(0.5), convective.full_flux)

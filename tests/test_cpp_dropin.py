@@ -28,7 +28,7 @@ def test_dropin_overload_and_lowering():
     lines = out.stdout.strip().splitlines()
     grids = [l.split() for l in lines if l.startswith("grid")]
     schemes = [l.split() for l in lines if l.startswith("scheme")]
-    assert len(grids) == 4 and len(schemes) == 4
+    assert len(grids) == 5 and len(schemes) == 5
     assert grids[0][1:8] == ["2", "3", "1", "8", "6", "4", "3"]
     assert [float(x) for x in grids[0][8:14]] == [0.0, 2.0, -1.0, 1.0, 0.0, 0.5]
     # cent_keep<2> + visc_lr(constant), FP64, increment
@@ -48,3 +48,8 @@ def test_dropin_overload_and_lowering():
     s = schemes[3]
     assert s[1:8] == ["3", "2", "1", "1", "1", "0", "0"] and s[s.index("sensor") + 1] == "1"
     assert [float(x) for x in s[8:11]] == [0.1, 0.2, 0.5]
+    # hybrid_scheme_t(cent_keep<4>, fweno_t, ducros_t(0.125), diss_flux) + visc
+    s = schemes[4]
+    assert s[1:3] == ["5", "4"] and s[5] == "1"
+    h = s.index("hyb")
+    assert s[h + 1:h + 3] == ["1", "1"] and float(s[h + 3]) == 0.125
