@@ -284,6 +284,32 @@ int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                      const gbns_bc_desc* bc, double* prims, double* work,
                      double dt, void* stream);
 
+/* ---- source terms ----------------------------------------------------
+ * Lowered forms of the point source a caller passes to
+ * spade::pde_algs::source_term (pde-algs/source_term.h:19-51), written as
+ * the flux_t (rho, rhoE, rhou, rhov, rhow) of the cell's primitives:
+ */
+#define GBNS_SOURCE_CONST       0  /* S = c[0..4] */
+#define GBNS_SOURCE_BODY_FORCE  1  /* f = c[2..4] per unit volume: S = (0, f_x u + f_y v + f_z w, f_x, f_y, f_z) */
+#define GBNS_SOURCE_BODY_ACCEL  2  /* g = c[2..4] per unit mass, rho = p/(R T):
+                                      S = (0, rho (g_x u + g_y v + g_z w), rho g_x, rho g_y, rho g_z) */
+
+typedef struct gbns_source_desc
+{
+    int32_t kind;          /* GBNS_SOURCE_* */
+    int32_t reserved;      /* must be 0 */
+    double  c[5];
+    gbns_gas_desc gas;
+} gbns_source_desc;
+
+/* rhs += S(prims)/jac on every interior cell, jac the cell's coordinate
+ * Jacobian (1 on identity coordinates).  Replaces
+ * spade::pde_algs::source_term(q, rhs, source_func)
+ * (pde-algs/source_term.h:19-51) for the lowered forms above.
+ * Asynchronous. */
+int gbns_source_term(const gbns_grid_desc* grid, const gbns_source_desc* source,
+                     const double* prims, double* rhs, void* stream);
+
 /* ---- batched form ----------------------------------------------------
  * Many independent grids ("instances") of uneven size advanced together:
  * each SSPRK3 stage is one persistent flux launch per kernel class (walking a

@@ -708,6 +708,51 @@ int oracle_flux_div(const gbns_grid_desc* g, const gbns_scheme_desc* S,
     return 0;
 }
 
+/* pde_algs::source_term (pde-algs/source_term.h:19-51) for the lowered
+ * point sources of gbns.h: rhs += S(q)/jac per interior cell, S in the
+ * operation order of the reference-side lambdas (oracle/ref_harness.cc). */
+int oracle_source_term(const gbns_grid_desc* g, const gbns_source_desc* src, const double* prims, double* rhs)
+{
+    geom_t G;
+    if (geom_init(g, &G)) return -1;
+    if (src->kind < GBNS_SOURCE_CONST || src->kind > GBNS_SOURCE_BODY_ACCEL) return -2;
+    for (int lb = 0; lb < G.nblk; ++lb)
+    {
+        double bmin[3], dx[3];
+        block_box(&G, lb, bmin, dx);
+        for (int k = 0; k < G.n[2]; ++k)
+        for (int j = 0; j < G.n[1]; ++j)
+        for (int i = 0; i < G.n[0]; ++i)
+        {
+            const double* w = prims + cell_off(&G, lb, i, j, k);
+            double* r = rhs + cell_off(&G, lb, i, j, k);
+            double s[5];
+            if (src->kind == GBNS_SOURCE_CONST)
+            {
+                for (int v = 0; v < 5; ++v) s[v] = src->c[v];
+            }
+            else
+            {
+                const double fu = src->c[2]*w[2] + src->c[3]*w[3] + src->c[4]*w[4];
+                if (src->kind == GBNS_SOURCE_BODY_FORCE)
+                {
+                    s[0] = 0.0; s[1] = fu; s[2] = src->c[2]; s[3] = src->c[3]; s[4] = src->c[4];
+                }
+                else
+                {
+                    const double rho = w[0]/(src->gas.R*w[1]);
+                    s[0] = 0.0; s[1] = rho*fu; s[2] = rho*src->c[2]; s[3] = rho*src->c[3]; s[4] = rho*src->c[4];
+                }
+            }
+            double jac = 1.0;
+            if (G.coords != GBNS_COORDS_IDENTITY)
+                jac = 1.0/(1.0*y_deriv(&G, bmin[1] + ((double)j + 0.5)*dx[1])*1.0);
+            for (int v = 0; v < 5; ++v) r[v] += s[v]/jac;
+        }
+    }
+    return 0;
+}
+
 /* Ghost fill: exchange resolved to the donor's interior, then walls.
  * Value of ghost (i,j,k) of block lb: for directions crossing a wall face
  * the index is mirrored first (boundary_fill.h:113-114) and the wall

@@ -45,6 +45,7 @@ def port():
         lib.oracle_reduce.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         lib.oracle_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
         lib.oracle_max_threads.restype = ctypes.c_int
+        lib.oracle_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), ctypes.c_void_p, ctypes.c_void_p]
         _port = lib
     return _port
 
@@ -62,6 +63,7 @@ def ref():
         lib.spade_ref_flux_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         lib.spade_ref_fill_ghosts.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.spade_ref_ssprk3.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.spade_ref_source_term.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -95,6 +97,10 @@ def reduce(grid, gas, prims, kind):
 
 def ssprk3_step(grid, scheme, bc, prims, work, dt, nthreads=0):
     _check(port().oracle_ssprk3_step(ctypes.byref(grid), ctypes.byref(scheme), ctypes.byref(bc), _ptr(prims), _ptr(work), float(dt), int(nthreads)), "oracle_ssprk3_step")
+
+
+def source_term(grid, src, prims, rhs):
+    _check(port().oracle_source_term(ctypes.byref(grid), ctypes.byref(src), _ptr(prims), _ptr(rhs)), "oracle_source_term")
 
 
 def max_threads():
@@ -156,3 +162,12 @@ def ref_ssprk3(ref_scheme, grid, scheme, bc, prims, dt, nsteps):
     ke = np.zeros(nsteps + 1)
     _check(ref().spade_ref_ssprk3(int(ref_scheme), ints.ctypes.data, reals.ctypes.data, float(dt), int(nsteps), _ptr(prims), _ptr(ke)), "spade_ref_ssprk3")
     return ke
+
+
+def ref_source_term(grid, scheme, src, prims, rhs):
+    """source_term through the reference (kind and c of `src`; the gas
+    constant comes from `scheme`)."""
+    ints, reals = _ref_problem(grid, scheme)
+    c = np.ascontiguousarray(np.array(list(src.c), dtype=np.float64))
+    _check(ref().spade_ref_source_term(int(src.kind), ints.ctypes.data, reals.ctypes.data, c.ctypes.data, _ptr(prims), _ptr(rhs)),
+           "spade_ref_source_term")

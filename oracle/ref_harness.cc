@@ -261,6 +261,66 @@ extern "C"
         return 0;
     }
 
+    // One source_term call (pde-algs/source_term.h:19-51) with a point
+    // source written as a lambda of the cell's primitive state:
+    //   kind 0: the constant flux_t c
+    //   kind 1: body force per unit volume f = c[2..4]: (0, f.u, f)
+    //   kind 2: acceleration g = c[2..4]: rho (0, g.u, g), rho = p/(R T)
+    // rhs (AoS5 with ghosts) is incremented in place.
+    int spade_ref_source_term(int kind, const int* ints, const double* reals, const double* c,
+                              const double* prims, double* rhs)
+    {
+        try
+        {
+            const problem_t pb = make_problem(ints, reals);
+            const double c0 = c[0], c1 = c[1], fx = c[2], fy = c[3], fz = c[4];
+            const double rgas = pb.rgas;
+            with_grid(pb, [&](auto& grid, auto& group)
+            {
+                spade::ctrs::array<int, 3> nexch(pb.ng, pb.ng, pb.ng);
+                spade::grid::grid_array q (grid, prim_t(0.0), nexch, spade::device::cpu);
+                spade::grid::grid_array r (grid, flux_t(0.0), nexch, spade::device::cpu);
+                copy_in(q, prims);
+                copy_in(r, rhs);
+                if (kind == 0)
+                {
+                    spade::pde_algs::source_term(q, r, [=](const prim_t&)
+                    {
+                        flux_t s;
+                        s[0] = c0; s[1] = c1; s[2] = fx; s[3] = fy; s[4] = fz;
+                        return s;
+                    });
+                }
+                else if (kind == 1)
+                {
+                    spade::pde_algs::source_term(q, r, [=](const prim_t& w)
+                    {
+                        flux_t s;
+                        s[0] = 0.0;
+                        s[1] = fx*w.u() + fy*w.v() + fz*w.w();
+                        s[2] = fx; s[3] = fy; s[4] = fz;
+                        return s;
+                    });
+                }
+                else
+                {
+                    spade::pde_algs::source_term(q, r, [=](const prim_t& w)
+                    {
+                        const double rho = w.p()/(rgas*w.T());
+                        flux_t s;
+                        s[0] = 0.0;
+                        s[1] = rho*(fx*w.u() + fy*w.v() + fz*w.w());
+                        s[2] = rho*fx; s[3] = rho*fy; s[4] = rho*fz;
+                        return s;
+                    });
+                }
+                copy_out(r, rhs);
+            });
+        }
+        catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_source_term: %s\n", e.what()); return -1; }
+        return 0;
+    }
+
     // Ghost fill through the reference's block exchange (periodic flags per
     // direction) followed, when wall_y != 0, by boundary_fill on y-min and
     // y-max with the isothermal no-slip wall.

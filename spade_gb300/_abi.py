@@ -99,6 +99,20 @@ class SchemeDesc(ctypes.Structure):
     ]
 
 
+SOURCE_CONST = 0
+SOURCE_BODY_FORCE = 1
+SOURCE_BODY_ACCEL = 2
+
+
+class SourceDesc(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("c", ctypes.c_double * 5),
+        ("gas", GasDesc),
+    ]
+
+
 class BcDesc(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32 * 6), ("t_wall", ctypes.c_double * 6)]
 

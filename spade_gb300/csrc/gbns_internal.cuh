@@ -21,6 +21,7 @@ namespace gbns
     // error reporting (per host thread)
     // ------------------------------------------------------------------
     int set_error(int code, const std::string& msg);
+    int sm_count();     // SMs of the current device
     int check_cuda(cudaError_t e, const char* what);
 
     // Device-side status words: kernels that give up on a bounded wait or

@@ -133,11 +133,11 @@ namespace gbns
         }
     }
 
-    static int sm_count()
+    int sm_count()
     {
         int dev = 0, n = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess) return 132;
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 132;
+        if (cudaGetDevice(&dev) != cudaSuccess) return 152;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) return 152;
         return n;
     }
 

@@ -115,3 +115,59 @@ def flux_div(prims, rhs, flux_func, traits=None, stream=None, variant=0):
     else:
         rc = _native.lib().gbns_flux_div(prims.desc(), scheme, prims.ptr(), rhs.ptr(), int(inc), _stream(stream))
     _native.check(rc)
+
+
+# ---------------------------------------------------------------- source_term
+
+class const_source_t:
+    """A constant point source: the flux_t (rho, rhoE, rhou, rhov, rhow)."""
+
+    def __init__(self, values):
+        values = [float(x) for x in values]
+        if len(values) != 5:
+            raise ValueError("a source is a flux_t of 5 values")
+        self.kind = _abi.SOURCE_CONST
+        self.c = values
+        self.R = 0.0
+
+
+class body_force_t:
+    """Body force per unit volume f: S = (0, f.u, f_x, f_y, f_z)."""
+
+    def __init__(self, fx, fy=0.0, fz=0.0):
+        self.kind = _abi.SOURCE_BODY_FORCE
+        self.c = [0.0, 0.0, float(fx), float(fy), float(fz)]
+        self.R = 0.0
+
+
+class body_accel_t:
+    """Acceleration g (force per unit mass): S = rho (0, g.u, g_x, g_y, g_z),
+    rho = p/(R T) from the gas."""
+
+    def __init__(self, gas, gx, gy=0.0, gz=0.0):
+        self.kind = _abi.SOURCE_BODY_ACCEL
+        self.c = [0.0, 0.0, float(gx), float(gy), float(gz)]
+        self.R = float(gas.R)
+
+
+def lower_source(src):
+    if not isinstance(src, (const_source_t, body_force_t, body_accel_t)):
+        raise _native.SpadeError(_abi.ERR_UNSUPPORTED, "source %r cannot be lowered to the GB300 kernels" % (src,))
+    d = _abi.SourceDesc()
+    d.kind = src.kind
+    for v in range(5):
+        d.c[v] = src.c[v]
+    d.gas.gamma = 1.4
+    d.gas.R = src.R
+    return d
+
+
+def source_term(q, rhs, source_func, stream=None):
+    """rhs += S(q)/jac on every interior cell: pde_algs::source_term(q, rhs,
+    source_func) (pde-algs/source_term.h:19-51) for the lowered point
+    sources const_source_t, body_force_t and body_accel_t.  Asynchronous on
+    the current torch stream."""
+    if q.shape != rhs.shape:
+        raise ValueError("q and rhs must live on the same grid")
+    d = lower_source(source_func)
+    _native.check(_native.lib().gbns_source_term(q.desc(), d, q.ptr(), rhs.ptr(), _stream(stream)))

@@ -79,6 +79,33 @@ def gen_flux():
     np.savez_compressed(os.path.join(OUT, "flux_div_ref.npz"), **out)
 
 
+SOURCE_C = (0.25, -1.5, 3.0, -0.75, 1.25)
+
+
+def source_desc(kind):
+    src = _abi.SourceDesc()
+    src.kind = kind
+    for v, x in enumerate(SOURCE_C):
+        src.c[v] = x
+    src.gas.gamma = P.GAMMA
+    src.gas.R = P.RGAS
+    return src
+
+
+def gen_source():
+    # pde_algs::source_term with the three lowered point-source forms
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    q = P.random_state(fg["nblk"], fg["ncell"], fg["ng"], seed=11)
+    r0 = P.random_state(fg["nblk"], fg["ncell"], fg["ng"], seed=13, p0=1.0, T0=1.0, u0=1.0)
+    out = {"rhs0": r0}
+    for kind in (_abi.SOURCE_CONST, _abi.SOURCE_BODY_FORCE, _abi.SOURCE_BODY_ACCEL):
+        r = r0.copy()
+        O.ref_source_term(grid, P.scheme(), source_desc(kind), q, r)
+        out["rhs_%d" % kind] = r
+    np.savez_compressed(os.path.join(OUT, "source_ref.npz"), **out)
+
+
 def gen_ghosts():
     gg = GHOST_GRID
     grid = _abi.grid_desc(gg["nblk"], gg["ncell"], gg["ng"], gg["bounds"])
@@ -159,6 +186,7 @@ if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("reference harness not built: make -C oracle ref")
     gen_flux()
+    gen_source()
     gen_ghosts()
     gen_tgv()
     gen_channel()

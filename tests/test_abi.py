@@ -168,3 +168,15 @@ def test_lower_hybrid_scheme():
     with pytest.raises(ValueError):
         convective.hybrid_scheme_t(convective.cent_keep(6, air()), convective.fweno_t(air()),
                                    state_sensor.const_sensor_t(0.5), convective.full_flux)
+
+
+def test_lower_sources_and_reject_callables():
+    d = pde_algs.lower_source(pde_algs.body_accel_t(air(), 9.81, 0.0, -1.0))
+    assert (d.kind, list(d.c), d.gas.R) == (_abi.SOURCE_BODY_ACCEL, [0.0, 0.0, 9.81, 0.0, -1.0], 287.0)
+    assert pde_algs.lower_source(pde_algs.body_force_t(2.0)).kind == _abi.SOURCE_BODY_FORCE
+    with pytest.raises(_native.SpadeError):
+        pde_algs.lower_source(lambda q: q)
+    g = _abi.grid_desc((1, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    bad = _abi.SourceDesc()
+    bad.kind = 7
+    assert _native.lib().gbns_source_term(g, bad, ctypes.c_void_p(16), ctypes.c_void_p(32), None) == _abi.ERR_INVALID

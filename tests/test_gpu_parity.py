@@ -398,3 +398,76 @@ def test_flux_div_rk_equals_flux_div_then_rk_stage(precision):
         assert np.array_equal(a, b)
     else:
         assert normwise(b, a) <= 1e-14
+
+
+@pytest.mark.gpu
+def test_resume_from_checkpoint_is_bitwise_identical():
+    """gbns_ssprk3_step: 3 steps, checkpoint (io.binary_write of the device
+    array), restart from the file into a fresh device array, 4 more steps ==
+    7 uninterrupted steps bit for bit, and both equal the oracle."""
+    import tempfile
+    import torch
+    from spade_gb300 import io
+    nblk, ncell, ng = (2, 1, 1), (8, 8, 8), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    tables = P.tgv_tables(nblk, ncell, ng)
+    q = P.tgv_state(nblk, ncell, ng, tables, seed=4)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    dt = P.tgv_dt(q, grid, ng)
+    s = P.tgv_scheme()
+    bc = P.periodic_bc()
+    L = lib()
+
+    def steps(dq, n):
+        work = torch.zeros(3 * dq.numel(), dtype=torch.float64, device="cuda")
+        for _ in range(n):
+            _native.check(L.gbns_ssprk3_step(grid, s, bc, ctypes.c_void_p(dq.data_ptr()), ctypes.c_void_p(work.data_ptr()),
+                                             ctypes.c_double(dt), stream()))
+        torch.cuda.synchronize()
+
+    full = dev(q)
+    steps(full, 7)
+    part = dev(q)
+    steps(part, 3)
+    with tempfile.TemporaryDirectory() as d:
+        f = os.path.join(d, "restart.bin")
+        io.binary_write(f, part)
+        fresh = torch.full_like(part, float("nan"))
+        io.binary_read(f, fresh)
+    steps(fresh, 4)
+    assert torch.equal(fresh, full)
+    ref = q.copy()
+    work = np.zeros((3,) + q.shape)
+    for _ in range(7):
+        O.ssprk3_step(grid, s, bc, ref, work, dt)
+    assert np.array_equal(interior(host(full), ng), interior(ref, ng))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", [_abi.SOURCE_CONST, _abi.SOURCE_BODY_FORCE, _abi.SOURCE_BODY_ACCEL])
+def test_source_term_bitwise_equals_reference(kind):
+    from golden.gen_golden import source_desc
+    g = load("source_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    q = dev(P.random_state(fg["nblk"], fg["ncell"], fg["ng"], seed=11))
+    r = dev(g["rhs0"])
+    _native.check(lib().gbns_source_term(grid, source_desc(kind), ctypes.c_void_p(q.data_ptr()),
+                                         ctypes.c_void_p(r.data_ptr()), stream()))
+    assert np.array_equal(host(r), g["rhs_%d" % kind])     # ghosts untouched, interior bit-identical
+
+
+@pytest.mark.gpu
+def test_source_term_stretched_matches_oracle():
+    from golden.gen_golden import source_desc
+    grid = _abi.grid_desc((2, 3, 1), (8, 6, 4), 2, (0.0, 1.0, -1.0, 1.0, 0.0, 0.5), coords=_abi.COORDS_TANH_Y,
+                          coord_param=(2.0, 0.0, 0.0, 0.0))
+    q = P.random_state((2, 3, 1), (8, 6, 4), 2, seed=17)
+    r0 = P.random_state((2, 3, 1), (8, 6, 4), 2, seed=18, p0=1.0, T0=1.0, u0=1.0)
+    src = source_desc(_abi.SOURCE_BODY_ACCEL)
+    want = r0.copy()
+    O.source_term(grid, src, q, want)
+    r = dev(r0)
+    qd = dev(q)
+    _native.check(lib().gbns_source_term(grid, src, ctypes.c_void_p(qd.data_ptr()), ctypes.c_void_p(r.data_ptr()), stream()))
+    assert np.array_equal(host(r), want)

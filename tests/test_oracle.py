@@ -118,3 +118,15 @@ def test_oracle_against_live_reference_random_states():
             O.ref_flux_div(rid, grid, s, q, a, increment=False)
             O.flux_div(grid, s, q, b, increment=False)
             assert np.array_equal(a, b), name
+
+
+@pytest.mark.parametrize("kind", [_abi.SOURCE_CONST, _abi.SOURCE_BODY_FORCE, _abi.SOURCE_BODY_ACCEL])
+def test_source_term_matches_reference_bitwise(kind):
+    from golden.gen_golden import source_desc
+    g = load("source_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    q = P.random_state(fg["nblk"], fg["ncell"], fg["ng"], seed=11)
+    r = g["rhs0"].copy()
+    O.source_term(grid, source_desc(kind), q, r)
+    assert np.array_equal(r, g["rhs_%d" % kind])
