@@ -277,9 +277,10 @@ def run_gpu(args, rank, world):
 
 
 def _read_traffic(cells):
-    """DRAM bytes per flux_div launch from the committed ncu summary, scaled
-    to this workload's cell count (traffic grows with the cells processed)."""
-    path = os.path.join(ROOT, "profiles", "flux_div_channel_fp64.md")
+    """DRAM bytes per fused flux_div launch (mean over the three SSPRK3
+    stages) from the committed ncu summary of a 2.1M-cell capture, scaled to
+    this workload's cell count (traffic grows with the cells processed)."""
+    path = os.path.join(ROOT, "profiles", "flux_div_rk_channel_fp64.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_cell:"):

@@ -20,8 +20,8 @@ namespace gbns
         {
             case GBNS_CONV_CENT_KEEP: return (s->order == 2 ? 4 : 1) + extra;
             case GBNS_CONV_TOTANI:    return 2 + extra;
-            case GBNS_CONV_FWENO:     return 3 + extra;
-            case GBNS_CONV_WENO5:     return 3 + extra;
+            case GBNS_CONV_FWENO:     return 4 + extra;
+            case GBNS_CONV_WENO5:     return 4 + extra;
             case GBNS_CONV_HYBRID:    return 2 + extra;
             default:                  return 1 + extra;
         }

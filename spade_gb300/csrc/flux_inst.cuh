@@ -126,14 +126,18 @@ namespace gbns
         {
             if (v == 1) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 4, 128);
             if (v == 2) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 16, 8, 4, 256);
-            if (GBNS_FP32 && v == 3) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
+            if (v == 3) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 8, 512);
+            if (GBNS_FP32 && v == 4) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
             GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
         }
         if (conv == GBNS_CONV_WENO5)
         {
             if (v == 1) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 8, 256);
             if (v == 2) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 4, 4, 128);
-            if (GBNS_FP32 && v == 3) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
+            // 16 warps on one 8^3 tile: twice the warps per SM of variant 1
+            // for latency hiding when one CTA fills shared memory (FP64)
+            if (v == 3) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 8, 512);
+            if (GBNS_FP32 && v == 4) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
             GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
         }
 #else

@@ -305,6 +305,28 @@ namespace gbns
         if (!smooth)
             return Real(1.0/3.0)*r0 + Real(2.0/3.0)*r1 + Real(2.0/3.0)*r2 + Real(1.0/3.0)*r3;
         const Real eps = Real(1e-16);
+        if constexpr (sizeof(Real) == 4)
+        {
+            // FP32: (d^2 + eps)^2 overflows once |d| passes ~4e9 (energy
+            // fluxes of ~1e8 with steep neighbours reach it).  Each weight
+            // is a ratio of two such terms, unchanged when both differences
+            // and eps are scaled by the pair's largest |d| (eps by its
+            // square); the floor keeps 1/s finite when both are zero (then
+            // e = 1, i.e. the unscaled eps-only weights).
+            auto wpair = [&](Real d0, Real d1) -> Real
+            {
+                const Real sc = fmaxf(fmaxf(fabsf(d0), fabsf(d1)), Real(1e-8));
+                const Real is = Real(1.0)/sc;
+                const Real e = (eps*is)*is;
+                Real x0 = d0*is, x1 = d1*is;
+                x0 = x0*x0 + e; x0 *= x0;
+                x1 = x1*x1 + e; x1 *= x1;
+                return x1/(x0 + x0 + x1);
+            };
+            const Real w0 = wpair(f0uk - f1uk, f1uk - f2uk);
+            const Real w3 = wpair(f2dk - f3dk, f1dk - f2dk);
+            return w0*r0 + (Real(1.0) - w0)*r1 + (Real(1.0) - w3)*r2 + w3*r3;
+        }
         Real a0 = (f0uk) - (f1uk), a1 = (f1uk) - (f2uk), a2 = (f1dk) - (f2dk), a3 = (f2dk) - (f3dk);
         a0 *= a0; a0 += eps; a0 *= a0;
         a1 *= a1; a1 += eps; a1 *= a1;
@@ -337,7 +359,7 @@ namespace gbns
     // upwind to downwind.  No reference counterpart.  In FP64 the nonlinear
     // weights share one division: w_k = g_k prod_{j!=k} D_j / sum, with
     // D_j = (eps + beta_j)^2 (the same weights as g_k/D_k normalised); FP32
-    // keeps the per-weight divisions because the products can overflow.
+    // first divides every beta and eps by the largest beta (see below).
     template <class Real>
     __device__ __forceinline__ Real weno5_side(Real a, Real b, Real c, Real d, Real e, int smooth)
     {
@@ -366,11 +388,24 @@ namespace gbns
         }
         else
         {
-            const Real a0 = Real(0.1)/d0;
-            const Real a1 = Real(0.6)/d1;
-            const Real a2 = Real(0.3)/d2;
-            const Real inv = Real(1.0)/(a0 + a1 + a2);
-            return (a0*p0 + a1*p1 + a2*p2)*inv;
+            // FP32: (eps + beta)^2 overflows for beta > ~1.8e19, reached by
+            // the energy equation's fluxes (~1e8) in steep regions; the
+            // weights g_k/D_k normalised are unchanged when every beta and
+            // eps are divided by the largest beta.  With the scaled D_k <= 1
+            // the product form (one division) cannot overflow; the floor
+            // keeps the sum positive when two stencils are perfectly smooth.
+            (void)d0; (void)d1; (void)d2;
+            const Real sc = fmaxf(fmaxf(b0, b1), fmaxf(b2, eps));
+            const Real is = Real(1.0)/sc;
+            const Real e = eps*is;
+            const Real fl = Real(1e-30);
+            const Real q0 = fmaxf((b0*is + e)*(b0*is + e), fl);
+            const Real q1 = fmaxf((b1*is + e)*(b1*is + e), fl);
+            const Real q2 = fmaxf((b2*is + e)*(b2*is + e), fl);
+            const Real a0 = Real(0.1)*(q1*q2);
+            const Real a1 = Real(0.6)*(q0*q2);
+            const Real a2 = Real(0.3)*(q0*q1);
+            return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
         }
     }
 

@@ -471,3 +471,20 @@ def test_source_term_stretched_matches_oracle():
     qd = dev(q)
     _native.check(lib().gbns_source_term(grid, src, ctypes.c_void_p(qd.data_ptr()), ctypes.c_void_p(r.data_ptr()), stream()))
     assert np.array_equal(host(r), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("conv", [_abi.CONV_FWENO, _abi.CONV_WENO5])
+def test_fp32_flux_weno_weights_do_not_overflow(conv):
+    """Energy fluxes of ~1e11 with order-one jumps between neighbours (p ~ 1e7,
+    |u| ~ 3e3) push (beta + eps)^2 past the FP32 range; the FP32 weights are
+    computed on scaled smoothness indicators, so the residual stays finite and
+    close to FP64 (found as inf/NaN after 38 steps of the 16.8M-cell channel)."""
+    nblk, ncell, ng = (2, 1, 1), (8, 8, 8), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    q = P.random_state(nblk, ncell, ng, seed=51, p0=1.0e7, T0=300.0, u0=3.0e3, rel=0.15)
+    r64 = interior(gpu_flux(grid, P.scheme(conv=conv, diss=1, visc=1), q), ng)
+    r32 = interior(gpu_flux(grid, P.scheme(conv=conv, diss=1, visc=1, precision=_abi.PREC_FP32_FLUX), q), ng)
+    assert np.isfinite(r32).all()
+    err = np.abs(r32 - r64).reshape(-1, 5).max(axis=0) / np.abs(r64).reshape(-1, 5).max(axis=0)
+    assert np.all(err < 1e-3), err
