@@ -28,10 +28,15 @@
  * and omni::compose of one of each (convective, dissipation, viscous).
  * Coordinates: coords::identity.
  *
+ * source_term: spade::gb300::const_source_t / body_force_t / body_accel_t
+ * passed to spade::pde_algs::source_term run on the GPU (gbns_source_term).
+ *
  * Define GBNS_DROPIN_HOOK before including to route the lowered call to a
  * user function `int GBNS_DROPIN_HOOK(const gbns_grid_desc*, const
  * gbns_scheme_desc*, const double*, double*, int)` instead of the library
- * (used by the host-only tests of the lowering).
+ * (used by the host-only tests of the lowering); GBNS_DROPIN_SOURCE_HOOK,
+ * `int (const gbns_grid_desc*, const gbns_source_desc*, const double*, double*)`,
+ * does the same for source_term.
  */
 #pragma once
 
@@ -350,3 +355,84 @@ namespace spade::pde_algs
         }
     }
 }
+
+namespace spade::gb300
+{
+    // Point sources with a GB300 kernel (gbns_source_desc).  Passing one of
+    // these instead of a lambda to spade::pde_algs::source_term selects the
+    // overload below (a non-template parameter beats the reference's
+    // template, pde-algs/source_term.h:19-51).
+    struct const_source_t
+    {
+        fluid_state::flux_t<double> value;   // (rho, rhoE, rhou, rhov, rhow)
+    };
+    struct body_force_t                      // force per unit volume
+    {
+        double fx, fy, fz;
+    };
+    struct body_accel_t                      // force per unit mass; rho = p/(R T)
+    {
+        fluid_state::ideal_gas_t<double> gas;
+        double gx, gy, gz;
+    };
+
+    inline gbns_source_desc lower_source(const const_source_t& f)
+    {
+        gbns_source_desc d{};
+        d.kind = GBNS_SOURCE_CONST;
+        for (int v = 0; v < 5; ++v) d.c[v] = f.value[v];
+        return d;
+    }
+    inline gbns_source_desc lower_source(const body_force_t& f)
+    {
+        gbns_source_desc d{};
+        d.kind = GBNS_SOURCE_BODY_FORCE;
+        d.c[2] = f.fx; d.c[3] = f.fy; d.c[4] = f.fz;
+        return d;
+    }
+    inline gbns_source_desc lower_source(const body_accel_t& f)
+    {
+        gbns_source_desc d{};
+        d.kind = GBNS_SOURCE_BODY_ACCEL;
+        d.c[2] = f.gx; d.c[3] = f.gy; d.c[4] = f.gz;
+        d.gas.gamma = f.gas.gamma;
+        d.gas.R = f.gas.R;
+        return d;
+    }
+
+    template <typename src_t>
+    concept lowered_source = std::same_as<src_t, const_source_t> || std::same_as<src_t, body_force_t> ||
+                             std::same_as<src_t, body_accel_t>;
+}
+
+namespace spade::pde_algs
+{
+    // rhs += S(q)/jac on the interior: pde_algs::source_term
+    // (pde-algs/source_term.h:19-51) on the GPU for the lowered sources.
+    template <grid::multiblock_array sol_arr_t, grid::multiblock_array rhs_arr_t, gb300::lowered_source src_t>
+    requires grid::has_centering_type<sol_arr_t, grid::cell_centered>
+    static void source_term(const sol_arr_t& q, rhs_arr_t& rhs, const src_t& source)
+    {
+        const gbns_grid_desc g = gb300::lower_grid(q);
+        const gbns_source_desc d = gb300::lower_source(source);
+        const double* qp = q.image().base;
+        double* r = rhs.image().base;
+#ifdef GBNS_DROPIN_SOURCE_HOOK
+        const int rc = GBNS_DROPIN_SOURCE_HOOK(&g, &d, qp, r);
+#else
+        static_assert(device::is_gpu<typename sol_arr_t::device_type> && device::is_gpu<typename rhs_arr_t::device_type>,
+                      "the gb300 source_term runs on device::gpu arrays");
+        int rc = gbns_source_term(&g, &d, qp, r, nullptr);
+        if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+#endif
+        if (rc != GBNS_OK)
+        {
+            char msg[512] = "drop-in hook failed";
+#ifndef GBNS_DROPIN_SOURCE_HOOK
+            gbns_last_error(msg, sizeof(msg));
+#endif
+            throw except::sp_exception(std::string("gb300 source_term failed: ") + msg);
+        }
+    }
+}
+

@@ -20,6 +20,16 @@ static int record(const gbns_grid_desc* g, const gbns_scheme_desc* s, const doub
 }
 #define GBNS_DROPIN_HOOK record
 
+static int g_src_calls = 0;
+static int record_source(const gbns_grid_desc* g, const gbns_source_desc* d, const double* q, double* r)
+{
+    ++g_src_calls;
+    std::printf("source %d %.17g %.17g %.17g %.17g %.17g R %.17g ptrs %d\n", d->kind, d->c[0], d->c[1], d->c[2], d->c[3],
+                d->c[4], d->gas.R, int(q != nullptr && r != nullptr));
+    return 0;
+}
+#define GBNS_DROPIN_SOURCE_HOOK record_source
+
 #include "spade.h"
 #include "spade_gb300.h"
 
@@ -64,7 +74,10 @@ int main(int argc, char** argv)
         spade::convective::hybrid_scheme_t hyb(spade::convective::cent_keep<4>(air), spade::convective::fweno_t<decltype(air)>(air),
                                                spade::state_sensor::ducros_t<real_t>(0.125), spade::convective::diss_flux);
         spade::pde_algs::flux_div(q, rhs, spade::omni::compose(hyb, visc), spade::algs::make_traits(spade::pde_algs::gb300));
+        // 6, 7: lowered point sources through the source_term overload
+        spade::pde_algs::source_term(q, rhs, spade::gb300::body_force_t{2.5, 0.0, -1.0});
+        spade::pde_algs::source_term(q, rhs, spade::gb300::body_accel_t{air, 0.0, -9.81, 0.0});
     });
-    std::printf("calls %d\n", g_calls);
-    return g_calls == 5 ? 0 : 1;
+    std::printf("calls %d sources %d\n", g_calls, g_src_calls);
+    return (g_calls == 5 && g_src_calls == 2) ? 0 : 1;
 }

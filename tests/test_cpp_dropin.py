@@ -53,3 +53,8 @@ def test_dropin_overload_and_lowering():
     assert s[1:3] == ["5", "4"] and s[5] == "1"
     h = s.index("hyb")
     assert s[h + 1:h + 3] == ["1", "1"] and float(s[h + 3]) == 0.125
+    # source_term overload: body force, then body acceleration with the gas R
+    srcs = [l.split() for l in lines if l.startswith("source")]
+    assert len(srcs) == 2
+    assert srcs[0][1] == "1" and [float(x) for x in srcs[0][4:7]] == [2.5, 0.0, -1.0]
+    assert srcs[1][1] == "2" and [float(x) for x in srcs[1][4:7]] == [0.0, -9.81, 0.0] and float(srcs[1][8]) == 287.0
