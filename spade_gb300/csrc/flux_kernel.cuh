@@ -76,7 +76,16 @@ namespace gbns
         static constexpr int CPT = (NCELL + NT - 1)/NT;
         static constexpr size_t STAGE_BYTES = DIRECT ? 0 : align128(size_t(BOXN)*5*sizeof(double));
         static constexpr size_t SOA_BYTES   = FP64 ? 0 : align128(size_t(BOXN)*5*sizeof(float));
-        static constexpr size_t DER_BYTES   = align128(size_t(NDER > 0 ? NDER : 1)*BOXN*sizeof(Real));
+        // FP64 fweno / WENO5: the Rusanov split (f+ and f- of the 5 equations)
+        // of every cell on the tile's lines along the current direction is
+        // computed once per cell and direction into shared memory instead of
+        // once per stencil point per face (each cell sits in 4 or 6 face
+        // stencils per direction); it takes the place of the derived buffer.
+        static constexpr bool SPLIT = FP64 && (CONV == GBNS_CONV_FWENO || CONV == GBNS_CONV_WENO5);
+        static constexpr int NL0 = (TX + 2*HC)*TY*TZ, NL1 = TX*(TY + 2*HC)*TZ, NL2 = TX*TY*(TZ + 2*HC);
+        static constexpr int NLMAX = cmax3(NL0, NL1, NL2);
+        static constexpr size_t DER_BYTES   = SPLIT ? align128(size_t(10)*NLMAX*sizeof(double))
+                                                    : align128(size_t(NDER > 0 ? NDER : 1)*BOXN*sizeof(Real));
         // face fluxes are kept in FP64 (converted once per face)
         static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFMAX*sizeof(double));
         // FP32 staged: the staging buffer is dead once converted, so derived
@@ -99,6 +108,7 @@ namespace gbns
         const double* stage;   // AoS doubles (FP64 compute)
         const float*  soa;     // SoA floats (FP32 compute)
         const Real*   der;     // derived per-cell values, SoA
+        const double* split;   // SPLIT: f+/f- per equation of the current direction's line cells
         __device__ __forceinline__ Real q(int v, int c) const
         {
             if constexpr (Cfg::FP64) return stage[c*5 + v];
@@ -136,6 +146,30 @@ namespace gbns
 
     // ------------------------------------------------------------------
     // per-cell derived quantities (computed once per staged cell)
+    // fweno_t per-point quantities (convective.h:360-376, 458-467): rho,
+    // h = rho (|u| + a)/2 (the Rusanov speed times rho/2) and the total
+    // specific energy e.
+    template <class Real>
+    __device__ __forceinline__ void fweno_derive(const SchemeR<Real>& S, Real p, Real T, Real u, Real v, Real w,
+                                                 Real& rho_o, Real& h_o, Real& e_o)
+    {
+        Real r = S.R*T;
+        Real h = u*u;
+        h += v*v;
+        h += w*w;
+        h = dev_sqrt(h);
+        h += dev_sqrt(r*S.gamma);
+        const Real rho = p/r;
+        h *= rho;
+        h *= Real(0.5);
+        Real e = u*u;
+        e += v*v;
+        e += w*w;
+        e *= Real(0.5);
+        e += (S.R*T)/S.gm1;
+        rho_o = rho; h_o = h; e_o = e;
+    }
+
     // ------------------------------------------------------------------
     template <class Cfg>
     __device__ __forceinline__ void derive_cell(const BoxView<Cfg>& V, typename Cfg::Real* der,
@@ -153,21 +187,8 @@ namespace gbns
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5 ||
                            Cfg::CONV == GBNS_CONV_HYBRID)
         {
-            // fweno_t per-point split (convective.h:360-376, 458-467)
-            Real r = S.R*T;
-            Real h = u*u;
-            h += v*v;
-            h += w*w;
-            h = dev_sqrt(h);
-            h += dev_sqrt(r*S.gamma);
-            const Real rho = p/r;
-            h *= rho;
-            h *= Real(0.5);
-            Real e = u*u;
-            e += v*v;
-            e += w*w;
-            e *= Real(0.5);
-            e += (S.R*T)/S.gm1;
+            Real rho, h, e;
+            fweno_derive<Real>(S, p, T, u, v, w, rho, h, e);
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = h;
             der[2*Cfg::BOXN + c] = e;
@@ -259,12 +280,12 @@ namespace gbns
     // fweno_t flux/dissipation of equation `eq` at one stencil point
     // (convective.h:442-493).
     template <class Cfg, int D>
-    __device__ __forceinline__ void fweno_point(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                                int c, int eq, typename Cfg::Real nD,
-                                                typename Cfg::Real& fl, typename Cfg::Real& ds)
+    __device__ __forceinline__ void fweno_point_v(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                  int c, typename Cfg::Real rho, typename Cfg::Real hsr,
+                                                  typename Cfg::Real engy_c, int eq, typename Cfg::Real nD,
+                                                  typename Cfg::Real& fl, typename Cfg::Real& ds)
     {
         using Real = typename Cfg::Real;
-        const Real rho = V.d(0, c), hsr = V.d(1, c);
         const Real un = V.q(2 + D, c)*nD;
         if (eq == 0)
         {
@@ -273,7 +294,7 @@ namespace gbns
         }
         else if (eq == 1)
         {
-            const Real engy = V.d(2, c);
+            const Real engy = engy_c;
             fl = (un*(Real(0.5)*rho))*(engy + S.R*V.q(1, c));
             ds = hsr*engy;
         }
@@ -290,14 +311,22 @@ namespace gbns
         }
     }
 
+    template <class Cfg, int D>
+    __device__ __forceinline__ void fweno_point(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                int c, int eq, typename Cfg::Real nD,
+                                                typename Cfg::Real& fl, typename Cfg::Real& ds)
+    {
+        fweno_point_v<Cfg, D>(V, S, c, V.d(0, c), V.d(1, c), V.d(2, c), eq, nD, fl, ds);
+    }
+
     // apply_weno of fweno_t (convective.h:378-427)
     template <class Real>
-    __device__ __forceinline__ Real fweno_apply(const Real fl[4], const Real ds[4], int smooth)
+    __device__ __forceinline__ Real fweno_apply_ud(const Real fu[4], const Real fd[4], int smooth)
     {
-        const Real f0uk = fl[0] + ds[0], f0dk = fl[0] - ds[0];
-        const Real f1uk = fl[1] + ds[1], f1dk = fl[1] - ds[1];
-        const Real f2uk = fl[2] + ds[2], f2dk = fl[2] - ds[2];
-        const Real f3uk = fl[3] + ds[3], f3dk = fl[3] - ds[3];
+        const Real f0uk = fu[0], f0dk = fd[0];
+        const Real f1uk = fu[1], f1dk = fd[1];
+        const Real f2uk = fu[2], f2dk = fd[2];
+        const Real f3uk = fu[3], f3dk = fd[3];
         const Real r0 = Real(-0.5)*(f0uk) + Real(1.5)*(f1uk);
         const Real r1 = Real( 0.5)*(f1uk) + Real(0.5)*(f2uk);
         const Real r2 = Real( 0.5)*(f1dk) + Real(0.5)*(f2dk);
@@ -339,19 +368,92 @@ namespace gbns
         return a0*r0 + a1*r1 + a2*r2 + a3*r3;
     }
 
+    template <class Real>
+    __device__ __forceinline__ Real fweno_apply(const Real fl[4], const Real ds[4], int smooth)
+    {
+        Real fu[4], fd[4];
+        #pragma unroll
+        for (int m = 0; m < 4; ++m) { fu[m] = fl[m] + ds[m]; fd[m] = fl[m] - ds[m]; }
+        return fweno_apply_ud<Real>(fu, fd, smooth);
+    }
+
+    // Line stride of the split cache along D and the cache index of a face's
+    // right cell (tile-local fx, fy, fz).
+    template <class Cfg, int D> struct SplitIdx
+    {
+        static constexpr int HC = Cfg::HC;
+        static constexpr int LX = Cfg::TX + (D == 0 ? 2*HC : 0);
+        static constexpr int LY = Cfg::TY + (D == 1 ? 2*HC : 0);
+        static constexpr int LZ = Cfg::TZ + (D == 2 ? 2*HC : 0);
+        static constexpr int NL = LX*LY*LZ;
+        static constexpr int LS = D == 0 ? 1 : (D == 1 ? LX : LX*LY);
+        __device__ __forceinline__ static int right(int fx, int fy, int fz)
+        {
+            return (fx + (D == 0 ? HC : 0)) + LX*((fy + (D == 1 ? HC : 0)) + LY*(fz + (D == 2 ? HC : 0)));
+        }
+    };
+
+    // Fills the split cache for direction D: f+ = fl + ds and f- = fl - ds of
+    // every equation at every cell of the tile's lines along D (the stencil
+    // cells of all faces of the pass), with the same operations fweno_point
+    // performs per face.
+    template <class Cfg, int D>
+    __device__ __forceinline__ void split_fill(const BoxView<Cfg>& V, const SchemeR<double>& S, double* P,
+                                               const YTabT<Cfg::STRETCH>& Y, int by, int j0, int ny, int shift)
+    {
+        using SI = SplitIdx<Cfg, D>;
+        constexpr int H = Cfg::H, HC = Cfg::HC;
+        for (int l = threadIdx.x; l < SI::NL; l += Cfg::NT)
+        {
+            const int lx = l % SI::LX, ly = (l / SI::LX) % SI::LY, lz = l / (SI::LX*SI::LY);
+            const int x = lx - (D == 0 ? HC : 0), y = ly - (D == 1 ? HC : 0), z = lz - (D == 2 ? HC : 0);
+            const int c = (z + H)*Cfg::SZ + (y + H)*Cfg::SY + (x + H + shift);
+            double nD = 1.0;
+            if constexpr (Cfg::STRETCH && D != 1)
+            {
+                if (j0 + y < ny) nD = Y.m_cell[by*ny + j0 + y];
+            }
+            double rho, hsr, engy;
+            fweno_derive<double>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
+            #pragma unroll
+            for (int eq = 0; eq < 5; ++eq)
+            {
+                double fl, ds;
+                fweno_point_v<Cfg, D>(V, S, c, rho, hsr, engy, eq, nD, fl, ds);
+                P[(2*eq)*Cfg::NLMAX + l] = fl + ds;
+                P[(2*eq + 1)*Cfg::NLMAX + l] = fl - ds;
+            }
+        }
+    }
+
     template <class Cfg, int D>
     __device__ __forceinline__ void conv_fweno(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                               int rc, typename Cfg::Real nD, typename Cfg::Real* out)
+                                               int rc, int lr, typename Cfg::Real nD, typename Cfg::Real* out)
     {
         using Real = typename Cfg::Real;
         constexpr int SD = DirStride<Cfg, D>::S;
         #pragma unroll
         for (int eq = 0; eq < 5; ++eq)
         {
-            Real fl[4], ds[4];
-            #pragma unroll
-            for (int m = 0; m < 4; ++m) fweno_point<Cfg, D>(V, S, rc + (m - 2)*SD, eq, nD, fl[m], ds[m]);
-            out[eq] = fweno_apply<Real>(fl, ds, S.smooth);
+            if constexpr (Cfg::SPLIT)
+            {
+                constexpr int LS = SplitIdx<Cfg, D>::LS;
+                Real fu[4], fd[4];
+                #pragma unroll
+                for (int m = 0; m < 4; ++m)
+                {
+                    fu[m] = V.split[(2*eq)*Cfg::NLMAX + lr + (m - 2)*LS];
+                    fd[m] = V.split[(2*eq + 1)*Cfg::NLMAX + lr + (m - 2)*LS];
+                }
+                out[eq] = fweno_apply_ud<Real>(fu, fd, S.smooth);
+            }
+            else
+            {
+                Real fl[4], ds[4];
+                #pragma unroll
+                for (int m = 0; m < 4; ++m) fweno_point<Cfg, D>(V, S, rc + (m - 2)*SD, eq, nD, fl[m], ds[m]);
+                out[eq] = fweno_apply<Real>(fl, ds, S.smooth);
+            }
         }
     }
 
@@ -411,7 +513,7 @@ namespace gbns
 
     template <class Cfg, int D>
     __device__ __forceinline__ void conv_weno5(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                               int rc, typename Cfg::Real nD, typename Cfg::Real* out)
+                                               int rc, int lr, typename Cfg::Real nD, typename Cfg::Real* out)
     {
         using Real = typename Cfg::Real;
         constexpr int SD = DirStride<Cfg, D>::S;
@@ -422,10 +524,19 @@ namespace gbns
             #pragma unroll
             for (int m = 0; m < 6; ++m)
             {
-                Real fl, ds;
-                fweno_point<Cfg, D>(V, S, rc + (m - 3)*SD, eq, nD, fl, ds);
-                up[m] = fl + ds;
-                dn[m] = fl - ds;
+                if constexpr (Cfg::SPLIT)
+                {
+                    constexpr int LS = SplitIdx<Cfg, D>::LS;
+                    up[m] = V.split[(2*eq)*Cfg::NLMAX + lr + (m - 3)*LS];
+                    dn[m] = V.split[(2*eq + 1)*Cfg::NLMAX + lr + (m - 3)*LS];
+                }
+                else
+                {
+                    Real fl, ds;
+                    fweno_point<Cfg, D>(V, S, rc + (m - 3)*SD, eq, nD, fl, ds);
+                    up[m] = fl + ds;
+                    dn[m] = fl - ds;
+                }
             }
             out[eq] = weno5_side<Real>(up[0], up[1], up[2], up[3], up[4], S.smooth)
                     + weno5_side<Real>(dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
@@ -565,7 +676,7 @@ namespace gbns
     // Composite face flux conv + (diss + visc)  (omni/compose.h:19-24)
     template <class Cfg, int D>
     __device__ __forceinline__ void face_flux(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                              int rc, typename Cfg::Real nD,
+                                              int rc, int lr, typename Cfg::Real nD,
                                               const typename Cfg::Real inv[3], typename Cfg::Real im,
                                               typename Cfg::Real* F)
     {
@@ -591,7 +702,7 @@ namespace gbns
                 blend = ducros_sensor<Real>(grad, S.hyb_param);
             }
             conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
-            conv_fweno<Cfg, D>(V, S, rc, nD, t1);
+            conv_fweno<Cfg, D>(V, S, rc, lr, nD, t1);
             const Real c0 = S.hyb_flux == GBNS_HYBRID_DISS_FLUX ? Real(1.0) : Real(1.0) - blend;
             #pragma unroll
             for (int v = 0; v < 5; ++v)
@@ -603,8 +714,8 @@ namespace gbns
         }
         else if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP) conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
         else if constexpr (Cfg::CONV == GBNS_CONV_TOTANI) conv_totani<Cfg, D>(V, S, rc, nD, t0);
-        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) conv_fweno<Cfg, D>(V, S, rc, nD, t0);
-        else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) conv_weno5<Cfg, D>(V, S, rc, nD, t0);
+        else if constexpr (Cfg::CONV == GBNS_CONV_FWENO) conv_fweno<Cfg, D>(V, S, rc, lr, nD, t0);
+        else if constexpr (Cfg::CONV == GBNS_CONV_WENO5) conv_weno5<Cfg, D>(V, S, rc, lr, nD, t0);
         // const_sensor_t dissipation runs before the gradient is formed, so
         // the gradient is not live across it; ducros_t needs the gradient first.
         if (hd && !ducros) diss_pressure<Cfg, D>(V, S, rc, S.sens, t1);
@@ -654,6 +765,11 @@ namespace gbns
         constexpr int EX = TX + (D == 0), EY = TY + (D == 1);
         const int tid = threadIdx.x;
         const int ny = G.n[1];
+        if constexpr (Cfg::SPLIT)
+        {
+            split_fill<Cfg, D>(V, S, const_cast<double*>(V.split), Y, b[1], j0, ny, shift);
+            __syncthreads();
+        }
         for (int f = tid; f < NF; f += Cfg::NT)
         {
             const int fx = f % EX;
@@ -678,7 +794,7 @@ namespace gbns
                         im = Real(Y.im_cell[b[1]*ny + gj]);
                     }
                 }
-                face_flux<Cfg, D>(V, S, rc, nD, inv, im, F);
+                face_flux<Cfg, D>(V, S, rc, SplitIdx<Cfg, D>::right(fx, fy, fz), nD, inv, im, F);
             }
             #pragma unroll
             for (int v = 0; v < 5; ++v) sF[v*Cfg::NFMAX + f] = double(F[v]);
@@ -839,11 +955,12 @@ namespace gbns
         V.stage = stage;
         V.soa = soa;
         V.der = der;
+        V.split = reinterpret_cast<const double*>(der);
         SchemeR<Real> S;
         S.load(SK);
 
         // ---- per-cell derived values on the stencil cross -------------------
-        if constexpr (Cfg::NDER > 0)
+        if constexpr (Cfg::NDER > 0 && !Cfg::SPLIT)
         {
             constexpr int HC = Cfg::HC;
             for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
@@ -900,7 +1017,8 @@ namespace gbns
                     for (int v = 0; v < 5; ++v) qv[v] = __ldg(A.prims + off + v);
                 }
                 double cs[5];
-                prim_to_cons(qv, SK.R, SK.gm1, cs);
+                if constexpr (Cfg::FP64) prim_to_cons(qv, SK.R, SK.gm1, cs);
+                else prim_to_cons_fast(qv, SK.R, SK.inv_gm1, cs);
                 for (int j = 0; j + 1 < A.rk_nres; ++j)
                 {
                     const double* rr = A.rk_res[j] + off;
@@ -911,7 +1029,8 @@ namespace gbns
                 #pragma unroll
                 for (int v = 0; v < 5; ++v) cs[v] += cl*relem[s][v];
                 double qn[5];
-                cons_to_prim(cs, SK.R, SK.gm1, qn);
+                if constexpr (Cfg::FP64) cons_to_prim(cs, SK.R, SK.gm1, qn);
+                else cons_to_prim_fast(cs, SK.inv_R, SK.gm1, qn);
                 double* o = A.q_out + off;
                 #pragma unroll
                 for (int v = 0; v < 5; ++v) o[v] = qn[v];

@@ -64,6 +64,7 @@ namespace gbns
         int hyb_flux, hyb_sensor;      // hybrid_scheme_t tag and blender kind
         double hyb_param;              // blender const_sensor_t alpha or ducros_t epsilon
         double gamma, R, gm1;          // gm1 = gamma - 1.0
+        double inv_gm1, inv_R;         // 1/(gamma - 1), 1/R (FP32-flux stage update)
         double spec_heat;              // gamma*R/(gamma - 1.0)        (viscous.h:67)
         double inv_gamma_avg;          // 1.0/(0.5*(gamma + gamma))    (convective.h:226,233)
         double R_avg;                  // 0.5*(R + R)                   (convective.h:224)
@@ -200,6 +201,36 @@ namespace gbns
         const double pp = gm1*(c[1] - 0.5*ru2);
         q[0] = pp;
         q[1] = pp/(R*rh);
+        q[2] = uu;
+        q[3] = vv;
+        q[4] = ww;
+    }
+
+    // The same conversions with two reciprocals instead of four divisions, for
+    // the FP32-flux form's stage update (FP64 state; not bit-identical to the
+    // reference's rounding, which only the FP64 drop-in promises).
+    __device__ __forceinline__ void prim_to_cons_fast(const double q[5], const double R, const double inv_gm1,
+                                                      double c[5])
+    {
+        const double rho = q[0]*(1.0/(R*q[1]));
+        const double rhoU2 = rho*(q[2]*q[2] + q[3]*q[3] + q[4]*q[4]);
+        c[0] = rho;
+        c[1] = 0.5*rhoU2 + q[0]*inv_gm1;
+        c[2] = rho*q[2];
+        c[3] = rho*q[3];
+        c[4] = rho*q[4];
+    }
+
+    __device__ __forceinline__ void cons_to_prim_fast(const double c[5], const double inv_R, const double gm1,
+                                                      double q[5])
+    {
+        const double rh = c[0];
+        const double invrho = 1.0/rh;
+        const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
+        const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
+        const double pp = gm1*(c[1] - 0.5*ru2);
+        q[0] = pp;
+        q[1] = (pp*invrho)*inv_R;
         q[2] = uu;
         q[3] = vv;
         q[4] = ww;

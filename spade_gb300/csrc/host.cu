@@ -217,6 +217,8 @@ namespace gbns
         const double gam = s->gas.gamma, R = s->gas.R;
         S.gamma = gam; S.R = R;
         S.gm1 = gam - 1.0;
+        S.inv_gm1 = 1.0/(gam - 1.0);
+        S.inv_R = 1.0/R;
         S.spec_heat = gam*R/(gam - 1.0);
         S.inv_gamma_avg = 1.0/(0.5*(gam + gam));
         S.R_avg = 0.5*(R + R);
