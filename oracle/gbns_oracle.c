@@ -390,24 +390,27 @@ static st5 flux_fweno(const ctx_t* C, const double* cells[4], const double ncell
  * parity unpinned. */
 static double weno5_side(double a, double b, double c, double d, double e, int smooth)
 {
-    const double p0 = (2.0*a - 7.0*b + 11.0*c)*(1.0/6.0);
-    const double p1 = (-b + 5.0*c + 2.0*d)*(1.0/6.0);
-    const double p2 = (2.0*c + 5.0*d - e)*(1.0/6.0);
-    if (!smooth) return 0.1*p0 + 0.6*p1 + 0.3*p2;
-    const double t0 = a - 2.0*b + c, s0 = a - 4.0*b + 3.0*c;
-    const double t1 = b - 2.0*c + d, s1 = b - d;
-    const double t2 = c - 2.0*d + e, s2 = 3.0*c - 4.0*d + e;
-    const double b0 = (13.0/12.0)*t0*t0 + 0.25*s0*s0;
-    const double b1 = (13.0/12.0)*t1*t1 + 0.25*s1*s1;
-    const double b2 = (13.0/12.0)*t2*t2 + 0.25*s2*s2;
+    /* Defined with explicit fused multiply-adds (C99 fma, correctly rounded
+     * like the GPU's), which the FP64 kernels reproduce bit for bit. */
+    const double c13 = 1.0/3.0, c16 = 1.0/6.0, c56 = 5.0/6.0, c76 = 7.0/6.0, c116 = 11.0/6.0;
+    const double p0 = fma(c13, a, fma(-c76, b, c116*c));
+    const double p1 = fma(-c16, b, fma(c56, c, c13*d));
+    const double p2 = fma(c13, c, fma(c56, d, (-c16)*e));
+    if (!smooth) return fma(0.1, p0, fma(0.6, p1, 0.3*p2));
+    const double t0 = fma(-2.0, b, a) + c, s0 = fma(3.0, c, fma(-4.0, b, a));
+    const double t1 = fma(-2.0, c, b) + d, s1 = b - d;
+    const double t2 = fma(-2.0, d, c) + e, s2 = fma(3.0, c, fma(-4.0, d, e));
+    const double k13 = 13.0/12.0;
+    const double b0 = fma(k13*t0, t0, (0.25*s0)*s0);
+    const double b1 = fma(k13*t1, t1, (0.25*s1)*s1);
+    const double b2 = fma(k13*t2, t2, (0.25*s2)*s2);
     const double eps = 1e-16;
-    const double d0 = (b0 + eps)*(b0 + eps);
-    const double d1 = (b1 + eps)*(b1 + eps);
-    const double d2 = (b2 + eps)*(b2 + eps);
+    const double e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
+    const double d0 = e0*e0, d1 = e1*e1, d2 = e2*e2;
     const double a0 = 0.1*(d1*d2);
     const double a1 = 0.6*(d0*d2);
     const double a2 = 0.3*(d0*d1);
-    return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
+    return fma(a0, p0, fma(a1, p1, a2*p2))/((a0 + a1) + a2);
 }
 
 static st5 flux_weno5(const ctx_t* C, const double* cells[6], const double ncell[6][3])
@@ -439,10 +442,12 @@ static void visc_law(const gbns_scheme_desc* S, double T, double* mu, double* be
     }
     if (S->visc_law == GBNS_LAW_SUTHERLAND)
     {
+        /* mu_ref (T/T_ref)^1.5 (T_ref + S)/(T + S); beta = -2/3 mu as a
+         * product with the rounded constant (no reference counterpart) */
         const double x = T/S->T_ref;
         const double m = S->mu*(x*sqrt(x))*((S->T_ref + S->S)/(T + S->S));
         *mu = m;
-        *beta = -2.0*m/3.0;
+        *beta = m*(-2.0/3.0);
         *alpha = m*(S->prandtl_inv > 0.0 ? S->prandtl_inv : 1.0/S->prandtl);
         return;
     }

@@ -465,28 +465,30 @@ namespace gbns
     template <class Real>
     __device__ __forceinline__ Real weno5_side(Real a, Real b, Real c, Real d, Real e, int smooth)
     {
-        const Real sixth = Real(1.0/6.0);
-        const Real p0 = (Real(2.0)*a - Real(7.0)*b + Real(11.0)*c)*sixth;
-        const Real p1 = (-b + Real(5.0)*c + Real(2.0)*d)*sixth;
-        const Real p2 = (Real(2.0)*c + Real(5.0)*d - e)*sixth;
-        if (!smooth) return Real(0.1)*p0 + Real(0.6)*p1 + Real(0.3)*p2;
-        const Real t0 = a - Real(2.0)*b + c, s0 = a - Real(4.0)*b + Real(3.0)*c;
-        const Real t1 = b - Real(2.0)*c + d, s1 = b - d;
-        const Real t2 = c - Real(2.0)*d + e, s2 = Real(3.0)*c - Real(4.0)*d + e;
+        // explicit fused multiply-adds: the definition the oracle restates
+        // with C99 fma, so FP64 results match it bit for bit
+        const Real c13 = Real(1.0/3.0), c16 = Real(1.0/6.0), c56 = Real(5.0/6.0), c76 = Real(7.0/6.0),
+                   c116 = Real(11.0/6.0);
+        const Real p0 = fma(c13, a, fma(-c76, b, c116*c));
+        const Real p1 = fma(-c16, b, fma(c56, c, c13*d));
+        const Real p2 = fma(c13, c, fma(c56, d, (-c16)*e));
+        if (!smooth) return fma(Real(0.1), p0, fma(Real(0.6), p1, Real(0.3)*p2));
+        const Real t0 = fma(Real(-2.0), b, a) + c, s0 = fma(Real(3.0), c, fma(Real(-4.0), b, a));
+        const Real t1 = fma(Real(-2.0), c, b) + d, s1 = b - d;
+        const Real t2 = fma(Real(-2.0), d, c) + e, s2 = fma(Real(3.0), c, fma(Real(-4.0), d, e));
         const Real k13 = Real(13.0/12.0);
-        const Real b0 = k13*t0*t0 + Real(0.25)*s0*s0;
-        const Real b1 = k13*t1*t1 + Real(0.25)*s1*s1;
-        const Real b2 = k13*t2*t2 + Real(0.25)*s2*s2;
+        const Real b0 = fma(k13*t0, t0, (Real(0.25)*s0)*s0);
+        const Real b1 = fma(k13*t1, t1, (Real(0.25)*s1)*s1);
+        const Real b2 = fma(k13*t2, t2, (Real(0.25)*s2)*s2);
         const Real eps = Real(1e-16);
-        const Real d0 = (b0 + eps)*(b0 + eps);
-        const Real d1 = (b1 + eps)*(b1 + eps);
-        const Real d2 = (b2 + eps)*(b2 + eps);
+        const Real e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
+        const Real d0 = e0*e0, d1 = e1*e1, d2 = e2*e2;
         if constexpr (sizeof(Real) == 8)
         {
             const Real a0 = Real(0.1)*(d1*d2);
             const Real a1 = Real(0.6)*(d0*d2);
             const Real a2 = Real(0.3)*(d0*d1);
-            return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
+            return fma(a0, p0, fma(a1, p1, a2*p2))/((a0 + a1) + a2);
         }
         else
         {
@@ -649,7 +651,7 @@ namespace gbns
         {
             const Real x = qf[1]/S.T_ref;
             visc = S.mu*(x*dev_sqrt(x))*(S.tref_plus_s/(qf[1] + S.S));
-            visc2 = Real(-2.0)*visc/Real(3.0);
+            visc2 = visc*Real(-2.0/3.0);
             dfs = visc*S.inv_pr;
         }
         const Real div = grad[0][1] + grad[1][2] + grad[2][3];
