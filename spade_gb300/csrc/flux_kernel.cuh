@@ -396,25 +396,23 @@ namespace gbns
     // Fills the split cache for direction D: f+ = fl + ds and f- = fl - ds of
     // every equation at every cell of the tile's lines along D (the stencil
     // cells of all faces of the pass), with the same operations fweno_point
-    // performs per face.
+    // performs per face.  The tile's own cells take rho, h and e from `dc`
+    // (computed once per tile, each thread for the cells it owns); the halo
+    // cells along D derive them here.
     template <class Cfg, int D>
     __device__ __forceinline__ void split_fill(const BoxView<Cfg>& V, const SchemeR<double>& S, double* P,
-                                               const YTabT<Cfg::STRETCH>& Y, int by, int j0, int ny, int shift)
+                                               const YTabT<Cfg::STRETCH>& Y, int by, int j0, int ny, int shift,
+                                               const double (&dc)[Cfg::CPT][3])
     {
         using SI = SplitIdx<Cfg, D>;
-        constexpr int H = Cfg::H, HC = Cfg::HC;
-        for (int l = threadIdx.x; l < SI::NL; l += Cfg::NT)
+        constexpr int H = Cfg::H, HC = Cfg::HC, TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ;
+        auto store = [&](int l, int c, int y, double rho, double hsr, double engy)
         {
-            const int lx = l % SI::LX, ly = (l / SI::LX) % SI::LY, lz = l / (SI::LX*SI::LY);
-            const int x = lx - (D == 0 ? HC : 0), y = ly - (D == 1 ? HC : 0), z = lz - (D == 2 ? HC : 0);
-            const int c = (z + H)*Cfg::SZ + (y + H)*Cfg::SY + (x + H + shift);
             double nD = 1.0;
             if constexpr (Cfg::STRETCH && D != 1)
             {
                 if (j0 + y < ny) nD = Y.m_cell[by*ny + j0 + y];
             }
-            double rho, hsr, engy;
-            fweno_derive<double>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
             #pragma unroll
             for (int eq = 0; eq < 5; ++eq)
             {
@@ -423,6 +421,33 @@ namespace gbns
                 P[(2*eq)*Cfg::NLMAX + l] = fl + ds;
                 P[(2*eq + 1)*Cfg::NLMAX + l] = fl - ds;
             }
+        };
+        #pragma unroll
+        for (int s = 0; s < Cfg::CPT; ++s)
+        {
+            const int cc = threadIdx.x + s*Cfg::NT;
+            if (cc >= Cfg::NCELL) break;
+            const int cx = cc % TX, cy = (cc / TX) % TY, cz = cc / (TX*TY);
+            const int c = (cz + H)*Cfg::SZ + (cy + H)*Cfg::SY + (cx + H + shift);
+            store(SI::right(cx, cy, cz), c, cy, dc[s][0], dc[s][1], dc[s][2]);
+        }
+        // halo cells of the lines: 2*HC layers along D
+        constexpr int TA = D == 0 ? TY : TX;              // first transverse extent
+        constexpr int NH = 2*HC*(D == 0 ? TY*TZ : (D == 1 ? TX*TZ : TX*TY));
+        for (int h = threadIdx.x; h < NH; h += Cfg::NT)
+        {
+            const int hd = h % (2*HC), t = h / (2*HC);
+            const int ld = hd < HC ? hd : hd + (D == 0 ? TX : (D == 1 ? TY : TZ));   // line coordinate along D
+            const int ta = t % TA, tb = t / TA;
+            const int lx = D == 0 ? ld : ta;
+            const int ly = D == 1 ? ld : (D == 0 ? ta : tb);
+            const int lz = D == 2 ? ld : tb;
+            const int l = lx + SI::LX*(ly + SI::LY*lz);
+            const int x = lx - (D == 0 ? HC : 0), y = ly - (D == 1 ? HC : 0), z = lz - (D == 2 ? HC : 0);
+            const int c = (z + H)*Cfg::SZ + (y + H)*Cfg::SY + (x + H + shift);
+            double rho, hsr, engy;
+            fweno_derive<double>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
+            store(l, c, y, rho, hsr, engy);
         }
     }
 
@@ -759,7 +784,8 @@ namespace gbns
                                               double* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
                                               int lb, const int b[3], int i0, int j0, int k0, int shift,
                                               const typename Cfg::Real inv[3],
-                                              double (&relem)[Cfg::CPT][5], const double invd[3])
+                                              double (&relem)[Cfg::CPT][5], const double invd[3],
+                                              const double (&dc)[Cfg::CPT][3])
     {
         using Real = typename Cfg::Real;
         constexpr int TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ, H = Cfg::H;
@@ -769,7 +795,7 @@ namespace gbns
         const int ny = G.n[1];
         if constexpr (Cfg::SPLIT)
         {
-            split_fill<Cfg, D>(V, S, const_cast<double*>(V.split), Y, b[1], j0, ny, shift);
+            split_fill<Cfg, D>(V, S, const_cast<double*>(V.split), Y, b[1], j0, ny, shift, dc);
             __syncthreads();
         }
         for (int f = tid; f < NF; f += Cfg::NT)
@@ -983,9 +1009,27 @@ namespace gbns
         #pragma unroll
         for (int d = 0; d < 3; ++d) { invd[d] = G.inv_dx[d][b[d]]; inv[d] = Real(invd[d]); }
 
-        face_pass<Cfg, 0>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
-        face_pass<Cfg, 1>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
-        face_pass<Cfg, 2>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd);
+        // SPLIT: rho, h, e of the cells this thread owns, shared by the three
+        // directions' split fills
+        double dc[Cfg::CPT][3];
+        #pragma unroll
+        for (int s = 0; s < Cfg::CPT; ++s) { dc[s][0] = dc[s][1] = dc[s][2] = 0.0; }
+        if constexpr (Cfg::SPLIT)
+        {
+            #pragma unroll
+            for (int s = 0; s < Cfg::CPT; ++s)
+            {
+                const int cc = tid + s*Cfg::NT;
+                if (cc >= Cfg::NCELL) break;
+                const int cx = cc % TX, cy = (cc / TX) % TY, cz = cc / (TX*TY);
+                const int c = (cz + H)*Cfg::SZ + (cy + H)*Cfg::SY + (cx + H + shift);
+                fweno_derive<double>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
+            }
+        }
+
+        face_pass<Cfg, 0>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
+        face_pass<Cfg, 1>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
+        face_pass<Cfg, 2>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
 
         // ---- write the residual (and the fused stage update) -----------------
         #pragma unroll
