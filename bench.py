@@ -339,7 +339,7 @@ def run_batch_form(args):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.batch_steps
         out[name] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms,
-                     "launches_per_step": 9, "graph": True}
+                     "launches_per_step": 6, "graph": True}
         b.close()
     # the same instances one grid at a time (one gbns_ssprk3_step per instance)
     works = [torch.zeros(3 * p.q.data.numel(), dtype=torch.float64, device="cuda") for p in probs]
@@ -358,7 +358,7 @@ def run_batch_form(args):
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / max(1, args.batch_steps // 2)
     out["fp64_one_grid_at_a_time"] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms,
-                                      "launches_per_step": 9 * len(probs)}
+                                      "launches_per_step": 6 * len(probs)}
     out["fp32_batched_vs_fp64_plain"] = out["fp32_flux"]["cell_steps_per_s"] / out["fp64_one_grid_at_a_time"]["cell_steps_per_s"]
     del probs, works
     torch.cuda.empty_cache()
@@ -587,6 +587,10 @@ def main():
         "health_bad_cells": r["health_bad_cells"],
         "fp32_flux": r["fp32"],
         "autotune": r["tuned"],
+        # one plain flux_div (overwrite mode, no stage update) with the tuned
+        # tile, from the autotuner's CUDA-event timings: cell-RHS/s
+        "flux_div_cell_rhs_per_s": {k: r["cells"] / (min(v["ms_per_variant"].values()) * 1e-3)
+                                    for k, v in r["tuned"].items()},
     }
     line.update(forms)
     if cpu is not None:

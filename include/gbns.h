@@ -313,8 +313,9 @@ int gbns_source_term(const gbns_grid_desc* grid, const gbns_source_desc* source,
 /* ---- batched form ----------------------------------------------------
  * Many independent grids ("instances") of uneven size advanced together:
  * each SSPRK3 stage is one persistent flux launch per kernel class (walking a
- * device work-list of tiles of every instance), one batched RK-stage launch
- * and one batched ghost fill; with use_graph the nine-launch step is captured
+ * device work-list of tiles of every instance, with the stage update fused
+ * into its epilogue) and one batched ghost fill; with use_graph the step
+ * (six launches for one kernel class) is captured
  * once in a CUDA graph and replayed.  Instance state stays resident in an
  * arena of hbm_budget_bytes allocated at creation; adding an instance that
  * does not fit returns GBNS_ERR_CAPACITY.  Every instance's result is

@@ -242,9 +242,9 @@ namespace
                     : launch_flux_batch_f64x(c, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, stage, b->stream);
                 if (rc) return rc;
             }
-            int rc = launch_rk_batch(b->d_blocks, nblk, b->d_insts, stage, b->stream);
-            if (rc) return rc;
-            rc = launch_ghost_batch(b->d_blocks, nblk, b->d_insts, b->stream);
+            // the stage update ran in the flux launch's epilogue; fill the
+            // ghosts of the state it wrote (stage 2: copy it back into q)
+            int rc = launch_ghost_batch(b->d_blocks, nblk, b->d_insts, stage == 0 ? 1 : (stage == 1 ? 0 : 2), b->stream);
             if (rc) return rc;
         }
         return GBNS_OK;

@@ -27,16 +27,39 @@ namespace gbns
             {
                 const TileItem w = items[base + it];
                 const InstK& I = insts[w.inst];
+                // The SSPRK3 stage fused into the flux launch, as gbns_ssprk3_step
+                // issues it, with R[2] as the second state buffer:
+                //   stage 0: q    -> R0, q1 into R[2]
+                //   stage 1: R[2] -> R1, q2 into q
+                //   stage 2: q    -> (no store), q3 into R[2]  (copied back by the ghost pass)
+                // coefficients: ratio_diff of consecutive ssprk3_t rows times dt
+                // (advance.h:80-95).
+                const double dt = I.dt;
                 FluxArgs A;
-                A.prims = I.q;
-                A.rhs = I.R[stage];
                 A.increment = 0;
                 A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
                 A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
                 A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
                 A.use_tma = 0;
-                A.rk_nres = 0;
-                A.write_rhs = 1;
+                A.rk_nres = stage + 1;
+                A.rk_res[0] = I.R[0];
+                A.rk_res[1] = I.R[1];
+                A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
+                if (stage == 0)
+                {
+                    A.prims = I.q; A.rhs = I.R[0]; A.write_rhs = 1; A.q_out = I.R[2];
+                    A.rk_coeff[0] = (1.0/1.0)*dt;
+                }
+                else if (stage == 1)
+                {
+                    A.prims = I.R[2]; A.rhs = I.R[1]; A.write_rhs = 1; A.q_out = I.q;
+                    A.rk_coeff[0] = (-3.0/4.0)*dt; A.rk_coeff[1] = (1.0/4.0)*dt;
+                }
+                else
+                {
+                    A.prims = I.q; A.rhs = nullptr; A.write_rhs = 0; A.q_out = I.R[2];
+                    A.rk_coeff[0] = (-1.0/12.0)*dt; A.rk_coeff[1] = (-1.0/12.0)*dt; A.rk_coeff[2] = (2.0/3.0)*dt;
+                }
                 if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, I.G, ytabs[I.ytab], I.S, A, w.lb, w.tile);
                 else flux_tile<Cfg>(smem_raw, nullptr, I.G, YTabNone{}, I.S, A, w.lb, w.tile);
                 __syncthreads();

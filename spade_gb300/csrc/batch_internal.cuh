@@ -27,7 +27,7 @@ namespace gbns
         SchemeK S;
         BcK bc;
         double* q;          // primitive state, AoS5 with ghosts
-        double* R[3];       // SSPRK3 residuals
+        double* R[3];       // R0, R1 and the second state buffer of the fused stages
         double dt;
         int ytab;           // index into the Y-metric table array, -1 for identity
         int pad;
@@ -60,9 +60,9 @@ namespace gbns
     int launch_flux_batch_f32(int cls, const TileItem* items, const int* offsets, const int* counts,
                               const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
 
-    // Batched RK stage (stage 0, 1, 2 of ssprk3_t) and ghost fill.
-    int launch_rk_batch(const BlockItem* items, const int* count, const InstK* insts, int stage, cudaStream_t st);
-    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, cudaStream_t st);
+    // Batched ghost fill (mode 0: q, 1: R[2], 2: copy R[2] into q and fill
+    // q's ghosts); the RK stage update runs in the flux launch's epilogue.
+    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, int mode, cudaStream_t st);
 
     int persistent_grid(int ctas_per_sm);
 }

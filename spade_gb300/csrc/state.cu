@@ -250,37 +250,13 @@ namespace gbns
         return sm_count()*ctas_per_sm;
     }
 
-    template <int NRES>
     __global__ void __launch_bounds__(256)
-    rk_batch_kernel(const BlockItem* __restrict__ items, const int* __restrict__ count, const InstK* __restrict__ insts)
+    ghost_batch_kernel(const BlockItem* __restrict__ items, const int* __restrict__ count, const InstK* __restrict__ insts,
+                       const int mode)
     {
-        const int n = *count;
-        for (int it = blockIdx.x; it < n; it += gridDim.x)
-        {
-            const BlockItem w = items[it];
-            const InstK& I = insts[w.inst];
-            const GeomK& G = I.G;
-            const double dt = I.dt;
-            // ratio_diff_t of consecutive ssprk3_t rows times dt (advance.h:80-95)
-            double coeff[3];
-            if (NRES == 1) { coeff[0] = (1.0/1.0)*dt; }
-            else if (NRES == 2) { coeff[0] = (-3.0/4.0)*dt; coeff[1] = (1.0/4.0)*dt; }
-            else { coeff[0] = (-1.0/12.0)*dt; coeff[1] = (-1.0/12.0)*dt; coeff[2] = (2.0/3.0)*dt; }
-            const double* res[3] = {I.R[0], I.R[1], I.R[2]};
-            const int ncell = G.n[0]*G.n[1]*G.n[2];
-            for (int c = threadIdx.x; c < ncell; c += blockDim.x)
-            {
-                const int i_ = c % G.n[0], j_ = (c / G.n[0]) % G.n[1], k_ = c / (G.n[0]*G.n[1]);
-                const long long off = (long long)w.lb*G.bstride +
-                    ((long long)((k_ + G.ng)*G.nj + (j_ + G.ng))*G.ni + (i_ + G.ng))*5;
-                rk_update_cell<NRES>(I.q, res, coeff, I.S.R, I.S.gm1, off);
-            }
-        }
-    }
-
-    __global__ void __launch_bounds__(256)
-    ghost_batch_kernel(const BlockItem* __restrict__ items, const int* __restrict__ count, const InstK* __restrict__ insts)
-    {
+        // mode 0: ghosts of q; 1: ghosts of R[2] (the fused stage's second
+        // state buffer); 2: q = R[2] on the interior with q's ghosts filled
+        // from R[2]'s interior donors (after the last fused stage)
         const int n = *count;
         for (int it = blockIdx.x; it < n; it += gridDim.x)
         {
@@ -288,26 +264,32 @@ namespace gbns
             const InstK& I = insts[w.inst];
             const GeomK& G = I.G;
             const int npad = G.ni*G.nj*G.nk;
+            double* dst = mode == 1 ? I.R[2] : I.q;
+            const double* src = mode == 0 ? I.q : I.R[2];
+            const long long base = (long long)w.lb*npad;
             for (int c = threadIdx.x; c < npad; c += blockDim.x)
             {
                 const int ii = c % G.ni, jj = (c / G.ni) % G.nj, kk = c / (G.ni*G.nj);
-                fill_one_ghost(I.q, G, I.bc, w.lb, ii, jj, kk);
+                const int i = ii - G.ng, j = jj - G.ng, k = kk - G.ng;
+                if (i >= 0 && i < G.n[0] && j >= 0 && j < G.n[1] && k >= 0 && k < G.n[2])
+                {
+                    if (mode == 2)
+                    {
+                        #pragma unroll
+                        for (int v = 0; v < 5; ++v) dst[(base + c)*5 + v] = src[(base + c)*5 + v];
+                    }
+                }
+                else
+                {
+                    fill_one_ghost_from(dst, src, G, I.bc, w.lb, ii, jj, kk);
+                }
             }
         }
     }
 
-    int launch_rk_batch(const BlockItem* items, const int* count, const InstK* insts, int stage, cudaStream_t st)
+    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, int mode, cudaStream_t st)
     {
-        const int grid = persistent_grid(8);
-        if (stage == 0) rk_batch_kernel<1><<<grid, 256, 0, st>>>(items, count, insts);
-        else if (stage == 1) rk_batch_kernel<2><<<grid, 256, 0, st>>>(items, count, insts);
-        else rk_batch_kernel<3><<<grid, 256, 0, st>>>(items, count, insts);
-        return check_cuda(cudaGetLastError(), "rk_batch launch");
-    }
-
-    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, cudaStream_t st)
-    {
-        ghost_batch_kernel<<<persistent_grid(8), 256, 0, st>>>(items, count, insts);
+        ghost_batch_kernel<<<persistent_grid(8), 256, 0, st>>>(items, count, insts, mode);
         return check_cuda(cudaGetLastError(), "ghost_batch launch");
     }
 
