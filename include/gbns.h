@@ -223,14 +223,22 @@ int gbns_reduce_async(const gbns_grid_desc* grid, const gbns_gas_desc* gas, cons
                       int kind, double* scratch, size_t scratch_len, void* stream);
 
 /* Device-side status: nonzero after a kernel gave up on a bounded wait
- * (GBNS_ERR_TIMEOUT class events).  reset != 0 clears it.  Synchronises
- * `stream`.  Replaces the reference's post-launch error check
- * (dispatch/execute.h:86-96). */
+ * (GBNS_DEV_*).  reset != 0 clears it.  Synchronises `stream`.  Replaces the
+ * reference's post-launch error check (dispatch/execute.h:86-96). */
+#define GBNS_DEV_OK           0
+#define GBNS_DEV_TMA_TIMEOUT  1   /* a tile's TMA halo copy did not complete within the poll limit */
 int gbns_device_status(int* status, int reset, void* stream);
 
 /* Measured FMA throughput of this GPU (FLOP/s) with dependent FMA chains:
  * fp64 != 0 -> double, else float.  Benchmark aid (no reference counterpart). */
 int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);
+
+/* Exercises the bounded-wait failure path of the flux kernel without a
+ * fault: a one-CTA kernel arms an mbarrier for TMA bytes that never arrive,
+ * gives up after a bounded poll and sets the device status word, which this
+ * call reads into *status (GBNS_DEV_TMA_TIMEOUT expected) and clears.  The
+ * context stays usable.  No counterpart in the reference. */
+int gbns_selftest_wait_timeout(int* status, void* stream);
 
 /* Reduction that allocates nothing.  For callers that cannot let the
  * library call cudaMalloc: work recorded into a CUDA graph while a stream is

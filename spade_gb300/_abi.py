@@ -99,6 +99,9 @@ class SchemeDesc(ctypes.Structure):
     ]
 
 
+DEV_OK = 0
+DEV_TMA_TIMEOUT = 1
+
 SOURCE_CONST = 0
 SOURCE_BODY_FORCE = 1
 SOURCE_BODY_ACCEL = 2

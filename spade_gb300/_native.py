@@ -44,6 +44,7 @@ def lib():
     L.gbns_copy_fill_ghosts.argtypes = [P(_abi.GridDesc), P(_abi.BcDesc), vp, vp, vp]
     L.gbns_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double, vp]
     L.gbns_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), vp, vp, vp]
+    L.gbns_selftest_wait_timeout.argtypes = [P(ctypes.c_int), vp]
     L.gbns_device_status.argtypes = [P(ctypes.c_int), ctypes.c_int, vp]
     L.gbns_batch_create.argtypes = [P(vp), ctypes.c_size_t, ctypes.c_int, ctypes.c_int, vp]
     L.gbns_batch_destroy.argtypes = [vp]

@@ -924,7 +924,7 @@ namespace gbns
                 mbar_expect_tx(bar, uint32_t(Cfg::BOXN)*5u*8u);
                 tma_load_4d(stage, tmap, bar, xs*5, ys, zs, lb);
             }
-            const bool ok = mbar_wait(bar, 0, MBAR_POLL_LIMIT);
+            const bool ok = mbar_wait(bar, 0, MBAR_WAIT_CYCLES);
             if (__syncthreads_or(!ok))
             {
                 if (tid == 0) atomicExch(&g_device_status, DEV_TMA_TIMEOUT);

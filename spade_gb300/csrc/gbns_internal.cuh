@@ -128,21 +128,24 @@ namespace gbns
     }
 
     // Bounded mbarrier wait: returns false if the phase did not complete
-    // within `limit` polls (then the caller flags an error and returns).
-    __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit)
+    // within `max_cycles` SM clock cycles (then the caller flags an error and
+    // returns).  Each try_wait suspends for at most ~2 us (suspend-time hint),
+    // so the bound holds whatever the hardware's default suspend window is.
+    __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long max_cycles)
     {
         const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
-        for (long long it = 0; it < limit; ++it)
+        const long long t0 = clock64();
+        for (;;)
         {
             uint32_t done;
             asm volatile(
                 "{\n\t.reg .pred p;\n\t"
-                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
                 "selp.u32 %0, 1, 0, p;\n\t}"
-                : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+                : "=r"(done) : "r"(addr), "r"(parity), "r"(2000u) : "memory");
             if (done) return true;
+            if (clock64() - t0 > max_cycles) return false;
         }
-        return false;
     }
 
     __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
@@ -177,7 +180,7 @@ namespace gbns
             : "memory");
     }
 
-    constexpr long long MBAR_POLL_LIMIT = 1ll << 24;   // ~tens of ms of polling
+    constexpr long long MBAR_WAIT_CYCLES = 2000000000ll;   // ~1 s at 2 GHz
 
     // fluid_state::convert_state prim -> cons and cons -> prim
     // (navier-stokes/fluid_state.h:151-184), in the reference's operation order.
@@ -238,8 +241,8 @@ namespace gbns
 
     enum device_status_code
     {
-        DEV_OK = 0,
-        DEV_TMA_TIMEOUT = 1,
+        DEV_OK = GBNS_DEV_OK,
+        DEV_TMA_TIMEOUT = GBNS_DEV_TMA_TIMEOUT,
         DEV_BAD_LAUNCH = 2
     };
 }

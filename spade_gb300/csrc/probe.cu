@@ -48,6 +48,47 @@ namespace gbns
     }
 }
 
+namespace gbns
+{
+    namespace { status_registrar tu_status_registrar; }
+
+    // The flux kernel's failure path, exercised on purpose: one CTA arms an
+    // mbarrier for 16 bytes of TMA data that no copy will deliver (a flag
+    // nothing sets), waits with a bounded poll, finds the phase incomplete,
+    // records DEV_TMA_TIMEOUT in the device status word and returns.  No
+    // copy is in flight, so nothing is left pending when the CTA exits.
+    __global__ void __launch_bounds__(32) wait_timeout_selftest_kernel(long long max_cycles)
+    {
+        __shared__ __align__(8) uint64_t bar;
+        if (threadIdx.x == 0)
+        {
+            mbar_init(&bar, 1);
+            mbar_expect_tx(&bar, 16u);
+        }
+        __syncwarp();
+        const bool ok = mbar_wait(&bar, 0, max_cycles);
+        if (__any_sync(0xffffffffu, !ok))
+        {
+            if (threadIdx.x == 0) atomicExch(&g_device_status, DEV_TMA_TIMEOUT);
+        }
+        __syncwarp();
+        if (threadIdx.x == 0) mbar_inval(&bar);
+    }
+}
+
+extern "C" int gbns_selftest_wait_timeout(int* status, void* stream)
+{
+    using namespace gbns;
+    if (!status) return set_error(GBNS_ERR_INVALID, "NULL output");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    int rc = read_device_status(status, 1, st);          // clear any earlier flag
+    if (rc) return rc;
+    wait_timeout_selftest_kernel<<<1, 32, 0, st>>>(20000000ll);    // ~10 ms
+    rc = check_cuda(cudaGetLastError(), "wait self-test launch");
+    if (rc) return rc;
+    return read_device_status(status, 1, st);            // the flag the timeout set; cleared again
+}
+
 extern "C" int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream)
 {
     if (!flops_per_s) return gbns::set_error(GBNS_ERR_INVALID, "NULL output");

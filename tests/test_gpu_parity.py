@@ -488,3 +488,22 @@ def test_fp32_flux_weno_weights_do_not_overflow(conv):
     assert np.isfinite(r32).all()
     err = np.abs(r32 - r64).reshape(-1, 5).max(axis=0) / np.abs(r64).reshape(-1, 5).max(axis=0)
     assert np.all(err < 1e-3), err
+
+
+@pytest.mark.gpu
+def test_bounded_wait_timeout_sets_status_and_context_survives():
+    """Failure detection without a fault: a kernel waits for TMA bytes that
+    never arrive, gives up after a bounded poll and flags the device status;
+    the host reads the flag, and the context keeps working (a flux_div right
+    after is still bit-identical to the reference)."""
+    st = ctypes.c_int(-1)
+    _native.check(lib().gbns_selftest_wait_timeout(ctypes.byref(st), stream()))
+    assert st.value == _abi.DEV_TMA_TIMEOUT
+    clean = ctypes.c_int(-1)
+    _native.check(lib().gbns_device_status(ctypes.byref(clean), 0, stream()))
+    assert clean.value == _abi.DEV_OK
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    r = gpu_flux(grid, P.scheme(**FLUX_CASES["ck2_visc"][1]), g["q"])
+    assert np.array_equal(interior(r, fg["ng"]), g["rhs_ck2_visc"])
