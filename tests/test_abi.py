@@ -180,3 +180,18 @@ def test_lower_sources_and_reject_callables():
     bad = _abi.SourceDesc()
     bad.kind = 7
     assert _native.lib().gbns_source_term(g, bad, ctypes.c_void_p(16), ctypes.c_void_p(32), None) == _abi.ERR_INVALID
+
+
+def test_size_limits_rejected_before_cuda():
+    """The descriptor limits (64 blocks per direction; stretched-y metric
+    tables of blocks_y*(ny+1) <= 1024 entries) fail with a message, not a
+    fault.  The 8x8x8-block, 32^3 channel is well inside both."""
+    import problems as P
+    n = ctypes.c_size_t(0)
+    g = _abi.grid_desc((65, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    assert _native.lib().gbns_array_size(g, ctypes.byref(n)) == _abi.ERR_INVALID
+    g = _abi.grid_desc((64, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    assert _native.lib().gbns_array_size(g, ctypes.byref(n)) == _abi.OK
+    g = _abi.grid_desc((1, 40, 1), (8, 32, 8), 3, (0, 1, -1, 1, 0, 1), coords=_abi.COORDS_TANH_Y, coord_param=(2.0, 0, 0, 0))
+    rc = _native.lib().gbns_flux_div(g, P.scheme(conv=_abi.CONV_WENO5), ctypes.c_void_p(16), ctypes.c_void_p(32), 0, None)
+    assert rc == _abi.ERR_UNSUPPORTED and "metric table" in _native.last_error()

@@ -61,3 +61,37 @@ def test_multirank_exchange_equals_single_device_fill(world, walls):
         mp.spawn(_worker, args=(world, _free_port(), (nblk, ncell, ng, bc), d), nprocs=world, join=True)
         got = np.concatenate([np.load(os.path.join(d, "r%d.npy" % r)) for r in range(world)])
     assert np.array_equal(got, want)
+
+
+def _leaver(rank, world, port, outdir):
+    """Rank 1 leaves between steps (after the first exchange, with nothing in
+    flight); rank 0's next exchange must end with an error, not hang."""
+    import datetime
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__))))
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world,
+                            timeout=datetime.timedelta(seconds=20))
+    nblk, ncell, ng = (2, 1, 1), (4, 4, 4), 2
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    full = P.random_state(nblk, ncell, ng, seed=78)
+    part = block_partition_t(2, world, rank)
+    local = torch.from_numpy(full[part.starts[rank]:part.starts[rank] + part.num_local_blocks].copy())
+    ex = halo_exchange_t(grid, P.periodic_bc(), part)
+    ex.exchange(local)
+    if rank == 1:
+        return                      # leaves without joining the next exchange
+    try:
+        ex.exchange(local)
+        outcome = "completed"
+    except Exception as e:          # the peer's socket closed: gloo raises
+        outcome = "error: " + type(e).__name__
+    with open(os.path.join(outdir, "outcome.txt"), "w") as f:
+        f.write(outcome)
+
+
+@pytest.mark.timeout(120)
+def test_rank_that_leaves_between_steps_is_detected():
+    with tempfile.TemporaryDirectory() as d:
+        mp.spawn(_leaver, args=(2, _free_port(), d), nprocs=2, join=True)
+        outcome = open(os.path.join(d, "outcome.txt")).read()
+    assert outcome.startswith("error"), outcome
