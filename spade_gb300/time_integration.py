@@ -126,10 +126,10 @@ class integrator_t:
 
 class ssprk3_stepper:
     """Fused native SSPRK3 step of `q` (gbns_ssprk3_step): three flux_div
-    launches, three fused stage updates and three ghost fills per step with
-    the reference's arithmetic.  With use_graph=True the first call captures
-    the nine launches of one step in a CUDA graph on a side stream and later
-    calls replay it (dt is fixed at capture)."""
+    launches with the stage update fused into their epilogue and three ghost
+    fills per step, with the reference's arithmetic.  With use_graph=True the
+    first call captures the six launches of one step in a CUDA graph on a
+    side stream and later calls replay it (dt is fixed at capture)."""
 
     def __init__(self, q, scheme_desc, bc_desc, dt, use_graph=False):
         self.q = q

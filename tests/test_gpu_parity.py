@@ -507,3 +507,28 @@ def test_bounded_wait_timeout_sets_status_and_context_survives():
     grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
     r = gpu_flux(grid, P.scheme(**FLUX_CASES["ck2_visc"][1]), g["q"])
     assert np.array_equal(interior(r, fg["ng"]), g["rhs_ck2_visc"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [_abi.PREC_FP64, _abi.PREC_FP32_FLUX])
+def test_ssprk3_stepper_graph_replay_equals_direct_steps(precision):
+    """time_integration.ssprk3_stepper(use_graph=True) captures one fused
+    step (six launches) in a CUDA graph and replays it; five replays equal
+    five direct gbns_ssprk3_step calls bit for bit."""
+    from spade_gb300 import workloads
+    from spade_gb300.time_integration import ssprk3_stepper
+    prob = workloads.taylor_green(nblk=(2, 1, 1), ncell=(16, 16, 16), ng=2, seed=9, rng="torch")
+    s = prob.scheme_desc(precision)
+    bc = prob.bc_desc()
+    q0 = prob.q.data.clone()
+    st = ssprk3_stepper(prob.q, s, bc, prob.dt, use_graph=True)
+    st.step(5)
+    torch.cuda.synchronize()
+    graphed = prob.q.data.clone()
+    prob.q.data.copy_(q0)
+    work = torch.zeros(3 * q0.numel(), dtype=torch.float64, device="cuda")
+    for _ in range(5):
+        _native.check(lib().gbns_ssprk3_step(prob.q.desc(), s, bc, ctypes.c_void_p(prob.q.ptr()),
+                                             ctypes.c_void_p(work.data_ptr()), ctypes.c_double(prob.dt), stream()))
+    torch.cuda.synchronize()
+    assert torch.equal(prob.q.data, graphed)
