@@ -86,8 +86,14 @@ namespace gbns
         static constexpr int NLMAX = cmax3(NL0, NL1, NL2);
         static constexpr size_t DER_BYTES   = SPLIT ? align128(size_t(10)*NLMAX*sizeof(double))
                                                     : align128(size_t(NDER > 0 ? NDER : 1)*BOXN*sizeof(Real));
+        // FP32-flux evaluates the faces of all three directions in one
+        // balanced loop (warp-aligned direction boundaries), which needs the
+        // face buffer for all of them; FP64 (split cache per direction) keeps
+        // one direction at a time.
+        static constexpr bool MERGED = !FP64 && (NF0 % 32 == 0) && ((NF0 + NF1) % 32 == 0);
+        static constexpr int NFS = MERGED ? NF0 + NF1 + NF2 : NFMAX;
         // face fluxes are kept in FP64 (converted once per face)
-        static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFMAX*sizeof(double));
+        static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFS*sizeof(double));
         // FP32 staged: the staging buffer is dead once converted, so derived
         // values and face fluxes reuse it when they fit.
         static constexpr bool REUSE = !FP64 && !DIRECT && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
@@ -779,59 +785,60 @@ namespace gbns
         double* q_out;
     };
 
+    // One face of direction D (tile-local face index f) into the face buffer
+    // at column `base + f` (row v of stride Cfg::NFS).
     template <class Cfg, int D>
-    __device__ __forceinline__ void face_pass(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
-                                              double* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
-                                              int lb, const int b[3], int i0, int j0, int k0, int shift,
-                                              const typename Cfg::Real inv[3],
-                                              double (&relem)[Cfg::CPT][5], const double invd[3],
-                                              const double (&dc)[Cfg::CPT][3])
+    __device__ __forceinline__ void face_one(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                             double* sF, int base, int f, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
+                                             const int b[3], int i0, int j0, int k0, int shift,
+                                             const typename Cfg::Real inv[3])
     {
         using Real = typename Cfg::Real;
-        constexpr int TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ, H = Cfg::H;
-        constexpr int NF = D == 0 ? Cfg::NF0 : (D == 1 ? Cfg::NF1 : Cfg::NF2);
+        constexpr int TX = Cfg::TX, TY = Cfg::TY, H = Cfg::H;
         constexpr int EX = TX + (D == 0), EY = TY + (D == 1);
-        const int tid = threadIdx.x;
         const int ny = G.n[1];
-        if constexpr (Cfg::SPLIT)
+        const int fx = f % EX;
+        const int r = f / EX;
+        const int fy = r % EY;
+        const int fz = r / EY;
+        const int gi = i0 + fx, gj = j0 + fy, gk = k0 + fz;
+        const bool valid = (D == 0 ? gi <= G.n[0] : gi < G.n[0]) &&
+                           (D == 1 ? gj <= G.n[1] : gj < G.n[1]) &&
+                           (D == 2 ? gk <= G.n[2] : gk < G.n[2]);
+        Real F[5] = {Real(0), Real(0), Real(0), Real(0), Real(0)};
+        if (valid)
         {
-            split_fill<Cfg, D>(V, S, const_cast<double*>(V.split), Y, b[1], j0, ny, shift, dc);
-            __syncthreads();
-        }
-        for (int f = tid; f < NF; f += Cfg::NT)
-        {
-            const int fx = f % EX;
-            const int r = f / EX;
-            const int fy = r % EY;
-            const int fz = r / EY;
-            const int gi = i0 + fx, gj = j0 + fy, gk = k0 + fz;
-            const bool valid = (D == 0 ? gi <= G.n[0] : gi < G.n[0]) &&
-                               (D == 1 ? gj <= G.n[1] : gj < G.n[1]) &&
-                               (D == 2 ? gk <= G.n[2] : gk < G.n[2]);
-            Real F[5] = {Real(0), Real(0), Real(0), Real(0), Real(0)};
-            if (valid)
+            const int rc = (fz + H)*Cfg::SZ + (fy + H)*Cfg::SY + (fx + H + shift);
+            Real nD = Real(1.0), im = Real(1.0);
+            if constexpr (Cfg::STRETCH)
             {
-                const int rc = (fz + H)*Cfg::SZ + (fy + H)*Cfg::SY + (fx + H + shift);
-                Real nD = Real(1.0), im = Real(1.0);
-                if constexpr (Cfg::STRETCH)
+                if constexpr (D == 1) im = Real(Y.im_face[b[1]*(ny + 1) + gj]);
+                else
                 {
-                    if constexpr (D == 1) im = Real(Y.im_face[b[1]*(ny + 1) + gj]);
-                    else
-                    {
-                        nD = Real(Y.m_cell[b[1]*ny + gj]);
-                        im = Real(Y.im_cell[b[1]*ny + gj]);
-                    }
+                    nD = Real(Y.m_cell[b[1]*ny + gj]);
+                    im = Real(Y.im_cell[b[1]*ny + gj]);
                 }
-                face_flux<Cfg, D>(V, S, rc, SplitIdx<Cfg, D>::right(fx, fy, fz), nD, inv, im, F);
             }
-            #pragma unroll
-            for (int v = 0; v < 5; ++v) sF[v*Cfg::NFMAX + f] = double(F[v]);
+            face_flux<Cfg, D>(V, S, rc, SplitIdx<Cfg, D>::right(fx, fy, fz), nD, inv, im, F);
         }
-        __syncthreads();
+        #pragma unroll
+        for (int v = 0; v < 5; ++v) sF[v*Cfg::NFS + base + f] = double(F[v]);
+    }
+
+    // Divergence of direction D into the cells this thread owns, in the
+    // reference's order (flux_div_basic.h:109-129): relem += F(i-1/2)*(jac*1*inv_dx);
+    // relem += F(i+1/2)*(jac*(-1)*inv_dx).
+    template <class Cfg, int D>
+    __device__ __forceinline__ void face_accumulate(const double* sF, int base, const GeomK& G,
+                                                    const YTabT<Cfg::STRETCH>& Y, const int b[3], int i0, int j0,
+                                                    int k0, double (&relem)[Cfg::CPT][5], const double invd[3])
+    {
+        constexpr int TX = Cfg::TX, TY = Cfg::TY;
+        const int ny = G.n[1];
         #pragma unroll
         for (int s = 0; s < Cfg::CPT; ++s)
         {
-            const int c = tid + s*Cfg::NT;
+            const int c = threadIdx.x + s*Cfg::NT;
             if (c >= Cfg::NCELL) break;
             const int cx = c % TX, cy = (c / TX) % TY, cz = c / (TX*TY);
             if (i0 + cx >= G.n[0] || j0 + cy >= G.n[1] || k0 + cz >= G.n[2]) continue;
@@ -846,10 +853,56 @@ namespace gbns
             #pragma unroll
             for (int v = 0; v < 5; ++v)
             {
-                relem[s][v] += sF[v*Cfg::NFMAX + fL]*multL;
-                relem[s][v] += sF[v*Cfg::NFMAX + fR]*multR;
+                relem[s][v] += sF[v*Cfg::NFS + base + fL]*multL;
+                relem[s][v] += sF[v*Cfg::NFS + base + fR]*multR;
             }
         }
+    }
+
+    // One direction: [split cache], its faces, then its share of the divergence.
+    template <class Cfg, int D>
+    __device__ __forceinline__ void face_pass(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                              double* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
+                                              int lb, const int b[3], int i0, int j0, int k0, int shift,
+                                              const typename Cfg::Real inv[3],
+                                              double (&relem)[Cfg::CPT][5], const double invd[3],
+                                              const double (&dc)[Cfg::CPT][3])
+    {
+        constexpr int NF = D == 0 ? Cfg::NF0 : (D == 1 ? Cfg::NF1 : Cfg::NF2);
+        if constexpr (Cfg::SPLIT)
+        {
+            split_fill<Cfg, D>(V, S, const_cast<double*>(V.split), Y, b[1], j0, G.n[1], shift, dc);
+            __syncthreads();
+        }
+        for (int f = threadIdx.x; f < NF; f += Cfg::NT)
+            face_one<Cfg, D>(V, S, sF, 0, f, G, Y, b, i0, j0, k0, shift, inv);
+        __syncthreads();
+        face_accumulate<Cfg, D>(sF, 0, G, Y, b, i0, j0, k0, relem, invd);
+        __syncthreads();
+    }
+
+    // All three directions' faces in one balanced loop (faces of one
+    // direction are contiguous, and NF0, NF0 + NF1 are multiples of the warp
+    // size for the merged shapes, so no warp mixes directions), then the
+    // divergence direction by direction in the same order as face_pass.
+    template <class Cfg>
+    __device__ __forceinline__ void face_pass_merged(const BoxView<Cfg>& V, const SchemeR<typename Cfg::Real>& S,
+                                                     double* sF, const GeomK& G, const YTabT<Cfg::STRETCH>& Y,
+                                                     const int b[3], int i0, int j0, int k0, int shift,
+                                                     const typename Cfg::Real inv[3],
+                                                     double (&relem)[Cfg::CPT][5], const double invd[3])
+    {
+        constexpr int N01 = Cfg::NF0 + Cfg::NF1, NALL = N01 + Cfg::NF2;
+        for (int f = threadIdx.x; f < NALL; f += Cfg::NT)
+        {
+            if (f < Cfg::NF0) face_one<Cfg, 0>(V, S, sF, 0, f, G, Y, b, i0, j0, k0, shift, inv);
+            else if (f < N01) face_one<Cfg, 1>(V, S, sF, Cfg::NF0, f - Cfg::NF0, G, Y, b, i0, j0, k0, shift, inv);
+            else face_one<Cfg, 2>(V, S, sF, N01, f - N01, G, Y, b, i0, j0, k0, shift, inv);
+        }
+        __syncthreads();
+        face_accumulate<Cfg, 0>(sF, 0, G, Y, b, i0, j0, k0, relem, invd);
+        face_accumulate<Cfg, 1>(sF, Cfg::NF0, G, Y, b, i0, j0, k0, relem, invd);
+        face_accumulate<Cfg, 2>(sF, N01, G, Y, b, i0, j0, k0, relem, invd);
         __syncthreads();
     }
 
@@ -1027,9 +1080,16 @@ namespace gbns
             }
         }
 
-        face_pass<Cfg, 0>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
-        face_pass<Cfg, 1>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
-        face_pass<Cfg, 2>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
+        if constexpr (Cfg::MERGED)
+        {
+            face_pass_merged<Cfg>(V, S, sF, G, Y, b, i0, j0, k0, shift, inv, relem, invd);
+        }
+        else
+        {
+            face_pass<Cfg, 0>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
+            face_pass<Cfg, 1>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
+            face_pass<Cfg, 2>(V, S, sF, G, Y, lb, b, i0, j0, k0, shift, inv, relem, invd, dc);
+        }
 
         // ---- write the residual (and the fused stage update) -----------------
         #pragma unroll
