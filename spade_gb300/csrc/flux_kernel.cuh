@@ -145,44 +145,6 @@ namespace gbns
         }
     };
 
-    // FP64 <-> FP32 conversions on the integer pipe.  On this GPU the FP64
-    // pipe (1/64 of FP32 throughput) also executes F2F conversions, and the
-    // FP32-flux kernel converts every staged value and every face flux.
-    // Normal-range values: round-to-nearest-even bit manipulation, identical
-    // to cvt.rn; zero, denormal, overflow, inf and nan fall back to the
-    // hardware conversion (rare).
-    __device__ __forceinline__ float f64_to_f32_rn(double d)
-    {
-        const unsigned int hi = static_cast<unsigned int>(__double2hiint(d));
-        const unsigned int lo = static_cast<unsigned int>(__double2loint(d));
-        const unsigned int sign = hi & 0x80000000u;
-        const int fe = int((hi >> 20) & 0x7ffu) - 1023 + 127;
-        if (fe >= 1 && fe <= 254)
-        {
-            const unsigned int m = ((hi & 0xfffffu) << 3) | (lo >> 29);
-            const unsigned int r = lo & 0x1fffffffu;
-            unsigned int v = (static_cast<unsigned int>(fe) << 23) | m;
-            if (r > 0x10000000u || (r == 0x10000000u && (m & 1u))) v += 1u;   // carry may reach inf: correct
-            return __uint_as_float(sign | v);
-        }
-        if (((hi << 1) | lo) == 0u) return __uint_as_float(sign);
-        return static_cast<float>(d);
-    }
-
-    __device__ __forceinline__ double f32_to_f64(float f)
-    {
-        const unsigned int u = __float_as_uint(f);
-        const unsigned int e = (u >> 23) & 0xffu;
-        if (e - 1u < 254u)
-            return __hiloint2double(static_cast<int>((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
-                                    static_cast<int>(u << 29));
-        if ((u << 1) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
-        return static_cast<double>(f);
-    }
-
-    template <class Real> __device__ __forceinline__ double to_f64(Real x) { return double(x); }
-    template <> __device__ __forceinline__ double to_f64<float>(float x) { return f32_to_f64(x); }
-
     __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
     __device__ __forceinline__ float  dev_sqrt(float x)  { return sqrtf(x); }
     __device__ __forceinline__ double dev_pow(double x, double y) { return pow(x, y); }
@@ -860,7 +822,7 @@ namespace gbns
             face_flux<Cfg, D>(V, S, rc, SplitIdx<Cfg, D>::right(fx, fy, fz), nD, inv, im, F);
         }
         #pragma unroll
-        for (int v = 0; v < 5; ++v) sF[v*Cfg::NFS + base + f] = to_f64<Real>(F[v]);
+        for (int v = 0; v < 5; ++v) sF[v*Cfg::NFS + base + f] = double(F[v]);
     }
 
     // Divergence of direction D into the cells this thread owns, in the
@@ -997,7 +959,7 @@ namespace gbns
                 {
                     const double* src = base + ((long long)(Z*G.nj + Y_)*G.ni + X)*5;
                     #pragma unroll
-                    for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = f64_to_f32_rn(__ldg(src + v));
+                    for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = float(__ldg(src + v));
                 }
                 else
                 {
@@ -1065,7 +1027,7 @@ namespace gbns
             for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
             {
                 #pragma unroll
-                for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = f64_to_f32_rn(stage[c*5 + v]);
+                for (int v = 0; v < 5; ++v) soa[v*Cfg::BOXN + c] = float(stage[c*5 + v]);
             }
             __syncthreads();
         }
