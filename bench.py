@@ -226,27 +226,32 @@ def run_gpu(args, rank, world):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / ke
 
-    # ---- FP32-flux form on the same workload (side measurement) ----------------
-    fp32 = None
-    if not args.no_fp32 and prec == _abi.PREC_FP64:
-        s32 = prob.scheme_desc(_abi.PREC_FP32_FLUX)
-        b32, t32 = autotune.tune(g, s32, qp, rptr[0], reps=3, use_cache=False)
-        tuned["fp32_flux"] = {"variant": b32, "ms_per_variant": t32}
+    # ---- other precision forms on the same workload (side measurements) --------
+    def side_form(precision, key, dtype):
+        sp = prob.scheme_desc(precision)
+        bv, tv = autotune.tune(g, sp, qp, rptr[0], reps=3, use_cache=False)
+        tuned[key] = {"variant": bv, "ms_per_variant": tv}
         w = torch.zeros(3 * n, dtype=torch.float64, device="cuda")
         for _ in range(2):
-            chk(lib.gbns_ssprk3_step(g, s32, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
+            chk(lib.gbns_ssprk3_step(g, sp, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
         torch.cuda.synchronize()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
         kk = max(3, args.steps)
         f0.record(stream)
         for _ in range(kk):
-            chk(lib.gbns_ssprk3_step(g, s32, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
+            chk(lib.gbns_ssprk3_step(g, sp, bc, qp, w.data_ptr(), ctypes.c_double(dt), st))
         f1.record(stream)
         torch.cuda.synchronize()
         fms = f0.elapsed_time(f1) / kk
-        fp32 = {"value": cells / (fms * 1e-3), "unit": UNIT, "ms_per_step": fms, "dtype": "f32-flux/f64-state",
+        return {"value": cells / (fms * 1e-3), "unit": UNIT, "ms_per_step": fms, "dtype": dtype,
                 "speedup_vs_fp64": (ms / args.steps) / fms}
+
+    fp32 = None
+    fma = None
+    if not args.no_fp32 and prec == _abi.PREC_FP64:
+        fp32 = side_form(_abi.PREC_FP32_FLUX, "fp32_flux", "f32-flux/f64-state")
+        fma = side_form(_abi.PREC_FP64_FMA, "fp64_fma", "f64 with FMA contraction (not bit-identical)")
 
     peaks = {}
     try:
@@ -270,7 +275,7 @@ def run_gpu(args, rank, world):
         "ms": ms, "cells": cells, "launches": launches, "flux_avg_ms": flux_avg_ms,
         "flux_share": sum(flux_ms) / ms, "achieved": achieved, "hbm_peak": hbm_peak, "peak_src": peak_src,
         "clocks": clk, "health_bad_cells": health.value, "e2e_ms": e2e_ms,
-        "h2d": host_q.numel() * 8, "d2h": host_q.numel() * 8, "fp32": fp32,
+        "h2d": host_q.numel() * 8, "d2h": host_q.numel() * 8, "fp32": fp32, "fma": fma,
         "fp64_fma_flops": fp64_rate.value, "fp32_fma_flops": fp32_rate.value, "traffic": traffic,
         "tuned": tuned,
     }
@@ -586,6 +591,7 @@ def main():
         "gpu_launches": r["launches"],
         "health_bad_cells": r["health_bad_cells"],
         "fp32_flux": r["fp32"],
+        "fp64_fma": r["fma"],
         "autotune": r["tuned"],
         # one plain flux_div (overwrite mode, no stage update) with the tuned
         # tile, from the autotuner's CUDA-event timings: cell-RHS/s

@@ -181,7 +181,8 @@ def test_flux_div_fp64_matches_oracle_unpinned_features(coords, case):
         assert np.array_equal(interior(r, ng), interior(ref, ng))
 
 
-@pytest.mark.parametrize("name", ["ck2_visc", "fweno_diss_visc", "totani_visc"])
+@pytest.mark.parametrize("name", ["ck2_visc", "fweno_diss_visc", "totani_visc", "ducros_diss", "fweno_ducros_visc",
+                                  "hyb_ck2_full", "hyb_ck4_diss_visc", "hyb_ck2_const_ducros_diss_visc"])
 def test_flux_div_fp32_flux_error_bounded(name):
     """FP32 face arithmetic, FP64 accumulation: normwise error vs the FP64
     reference stays at single-precision level."""
