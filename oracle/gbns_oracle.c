@@ -382,35 +382,54 @@ static st5 flux_fweno(const ctx_t* C, const double* cells[4], const double ncell
 }
 
 /* 5th-order WENO-JS (Jiang & Shu 1996) on the same per-point Rusanov split
- * as fweno_t.  cells[m], m = 0..5, at face offsets -5,-3,-1,1,3,5.  The
+ * as fweno_t: cells[m], m = 0..5, at face offsets -5,-3,-1,1,3,5; the
  * upwind part reconstructs f+ = fl+ds from cells 0..4, the downwind part
- * f- = fl-ds from cells 5..1 (mirrored); F = f+ + f-.  The nonlinear
- * weights g_k/D_k, D_k = (eps + beta_k)^2, are normalised with one
- * division as g_k prod_{j!=k} D_j / sum.  No reference counterpart:
- * parity unpinned. */
-static double weno5_side(double a, double b, double c, double d, double e, int smooth)
+ * f- = fl-ds from cells 5..1 (mirrored).  No reference counterpart: parity
+ * unpinned. */
+/* The WENO5 face flux as the FP64 kernels define it: per side (values a..e
+ * upwind to downwind) q_k = 6 p_k, B_k = 4 beta_k, E_k = (B_k + 4 eps)^2,
+ * a_k = g_k prod_{j!=k} E_j, N = sum a_k q_k, D = sum a_k, and both sides
+ * share one division F = (N_u D_d + N_d D_u)/(6 D_u D_d) while that
+ * denominator stays below 1e300 (else each side is divided separately). */
+typedef struct { double N, D; } weno5_nd_t;
+
+static weno5_nd_t weno5_nd(double a, double b, double c, double d, double e)
 {
-    /* Defined with explicit fused multiply-adds (C99 fma, correctly rounded
-     * like the GPU's), which the FP64 kernels reproduce bit for bit. */
-    const double c13 = 1.0/3.0, c16 = 1.0/6.0, c56 = 5.0/6.0, c76 = 7.0/6.0, c116 = 11.0/6.0;
-    const double p0 = fma(c13, a, fma(-c76, b, c116*c));
-    const double p1 = fma(-c16, b, fma(c56, c, c13*d));
-    const double p2 = fma(c13, c, fma(c56, d, (-c16)*e));
-    if (!smooth) return fma(0.1, p0, fma(0.6, p1, 0.3*p2));
+    const double q0 = fma(2.0, a, fma(-7.0, b, 11.0*c));
+    const double q1 = fma(5.0, c, fma(2.0, d, -b));
+    const double q2 = fma(2.0, c, fma(5.0, d, -e));
     const double t0 = fma(-2.0, b, a) + c, s0 = fma(3.0, c, fma(-4.0, b, a));
     const double t1 = fma(-2.0, c, b) + d, s1 = b - d;
     const double t2 = fma(-2.0, d, c) + e, s2 = fma(3.0, c, fma(-4.0, d, e));
-    const double k13 = 13.0/12.0;
-    const double b0 = fma(k13*t0, t0, (0.25*s0)*s0);
-    const double b1 = fma(k13*t1, t1, (0.25*s1)*s1);
-    const double b2 = fma(k13*t2, t2, (0.25*s2)*s2);
-    const double eps = 1e-16;
-    const double e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
-    const double d0 = e0*e0, d1 = e1*e1, d2 = e2*e2;
-    const double a0 = 0.1*(d1*d2);
-    const double a1 = 0.6*(d0*d2);
-    const double a2 = 0.3*(d0*d1);
-    return fma(a0, p0, fma(a1, p1, a2*p2))/((a0 + a1) + a2);
+    const double k = 13.0/3.0, eps4 = 4e-16;
+    const double e0 = fma(k*t0, t0, s0*s0) + eps4;
+    const double e1 = fma(k*t1, t1, s1*s1) + eps4;
+    const double e2 = fma(k*t2, t2, s2*s2) + eps4;
+    const double E0 = e0*e0, E1 = e1*e1, E2 = e2*e2;
+    const double a0 = 0.1*(E1*E2), a1 = 0.6*(E0*E2), a2 = 0.3*(E0*E1);
+    weno5_nd_t r;
+    r.N = fma(a0, q0, fma(a1, q1, a2*q2));
+    r.D = (a0 + a1) + a2;
+    return r;
+}
+
+static double weno5_pair(const double up[6], const double dn[6], int smooth)
+{
+    const double ua = up[0], ub = up[1], uc = up[2], ud = up[3], ue = up[4];
+    const double da = dn[5], db = dn[4], dc = dn[3], dd = dn[2], de = dn[1];
+    if (!smooth)
+    {
+        const double pu = fma(0.1, fma(2.0, ua, fma(-7.0, ub, 11.0*uc)),
+                              fma(0.6, fma(5.0, uc, fma(2.0, ud, -ub)), 0.3*fma(2.0, uc, fma(5.0, ud, -ue))));
+        const double pd = fma(0.1, fma(2.0, da, fma(-7.0, db, 11.0*dc)),
+                              fma(0.6, fma(5.0, dc, fma(2.0, dd, -db)), 0.3*fma(2.0, dc, fma(5.0, dd, -de))));
+        return (pu + pd)*(1.0/6.0);
+    }
+    const weno5_nd_t u = weno5_nd(ua, ub, uc, ud, ue);
+    const weno5_nd_t d = weno5_nd(da, db, dc, dd, de);
+    const double den = 6.0*(u.D*d.D);
+    if (den < 1.0e300) return fma(u.N, d.D, d.N*u.D)/den;
+    return u.N/(6.0*u.D) + d.N/(6.0*d.D);
 }
 
 static st5 flux_weno5(const ctx_t* C, const double* cells[6], const double ncell[6][3])
@@ -423,8 +442,7 @@ static st5 flux_weno5(const ctx_t* C, const double* cells[6], const double ncell
     {
         double up[6], dn[6];
         for (int m = 0; m < 6; ++m) { up[m] = fl[m][v] + ds[m][v]; dn[m] = fl[m][v] - ds[m][v]; }
-        F.v[v] = weno5_side(up[0], up[1], up[2], up[3], up[4], sm)
-               + weno5_side(dn[5], dn[4], dn[3], dn[2], dn[1], sm);
+        F.v[v] = weno5_pair(up, dn, sm);
     }
     return F;
 }

@@ -488,60 +488,91 @@ namespace gbns
         }
     }
 
-    // 5th-order WENO-JS side reconstruction (Jiang & Shu 1996); cells a..e
-    // upwind to downwind.  No reference counterpart.  In FP64 the nonlinear
-    // weights share one division: w_k = g_k prod_{j!=k} D_j / sum, with
-    // D_j = (eps + beta_j)^2 (the same weights as g_k/D_k normalised); FP32
-    // first divides every beta and eps by the largest beta (see below).
-    template <class Real>
-    __device__ __forceinline__ Real weno5_side(Real a, Real b, Real c, Real d, Real e, int smooth)
+    // FP32 5th-order WENO-JS side reconstruction (Jiang & Shu 1996); cells
+    // a..e upwind to downwind.  No reference counterpart.
+    __device__ __forceinline__ float weno5_side(float a, float b, float c, float d, float e, int smooth)
     {
-        // explicit fused multiply-adds: the definition the oracle restates
-        // with C99 fma, so FP64 results match it bit for bit
-        const Real c13 = Real(1.0/3.0), c16 = Real(1.0/6.0), c56 = Real(5.0/6.0), c76 = Real(7.0/6.0),
-                   c116 = Real(11.0/6.0);
-        const Real p0 = fma(c13, a, fma(-c76, b, c116*c));
-        const Real p1 = fma(-c16, b, fma(c56, c, c13*d));
-        const Real p2 = fma(c13, c, fma(c56, d, (-c16)*e));
-        if (!smooth) return fma(Real(0.1), p0, fma(Real(0.6), p1, Real(0.3)*p2));
-        const Real t0 = fma(Real(-2.0), b, a) + c, s0 = fma(Real(3.0), c, fma(Real(-4.0), b, a));
-        const Real t1 = fma(Real(-2.0), c, b) + d, s1 = b - d;
-        const Real t2 = fma(Real(-2.0), d, c) + e, s2 = fma(Real(3.0), c, fma(Real(-4.0), d, e));
-        const Real k13 = Real(13.0/12.0);
-        const Real b0 = fma(k13*t0, t0, (Real(0.25)*s0)*s0);
-        const Real b1 = fma(k13*t1, t1, (Real(0.25)*s1)*s1);
-        const Real b2 = fma(k13*t2, t2, (Real(0.25)*s2)*s2);
-        const Real eps = Real(1e-16);
-        const Real e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
-        const Real d0 = e0*e0, d1 = e1*e1, d2 = e2*e2;
-        if constexpr (sizeof(Real) == 8)
+        const float c13 = 1.0f/3.0f, c16 = 1.0f/6.0f, c56 = 5.0f/6.0f, c76 = 7.0f/6.0f, c116 = 11.0f/6.0f;
+        const float p0 = fmaf(c13, a, fmaf(-c76, b, c116*c));
+        const float p1 = fmaf(-c16, b, fmaf(c56, c, c13*d));
+        const float p2 = fmaf(c13, c, fmaf(c56, d, (-c16)*e));
+        if (!smooth) return fmaf(0.1f, p0, fmaf(0.6f, p1, 0.3f*p2));
+        const float t0 = fmaf(-2.0f, b, a) + c, s0 = fmaf(3.0f, c, fmaf(-4.0f, b, a));
+        const float t1 = fmaf(-2.0f, c, b) + d, s1 = b - d;
+        const float t2 = fmaf(-2.0f, d, c) + e, s2 = fmaf(3.0f, c, fmaf(-4.0f, d, e));
+        const float k13 = 13.0f/12.0f;
+        const float b0 = fmaf(k13*t0, t0, (0.25f*s0)*s0);
+        const float b1 = fmaf(k13*t1, t1, (0.25f*s1)*s1);
+        const float b2 = fmaf(k13*t2, t2, (0.25f*s2)*s2);
+        // (eps + beta)^2 overflows FP32 for beta > ~1.8e19, reached by the
+        // energy equation's fluxes (~1e8) in steep regions; the weights
+        // g_k/D_k normalised are unchanged when every beta and eps are
+        // divided by the largest beta.  With the scaled D_k <= 1 the product
+        // form (one division) cannot overflow; the floor keeps the sum
+        // positive when two stencils are perfectly smooth.
+        const float eps = 1e-16f;
+        const float sc = fmaxf(fmaxf(b0, b1), fmaxf(b2, eps));
+        const float is = 1.0f/sc;
+        const float ee = eps*is;
+        const float fl = 1e-30f;
+        const float q0 = fmaxf((b0*is + ee)*(b0*is + ee), fl);
+        const float q1 = fmaxf((b1*is + ee)*(b1*is + ee), fl);
+        const float q2 = fmaxf((b2*is + ee)*(b2*is + ee), fl);
+        const float a0 = 0.1f*(q1*q2);
+        const float a1 = 0.6f*(q0*q2);
+        const float a2 = 0.3f*(q0*q1);
+        return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
+    }
+
+    // FP64 WENO5-JS face flux F = F(f+ side) + F(f- side), each side a..e
+    // upwind to downwind (no reference counterpart; the oracle restates it
+    // operation for operation with C99 fma).  Per side, with q_k = 6 p_k the
+    // candidate polynomials and B_k = 4 beta_k the smoothness indicators
+    // (both scalings cancel in the normalised weights):
+    //   E_k = (B_k + 4 eps)^2,  a_k = g_k prod_{j!=k} E_j,  N = sum a_k q_k,  D = sum a_k
+    // and the two sides share one division:
+    //   F = (N_u D_d + N_d D_u) / (6 D_u D_d)
+    // (D_u D_d stays finite for flux differences below ~1e19; otherwise the
+    // sides are divided separately).
+    struct Weno5Side { double N, D; };
+
+    __device__ __forceinline__ Weno5Side weno5_nd(double a, double b, double c, double d, double e)
+    {
+        const double q0 = fma(2.0, a, fma(-7.0, b, 11.0*c));
+        const double q1 = fma(5.0, c, fma(2.0, d, -b));
+        const double q2 = fma(2.0, c, fma(5.0, d, -e));
+        const double t0 = fma(-2.0, b, a) + c, s0 = fma(3.0, c, fma(-4.0, b, a));
+        const double t1 = fma(-2.0, c, b) + d, s1 = b - d;
+        const double t2 = fma(-2.0, d, c) + e, s2 = fma(3.0, c, fma(-4.0, d, e));
+        const double k = 13.0/3.0, eps4 = 4e-16;
+        const double e0 = fma(k*t0, t0, s0*s0) + eps4;
+        const double e1 = fma(k*t1, t1, s1*s1) + eps4;
+        const double e2 = fma(k*t2, t2, s2*s2) + eps4;
+        const double E0 = e0*e0, E1 = e1*e1, E2 = e2*e2;
+        const double a0 = 0.1*(E1*E2), a1 = 0.6*(E0*E2), a2 = 0.3*(E0*E1);
+        Weno5Side r;
+        r.N = fma(a0, q0, fma(a1, q1, a2*q2));
+        r.D = (a0 + a1) + a2;
+        return r;
+    }
+
+    __device__ __forceinline__ double weno5_pair(double ua, double ub, double uc, double ud, double ue,
+                                                 double da, double db, double dc, double dd, double de, int smooth)
+    {
+        if (!smooth)
         {
-            const Real a0 = Real(0.1)*(d1*d2);
-            const Real a1 = Real(0.6)*(d0*d2);
-            const Real a2 = Real(0.3)*(d0*d1);
-            return fma(a0, p0, fma(a1, p1, a2*p2))/((a0 + a1) + a2);
+            const double pu = fma(0.1, fma(2.0, ua, fma(-7.0, ub, 11.0*uc)),
+                                  fma(0.6, fma(5.0, uc, fma(2.0, ud, -ub)), 0.3*fma(2.0, uc, fma(5.0, ud, -ue))));
+            const double pd = fma(0.1, fma(2.0, da, fma(-7.0, db, 11.0*dc)),
+                                  fma(0.6, fma(5.0, dc, fma(2.0, dd, -db)), 0.3*fma(2.0, dc, fma(5.0, dd, -de))));
+            return (pu + pd)*(1.0/6.0);
         }
-        else
-        {
-            // FP32: (eps + beta)^2 overflows for beta > ~1.8e19, reached by
-            // the energy equation's fluxes (~1e8) in steep regions; the
-            // weights g_k/D_k normalised are unchanged when every beta and
-            // eps are divided by the largest beta.  With the scaled D_k <= 1
-            // the product form (one division) cannot overflow; the floor
-            // keeps the sum positive when two stencils are perfectly smooth.
-            (void)d0; (void)d1; (void)d2;
-            const Real sc = fmaxf(fmaxf(b0, b1), fmaxf(b2, eps));
-            const Real is = Real(1.0)/sc;
-            const Real e = eps*is;
-            const Real fl = Real(1e-30);
-            const Real q0 = fmaxf((b0*is + e)*(b0*is + e), fl);
-            const Real q1 = fmaxf((b1*is + e)*(b1*is + e), fl);
-            const Real q2 = fmaxf((b2*is + e)*(b2*is + e), fl);
-            const Real a0 = Real(0.1)*(q1*q2);
-            const Real a1 = Real(0.6)*(q0*q2);
-            const Real a2 = Real(0.3)*(q0*q1);
-            return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
-        }
+        const Weno5Side u = weno5_nd(ua, ub, uc, ud, ue);
+        const Weno5Side d = weno5_nd(da, db, dc, dd, de);
+        const double den = 6.0*(u.D*d.D);
+        if (den < 1.0e300)
+            return fma(u.N, d.D, d.N*u.D)/den;
+        return u.N/(6.0*u.D) + d.N/(6.0*d.D);
     }
 
     template <class Cfg, int D>
@@ -571,8 +602,11 @@ namespace gbns
                     dn[m] = fl - ds;
                 }
             }
-            out[eq] = weno5_side<Real>(up[0], up[1], up[2], up[3], up[4], S.smooth)
-                    + weno5_side<Real>(dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
+            if constexpr (sizeof(Real) == 8)
+                out[eq] = weno5_pair(up[0], up[1], up[2], up[3], up[4], dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
+            else
+                out[eq] = weno5_side(up[0], up[1], up[2], up[3], up[4], S.smooth)
+                        + weno5_side(dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
         }
     }
 
