@@ -52,3 +52,31 @@ def transform_reduce(q, gas, kind, stream=None):
     _native.check(_native.lib().gbns_reduce(q.desc(), gas.desc(), q.ptr(), int(kind),
                                             out.ctypes.data_as(ctypes.c_void_p), _stream(stream)))
     return out if kind == _abi.RED_CONSERVED else float(out[0])
+
+
+include_exchanges = "include_exchanges"
+exclude_exchanges = "exclude_exchanges"
+
+
+def fill_array(q, func, exchange_policy=include_exchanges):
+    """algs::fill_array(array, kernel, exchange_policy)
+    (algs/transform_inplace.h:97-101): q = func(x, y, z) at every cell centre
+    (ghosts too with include_exchanges).  func receives the physical
+    coordinates as torch tensors on q's device (broadcastable shapes) and
+    returns the five primitives (p, T, u, v, w), each a tensor or a number.
+    Host-side initialisation: not a hot path."""
+    import torch
+    ng = q.ng
+    x, y, z = (torch.from_numpy(np.ascontiguousarray(a)).to(q.data.device) for a in q.grid.get_coords(ng))
+    vals = func(x, y, z)
+    if len(vals) != 5:
+        raise ValueError("fill_array: func must return (p, T, u, v, w)")
+    full = q.data.shape[:-1]
+    target = q.data if exchange_policy == include_exchanges else q.interior()
+    for v, val in enumerate(vals):
+        t = torch.as_tensor(val, dtype=torch.float64, device=q.data.device).expand(full)
+        if exchange_policy == include_exchanges:
+            target[..., v] = t
+        else:
+            target[..., v] = t[:, ng:-ng, ng:-ng, ng:-ng]
+    return q

@@ -54,6 +54,30 @@ class cartesian_grid_t:
         return _abi.grid_desc(self.blocks.num_blocks, self.cells, ng, self.blocks.bounds,
                               self.coord_sys.kind, self.coord_sys.params)
 
+    def get_coords(self, ng):
+        """Physical cell-centre coordinates of every cell, ghosts included
+        (cartesian_grid_t::get_coords, cartesian_grid.h:290-310): numpy arrays
+        x (nb, 1, 1, ni), y (nb, 1, nj, 1), z (nb, nk, 1, 1) that broadcast to
+        the grid_array shape without the variable axis.  Block boxes and
+        spacing use the reference's arithmetic; y goes through the
+        coordinate map when the system stretches it."""
+        nb = self.blocks.num_blocks
+        nlb = self.get_num_global_blocks()
+        out = []
+        for d in range(3):
+            idx = np.arange(-ng, self.cells[d] + ng, dtype=np.float64)
+            c = np.empty((nlb, self.cells[d] + 2 * ng))
+            for lb in range(nlb):
+                b = [lb % nb[0], (lb // nb[0]) % nb[1], lb // (nb[0] * nb[1])][d]
+                lo, hi = self.blocks.bounds[2 * d], self.blocks.bounds[2 * d + 1]
+                bsize = (hi - lo) / nb[d]
+                mn = lo + b * bsize
+                c[lb] = mn + (idx + 0.5) * (((mn + bsize) - mn) / self.cells[d])
+            if d == 1 and getattr(self.coord_sys, "kind", _abi.COORDS_IDENTITY) != _abi.COORDS_IDENTITY:
+                c = self.coord_sys.map_y(c, self.blocks.bounds[2], self.blocks.bounds[3])
+            out.append(c)
+        return out[0][:, None, None, :], out[1][:, None, :, None], out[2][:, :, None, None]
+
     def get_dx(self, i, lb=0):
         """Block spacing exactly as the reference computes it."""
         nb = self.blocks.num_blocks[i]

@@ -195,3 +195,28 @@ def test_size_limits_rejected_before_cuda():
     g = _abi.grid_desc((1, 40, 1), (8, 32, 8), 3, (0, 1, -1, 1, 0, 1), coords=_abi.COORDS_TANH_Y, coord_param=(2.0, 0, 0, 0))
     rc = _native.lib().gbns_flux_div(g, P.scheme(conv=_abi.CONV_WENO5), ctypes.c_void_p(16), ctypes.c_void_p(32), 0, None)
     assert rc == _abi.ERR_UNSUPPORTED and "metric table" in _native.last_error()
+
+
+def test_fill_array_and_physical_coordinates_on_cpu_tensors():
+    """algs.fill_array evaluates a function of the physical cell centres
+    (stretched y through the coordinate map) into a grid_array; CPU tensors."""
+    from spade_gb300 import grid, coords, algs
+    blocks = grid.cartesian_blocks_t((2, 2, 1), (0.0, 2.0, -1.0, 1.0, 0.0, 1.0))
+    cs = coords.diagonal_coords(coords.identity_1D(), coords.tanh_stretch_1D(2.0), coords.identity_1D())
+    g = grid.cartesian_grid_t((4, 4, 2), blocks, cs)
+    q = grid.grid_array(g, 0.0, 2, device="cpu")
+    algs.fill_array(q, lambda x, y, z: (x + 0 * y, y + 0 * x, z + 0 * x, 1.0, -1.0))
+    d = q.data.numpy()
+    ng = 2
+    # x of block 1 (x-index 1), interior cell 0 = 1.0 + 0.5*0.25
+    assert abs(d[1, ng, ng, ng, 0] - 1.125) < 1e-15
+    # y of the first interior row of a y-min block: the stretched map of eta = -1 + 0.5*0.25
+    eta = -1.0 + 0.125
+    want = np.tanh(2.0 * eta) / np.tanh(2.0)
+    assert abs(d[0, ng, ng, ng, 1] - want) < 1e-15
+    assert np.all(d[..., 3] == 1.0) and np.all(d[..., 4] == -1.0)
+    # exclude_exchanges leaves the ghosts alone
+    q2 = grid.grid_array(g, 7.0, 2, device="cpu")
+    algs.fill_array(q2, lambda x, y, z: (x, y, z, 0.0, 0.0), algs.exclude_exchanges)
+    d2 = q2.data.numpy()
+    assert np.all(d2[:, 0] == 7.0) and d2[0, ng, ng, ng, 3] == 0.0
