@@ -8,8 +8,9 @@ every compute call goes through the C ABI of libgbns.so (include/gbns.h).
 """
 from . import _abi
 from . import fluid_state, coords, boundary, state_sensor, viscous_laws, viscous, convective, omni
-from . import grid, algs, pde_algs, time_integration
+from . import grid, algs, pde_algs, time_integration, io, parallel
 from ._native import SpadeError, lib as native_lib, LIB_PATH
 
 __all__ = ["fluid_state", "coords", "boundary", "state_sensor", "viscous_laws", "viscous", "convective",
-           "omni", "grid", "algs", "pde_algs", "time_integration", "SpadeError", "native_lib", "LIB_PATH"]
+           "omni", "grid", "algs", "pde_algs", "time_integration", "io", "parallel", "SpadeError", "native_lib",
+           "LIB_PATH"]
