@@ -315,6 +315,29 @@ def batch_instances(n, seed=0):
     return out
 
 
+def run_small_tgv(args):
+    """The reference's CPU-runnable case (Taylor-Green, 2x2x2 blocks of 16^3
+    = 32,768 cells, cent_keep<2> + visc_lr, SSPRK3) on the GPU: 20 steps with
+    the fused step replayed from a CUDA graph, i.e. the per-step latency of a
+    launch-bound problem, next to the same steps on the host cores."""
+    import torch
+    from spade_gb300 import _abi, workloads
+    from spade_gb300.time_integration import ssprk3_stepper
+    prob = workloads.taylor_green(nblk=(2, 2, 2), ncell=(16, 16, 16), ng=2, rng="torch", seed=0)
+    st = ssprk3_stepper(prob.q, prob.scheme_desc(_abi.PREC_FP64), prob.bc_desc(), prob.dt, use_graph=True)
+    st.step(3)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    st.step(20)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 20
+    return {"workload": "Taylor-Green 2x2x2 blocks of 16^3 (32,768 cells), cent_keep<2> + visc_lr(constant), "
+                        "FP64, fused step replayed from a CUDA graph", "steps": 20, "ms_per_step": ms,
+            "cell_steps_per_s": 32768 / (ms * 1e-3)}
+
+
 def run_batch_form(args):
     import torch
     from spade_gb300 import _abi, _native, workloads
@@ -565,6 +588,7 @@ def main():
         return
     forms = {}
     if not args.no_forms:
+        forms["small_tgv"] = run_small_tgv(args)
         forms["batch_form"] = run_batch_form(args)
         forms["serve_form"] = run_serve_form(args)
     cpu = None
