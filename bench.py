@@ -592,8 +592,10 @@ def main():
         forms["batch_form"] = run_batch_form(args)
         forms["serve_form"] = run_serve_form(args)
     cpu = None
+    cpu1 = None
     if world == 1 and not args.no_cpu_baseline:
         cpu = cpu_sample(steps=1, nblk=(4, 4, 2))
+        cpu1 = cpu_sample(steps=1, nblk=(1, 2, 1), threads=1)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -625,6 +627,7 @@ def main():
     line.update(forms)
     if cpu is not None:
         line["cpu_baseline"] = cpu
+        line["cpu_baseline_1core"] = cpu1
     print(json.dumps(line))
 
 
