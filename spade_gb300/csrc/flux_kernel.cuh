@@ -37,8 +37,6 @@ namespace gbns
             (CONV == GBNS_CONV_HYBRID) ? 4 :
             (CONV == GBNS_CONV_FWENO || CONV == GBNS_CONV_WENO5) ? 3 :
             (CONV == GBNS_CONV_CENT_KEEP || CONV == GBNS_CONV_TOTANI) ? 2 : 0;
-        // slot of the centred internal energy p/(rho (gamma-1))
-        static constexpr int CK_E = (CONV == GBNS_CONV_HYBRID) ? 3 : 1;
     };
 
     template <bool S> using YTabT = typename std::conditional<S, YTabK, YTabNone>::type;
@@ -81,11 +79,19 @@ namespace gbns
         // computed once per cell and direction into shared memory instead of
         // once per stencil point per face (each cell sits in 4 or 6 face
         // stencils per direction); it takes the place of the derived buffer.
-        static constexpr bool SPLIT = FP64 && (CONV == GBNS_CONV_FWENO || CONV == GBNS_CONV_WENO5);
+        // The hybrid scheme's fweno half uses the same cache; its centred half
+        // keeps (rho, e) per box cell after it (NDERB = 2).
+        static constexpr bool SPLIT = FP64 && (CONV == GBNS_CONV_FWENO || CONV == GBNS_CONV_WENO5 ||
+                                               CONV == GBNS_CONV_HYBRID);
         static constexpr int NL0 = (TX + 2*HC)*TY*TZ, NL1 = TX*(TY + 2*HC)*TZ, NL2 = TX*TY*(TZ + 2*HC);
         static constexpr int NLMAX = cmax3(NL0, NL1, NL2);
-        static constexpr size_t DER_BYTES   = SPLIT ? align128(size_t(10)*NLMAX*sizeof(double))
-                                                    : align128(size_t(NDER > 0 ? NDER : 1)*BOXN*sizeof(Real));
+        // derived values per box cell kept in the der buffer
+        static constexpr int NDERB = SPLIT ? (CONV == GBNS_CONV_HYBRID ? 2 : 0) : NDER;
+        // slot of the centred internal energy p/(rho (gamma-1))
+        static constexpr int CK_E = (CONV == GBNS_CONV_HYBRID && !SPLIT) ? 3 : 1;
+        static constexpr size_t SPLIT_BYTES = SPLIT ? align128(size_t(10)*NLMAX*sizeof(double)) : 0;
+        static constexpr size_t DER_BYTES   = SPLIT_BYTES +
+            ((SPLIT && NDERB == 0) ? 0 : align128(size_t(NDERB > 0 ? NDERB : 1)*BOXN*sizeof(Real)));
         // FP32-flux evaluates the faces of all three directions in one
         // balanced loop (warp-aligned direction boundaries), which needs the
         // face buffer for all of them; FP64 (split cache per direction) keeps
@@ -183,9 +189,10 @@ namespace gbns
     {
         using Real = typename Cfg::Real;
         const Real p = V.q(0, c), T = V.q(1, c), u = V.q(2, c), v = V.q(3, c), w = V.q(4, c);
-        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP || Cfg::CONV == GBNS_CONV_TOTANI)
+        if constexpr (Cfg::CONV == GBNS_CONV_CENT_KEEP || Cfg::CONV == GBNS_CONV_TOTANI ||
+                      (Cfg::CONV == GBNS_CONV_HYBRID && Cfg::SPLIT))
         {
-            // convective.h:130-131 / 80-84
+            // convective.h:130-131 / 80-84 (the hybrid's fweno half reads the split cache)
             const Real rho = p/(S.R*T);
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = p/(rho*S.gm1);
@@ -229,7 +236,7 @@ namespace gbns
             const int c = rc + (m - hw)*SD;
             un[m]  = V.q(2 + D, c)*nD;
             rho[m] = V.d(0, c);
-            eng[m] = V.d(ConvTraits<Cfg::CONV, Cfg::ORDER>::CK_E, c);
+            eng[m] = V.d(Cfg::CK_E, c);
         }
         Real cc = 0, mx = 0, my = 0, mz = 0, g = 0, k = 0, ie = 0, pp = 0;
         #pragma unroll
@@ -1069,13 +1076,15 @@ namespace gbns
         BoxView<Cfg> V;
         V.stage = stage;
         V.soa = soa;
-        V.der = der;
         V.split = reinterpret_cast<const double*>(der);
+        if constexpr (Cfg::SPLIT)
+            der = reinterpret_cast<Real*>(reinterpret_cast<unsigned char*>(der) + Cfg::SPLIT_BYTES);
+        V.der = der;
         SchemeR<Real> S;
         S.load(SK);
 
         // ---- per-cell derived values on the stencil cross -------------------
-        if constexpr (Cfg::NDER > 0 && !Cfg::SPLIT)
+        if constexpr (Cfg::NDERB > 0)
         {
             constexpr int HC = Cfg::HC;
             for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
