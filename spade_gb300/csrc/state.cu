@@ -86,49 +86,107 @@ namespace gbns
         fill_one_ghost_from(q, q, G, bc, lb, ii, jj, kk);
     }
 
-    // One thread per padded cell; interior cells return at once.
+    // Ghost cells of one block enumerated directly (no thread visits an
+    // interior cell): the two z slabs of full ni*nj planes, then for interior
+    // k the two y slabs of full rows, then for interior k, j the 2*ng x cells.
+    // Consecutive t are consecutive cells along x, so loads and stores coalesce.
+    __device__ __forceinline__ long long ghosts_per_block(const GeomK& G)
+    {
+        return (long long)G.ni*G.nj*G.nk - (long long)G.n[0]*G.n[1]*G.n[2];
+    }
+
+    __device__ __forceinline__ void ghost_cell(long long t, const GeomK& G, int& ii, int& jj, int& kk)
+    {
+        const int ng = G.ng, ni = G.ni, nj = G.nj;
+        const long long plane = (long long)ni*nj;
+        const long long zs = 2ll*ng*plane;
+        if (t < zs)
+        {
+            const int k = int(t / plane);
+            const int r = int(t - k*plane);
+            kk = k < ng ? k : k + G.n[2];
+            jj = r / ni;
+            ii = r - jj*ni;
+            return;
+        }
+        t -= zs;
+        const long long yrow = 2ll*ng*ni;
+        const long long ys = (long long)G.n[2]*yrow;
+        if (t < ys)
+        {
+            const int k = int(t / yrow);
+            const int r = int(t - k*yrow);
+            kk = ng + k;
+            const int j = r / ni;
+            jj = j < ng ? j : j + G.n[1];
+            ii = r - j*ni;
+            return;
+        }
+        t -= ys;
+        const int xr = 2*ng;
+        const long long xplane = (long long)G.n[1]*xr;
+        const int k = int(t / xplane);
+        const int r = int(t - k*xplane);
+        kk = ng + k;
+        jj = ng + r / xr;
+        const int i = r - (r / xr)*xr;
+        ii = i < ng ? i : i + G.n[0];
+    }
+
+    // Interior cell c (x fastest) of one block: its padded indices.
+    __device__ __forceinline__ long long interior_offset(long long c, const GeomK& G, int lb)
+    {
+        const int i = int(c % G.n[0]);
+        const long long r = c / G.n[0];
+        const int j = int(r % G.n[1]);
+        const int k = int(r / G.n[1]);
+        return (long long)lb*G.bstride + ((long long)((k + G.ng)*G.nj + (j + G.ng))*G.ni + (i + G.ng))*5;
+    }
+
+    // One thread per ghost cell.
     __global__ void __launch_bounds__(256)
     fill_ghosts_kernel(double* __restrict__ q, const __grid_constant__ GeomK G, const BcK bc)
     {
-        const long long per_block = (long long)G.ni*G.nj*G.nk;
+        const long long per_block = ghosts_per_block(G);
         const long long total = per_block*G.nblk;
         for (long long idx = blockIdx.x*(long long)blockDim.x + threadIdx.x; idx < total;
              idx += (long long)gridDim.x*blockDim.x)
         {
             const int lb = int(idx / per_block);
-            const long long rem = idx - lb*per_block;
-            const int kk = int(rem / ((long long)G.ni*G.nj));
-            const int jj = int((rem / G.ni) % G.nj);
-            const int ii = int(rem % G.ni);
+            int ii, jj, kk;
+            ghost_cell(idx - lb*per_block, G, ii, jj, kk);
             fill_one_ghost(q, G, bc, lb, ii, jj, kk);
         }
     }
 
     // dst = src on interior cells; dst ghosts filled from src's interior
     // donors (the ghost fill of the state that the last fused stage wrote to
-    // the scratch buffer, landing in the caller's array).
+    // the scratch buffer, landing in the caller's array).  Ghost cells first,
+    // then the interior copy, in one grid-stride range.
     __global__ void __launch_bounds__(256)
     copy_fill_kernel(double* __restrict__ dst, const double* __restrict__ src, const __grid_constant__ GeomK G, const BcK bc)
     {
-        const long long per_block = (long long)G.ni*G.nj*G.nk;
-        const long long total = per_block*G.nblk;
+        const long long gpb = ghosts_per_block(G);
+        const long long ipb = (long long)G.n[0]*G.n[1]*G.n[2];
+        const long long ng_total = gpb*G.nblk;
+        const long long total = ng_total + ipb*G.nblk;
         for (long long idx = blockIdx.x*(long long)blockDim.x + threadIdx.x; idx < total;
              idx += (long long)gridDim.x*blockDim.x)
         {
-            const int lb = int(idx / per_block);
-            const long long rem = idx - lb*per_block;
-            const int kk = int(rem / ((long long)G.ni*G.nj));
-            const int jj = int((rem / G.ni) % G.nj);
-            const int ii = int(rem % G.ni);
-            const int i = ii - G.ng, j = jj - G.ng, k = kk - G.ng;
-            if (i >= 0 && i < G.n[0] && j >= 0 && j < G.n[1] && k >= 0 && k < G.n[2])
+            if (idx < ng_total)
             {
-                #pragma unroll
-                for (int v = 0; v < 5; ++v) dst[idx*5 + v] = src[idx*5 + v];
+                const int lb = int(idx / gpb);
+                int ii, jj, kk;
+                ghost_cell(idx - lb*gpb, G, ii, jj, kk);
+                fill_one_ghost_from(dst, src, G, bc, lb, ii, jj, kk);
             }
             else
             {
-                fill_one_ghost_from(dst, src, G, bc, lb, ii, jj, kk);
+                const long long c = idx - ng_total;
+                const int lb = int(c / ipb);
+                const long long off = interior_offset(c - lb*ipb, G, lb);
+                #pragma unroll
+                for (int v = 0; v < 5; ++v) dst[off + v] = src[off + v];
             }
         }
     }
@@ -152,7 +210,7 @@ namespace gbns
     {
         BcK k;
         for (int i = 0; i < 6; ++i) { k.kind[i] = bc->kind[i]; k.t_wall[i] = bc->t_wall[i]; }
-        const long long total = (long long)G.ni*G.nj*G.nk*G.nblk;
+        const long long total = (long long)G.ni*G.nj*G.nk*G.nblk;   // ghosts + interior
         copy_fill_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(dst, src, G, k);
         return check_cuda(cudaGetLastError(), "copy_fill launch");
     }
@@ -161,7 +219,7 @@ namespace gbns
     {
         BcK k;
         for (int i = 0; i < 6; ++i) { k.kind[i] = bc->kind[i]; k.t_wall[i] = bc->t_wall[i]; }
-        const long long total = (long long)G.ni*G.nj*G.nk*G.nblk;
+        const long long total = ((long long)G.ni*G.nj*G.nk - (long long)G.n[0]*G.n[1]*G.n[2])*G.nblk;
         fill_ghosts_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(prims, G, k);
         return check_cuda(cudaGetLastError(), "fill_ghosts launch");
     }
@@ -263,25 +321,23 @@ namespace gbns
             const BlockItem w = items[it];
             const InstK& I = insts[w.inst];
             const GeomK& G = I.G;
-            const int npad = G.ni*G.nj*G.nk;
             double* dst = mode == 1 ? I.R[2] : I.q;
             const double* src = mode == 0 ? I.q : I.R[2];
-            const long long base = (long long)w.lb*npad;
-            for (int c = threadIdx.x; c < npad; c += blockDim.x)
+            const int gpb = int(ghosts_per_block(G));
+            for (int t = threadIdx.x; t < gpb; t += blockDim.x)
             {
-                const int ii = c % G.ni, jj = (c / G.ni) % G.nj, kk = c / (G.ni*G.nj);
-                const int i = ii - G.ng, j = jj - G.ng, k = kk - G.ng;
-                if (i >= 0 && i < G.n[0] && j >= 0 && j < G.n[1] && k >= 0 && k < G.n[2])
+                int ii, jj, kk;
+                ghost_cell(t, G, ii, jj, kk);
+                fill_one_ghost_from(dst, src, G, I.bc, w.lb, ii, jj, kk);
+            }
+            if (mode == 2)
+            {
+                const int ipb = G.n[0]*G.n[1]*G.n[2];
+                for (int c = threadIdx.x; c < ipb; c += blockDim.x)
                 {
-                    if (mode == 2)
-                    {
-                        #pragma unroll
-                        for (int v = 0; v < 5; ++v) dst[(base + c)*5 + v] = src[(base + c)*5 + v];
-                    }
-                }
-                else
-                {
-                    fill_one_ghost_from(dst, src, G, I.bc, w.lb, ii, jj, kk);
+                    const long long off = interior_offset(c, G, w.lb);
+                    #pragma unroll
+                    for (int v = 0; v < 5; ++v) dst[off + v] = src[off + v];
                 }
             }
         }
