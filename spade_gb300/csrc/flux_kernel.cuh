@@ -3,17 +3,20 @@
 // One CTA owns one TX*TY*TZ tile of one grid block.  It stages the tile plus
 // an H-cell halo (AoS5 doubles, straight from the grid_array layout) into
 // shared memory with one 4-D TMA copy (or coalesced loads when the row pitch
-// is not 16-byte aligned), derives the per-cell quantities every face of the
-// stencil shares (rho, e or the Rusanov split) once per cell, evaluates each
-// face flux ONCE (the reference's flux_div_basic, flux_div_basic.h:47-76,
-// evaluates every face twice) into a shared face buffer, and accumulates
+// is not 16-byte aligned; FP32-flux can load the stencil cells straight into
+// FP32), derives the per-cell quantities every face of the stencil shares
+// (rho, e; for fweno/WENO5 in FP64 the Rusanov split f+/f- of each line cell,
+// cached per direction), evaluates each face flux ONCE (the reference's
+// flux_div_basic, flux_div_basic.h:47-76, evaluates every face twice) into a
+// shared face buffer, and accumulates
 //     rhs(cell) += jac*F(i-1/2)*inv_dx - jac*F(i+1/2)*inv_dx
 // per direction in FP64 registers in the reference's order
-// (flux_div_basic.h:109-129), then writes the AoS5 residual.
+// (flux_div_basic.h:109-129).  The epilogue writes the AoS5 residual and/or
+// applies the SSPRK3 stage update to the tile's cells (gbns_flux_div_rk).
 //
 // Real = double: every operation in FP64 (the drop-in).
 // Real = float : per-cell derivation and face fluxes in FP32, state read and
-//                divergence accumulated and written in FP64.
+//                divergence accumulated, stage update and state in FP64.
 #pragma once
 
 #include <type_traits>
