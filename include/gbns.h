@@ -328,8 +328,8 @@ int gbns_source_term(const gbns_grid_desc* grid, const gbns_source_desc* source,
  * arena of hbm_budget_bytes allocated at creation; adding an instance that
  * does not fit returns GBNS_ERR_CAPACITY.  Every instance's result is
  * bit-identical to advancing it alone (gbns_ssprk3_step).  Supported kernel
- * classes: cent_keep<2>, totani_lr, fweno_t and WENO5 on identity grids,
- * WENO5 on stretched-y grids; precision GBNS_PREC_FP64 or GBNS_PREC_FP32_FLUX
+ * classes: cent_keep<2>, totani_lr, fweno_t, WENO5 and hybrid_scheme_t of
+ * cent_keep<2> and fweno_t on identity grids, WENO5 on stretched-y grids; precision GBNS_PREC_FP64 or GBNS_PREC_FP32_FLUX
  * (one per batch).  All calls are ordered on the batch's stream.
  * No counterpart in the reference (its integrator advances one grid,
  * time-integration/integrator.h:52-55). */

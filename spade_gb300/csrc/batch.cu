@@ -17,6 +17,7 @@ namespace gbns
         if (s->convective == GBNS_CONV_TOTANI && id) return BCLASS_TOTANI_ID;
         if (s->convective == GBNS_CONV_FWENO && id) return BCLASS_FWENO_ID;
         if (s->convective == GBNS_CONV_WENO5) return id ? BCLASS_WENO5_ID : BCLASS_WENO5_ST;
+        if (s->convective == GBNS_CONV_HYBRID && s->order == 2 && id) return BCLASS_HYB2_ID;
         return -1;
     }
 
@@ -24,6 +25,7 @@ namespace gbns
     {
         tile[0] = 8; tile[1] = 8; tile[2] = 8;
         if ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) && precision == GBNS_PREC_FP32_FLUX) tile[2] = 4;
+        if (cls == BCLASS_HYB2_ID) tile[2] = 4;
     }
 
     // First-fit allocator over one device allocation (offsets in bytes).

@@ -97,6 +97,7 @@ namespace gbns
             case BCLASS_WENO5_ST:  GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 256);
             case BCLASS_WENO5_ID:  GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 256);
 #endif
+            case BCLASS_HYB2_ID:   GBNS_BRUN(GBNS_CONV_HYBRID, 2, false, 8, 8, 4, 256);
         }
         return set_error(GBNS_ERR_UNSUPPORTED, "no batched kernel for this class");
     }

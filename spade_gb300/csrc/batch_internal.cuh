@@ -44,6 +44,7 @@ namespace gbns
         BCLASS_FWENO_ID,       // fweno_t, identity
         BCLASS_WENO5_ST,       // WENO5, stretched y (channel)
         BCLASS_WENO5_ID,       // WENO5, identity
+        BCLASS_HYB2_ID,        // hybrid_scheme_t(cent_keep<2>, fweno_t), identity
         BCLASS_COUNT
     };
 

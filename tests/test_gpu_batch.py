@@ -52,6 +52,18 @@ def channel_instance(seed, precision=_abi.PREC_FP64):
     return grid, s, bc, q, 2e-6
 
 
+def hybrid_instance(seed, precision=_abi.PREC_FP64):
+    """Taylor-Green field under hybrid_scheme_t(cent_keep<2>, fweno_t,
+    ducros_t, full_flux) + visc_lr."""
+    grid, s, bc, q, dt = tgv_instance((2, 1, 1), seed, precision, mach=0.2)
+    s.convective = _abi.CONV_HYBRID
+    s.order = 2
+    s.hybrid_flux = _abi.HYBRID_FULL_FLUX
+    s.hybrid_sensor = _abi.SENSOR_DUCROS
+    s.hybrid_param = 1e-3
+    return grid, s, bc, q, dt
+
+
 def alone(grid, s, bc, q, dt, nsteps):
     qd = torch.from_numpy(q).cuda()
     work = torch.zeros(3 * qd.numel(), dtype=torch.float64, device="cuda")
@@ -66,7 +78,7 @@ def alone(grid, s, bc, q, dt, nsteps):
 def test_batch_bitwise_equals_alone(precision, use_graph):
     insts = [tgv_instance((1, 1, 1), 1, precision), tgv_instance((2, 1, 1), 2, precision, mach=0.3, re=300.0),
              tgv_instance((2, 2, 2), 3, precision, re=3000.0), channel_instance(4, precision),
-             tgv_instance((2, 2, 1), 5, precision)]
+             tgv_instance((2, 2, 1), 5, precision), hybrid_instance(6, precision)]
     b = batch_t(512 << 20, precision, use_graph)
     slots = []
     keep = []
