@@ -281,18 +281,25 @@ def run_gpu(args, rank, world):
     }
 
 
-def _read_traffic(cells):
-    """DRAM bytes per fused flux_div launch (mean over the three SSPRK3
-    stages) from the committed ncu summary of a 2.1M-cell capture, scaled to
-    this workload's cell count (traffic grows with the cells processed)."""
+def _profile_value(key):
+    """A `key: value` line of the committed ncu summary of the fused FP64
+    flux kernel (2.1M-cell capture of the channel scheme)."""
     path = os.path.join(ROOT, "profiles", "flux_div_rk_channel_fp64.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_cell:"):
-                return float(line.split(":")[1]) * cells
+            if line.startswith(key + ":"):
+                return float(line.split(":")[1])
     except Exception:
         pass
     return None
+
+
+def _read_traffic(cells):
+    """DRAM bytes per fused flux_div launch (mean over the three SSPRK3
+    stages) from the committed ncu summary, scaled to this workload's cell
+    count (traffic grows with the cells processed)."""
+    v = _profile_value("traffic_bytes_per_cell")
+    return None if v is None else v * cells
 
 
 # ---------------------------------------------------------------------------
@@ -612,7 +619,9 @@ def main():
                      "alg_bytes_per_cell": ALG_BYTES_FUSED, "avg_launch_ms": r["flux_avg_ms"],
                      "share_of_step": r["flux_share"]},
         "fp64_roof": {"fma_rate_tflops": r["fp64_fma_flops"] / 1e12, "fp32_fma_rate_tflops": r["fp32_fma_flops"] / 1e12,
-                      "note": "measured DFMA/FFMA chains on this GPU"},
+                      "note": "measured DFMA/FFMA chains on this GPU; the FP64 kernel is bound by the FP64 pipe",
+                      "fp64_pipe_active_frac_ncu": _profile_value("fp64_pipe_active_frac"),
+                      "pipe_source": "profiles/flux_div_rk_channel_fp64.md (sm__pipe_fp64_cycles_active, 2.1M-cell capture)"},
         "step_bytes": {"alg_bytes_per_cell_step": ALG_BYTES_STEP,
                        "achieved_gbs": ALG_BYTES_STEP * cells_all * args.steps / (r["ms"] * 1e-3) / 1e9},
         "clocks": r["clocks"],
