@@ -344,10 +344,24 @@ def run_small_tgv(args):
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / 20
-    return {"workload": "Taylor-Green 2x2x2 blocks of 16^3 (32,768 cells), cent_keep<2> + visc_lr(constant), "
-                        "FP64, fused step replayed from a CUDA graph", "steps": 20, "ms_per_step": ms,
-            "tile_variant": best,
-            "cell_steps_per_s": 32768 / (ms * 1e-3)}
+    out = {"workload": "Taylor-Green 2x2x2 blocks of 16^3 (32,768 cells), cent_keep<2> + visc_lr(constant), "
+                       "FP64, fused step replayed from a CUDA graph", "steps": 20, "ms_per_step": ms,
+           "tile_variant": best, "cell_steps_per_s": 32768 / (ms * 1e-3)}
+    if not args.no_cpu_baseline:
+        # the same 20 steps on the host cores (the oracle restatement, bit-identical
+        # to the reference's CPU path for this scheme)
+        import numpy as np
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        from oracle import oracle as O
+        q = prob.q.data.cpu().numpy().copy()
+        work = np.zeros((3,) + q.shape)
+        t = time.perf_counter()
+        for _ in range(20):
+            O.ssprk3_step(prob.q.desc(), s, prob.bc_desc(), q, work, prob.dt)
+        el = time.perf_counter() - t
+        out["cpu_baseline"] = {"ms_per_step": el / 20 * 1e3, "cell_steps_per_s": 32768 * 20 / el,
+                               "cores": O.max_threads(), "kind": "port"}
+    return out
 
 
 def run_batch_form(args):
