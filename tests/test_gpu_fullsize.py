@@ -94,3 +94,26 @@ def test_periodic_tgv_2m_cells_residual_telescopes():
     total = inner.sum(dim=0)
     scale = inner.abs().sum(dim=0)
     assert torch.all(total.abs() <= 1e-11 * scale), (total, scale)
+
+
+@pytest.mark.parametrize("nblk,ncell", [((64, 1, 1), (8, 8, 8)), ((1, 1, 1), (96, 96, 96)), ((3, 5, 7), (12, 10, 6))])
+def test_extreme_block_shapes_variants_identical(nblk, ncell):
+    """Many small blocks (64 along x, the descriptor maximum), one large block
+    (96^3), and odd block counts with ragged tiles: every tile variant gives
+    the same finite residual (bit for bit)."""
+    ng = 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, -1.0, 1.0, 0.0, 1.0), _abi.COORDS_TANH_Y, (2.0, 0, 0, 0))
+    import problems as P
+    q = torch.from_numpy(P.random_state(nblk, ncell, ng, seed=61, rel=0.01, u0=5.0)).cuda()
+    s = P.scheme(conv=_abi.CONV_WENO5, diss=1, visc=1, law=_abi.LAW_SUTHERLAND, mu=0.05, eps_p=3.0, eps_T=3.0, alpha=1.0)
+    ref = None
+    for v in range(_lib().gbns_flux_variant_count(s)):
+        r = torch.zeros_like(q)
+        _native.check(_lib().gbns_flux_div_variant(grid, s, ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(r.data_ptr()),
+                                                   0, v, _st()))
+        torch.cuda.synchronize()
+        if ref is None:
+            ref = r
+            assert torch.isfinite(r).all()
+        else:
+            assert torch.equal(r, ref), v
