@@ -533,3 +533,40 @@ def test_ssprk3_stepper_graph_replay_equals_direct_steps(precision):
                                              ctypes.c_void_p(work.data_ptr()), ctypes.c_double(prob.dt), stream()))
     torch.cuda.synchronize()
     assert torch.equal(prob.q.data, graphed)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", [_abi.RED_MAX_WAVESPEED, _abi.RED_KINETIC, _abi.RED_CONSERVED, _abi.RED_HEALTH])
+def test_reduce_async_with_caller_scratch_equals_reduce(kind):
+    """gbns_reduce_async (caller-owned device scratch, result left on the
+    device) gives exactly gbns_reduce's values (same partition, same order)."""
+    nblk, ncell, ng = (3, 2, 2), (7, 6, 5), 2
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, -1.0, 1.0, 0.0, 2.0))
+    q = np.abs(P.random_state(nblk, ncell, ng, seed=82))
+    qd = dev(q)
+    want = np.zeros(5)
+    _native.check(lib().gbns_reduce(grid, P.gas_desc(), qd.data_ptr(), kind, want.ctypes.data_as(ctypes.c_void_p), stream()))
+    nd, off = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    _native.check(lib().gbns_reduce_scratch_size(grid, ctypes.byref(nd), ctypes.byref(off)))
+    scratch = torch.zeros(nd.value, dtype=torch.float64, device="cuda")
+    _native.check(lib().gbns_reduce_async(grid, P.gas_desc(), qd.data_ptr(), kind, scratch.data_ptr(), nd.value, stream()))
+    got = scratch[off.value:off.value + 5].cpu().numpy()
+    n = 5 if kind == _abi.RED_CONSERVED else 1
+    assert np.array_equal(got[:n], want[:n])
+    with pytest.raises(_native.SpadeError):
+        _native.check(lib().gbns_reduce_async(grid, P.gas_desc(), qd.data_ptr(), kind, scratch.data_ptr(), 1, stream()))
+
+
+@pytest.mark.gpu
+def test_copy_fill_ghosts_equals_copy_then_fill():
+    """gbns_copy_fill_ghosts(dst, src) == (dst = src interior; fill dst's ghosts)
+    bit for bit, walls included; src is left untouched."""
+    g = load("ghosts_ref.npz")
+    gg = GHOST_GRID
+    grid = _abi.grid_desc(gg["nblk"], gg["ncell"], gg["ng"], gg["bounds"])
+    src = dev(g["q"])
+    dst = torch.full_like(src, float("nan"))
+    _native.check(lib().gbns_copy_fill_ghosts(grid, P.channel_bc(290.0), ctypes.c_void_p(dst.data_ptr()),
+                                              ctypes.c_void_p(src.data_ptr()), stream()))
+    assert np.array_equal(host(dst), g["walls"])
+    assert np.array_equal(host(src), g["q"])
