@@ -292,6 +292,17 @@ int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                      const gbns_bc_desc* bc, double* prims, double* work,
                      double dt, void* stream);
 
+/* nsteps gbns_ssprk3_step calls replayed from a CUDA graph of one step (six
+ * launches).  The graph is captured on the first call for these arguments
+ * (descriptors, prims, work, dt, device) and reused while they stay the same
+ * (up to 8 are kept).  Results are bit-identical to the plain calls; for small
+ * grids the launch overhead disappears.  The first call for new arguments
+ * captures, which must not happen while `stream` is itself being captured.
+ * No counterpart in the reference (its integrator launches every kernel). */
+int gbns_ssprk3_run(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                    const gbns_bc_desc* bc, double* prims, double* work,
+                    double dt, int nsteps, void* stream);
+
 /* ---- source terms ----------------------------------------------------
  * Lowered forms of the point source a caller passes to
  * spade::pde_algs::source_term (pde-algs/source_term.h:19-51), written as

@@ -43,6 +43,8 @@ def lib():
     L.gbns_flux_div_rk.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, ctypes.c_int, vp, vp, vp, vp]
     L.gbns_copy_fill_ghosts.argtypes = [P(_abi.GridDesc), P(_abi.BcDesc), vp, vp, vp]
     L.gbns_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double, vp]
+    L.gbns_ssprk3_run.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double,
+                                  ctypes.c_int, vp]
     L.gbns_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), vp, vp, vp]
     L.gbns_selftest_wait_timeout.argtypes = [P(ctypes.c_int), vp]
     L.gbns_device_status.argtypes = [P(ctypes.c_int), ctypes.c_int, vp]

@@ -287,6 +287,29 @@ namespace gbns
 
 using namespace gbns;
 
+namespace gbns
+{
+    // Graphs of one fused SSPRK3 step (gbns_ssprk3_run), keyed on the
+    // descriptors, pointers, dt and device they bake in; at most 8 kept.
+    struct StepKey
+    {
+        gbns_grid_desc grid;
+        gbns_scheme_desc scheme;
+        gbns_bc_desc bc;
+        double* prims;
+        double* work;
+        double dt;
+        int device;
+    };
+    struct StepGraph
+    {
+        StepKey key;
+        cudaGraphExec_t exec;
+    };
+    static std::mutex& step_graphs_mu() { static std::mutex m; return m; }
+    static std::vector<StepGraph>& step_graphs() { static std::vector<StepGraph> v; return v; }
+}
+
 extern "C"
 {
     int gbns_version(void) { return GBNS_ABI_VERSION; }
@@ -461,6 +484,63 @@ extern "C"
         if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
         if ((rc = gbns_flux_div_rk(grid, scheme, prims, nullptr, 0, 3, e2, c3, B, stream))) return rc;
         return gbns_copy_fill_ghosts(grid, bc, prims, B, stream);
+    }
+
+    int gbns_ssprk3_run(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const gbns_bc_desc* bc,
+                        double* prims, double* work, double dt, int nsteps, void* stream)
+    {
+        using namespace gbns;
+        if (nsteps < 0) return set_error(GBNS_ERR_INVALID, "nsteps must be >= 0");
+        if (!grid || !scheme || !bc || !prims || !work) return set_error(GBNS_ERR_INVALID, "NULL argument");
+        if (nsteps == 0) return GBNS_OK;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        // the graph of one step is keyed on everything it bakes in
+        StepKey key;
+        std::memset(&key, 0, sizeof(key));
+        key.grid = *grid; key.scheme = *scheme; key.bc = *bc;
+        key.prims = prims; key.work = work; key.dt = dt;
+        int rc = check_cuda(cudaGetDevice(&key.device), "cudaGetDevice");
+        if (rc) return rc;
+        cudaGraphExec_t exec = nullptr;
+        {
+            std::lock_guard<std::mutex> lk(step_graphs_mu());
+            for (auto& e : step_graphs())
+                if (std::memcmp(&e.key, &key, sizeof(key)) == 0) { exec = e.exec; break; }
+        }
+        if (!exec)
+        {
+            // capture one step on a private stream that waits for the caller's
+            // work, so the captured launches see the caller's ordering
+            cudaStream_t cs = nullptr;
+            cudaEvent_t ev = nullptr;
+            rc = check_cuda(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "capture stream");
+            if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "capture event");
+            if (!rc) rc = check_cuda(cudaEventRecord(ev, st), "capture event record");
+            if (!rc) rc = check_cuda(cudaStreamWaitEvent(cs, ev, 0), "capture stream wait");
+            cudaGraph_t graph = nullptr;
+            if (!rc) rc = check_cuda(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture");
+            if (!rc)
+            {
+                const int lrc = gbns_ssprk3_step(grid, scheme, bc, prims, work, dt, cs);
+                const int erc = check_cuda(cudaStreamEndCapture(cs, &graph), "end capture");
+                rc = lrc ? lrc : erc;
+            }
+            if (!rc) rc = check_cuda(cudaGraphInstantiate(&exec, graph, 0), "graph instantiate");
+            if (graph) cudaGraphDestroy(graph);
+            if (ev) cudaEventDestroy(ev);
+            if (cs) cudaStreamDestroy(cs);
+            if (rc) return rc;
+            std::lock_guard<std::mutex> lk(step_graphs_mu());
+            auto& cache = step_graphs();
+            if (cache.size() >= 8) { cudaGraphExecDestroy(cache.front().exec); cache.erase(cache.begin()); }
+            cache.push_back(StepGraph{key, exec});
+        }
+        for (int i = 0; i < nsteps; ++i)
+        {
+            rc = check_cuda(cudaGraphLaunch(exec, st), "graph launch");
+            if (rc) return rc;
+        }
+        return GBNS_OK;
     }
 
     int gbns_device_status(int* status, int reset, void* stream)

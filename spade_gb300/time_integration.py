@@ -128,8 +128,8 @@ class ssprk3_stepper:
     """Fused native SSPRK3 step of `q` (gbns_ssprk3_step): three flux_div
     launches with the stage update fused into their epilogue and three ghost
     fills per step, with the reference's arithmetic.  With use_graph=True the
-    first call captures the six launches of one step in a CUDA graph on a
-    side stream and later calls replay it (dt is fixed at capture)."""
+    steps are replayed from a CUDA graph of one step that the library captures
+    on first use (gbns_ssprk3_run; dt is fixed per graph)."""
 
     def __init__(self, q, scheme_desc, bc_desc, dt, use_graph=False):
         self.q = q
@@ -141,27 +141,14 @@ class ssprk3_stepper:
             n *= s
         self.work = torch.zeros(3 * n, dtype=torch.float64, device=q.data.device)
         self.use_graph = use_graph
-        self.graph = None
 
-    def _launch(self, stream):
-        _native.check(_native.lib().gbns_ssprk3_step(self.q.desc(), self.scheme, self.bc, self.q.ptr(),
-                                                     self.work.data_ptr(), ctypes.c_double(self.dt), stream))
-
-    def step(self, nsteps=1):
-        if not self.use_graph:
-            st = _stream(None)
-            for _ in range(nsteps):
-                self._launch(st)
+    def step(self, nsteps=1, stream=None):
+        st = _stream(stream)
+        L = _native.lib()
+        if self.use_graph:
+            _native.check(L.gbns_ssprk3_run(self.q.desc(), self.scheme, self.bc, self.q.ptr(), self.work.data_ptr(),
+                                            ctypes.c_double(self.dt), int(nsteps), st))
             return
-        if self.graph is None:
-            side = torch.cuda.Stream()
-            side.wait_stream(torch.cuda.current_stream())
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.stream(side):
-                with torch.cuda.graph(g, stream=side):
-                    self._launch(int(side.cuda_stream))
-            torch.cuda.current_stream().wait_stream(side)
-            self.graph = g
-            # capture does not execute; run the first step by replay
         for _ in range(nsteps):
-            self.graph.replay()
+            _native.check(L.gbns_ssprk3_step(self.q.desc(), self.scheme, self.bc, self.q.ptr(), self.work.data_ptr(),
+                                             ctypes.c_double(self.dt), st))

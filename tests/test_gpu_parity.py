@@ -570,3 +570,31 @@ def test_copy_fill_ghosts_equals_copy_then_fill():
                                               ctypes.c_void_p(src.data_ptr()), stream()))
     assert np.array_equal(host(dst), g["walls"])
     assert np.array_equal(host(src), g["q"])
+
+
+@pytest.mark.gpu
+def test_ssprk3_run_graph_equals_steps():
+    """gbns_ssprk3_run (one step captured as a CUDA graph inside the library,
+    replayed nsteps times; a second call reuses the graph) equals the same
+    number of gbns_ssprk3_step calls bit for bit, and matches the oracle."""
+    nblk, ncell, ng = (2, 1, 1), (8, 8, 8), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    q = P.tgv_state(nblk, ncell, ng, P.tgv_tables(nblk, ncell, ng), seed=6)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    dt = P.tgv_dt(q, grid, ng)
+    s, bc = P.tgv_scheme(), P.periodic_bc()
+    a, b = dev(q), dev(q)
+    wa = torch.zeros(3 * a.numel(), dtype=torch.float64, device="cuda")
+    wb = torch.zeros_like(wa)
+    for _ in range(6):
+        _native.check(lib().gbns_ssprk3_step(grid, s, bc, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(wa.data_ptr()),
+                                             ctypes.c_double(dt), stream()))
+    for n in (2, 4):
+        _native.check(lib().gbns_ssprk3_run(grid, s, bc, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(wb.data_ptr()),
+                                            ctypes.c_double(dt), n, stream()))
+    assert torch.equal(a, b)
+    ref = q.copy()
+    work = np.zeros((3,) + q.shape)
+    for _ in range(6):
+        O.ssprk3_step(grid, s, bc, ref, work, dt)
+    assert np.array_equal(interior(host(b), ng), interior(ref, ng))
