@@ -497,7 +497,9 @@ extern "C"
         // the graph of one step is keyed on everything it bakes in
         StepKey key;
         std::memset(&key, 0, sizeof(key));
-        key.grid = *grid; key.scheme = *scheme; key.bc = *bc;
+        std::memcpy(&key.grid, grid, sizeof(*grid));
+        std::memcpy(&key.scheme, scheme, sizeof(*scheme));
+        std::memcpy(&key.bc, bc, sizeof(*bc));
         key.prims = prims; key.work = work; key.dt = dt;
         int rc = check_cuda(cudaGetDevice(&key.device), "cudaGetDevice");
         if (rc) return rc;
@@ -532,7 +534,13 @@ extern "C"
             if (rc) return rc;
             std::lock_guard<std::mutex> lk(step_graphs_mu());
             auto& cache = step_graphs();
-            if (cache.size() >= 8) { cudaGraphExecDestroy(cache.front().exec); cache.erase(cache.begin()); }
+            if (cache.size() >= 8)
+            {
+                // the evicted graph may still be in flight on any stream
+                cudaDeviceSynchronize();
+                cudaGraphExecDestroy(cache.front().exec);
+                cache.erase(cache.begin());
+            }
             cache.push_back(StepGraph{key, exec});
         }
         for (int i = 0; i < nsteps; ++i)
