@@ -21,6 +21,7 @@
 
 #include <type_traits>
 #include "gbns_internal.cuh"
+#include "fp64_int.cuh"
 
 namespace gbns
 {
@@ -106,8 +107,12 @@ namespace gbns
         // FP32 staged: the staging buffer is dead once converted, so derived
         // values and face fluxes reuse it when they fit.
         static constexpr bool REUSE = !FP64 && !DIRECT && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
-        static constexpr size_t SMEM_BYTES = 128 /*mbarrier*/ + STAGE_BYTES + SOA_BYTES +
-                                             (REUSE ? 0 : DER_BYTES + FLX_BYTES);
+        // FP32-flux on stretched grids: the tile's rows of the y-metric
+        // tables (m, 1/m at cell centres, 1/m at y-faces) as floats, converted
+        // once per tile instead of once per face
+        static constexpr size_t YM_BYTES = (!FP64 && STRETCH) ? align128(size_t(3)*(TY + 1)*sizeof(float)) : 0;
+        static constexpr size_t YM_OFF = 128 + STAGE_BYTES + SOA_BYTES + (REUSE ? 0 : DER_BYTES + FLX_BYTES);
+        static constexpr size_t SMEM_BYTES = YM_OFF + YM_BYTES;
         static_assert(SMEM_BYTES <= 227*1024, "tile does not fit in shared memory");
         // CTAs per SM that shared memory allows (the register budget follows)
         static constexpr int MINB_RAW = int((227*1024) / (SMEM_BYTES + 1024));
@@ -124,6 +129,7 @@ namespace gbns
         const float*  soa;     // SoA floats (FP32 compute)
         const Real*   der;     // derived per-cell values, SoA
         const double* split;   // SPLIT: f+/f- per equation of the current direction's line cells
+        const float*  ymet;    // FP32 stretched: m_cell, im_cell, im_face rows of the tile (TY + 1 each)
         __device__ __forceinline__ Real q(int v, int c) const
         {
             if constexpr (Cfg::FP64) return stage[c*5 + v];
@@ -142,6 +148,18 @@ namespace gbns
         Real hyb_param;
         __device__ __forceinline__ void load(const SchemeK& s)
         {
+            diss = s.diss; visc = s.visc; law = s.law; smooth = s.smooth; sensor = s.sensor;
+            hyb_flux = s.hyb_flux; hyb_sensor = s.hyb_sensor;
+            if constexpr (sizeof(Real) == 4)
+            {
+                const auto& f = s.f32;
+                gamma = f.gamma; R = f.R; gm1 = f.gm1; spec_heat = f.spec_heat; inv_gamma_avg = f.inv_gamma_avg;
+                R_avg = f.R_avg; eps_p = f.eps_p; eps_T = f.eps_T; sens = f.sens; mu = f.mu; beta_c = f.beta_c;
+                alpha_c = f.alpha_c; T_ref = f.T_ref; power = f.power; inv_pr = f.inv_pr; prandtl = f.prandtl;
+                tref_plus_s = f.tref_plus_s; S = f.S; hyb_param = f.hyb_param;
+                for (int i = 0; i < 4; ++i) ck_a[i] = f.ck_a[i];
+                return;
+            }
             gamma = Real(s.gamma); R = Real(s.R); gm1 = Real(s.gm1); spec_heat = Real(s.spec_heat);
             inv_gamma_avg = Real(s.inv_gamma_avg); R_avg = Real(s.R_avg);
             eps_p = Real(s.eps_p); eps_T = Real(s.eps_T); sens = Real(s.sens);
@@ -149,8 +167,7 @@ namespace gbns
             T_ref = Real(s.T_ref); power = Real(s.power); inv_pr = Real(s.inv_pr); prandtl = Real(s.prandtl);
             tref_plus_s = Real(s.tref_plus_s); S = Real(s.S);
             for (int i = 0; i < 4; ++i) ck_a[i] = Real(s.ck_a[i]);
-            diss = s.diss; visc = s.visc; law = s.law; smooth = s.smooth; sensor = s.sensor;
-            hyb_flux = s.hyb_flux; hyb_sensor = s.hyb_sensor; hyb_param = Real(s.hyb_param);
+            hyb_param = Real(s.hyb_param);
         }
     };
 
@@ -548,6 +565,9 @@ namespace gbns
 
     __device__ __forceinline__ Weno5Side weno5_nd(double a, double b, double c, double d, double e)
     {
+        // the six independent smoothness products go to the integer pipes
+        // (dmul_int, bit-identical to a*b); the rest stay on the FP64 unit,
+        // whose latency is shorter at this kernel's 8-16 warps per SM
         const double q0 = fma(2.0, a, fma(-7.0, b, 11.0*c));
         const double q1 = fma(5.0, c, fma(2.0, d, -b));
         const double q2 = fma(2.0, c, fma(5.0, d, -e));
@@ -555,9 +575,9 @@ namespace gbns
         const double t1 = fma(-2.0, c, b) + d, s1 = b - d;
         const double t2 = fma(-2.0, d, c) + e, s2 = fma(3.0, c, fma(-4.0, d, e));
         const double k = 13.0/3.0, eps4 = 4e-16;
-        const double e0 = fma(k*t0, t0, s0*s0) + eps4;
-        const double e1 = fma(k*t1, t1, s1*s1) + eps4;
-        const double e2 = fma(k*t2, t2, s2*s2) + eps4;
+        const double e0 = fma(dmul_int(k, t0), t0, dmul_int(s0, s0)) + eps4;
+        const double e1 = fma(dmul_int(k, t1), t1, dmul_int(s1, s1)) + eps4;
+        const double e2 = fma(dmul_int(k, t2), t2, dmul_int(s2, s2)) + eps4;
         const double E0 = e0*e0, E1 = e1*e1, E2 = e2*e2;
         const double a0 = 0.1*(E1*E2), a1 = 0.6*(E0*E2), a2 = 0.3*(E0*E1);
         Weno5Side r;
@@ -856,7 +876,16 @@ namespace gbns
             Real nD = Real(1.0), im = Real(1.0);
             if constexpr (Cfg::STRETCH)
             {
-                if constexpr (D == 1) im = Real(Y.im_face[b[1]*(ny + 1) + gj]);
+                if constexpr (!Cfg::FP64)
+                {
+                    if constexpr (D == 1) im = V.ymet[2*(TY + 1) + fy];
+                    else
+                    {
+                        nD = V.ymet[fy];
+                        im = V.ymet[(TY + 1) + fy];
+                    }
+                }
+                else if constexpr (D == 1) im = Real(Y.im_face[b[1]*(ny + 1) + gj]);
                 else
                 {
                     nD = Real(Y.m_cell[b[1]*ny + gj]);
@@ -1063,6 +1092,18 @@ namespace gbns
                 }
             }
         }
+        float* ymet = reinterpret_cast<float*>(smem_raw + Cfg::YM_OFF);
+        if constexpr (!Cfg::FP64 && Cfg::STRETCH)
+        {
+            const int ny = G.n[1];
+            for (int j = tid; j < TY + 1; j += Cfg::NT)
+            {
+                const int gj = j0 + j;
+                ymet[j] = gj < ny ? float(Y.m_cell[b[1]*ny + gj]) : 0.0f;
+                ymet[(TY + 1) + j] = gj < ny ? float(Y.im_cell[b[1]*ny + gj]) : 0.0f;
+                ymet[2*(TY + 1) + j] = gj <= ny ? float(Y.im_face[b[1]*(ny + 1) + gj]) : 0.0f;
+            }
+        }
         __syncthreads();
 
         // ---- FP32 staged: convert the box to SoA floats -------------------
@@ -1080,6 +1121,7 @@ namespace gbns
         V.stage = stage;
         V.soa = soa;
         V.split = reinterpret_cast<const double*>(der);
+        V.ymet = ymet;
         if constexpr (Cfg::SPLIT)
             der = reinterpret_cast<Real*>(reinterpret_cast<unsigned char*>(der) + Cfg::SPLIT_BYTES);
         V.der = der;
@@ -1106,7 +1148,12 @@ namespace gbns
         double invd[3];
         Real inv[3];
         #pragma unroll
-        for (int d = 0; d < 3; ++d) { invd[d] = G.inv_dx[d][b[d]]; inv[d] = Real(invd[d]); }
+        for (int d = 0; d < 3; ++d)
+        {
+            invd[d] = G.inv_dx[d][b[d]];
+            if constexpr (sizeof(Real) == 4) inv[d] = G.inv_dx_f[d][b[d]];
+            else inv[d] = invd[d];
+        }
 
         // SPLIT: rho, h, e of the cells this thread owns, shared by the three
         // directions' split fills

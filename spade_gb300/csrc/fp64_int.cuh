@@ -1,0 +1,49 @@
+// IEEE 754 binary64 multiplication computed on the integer pipes.
+//
+// GB300 executes FP64 at 1/64 of its FP32 rate (two FP64 lanes per SM and
+// clock) while its integer multiply-add and logic pipes are mostly idle in the
+// flux kernel. dmul_int returns exactly the bits of the hardware multiply
+// (round to nearest, ties to even) and leaves the FP64 pipe free, so the FP64
+// kernels send part of their products here and the rest to the FP64 unit.
+//
+// Method: the textbook software binary multiplication (Muller et al.,
+// "Handbook of Floating-Point Arithmetic", 2nd ed., 2018) — multiply the two
+// 53-bit significands exactly (a 106-bit product from 64x64-bit integer
+// multiplies), normalise by at most one bit, round to nearest even with a
+// round bit and a sticky bit, and add the biased exponent so that a carry out
+// of the significand rounding increments the exponent (overflow to infinity
+// comes out of the same addition). Zero, subnormal, infinite and NaN operands,
+// and products whose exponent leaves the normal range, go to the hardware
+// multiply, so the function is exact for every input.
+#pragma once
+#include <cstdint>
+
+namespace gbns
+{
+    __device__ __forceinline__ double dmul_int(double a, double b)
+    {
+        constexpr uint64_t M52 = 0x000FFFFFFFFFFFFFull, H53 = 0x0010000000000000ull, SGN = 0x8000000000000000ull;
+        const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
+        const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+        // biased exponent of the product when the significand product is in [1, 2)
+        int e = (int)ea + (int)eb - 1023;
+        if (ea - 1u >= 2046u || eb - 1u >= 2046u || (unsigned)(e - 1) >= 2045u) return __dmul_rn(a, b);
+        // significands with the hidden bit at bit 63: the product is in [2^126, 2^128)
+        const uint64_t ma = ((ua & M52) | H53) << 11, mb = ((ub & M52) | H53) << 11;
+        uint64_t hi = __umul64hi(ma, mb);
+        uint64_t lo = ma*mb;
+        const uint32_t top = (uint32_t)(hi >> 63);
+        e += (int)top;
+        if (!top)
+        {
+            hi = (hi << 1) | (lo >> 63);
+            lo <<= 1;
+        }
+        // 53 result bits, then the 11 bits below them, then the sticky word
+        const uint64_t m = hi >> 11;
+        const uint32_t rem = (uint32_t)hi & 0x7ffu;
+        const uint32_t up = (uint32_t)(rem > 0x400u) | ((uint32_t)(rem == 0x400u) & ((uint32_t)(lo != 0) | (uint32_t)(m & 1)));
+        const uint64_t r = ((ua ^ ub) & SGN) | ((((uint64_t)(e - 1)) << 52) + m + up);
+        return __longlong_as_double((long long)r);
+    }
+}

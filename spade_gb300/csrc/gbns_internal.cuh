@@ -43,6 +43,7 @@ namespace gbns
         int nblk;           // total blocks
         long long bstride;  // doubles per block (5*ni*nj*nk)
         double inv_dx[3][MAX_BLK_PER_DIM];   // 1/dx per direction per block index (grid_geometry.h:91-99)
+        float inv_dx_f[3][MAX_BLK_PER_DIM];  // the same rounded to float (FP32-flux faces)
     };
 
     // Stretched-y metric tables, per block row by:
@@ -72,6 +73,15 @@ namespace gbns
         double mu, beta_c, alpha_c;    // constant law: mu, -2.0*mu/3.0, mu*(1.0/Pr)
         double T_ref, power, inv_pr, prandtl, tref_plus_s, S;
         double ck_a[4];                // cent_keep centred coefficients a(1..order/2)
+        // the FP32-flux kernels' copies, rounded once on the host (the same
+        // bits a device conversion gives) so no thread converts them
+        struct
+        {
+            float gamma, R, gm1, spec_heat, inv_gamma_avg, R_avg, eps_p, eps_T, sens;
+            float mu, beta_c, alpha_c, T_ref, power, inv_pr, prandtl, tref_plus_s, S;
+            float ck_a[4];
+            float hyb_param;
+        } f32;
     };
 
     // Host helpers ------------------------------------------------------

@@ -128,6 +128,7 @@ namespace gbns
                 double mn, dx;
                 block_dx(g, d, b, &mn, &dx);
                 G.inv_dx[d][b] = 1.0/dx;
+                G.inv_dx_f[d][b] = float(G.inv_dx[d][b]);
             }
         return GBNS_OK;
     }
@@ -232,6 +233,14 @@ namespace gbns
         S.S = s->S;
         if (s->convective == GBNS_CONV_CENT_KEEP || s->convective == GBNS_CONV_HYBRID)
             for (int ii = 1; ii <= s->order/2; ++ii) S.ck_a[ii - 1] = cfd_coeff(ii, s->order);
+        S.f32.gamma = float(S.gamma); S.f32.R = float(S.R); S.f32.gm1 = float(S.gm1);
+        S.f32.spec_heat = float(S.spec_heat); S.f32.inv_gamma_avg = float(S.inv_gamma_avg);
+        S.f32.R_avg = float(S.R_avg); S.f32.eps_p = float(S.eps_p); S.f32.eps_T = float(S.eps_T);
+        S.f32.sens = float(S.sens); S.f32.mu = float(S.mu); S.f32.beta_c = float(S.beta_c);
+        S.f32.alpha_c = float(S.alpha_c); S.f32.T_ref = float(S.T_ref); S.f32.power = float(S.power);
+        S.f32.inv_pr = float(S.inv_pr); S.f32.prandtl = float(S.prandtl); S.f32.tref_plus_s = float(S.tref_plus_s);
+        S.f32.S = float(S.S); S.f32.hyb_param = float(S.hyb_param);
+        for (int ii = 0; ii < 4; ++ii) S.f32.ck_a[ii] = float(S.ck_a[ii]);
         return GBNS_OK;
     }
 
