@@ -240,6 +240,13 @@ int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);
  * context stays usable.  No counterpart in the reference. */
 int gbns_selftest_wait_timeout(int* status, void* stream);
 
+/* Checks the integer-pipe FP64 multiply the flux kernels use for part of
+ * their products against the hardware multiply on `npairs` generated operand
+ * pairs (all bit patterns, range edges, exact products and ties, zeros,
+ * subnormals, infinities, NaNs); *mismatches = pairs whose bits differ (NaN
+ * results compare equal).  Synchronises `stream`.  No reference counterpart. */
+int gbns_selftest_dmul_int(uint64_t npairs, uint64_t seed, uint64_t* mismatches, void* stream);
+
 /* Reduction that allocates nothing.  For callers that cannot let the
  * library call cudaMalloc: work recorded into a CUDA graph while a stream is
  * being captured (allocation is not allowed during capture) and applications

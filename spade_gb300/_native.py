@@ -47,6 +47,7 @@ def lib():
                                   ctypes.c_int, vp]
     L.gbns_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), vp, vp, vp]
     L.gbns_selftest_wait_timeout.argtypes = [P(ctypes.c_int), vp]
+    L.gbns_selftest_dmul_int.argtypes = [ctypes.c_uint64, ctypes.c_uint64, P(ctypes.c_uint64), vp]
     L.gbns_device_status.argtypes = [P(ctypes.c_int), ctypes.c_int, vp]
     L.gbns_batch_create.argtypes = [P(vp), ctypes.c_size_t, ctypes.c_int, ctypes.c_int, vp]
     L.gbns_batch_destroy.argtypes = [vp]

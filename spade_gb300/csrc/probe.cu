@@ -2,6 +2,7 @@
 // this GPU (independent dependent-FMA chains per thread, timed with CUDA
 // events).  Used to state the arithmetic roof next to the HBM roof.
 #include "gbns_internal.cuh"
+#include "fp64_int.cuh"
 
 namespace gbns
 {
@@ -87,6 +88,74 @@ extern "C" int gbns_selftest_wait_timeout(int* status, void* stream)
     rc = check_cuda(cudaGetLastError(), "wait self-test launch");
     if (rc) return rc;
     return read_device_status(status, 1, st);            // the flag the timeout set; cleared again
+}
+
+namespace gbns
+{
+    __device__ __forceinline__ uint64_t mix64(uint64_t x)
+    {
+        x += 0x9E3779B97F4A7C15ull;
+        x = (x ^ (x >> 30))*0xBF58476D1CE4E5B9ull;
+        x = (x ^ (x >> 27))*0x94D049BB133111EBull;
+        return x ^ (x >> 31);
+    }
+
+    // Operand bits for pair k: all bit patterns, exponent bands where the
+    // product leaves the normal range, significands with few set bits (exact
+    // products and ties), zeros, subnormals, infinities and NaNs.
+    __device__ __forceinline__ uint64_t dmul_operand(uint64_t k, int which)
+    {
+        constexpr uint64_t SG = 0x8000000000000000ull, MM = 0x000FFFFFFFFFFFFFull;
+        const uint64_t r = mix64(2*k + which), r2 = mix64(r);
+        switch ((int)(mix64(k ^ 0x5bd1e995ull) % 8))
+        {
+        case 0: return r;
+        case 1: return (r & (SG | MM)) | (uint64_t(991 + r2 % 64) << 52);
+        case 2: return (r & (SG | MM)) | (uint64_t(1 + r2 % 8) << 52);
+        case 3: return (r & (SG | MM)) | (uint64_t(2040 + r2 % 7) << 52);
+        case 4: return (r & (SG | 0x000FFF0000000000ull)) | (uint64_t(1020 + r2 % 8) << 52);
+        case 5: return (r & (SG | 0xFFull)) | (uint64_t(1000 + r2 % 60) << 52);
+        case 6: return (r & (SG | MM)) | (uint64_t(r2 % 3) << 52);
+        default: return (r & (SG | MM)) | (uint64_t(2046 + r2 % 2) << 52);
+        }
+    }
+
+    __global__ void __launch_bounds__(256) dmul_int_check_kernel(uint64_t n, uint64_t seed,
+                                                                 unsigned long long* bad)
+    {
+        for (uint64_t i = blockIdx.x*(uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x*blockDim.x)
+        {
+            const uint64_t k = i + seed;
+            const double a = __longlong_as_double((long long)dmul_operand(k, 0));
+            const double b = __longlong_as_double((long long)dmul_operand(k, 1));
+            const double h = __dmul_rn(a, b), e = dmul_int(a, b);
+            const bool same = __double_as_longlong(h) == __double_as_longlong(e) || (h != h && e != e);
+            if (!same) atomicAdd(bad, 1ull);
+        }
+    }
+}
+
+extern "C" int gbns_selftest_dmul_int(uint64_t npairs, uint64_t seed, uint64_t* mismatches, void* stream)
+{
+    using namespace gbns;
+    if (!mismatches) return set_error(GBNS_ERR_INVALID, "NULL output");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    unsigned long long* d = nullptr;
+    int rc = check_cuda(cudaMalloc(&d, sizeof(unsigned long long)), "self-test counter");
+    if (rc) return rc;
+    unsigned long long h = 0;
+    rc = check_cuda(cudaMemsetAsync(d, 0, sizeof(h), st), "self-test counter reset");
+    if (!rc && npairs)
+    {
+        dmul_int_check_kernel<<<sm_count()*8, 256, 0, st>>>(npairs, seed, d);
+        rc = check_cuda(cudaGetLastError(), "dmul_int self-test launch");
+    }
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st), "self-test read");
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "dmul_int self-test");
+    cudaFree(d);
+    if (rc) return rc;
+    *mismatches = h;
+    return GBNS_OK;
 }
 
 extern "C" int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream)

@@ -1,0 +1,60 @@
+// Host check of the integer FP64 multiply (spade_gb300/csrc/fp64_int.cuh):
+// the header is compiled for the CPU with its CUDA intrinsics replaced by
+// portable equivalents and compared bit for bit with the host's IEEE
+// multiply (round to nearest even) on generated operand pairs.
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#define __device__
+#define __forceinline__ inline
+static inline long long __double_as_longlong(double d) { long long x; std::memcpy(&x, &d, 8); return x; }
+static inline double __longlong_as_double(long long x) { double d; std::memcpy(&d, &x, 8); return d; }
+static inline uint64_t __umul64hi(uint64_t a, uint64_t b) { return (uint64_t)(((unsigned __int128)a*b) >> 64); }
+static inline double __dmul_rn(double a, double b) { volatile double r = a*b; return r; }
+#include "fp64_int.cuh"
+
+static uint64_t mix64(uint64_t x)
+{
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30))*0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27))*0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+
+static uint64_t operand(uint64_t k, int which)
+{
+    const uint64_t SG = 0x8000000000000000ull, MM = 0x000FFFFFFFFFFFFFull;
+    const uint64_t r = mix64(2*k + which), r2 = mix64(r);
+    switch ((int)(mix64(k ^ 0x5bd1e995ull) % 8))
+    {
+    case 0: return r;
+    case 1: return (r & (SG | MM)) | (uint64_t(991 + r2 % 64) << 52);
+    case 2: return (r & (SG | MM)) | (uint64_t(1 + r2 % 8) << 52);
+    case 3: return (r & (SG | MM)) | (uint64_t(2040 + r2 % 7) << 52);
+    case 4: return (r & (SG | 0x000FFF0000000000ull)) | (uint64_t(1020 + r2 % 8) << 52);
+    case 5: return (r & (SG | 0xFFull)) | (uint64_t(1000 + r2 % 60) << 52);
+    case 6: return (r & (SG | MM)) | (uint64_t(r2 % 3) << 52);
+    default: return (r & (SG | MM)) | (uint64_t(2046 + r2 % 2) << 52);
+    }
+}
+
+int main(int argc, char** argv)
+{
+    const uint64_t n = argc > 1 ? std::strtoull(argv[1], nullptr, 10) : 20000000ull;
+    uint64_t bad = 0;
+    for (uint64_t k = 0; k < n; ++k)
+    {
+        const double a = __longlong_as_double((long long)operand(k, 0));
+        const double b = __longlong_as_double((long long)operand(k, 1));
+        const double h = __dmul_rn(a, b), e = gbns::dmul_int(a, b);
+        if (__double_as_longlong(h) != __double_as_longlong(e) && !(h != h && e != e))
+        {
+            if (!bad) std::printf("first mismatch: a=%a b=%a hw=%a int=%a\n", a, b, h, e);
+            ++bad;
+        }
+    }
+    std::printf("pairs %llu mismatches %llu\n", (unsigned long long)n, (unsigned long long)bad);
+    return bad ? 1 : 0;
+}

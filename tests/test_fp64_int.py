@@ -1,0 +1,21 @@
+"""The integer-pipe FP64 multiply of the flux kernels (fp64_int.cuh),
+compiled for the host and compared bit for bit with the CPU's IEEE multiply
+on generated operand pairs (the GPU comparison with the hardware multiply is
+tests/test_gpu_parity.py::test_integer_pipe_multiply_matches_hardware)."""
+import os
+import subprocess
+import tempfile
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_dmul_int_matches_ieee_multiply():
+    with tempfile.TemporaryDirectory() as d:
+        exe = os.path.join(d, "dmul_int_host")
+        cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + os.path.join(ROOT, "spade_gb300", "csrc"),
+               os.path.join(ROOT, "tests", "cpp", "dmul_int_host.cc"), "-o", exe]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out = subprocess.run([exe, "20000000"], capture_output=True, text=True, timeout=300)
+        assert out.returncode == 0, out.stdout + out.stderr
+        assert "mismatches 0" in out.stdout
