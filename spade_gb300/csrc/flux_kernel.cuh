@@ -515,40 +515,53 @@ namespace gbns
         }
     }
 
-    // FP32 5th-order WENO-JS side reconstruction (Jiang & Shu 1996); cells
-    // a..e upwind to downwind.  No reference counterpart.
-    __device__ __forceinline__ float weno5_side(float a, float b, float c, float d, float e, int smooth)
+    // FP32 5th-order WENO-JS side reconstruction (Jiang & Shu 1996) for two
+    // independent stencils at once, lane x and lane y of float2, cells a..e
+    // upwind to downwind; no reference counterpart.  The arithmetic runs on
+    // Blackwell's paired FP32 instructions (FFMA2, FMUL2, FADD2: one
+    // instruction for both lanes); the maxima and the two divisions stay per
+    // lane.  The FP32-flux face flux evaluates its f+ and f- sides as one pair.
+    // (eps + beta)^2 overflows FP32 for beta > ~1.8e19, reached by the energy
+    // equation's fluxes (~1e8) in steep regions; the normalised weights
+    // g_k/D_k are unchanged when every beta and eps are divided by the largest
+    // beta.  With the scaled D_k <= 1 the product form (one division) cannot
+    // overflow; the floor keeps the sum positive when two stencils are
+    // perfectly smooth.
+    __device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+    __device__ __forceinline__ float2 max2(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
+
+    __device__ __forceinline__ float2 weno5_side2(float2 a, float2 b, float2 c, float2 d, float2 e, int smooth)
     {
         const float c13 = 1.0f/3.0f, c16 = 1.0f/6.0f, c56 = 5.0f/6.0f, c76 = 7.0f/6.0f, c116 = 11.0f/6.0f;
-        const float p0 = fmaf(c13, a, fmaf(-c76, b, c116*c));
-        const float p1 = fmaf(-c16, b, fmaf(c56, c, c13*d));
-        const float p2 = fmaf(c13, c, fmaf(c56, d, (-c16)*e));
-        if (!smooth) return fmaf(0.1f, p0, fmaf(0.6f, p1, 0.3f*p2));
-        const float t0 = fmaf(-2.0f, b, a) + c, s0 = fmaf(3.0f, c, fmaf(-4.0f, b, a));
-        const float t1 = fmaf(-2.0f, c, b) + d, s1 = b - d;
-        const float t2 = fmaf(-2.0f, d, c) + e, s2 = fmaf(3.0f, c, fmaf(-4.0f, d, e));
-        const float k13 = 13.0f/12.0f;
-        const float b0 = fmaf(k13*t0, t0, (0.25f*s0)*s0);
-        const float b1 = fmaf(k13*t1, t1, (0.25f*s1)*s1);
-        const float b2 = fmaf(k13*t2, t2, (0.25f*s2)*s2);
-        // (eps + beta)^2 overflows FP32 for beta > ~1.8e19, reached by the
-        // energy equation's fluxes (~1e8) in steep regions; the weights
-        // g_k/D_k normalised are unchanged when every beta and eps are
-        // divided by the largest beta.  With the scaled D_k <= 1 the product
-        // form (one division) cannot overflow; the floor keeps the sum
-        // positive when two stencils are perfectly smooth.
+        const float2 p0 = __ffma2_rn(bc2(c13), a, __ffma2_rn(bc2(-c76), b, __fmul2_rn(bc2(c116), c)));
+        const float2 p1 = __ffma2_rn(bc2(-c16), b, __ffma2_rn(bc2(c56), c, __fmul2_rn(bc2(c13), d)));
+        const float2 p2 = __ffma2_rn(bc2(c13), c, __ffma2_rn(bc2(c56), d, __fmul2_rn(bc2(-c16), e)));
+        if (!smooth) return __ffma2_rn(bc2(0.1f), p0, __ffma2_rn(bc2(0.6f), p1, __fmul2_rn(bc2(0.3f), p2)));
+        const float2 t0 = __fadd2_rn(__ffma2_rn(bc2(-2.0f), b, a), c);
+        const float2 s0 = __ffma2_rn(bc2(3.0f), c, __ffma2_rn(bc2(-4.0f), b, a));
+        const float2 t1 = __fadd2_rn(__ffma2_rn(bc2(-2.0f), c, b), d);
+        const float2 s1 = __ffma2_rn(bc2(-1.0f), d, b);
+        const float2 t2 = __fadd2_rn(__ffma2_rn(bc2(-2.0f), d, c), e);
+        const float2 s2 = __ffma2_rn(bc2(3.0f), c, __ffma2_rn(bc2(-4.0f), d, e));
+        const float2 k13 = bc2(13.0f/12.0f), q4 = bc2(0.25f);
+        const float2 b0 = __ffma2_rn(__fmul2_rn(k13, t0), t0, __fmul2_rn(__fmul2_rn(q4, s0), s0));
+        const float2 b1 = __ffma2_rn(__fmul2_rn(k13, t1), t1, __fmul2_rn(__fmul2_rn(q4, s1), s1));
+        const float2 b2 = __ffma2_rn(__fmul2_rn(k13, t2), t2, __fmul2_rn(__fmul2_rn(q4, s2), s2));
         const float eps = 1e-16f;
-        const float sc = fmaxf(fmaxf(b0, b1), fmaxf(b2, eps));
-        const float is = 1.0f/sc;
-        const float ee = eps*is;
-        const float fl = 1e-30f;
-        const float q0 = fmaxf((b0*is + ee)*(b0*is + ee), fl);
-        const float q1 = fmaxf((b1*is + ee)*(b1*is + ee), fl);
-        const float q2 = fmaxf((b2*is + ee)*(b2*is + ee), fl);
-        const float a0 = 0.1f*(q1*q2);
-        const float a1 = 0.6f*(q0*q2);
-        const float a2 = 0.3f*(q0*q1);
-        return (a0*p0 + a1*p1 + a2*p2)/(a0 + a1 + a2);
+        const float2 sc = max2(max2(b0, b1), max2(b2, bc2(eps)));
+        const float2 is = make_float2(1.0f/sc.x, 1.0f/sc.y);
+        const float2 ee = __fmul2_rn(bc2(eps), is);
+        const float2 fl = bc2(1e-30f);
+        const float2 u0 = __ffma2_rn(b0, is, ee), u1 = __ffma2_rn(b1, is, ee), u2 = __ffma2_rn(b2, is, ee);
+        const float2 q0 = max2(__fmul2_rn(u0, u0), fl);
+        const float2 q1 = max2(__fmul2_rn(u1, u1), fl);
+        const float2 q2 = max2(__fmul2_rn(u2, u2), fl);
+        const float2 a0 = __fmul2_rn(bc2(0.1f), __fmul2_rn(q1, q2));
+        const float2 a1 = __fmul2_rn(bc2(0.6f), __fmul2_rn(q0, q2));
+        const float2 a2 = __fmul2_rn(bc2(0.3f), __fmul2_rn(q0, q1));
+        const float2 num = __ffma2_rn(a2, p2, __ffma2_rn(a1, p1, __fmul2_rn(a0, p0)));
+        const float2 den = __fadd2_rn(__fadd2_rn(a0, a1), a2);
+        return make_float2(num.x/den.x, num.y/den.y);
     }
 
     // FP64 WENO5-JS face flux F = F(f+ side) + F(f- side), each side a..e
@@ -635,8 +648,12 @@ namespace gbns
             if constexpr (sizeof(Real) == 8)
                 out[eq] = weno5_pair(up[0], up[1], up[2], up[3], up[4], dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
             else
-                out[eq] = weno5_side(up[0], up[1], up[2], up[3], up[4], S.smooth)
-                        + weno5_side(dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
+            {
+                const float2 f = weno5_side2(make_float2(up[0], dn[5]), make_float2(up[1], dn[4]),
+                                             make_float2(up[2], dn[3]), make_float2(up[3], dn[2]),
+                                             make_float2(up[4], dn[1]), S.smooth);
+                out[eq] = f.x + f.y;
+            }
         }
     }
 
