@@ -609,3 +609,26 @@ def test_ssprk3_run_graph_equals_steps():
     for _ in range(6):
         O.ssprk3_step(grid, s, bc, ref, work, dt)
     assert np.array_equal(interior(host(b), ng), interior(ref, ng))
+
+
+@pytest.mark.gpu
+def test_ssprk3_run_graph_cache_eviction():
+    """More distinct step configurations than the graph cache holds (eight):
+    every call with a new time step captures a new graph and evicts the
+    oldest; results still equal gbns_ssprk3_step with the same time steps."""
+    nblk, ncell, ng = (1, 1, 1), (8, 8, 8), 2
+    grid = P.tgv_grid(nblk, ncell, ng)
+    q = P.tgv_state(nblk, ncell, ng, P.tgv_tables(nblk, ncell, ng), seed=9)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    dt0 = P.tgv_dt(q, grid, ng)
+    s, bc = P.tgv_scheme(), P.periodic_bc()
+    a, b = dev(q), dev(q)
+    wa = torch.zeros(3 * a.numel(), dtype=torch.float64, device="cuda")
+    wb = torch.zeros_like(wa)
+    dts = [dt0 * (0.5 + 0.05 * k) for k in range(10)] + [dt0 * 0.5, dt0 * 0.55]
+    for dt in dts:
+        _native.check(lib().gbns_ssprk3_step(grid, s, bc, ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(wa.data_ptr()),
+                                             ctypes.c_double(dt), stream()))
+        _native.check(lib().gbns_ssprk3_run(grid, s, bc, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(wb.data_ptr()),
+                                            ctypes.c_double(dt), 1, stream()))
+    assert torch.equal(a, b)
