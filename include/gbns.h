@@ -229,6 +229,18 @@ int gbns_reduce_async(const gbns_grid_desc* grid, const gbns_gas_desc* gas, cons
 #define GBNS_DEV_TMA_TIMEOUT  1   /* a tile's TMA halo copy did not complete within the poll limit */
 int gbns_device_status(int* status, int reset, void* stream);
 
+/* pde_algs::boundary_flux (pde-algs/boundary_flux.h:16-105): for every
+ * selected domain boundary (apply[2*d + side], side 0 = min, 1 = max, applied
+ * in that order) of every block on it, the flux F of each face of the boundary
+ * plane (transverse cell indices -1 .. n-1, as the reference's loop) is added
+ * to the two cells the face separates: rhs(il) -= F/dx, rhs(ir) += F/dx (the
+ * interior cell and the ghost cell beyond it), F the face flux of
+ * gbns_flux_div for `scheme`, computed in FP64 without FMA contraction for
+ * every precision.  Identity coordinates only; needs the scheme's halo in
+ * ghost layers (at least 2 with face gradients). */
+int gbns_boundary_flux(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
+                       double* rhs, const int* apply, void* stream);
+
 /* Measured FMA throughput of this GPU (FLOP/s) with dependent FMA chains:
  * fp64 != 0 -> double, else float.  Benchmark aid (no reference counterpart). */
 int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);

@@ -731,6 +731,66 @@ int oracle_flux_div(const gbns_grid_desc* g, const gbns_scheme_desc* S,
     return 0;
 }
 
+/* pde_algs::boundary_flux (pde-algs/boundary_flux.h:16-105), restated from
+ * its loop (the reference's version does not compile against its current grid
+ * headers, so this restatement is unpinned): for each block, for dir = 0..5
+ * (rdir = dir/2, mdir = dir%2), if the block lies on that domain boundary and
+ * apply[dir] is set, every face between cell il and ir = il + e_rdir with
+ * il[rdir] = -1 (mdir 0) or n-1 (mdir 1) and the transverse indices in
+ * [-1, n) (flux_bounds.min = -1 in every direction, boundary_flux.h:37-58)
+ * adds accum = 0 + F (the composite face flux) as
+ * rhs(il) -= jac_l*accum/dx, rhs(ir) += jac_r*accum/dx (:76-99), with dx the
+ * block's spacing along rdir and jac = 1 (identity coordinates). */
+int oracle_boundary_flux(const gbns_grid_desc* g, const gbns_scheme_desc* S, const double* prims, double* rhs,
+                         const int* apply)
+{
+    geom_t G;
+    if (geom_init(g, &G)) return -1;
+    if (G.coords != GBNS_COORDS_IDENTITY) return -3;
+    int halo = stencil_halo(S);
+    const int grad = S->viscous || (S->dissipation && S->sensor == GBNS_SENSOR_DUCROS) ||
+                     (S->convective == GBNS_CONV_HYBRID && S->hybrid_sensor == GBNS_SENSOR_DUCROS);
+    if (grad && halo < 2) halo = 2;
+    if (halo > G.ng) return -2;
+    for (int lb = 0; lb < G.nblk; ++lb)
+    {
+        int b[3];
+        block_pos(&G, lb, b);
+        ctx_t C;
+        C.G = &G; C.S = S; C.q = prims; C.lb = lb;
+        block_box(&G, lb, C.bmin, C.dx);
+        for (int d = 0; d < 3; ++d) C.inv_dx[d] = 1.0/C.dx[d];
+        for (int dir = 0; dir < 6; ++dir)
+        {
+            const int rdir = dir/2, mdir = dir%2;
+            const int on_boundary = mdir == 0 ? b[rdir] == 0 : b[rdir] == G.nb[rdir] - 1;
+            if (!(on_boundary && apply[dir])) continue;
+            int lo[3] = {-1, -1, -1}, hi[3] = {G.n[0], G.n[1], G.n[2]};
+            if (mdir == 0) hi[rdir] = 0;
+            else lo[rdir] = G.n[rdir] - 1;
+            const double dx = C.dx[rdir];
+            for (int k = lo[2]; k < hi[2]; ++k)
+            for (int j = lo[1]; j < hi[1]; ++j)
+            for (int i = lo[0]; i < hi[0]; ++i)
+            {
+                const int ir[3] = {i + (rdir == 0), j + (rdir == 1), k + (rdir == 2)};
+                const st5 F = face_flux(&C, rdir, ir[0], ir[1], ir[2]);
+                double* rl = rhs + cell_off(&G, lb, i, j, k);
+                double* rr = rhs + cell_off(&G, lb, ir[0], ir[1], ir[2]);
+                const double jac_l = 1.0, jac_r = 1.0;
+                for (int v = 0; v < 5; ++v)
+                {
+                    double accum = 0.0;
+                    accum += F.v[v];
+                    rl[v] -= jac_l*accum/dx;
+                    rr[v] += jac_r*accum/dx;
+                }
+            }
+        }
+    }
+    return 0;
+}
+
 /* pde_algs::source_term (pde-algs/source_term.h:19-51) for the lowered
  * point sources of gbns.h: rhs += S(q)/jac per interior cell, S in the
  * operation order of the reference-side lambdas (oracle/ref_harness.cc). */

@@ -46,6 +46,7 @@ def port():
         lib.oracle_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
         lib.oracle_max_threads.restype = ctypes.c_int
         lib.oracle_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), ctypes.c_void_p, ctypes.c_void_p]
+        lib.oracle_boundary_flux.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_int)]
         _port = lib
     return _port
 
@@ -101,6 +102,13 @@ def ssprk3_step(grid, scheme, bc, prims, work, dt, nthreads=0):
 
 def source_term(grid, src, prims, rhs):
     _check(port().oracle_source_term(ctypes.byref(grid), ctypes.byref(src), _ptr(prims), _ptr(rhs)), "oracle_source_term")
+
+
+def boundary_flux(grid, scheme, prims, rhs, apply):
+    """apply: six flags in the order xmin, xmax, ymin, ymax, zmin, zmax."""
+    flags = (ctypes.c_int * 6)(*[int(bool(a)) for a in apply])
+    _check(port().oracle_boundary_flux(ctypes.byref(grid), ctypes.byref(scheme), _ptr(prims), _ptr(rhs), flags),
+           "oracle_boundary_flux")
 
 
 def max_threads():

@@ -84,6 +84,19 @@ namespace gbns
         } f32;
     };
 
+    // Arguments of one boundary_flux launch (one boundary of direction D).
+    struct BndArgs
+    {
+        const double* prims;
+        double* rhs;
+        int side;                      // 0: the min boundary of direction D, 1: the max boundary
+        int ntile1, ntile2;            // 8-face patches per block along the two transverse directions
+        double dx[MAX_BLK_PER_DIM];    // block spacing along D (grid_geometry.h:85-89)
+    };
+    int boundary_flux_launch_d0(const GeomK& G, const SchemeK& S, const BndArgs& A, int conv, int order, cudaStream_t st);
+    int boundary_flux_launch_d1(const GeomK& G, const SchemeK& S, const BndArgs& A, int conv, int order, cudaStream_t st);
+    int boundary_flux_launch_d2(const GeomK& G, const SchemeK& S, const BndArgs& A, int conv, int order, cudaStream_t st);
+
     // Host helpers ------------------------------------------------------
     int make_geom(const gbns_grid_desc* g, GeomK& G);
     int make_ytab(const gbns_grid_desc* g, const GeomK& G, YTabK& Y);

@@ -495,6 +495,56 @@ extern "C"
         return gbns_copy_fill_ghosts(grid, bc, prims, B, stream);
     }
 
+    int gbns_boundary_flux(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
+                           double* rhs, const int* apply, void* stream)
+    {
+        using namespace gbns;
+        GeomK G;
+        SchemeK S;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        rc = make_scheme(scheme, S);
+        if (rc) return rc;
+        if (!prims || !rhs || !apply) return set_error(GBNS_ERR_INVALID, "NULL argument");
+        if (prims == rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
+        if (grid->coords != GBNS_COORDS_IDENTITY)
+            return set_error(GBNS_ERR_UNSUPPORTED, "boundary_flux supports identity coordinates (the reference "
+                                                   "evaluates the Jacobian at ghost cells)");
+        // faces in the transverse ghost row take face gradients one layer further out
+        int halo = scheme_halo(scheme);
+        const bool grad = scheme->viscous || (scheme->dissipation && scheme->sensor == GBNS_SENSOR_DUCROS) ||
+                          (scheme->convective == GBNS_CONV_HYBRID && scheme->hybrid_sensor == GBNS_SENSOR_DUCROS);
+        if (grad && halo < 2) halo = 2;
+        if (halo > G.ng)
+            return set_error(GBNS_ERR_INVALID, "boundary_flux needs " + std::to_string(halo) + " ghost layers, grid has " +
+                             std::to_string(G.ng));
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        // boundaries in the reference's order: dir = 2*direction + side
+        for (int dir = 0; dir < 6; ++dir)
+        {
+            if (!apply[dir]) continue;
+            const int D = dir/2;
+            const int ta = D == 0 ? 1 : 0, tb = D == 2 ? 1 : 2;
+            BndArgs A;
+            std::memset(&A, 0, sizeof(A));
+            A.prims = prims;
+            A.rhs = rhs;
+            A.side = dir % 2;
+            A.ntile1 = (G.n[ta] + 1 + 7)/8;
+            A.ntile2 = (G.n[tb] + 1 + 7)/8;
+            for (int b = 0; b < G.nb[D]; ++b)
+            {
+                double mn = 0.0;
+                block_dx(grid, D, b, &mn, &A.dx[b]);
+            }
+            if (D == 0) rc = boundary_flux_launch_d0(G, S, A, scheme->convective, scheme->order, st);
+            else if (D == 1) rc = boundary_flux_launch_d1(G, S, A, scheme->convective, scheme->order, st);
+            else rc = boundary_flux_launch_d2(G, S, A, scheme->convective, scheme->order, st);
+            if (rc) return rc;
+        }
+        return GBNS_OK;
+    }
+
     int gbns_ssprk3_run(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const gbns_bc_desc* bc,
                         double* prims, double* work, double dt, int nsteps, void* stream)
     {

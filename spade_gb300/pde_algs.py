@@ -1,6 +1,8 @@
 """pde_algs::flux_div and its traits (pde-algs/flux-div/flux_div.h:16-56,
-pde-algs/pde_traits.h:5-20, pde-algs/flux-div/tags.h:5-33), lowered onto
-libgbns.so."""
+pde-algs/pde_traits.h:5-20, pde-algs/flux-div/tags.h:5-33), source_term and
+boundary_flux, lowered onto libgbns.so."""
+import ctypes
+
 from . import _abi, _native, convective, viscous, omni
 from .grid import _stream
 
@@ -171,3 +173,51 @@ def source_term(q, rhs, source_func, stream=None):
         raise ValueError("q and rhs must live on the same grid")
     d = lower_source(source_func)
     _native.check(_native.lib().gbns_source_term(q.desc(), d, q.ptr(), rhs.ptr(), _stream(stream)))
+
+
+# -------------------------------------------------------------- boundary_flux
+
+class bound_box_t:
+    """bound_box_t<bool, 3>: one flag per domain boundary, min(i) / max(i)."""
+
+    def __init__(self, value=False):
+        self._min = [bool(value)] * 3
+        self._max = [bool(value)] * 3
+
+    def min(self, i, value=None):
+        if value is None:
+            return self._min[i]
+        self._min[i] = bool(value)
+
+    def max(self, i, value=None):
+        if value is None:
+            return self._max[i]
+        self._max[i] = bool(value)
+
+    def __invert__(self):
+        out = bound_box_t()
+        out._min = [not v for v in self._min]
+        out._max = [not v for v in self._max]
+        return out
+
+    def flags(self):
+        """The six flags in the order xmin, xmax, ymin, ymax, zmin, zmax."""
+        return [f for i in range(3) for f in (self._min[i], self._max[i])]
+
+
+def boundary_flux(prims, rhs, apply_to_boundary, flux_func, stream=None):
+    """pde_algs::boundary_flux(prims, rhs, apply_to_boundary, flux_func)
+    (pde-algs/boundary_flux.h:16-105): for each selected domain boundary the
+    faces of the boundary plane (transverse indices -1 .. n-1) add their flux
+    F to the two cells they separate, rhs(il) -= F/dx and rhs(ir) += F/dx.
+    apply_to_boundary is a bound_box_t or six flags (xmin, xmax, ymin, ymax,
+    zmin, zmax).  FP64 without FMA contraction; identity coordinates.
+    Asynchronous on the current torch stream."""
+    if prims.shape != rhs.shape:
+        raise ValueError("prims and rhs must live on the same grid")
+    flags = apply_to_boundary.flags() if isinstance(apply_to_boundary, bound_box_t) else list(apply_to_boundary)
+    if len(flags) != 6:
+        raise ValueError("apply_to_boundary needs six flags")
+    scheme = flux_func if isinstance(flux_func, _abi.SchemeDesc) else lower(flux_func, _abi.PREC_FP64)
+    arr = (ctypes.c_int * 6)(*[int(bool(f)) for f in flags])
+    _native.check(_native.lib().gbns_boundary_flux(prims.desc(), scheme, prims.ptr(), rhs.ptr(), arr, _stream(stream)))

@@ -632,3 +632,61 @@ def test_ssprk3_run_graph_cache_eviction():
         _native.check(lib().gbns_ssprk3_run(grid, s, bc, ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(wb.data_ptr()),
                                             ctypes.c_double(dt), 1, stream()))
     assert torch.equal(a, b)
+
+
+# ------------------------------------------------------------ boundary_flux
+
+@pytest.mark.parametrize("case", ["ck2_visc", "ck4", "totani_visc", "fweno_diss_visc", "weno5_diss_suth",
+                                  "hyb_ck2_ducros_visc", "diss_ducros"])
+@pytest.mark.parametrize("apply", [(1, 1, 1, 1, 1, 1), (0, 1, 1, 0, 0, 1)])
+def test_boundary_flux_matches_restatement_bitwise(case, apply):
+    """gbns_boundary_flux equals the oracle's restatement of
+    pde_algs::boundary_flux bit for bit over the whole array (ghost cells
+    included), accumulating into an existing rhs; block sizes that are not
+    multiples of the 8x8 face patches."""
+    kw = {
+        "ck2_visc": dict(conv=_abi.CONV_CENT_KEEP, order=2, visc=1),
+        "ck4": dict(conv=_abi.CONV_CENT_KEEP, order=4),
+        "totani_visc": dict(conv=_abi.CONV_TOTANI, visc=1),
+        "fweno_diss_visc": dict(conv=_abi.CONV_FWENO, diss=1, visc=1),
+        "weno5_diss_suth": dict(conv=_abi.CONV_WENO5, diss=1, visc=1, law=_abi.LAW_SUTHERLAND),
+        "hyb_ck2_ducros_visc": dict(conv=_abi.CONV_HYBRID, order=2, visc=1, hybrid_sensor=_abi.SENSOR_DUCROS,
+                                    hybrid_param=1e-3),
+        "diss_ducros": dict(conv=_abi.CONV_NONE, diss=1, sensor=_abi.SENSOR_DUCROS, alpha=1e-3),
+    }[case]
+    nblk, ncell, ng = (2, 2, 2), (9, 7, 10), 3
+    grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 2.0, 0.0, 1.0, 0.0, 1.5))
+    q = P.random_state(nblk, ncell, ng, seed=53)
+    r0 = P.random_state(nblk, ncell, ng, seed=54)
+    s = P.scheme(**kw)
+    ref = r0.copy()
+    O.boundary_flux(grid, s, q, ref, apply)
+    qd, rd = dev(q), dev(r0)
+    flags = (ctypes.c_int * 6)(*apply)
+    _native.check(lib().gbns_boundary_flux(grid, s, qd.data_ptr(), rd.data_ptr(), flags, stream()))
+    assert np.array_equal(host(rd), ref)
+
+
+def test_boundary_flux_python_api_and_errors():
+    """pde_algs.boundary_flux on grid_arrays with a bound_box_t equals the
+    restatement; stretched grids are rejected with GBNS_ERR_UNSUPPORTED and
+    leave rhs untouched."""
+    from spade_gb300 import grid as sg, pde_algs
+    blocks = sg.cartesian_blocks_t((1, 2, 1), (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    g = sg.cartesian_grid_t((8, 8, 8), blocks)
+    nblk, ncell, ng = (1, 2, 1), (8, 8, 8), 3
+    q = P.random_state(nblk, ncell, ng, seed=55)
+    qa = sg.grid_array(g, 0.0, ng, data=dev(q))
+    ra = sg.grid_array(g, 0.0, ng)
+    s = P.scheme(conv=_abi.CONV_WENO5, diss=1, visc=1)
+    bb = pde_algs.bound_box_t(False)
+    bb.max(1, True)
+    pde_algs.boundary_flux(qa, ra, bb, s)
+    ref = np.zeros_like(q)
+    O.boundary_flux(qa.desc(), s, q, ref, bb.flags())
+    assert np.array_equal(host(ra.data), ref)
+    stretched = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, -1.0, 1.0, 0.0, 1.0), _abi.COORDS_TANH_Y, (2.0, 0, 0, 0))
+    rd2 = dev(np.zeros_like(q))
+    rc = lib().gbns_boundary_flux(stretched, s, qa.ptr(), rd2.data_ptr(), (ctypes.c_int * 6)(*bb.flags()), stream())
+    assert rc == _abi.ERR_UNSUPPORTED
+    assert not host(rd2).any()
