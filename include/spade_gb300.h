@@ -31,12 +31,20 @@
  * source_term: spade::gb300::const_source_t / body_force_t / body_accel_t
  * passed to spade::pde_algs::source_term run on the GPU (gbns_source_term).
  *
+ * boundary_flux: the reference's call with the gb300 traits appended,
+ *     spade::pde_algs::boundary_flux(prims, rhs, apply_to_boundary, flux_func,
+ *                                    spade::algs::make_traits(spade::pde_algs::gb300));
+ * runs gbns_boundary_flux (the overload below is more specialised than the
+ * reference's variadic template, pde-algs/boundary_flux.h:10-20).
+ *
  * Define GBNS_DROPIN_HOOK before including to route the lowered call to a
  * user function `int GBNS_DROPIN_HOOK(const gbns_grid_desc*, const
  * gbns_scheme_desc*, const double*, double*, int)` instead of the library
  * (used by the host-only tests of the lowering); GBNS_DROPIN_SOURCE_HOOK,
  * `int (const gbns_grid_desc*, const gbns_source_desc*, const double*, double*)`,
- * does the same for source_term.
+ * does the same for source_term, and GBNS_DROPIN_BFLUX_HOOK, `int (const
+ * gbns_grid_desc*, const gbns_scheme_desc*, const double*, double*, const int*)`,
+ * for boundary_flux.
  */
 #pragma once
 
@@ -436,3 +444,52 @@ namespace spade::pde_algs
     }
 }
 
+namespace spade::pde_algs
+{
+    // pde_algs::boundary_flux (pde-algs/boundary_flux.h:16-105) on the GPU:
+    // the faces of the selected domain boundaries add their flux to the two
+    // cells they separate.  Selected by the gb300 traits after the flux
+    // functor; the flags go to gbns_boundary_flux in the order min(0), max(0),
+    // min(1), max(1), min(2), max(2).
+    template <
+        grid::multiblock_array sol_arr_t,
+        grid::multiblock_array rhs_arr_t,
+        typename flux_func_t,
+        typename alg_traits_t>
+    requires
+        grid::has_centering_type<sol_arr_t, grid::cell_centered> && gb300::selects_gb300<alg_traits_t>
+    static void boundary_flux(
+        const sol_arr_t& prims,
+        rhs_arr_t& rhs,
+        const bound_box_t<bool, sol_arr_t::grid_type::dim()>& apply_to_boundary,
+        const flux_func_t& flux_func,
+        const alg_traits_t&)
+    {
+        const gbns_grid_desc g = gb300::lower_grid(prims);
+        const gbns_scheme_desc s = gb300::lower_scheme(flux_func, GBNS_PREC_FP64);
+        int apply[6] = {0, 0, 0, 0, 0, 0};
+        for (int d = 0; d < int(sol_arr_t::grid_type::dim()); ++d)
+        {
+            apply[2*d] = apply_to_boundary.min(d) ? 1 : 0;
+            apply[2*d + 1] = apply_to_boundary.max(d) ? 1 : 0;
+        }
+        const double* q = prims.image().base;
+        double* r = rhs.image().base;
+#ifdef GBNS_DROPIN_BFLUX_HOOK
+        const int rc = GBNS_DROPIN_BFLUX_HOOK(&g, &s, q, r, apply);
+#else
+        static_assert(device::is_gpu<typename sol_arr_t::device_type> && device::is_gpu<typename rhs_arr_t::device_type>,
+                      "the gb300 boundary_flux runs on device::gpu arrays");
+        int rc = gbns_boundary_flux(&g, &s, q, r, apply, nullptr);
+        if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+#endif
+        if (rc != GBNS_OK)
+        {
+            char msg[512] = "drop-in hook failed";
+#ifndef GBNS_DROPIN_BFLUX_HOOK
+            gbns_last_error(msg, sizeof(msg));
+#endif
+            throw except::sp_exception(std::string("gb300 boundary_flux failed: ") + msg);
+        }
+    }
+}

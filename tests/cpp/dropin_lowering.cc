@@ -30,6 +30,16 @@ static int record_source(const gbns_grid_desc* g, const gbns_source_desc* d, con
 }
 #define GBNS_DROPIN_SOURCE_HOOK record_source
 
+static int g_bf_calls = 0;
+static int record_bflux(const gbns_grid_desc* g, const gbns_scheme_desc* s, const double* q, double* r, const int* apply)
+{
+    ++g_bf_calls;
+    std::printf("bflux %d %d %d %d %d %d conv %d order %d visc %d ng %d ptrs %d\n", apply[0], apply[1], apply[2], apply[3],
+                apply[4], apply[5], s->convective, s->order, s->viscous, g->ng, int(q != nullptr && r != nullptr));
+    return 0;
+}
+#define GBNS_DROPIN_BFLUX_HOOK record_bflux
+
 #include "spade.h"
 #include "spade_gb300.h"
 
@@ -77,7 +87,13 @@ int main(int argc, char** argv)
         // 6, 7: lowered point sources through the source_term overload
         spade::pde_algs::source_term(q, rhs, spade::gb300::body_force_t{2.5, 0.0, -1.0});
         spade::pde_algs::source_term(q, rhs, spade::gb300::body_accel_t{air, 0.0, -9.81, 0.0});
+        // 8: boundary_flux on the y walls with the gb300 traits appended
+        spade::bound_box_t<bool, 3> walls = false;
+        walls.min(1) = true;
+        walls.max(1) = true;
+        spade::pde_algs::boundary_flux(q, rhs, walls, spade::omni::compose(spade::convective::cent_keep<4>(air), visc),
+                                       spade::algs::make_traits(spade::pde_algs::gb300));
     });
-    std::printf("calls %d sources %d\n", g_calls, g_src_calls);
-    return (g_calls == 5 && g_src_calls == 2) ? 0 : 1;
+    std::printf("calls %d sources %d bflux %d\n", g_calls, g_src_calls, g_bf_calls);
+    return (g_calls == 5 && g_src_calls == 2 && g_bf_calls == 1) ? 0 : 1;
 }

@@ -58,3 +58,9 @@ def test_dropin_overload_and_lowering():
     assert len(srcs) == 2
     assert srcs[0][1] == "1" and [float(x) for x in srcs[0][4:7]] == [2.5, 0.0, -1.0]
     assert srcs[1][1] == "2" and [float(x) for x in srcs[1][4:7]] == [0.0, -9.81, 0.0] and float(srcs[1][8]) == 287.0
+    # boundary_flux overload: y-min and y-max flags, cent_keep<4> + visc_lr lowered
+    bf = [l.split() for l in lines if l.startswith("bflux")]
+    assert len(bf) == 1
+    assert bf[0][1:7] == ["0", "0", "1", "1", "0", "0"]
+    assert bf[0][bf[0].index("conv") + 1] == "1" and bf[0][bf[0].index("order") + 1] == "4"
+    assert bf[0][bf[0].index("visc") + 1] == "1" and bf[0][bf[0].index("ng") + 1] == "3"
