@@ -562,13 +562,24 @@ extern "C"
         key.prims = prims; key.work = work; key.dt = dt;
         int rc = check_cuda(cudaGetDevice(&key.device), "cudaGetDevice");
         if (rc) return rc;
-        cudaGraphExec_t exec = nullptr;
+        // launches the cached graph of `key` nsteps times; false if none is cached.
+        // Runs under the cache lock, so no other thread can evict the graph
+        // between lookup and launch.
+        auto replay = [&](int& out) -> bool
         {
             std::lock_guard<std::mutex> lk(step_graphs_mu());
             for (auto& e : step_graphs())
-                if (std::memcmp(&e.key, &key, sizeof(key)) == 0) { exec = e.exec; break; }
-        }
-        if (!exec)
+                if (std::memcmp(&e.key, &key, sizeof(key)) == 0)
+                {
+                    out = GBNS_OK;
+                    for (int i = 0; i < nsteps && out == GBNS_OK; ++i)
+                        out = check_cuda(cudaGraphLaunch(e.exec, st), "graph launch");
+                    return true;
+                }
+            return false;
+        };
+        if (replay(rc)) return rc;
+        cudaGraphExec_t exec = nullptr;
         {
             // capture one step on a private stream that waits for the caller's
             // work, so the captured launches see the caller's ordering
@@ -595,19 +606,16 @@ extern "C"
             auto& cache = step_graphs();
             if (cache.size() >= 8)
             {
-                // the evicted graph may still be in flight on any stream
-                cudaDeviceSynchronize();
+                // an evicted graph still in flight is freed by the driver when
+                // it completes (cuGraphExecDestroy semantics)
                 cudaGraphExecDestroy(cache.front().exec);
                 cache.erase(cache.begin());
             }
             cache.push_back(StepGraph{key, exec});
+            for (int i = 0; i < nsteps && rc == GBNS_OK; ++i)
+                rc = check_cuda(cudaGraphLaunch(exec, st), "graph launch");
         }
-        for (int i = 0; i < nsteps; ++i)
-        {
-            rc = check_cuda(cudaGraphLaunch(exec, st), "graph launch");
-            if (rc) return rc;
-        }
-        return GBNS_OK;
+        return rc;
     }
 
     int gbns_device_status(int* status, int reset, void* stream)
