@@ -14,16 +14,17 @@ namespace gbns
     int flux_variant_count(const gbns_scheme_desc* s)
     {
         if (!s) return 0;
-        // FP32-flux adds one variant: the TMA-staged FP64 box.
-        const int extra = s->precision == GBNS_PREC_FP32_FLUX ? 1 : 0;
+        // FP32-flux adds one variant (the TMA-staged FP64 box); FP64 adds
+        // 576-thread 8x8x8 tiles (and a 768-thread one for WENO5) in its place.
+        const bool fp32 = s->precision == GBNS_PREC_FP32_FLUX;
         switch (s->convective)
         {
-            case GBNS_CONV_CENT_KEEP: return (s->order == 2 ? 4 : 1) + extra;
-            case GBNS_CONV_TOTANI:    return 2 + extra;
-            case GBNS_CONV_FWENO:     return 4 + extra;
-            case GBNS_CONV_WENO5:     return 4 + extra;
-            case GBNS_CONV_HYBRID:    return 2 + extra;
-            default:                  return 1 + extra;
+            case GBNS_CONV_CENT_KEEP: return (s->order == 2 ? 5 : (s->order == 4 ? 2 : 1 + (fp32 ? 1 : 0)));
+            case GBNS_CONV_TOTANI:    return 3;
+            case GBNS_CONV_FWENO:     return 5;
+            case GBNS_CONV_WENO5:     return fp32 ? 5 : 6;
+            case GBNS_CONV_HYBRID:    return 3;
+            default:                  return fp32 ? 2 : 1;
         }
     }
 

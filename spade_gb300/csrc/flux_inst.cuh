@@ -96,11 +96,17 @@ namespace gbns
                 if (v == 1) GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 16, 8, 4, 256);
                 if (v == 2) GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 8, 8, 4, 128);
                 if (v == 3) GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 16, 8, 8, 256);
+#if !GBNS_FP32
+                if (v == 4) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 576);
+#endif
                 if (GBNS_FP32 && v == 4) GBNS_RUN(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 256);
                 GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 2, 8, 8, 8, 256);
             }
             if (order == 4)
             {
+#if !GBNS_FP32
+                if (v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 576);
+#endif
                 if (GBNS_FP32 && v == 1) GBNS_RUN(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 256);
                 GBNS_RUN_D(GBNS_CONV_CENT_KEEP, 4, 8, 8, 8, 256);
             }
@@ -118,6 +124,9 @@ namespace gbns
         if (conv == GBNS_CONV_TOTANI)
         {
             if (v == 1) GBNS_RUN_D(GBNS_CONV_TOTANI, 2, 16, 8, 4, 256);
+#if !GBNS_FP32
+            if (v == 2) GBNS_RUN(GBNS_CONV_TOTANI, 2, 8, 8, 8, 576);
+#endif
             if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
             GBNS_RUN_D(GBNS_CONV_TOTANI, 2, 8, 8, 8, 256);
         }
@@ -127,6 +136,9 @@ namespace gbns
             if (v == 1) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 4, 128);
             if (v == 2) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 16, 8, 4, 256);
             if (v == 3) GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 8, 512);
+#if !GBNS_FP32
+            if (v == 4) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 576);
+#endif
             if (GBNS_FP32 && v == 4) GBNS_RUN(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
             GBNS_RUN_D(GBNS_CONV_FWENO, 2, 8, 8, 8, 256);
         }
@@ -137,6 +149,13 @@ namespace gbns
             // 16 warps on one 8^3 tile: twice the warps per SM of variant 1
             // for latency hiding when one CTA fills shared memory (FP64)
             if (v == 3) GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 8, 512);
+#if !GBNS_FP32
+            // 18 warps at 96 registers and 24 at 80 (no or light spills in
+            // FP64): one round covers each direction's 576 faces, so the face
+            // loop has no tail run by two warps alone
+            if (v == 4) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 8, 576);
+            if (v == 5) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 8, 768);
+#endif
             if (GBNS_FP32 && v == 4) GBNS_RUN(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
             GBNS_RUN_D(GBNS_CONV_WENO5, 2, 8, 8, 4, 256);
         }
@@ -146,12 +165,18 @@ namespace gbns
             if (order == 2)
             {
                 if (v == 1) GBNS_RUN_D(GBNS_CONV_HYBRID, 2, 8, 8, 8, 256);
+#if !GBNS_FP32
+                if (v == 2) GBNS_RUN(GBNS_CONV_HYBRID, 2, 8, 8, 8, 576);
+#endif
                 if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_HYBRID, 2, 8, 8, 4, 256);
                 GBNS_RUN_D(GBNS_CONV_HYBRID, 2, 8, 8, 4, 256);
             }
             if (order == 4)
             {
                 if (v == 1) GBNS_RUN_D(GBNS_CONV_HYBRID, 4, 8, 8, 8, 256);
+#if !GBNS_FP32
+                if (v == 2) GBNS_RUN(GBNS_CONV_HYBRID, 4, 8, 8, 8, 576);
+#endif
                 if (GBNS_FP32 && v == 2) GBNS_RUN(GBNS_CONV_HYBRID, 4, 8, 8, 4, 256);
                 GBNS_RUN_D(GBNS_CONV_HYBRID, 4, 8, 8, 4, 256);
             }

@@ -116,7 +116,9 @@ namespace gbns
         static_assert(SMEM_BYTES <= 227*1024, "tile does not fit in shared memory");
         // CTAs per SM that shared memory allows (the register budget follows)
         static constexpr int MINB_RAW = int((227*1024) / (SMEM_BYTES + 1024));
-        static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW);
+        // (tiles of more than 512 threads run one CTA per SM: two would leave
+        // fewer than 57 registers per thread)
+        static constexpr int MINB = NT > 512 ? 1 : (MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW));
         static_assert(5*BXE <= 256, "TMA box inner extent exceeds 256 elements");
     };
 
