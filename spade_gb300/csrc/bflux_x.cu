@@ -8,7 +8,7 @@ namespace gbns
 
     int boundary_flux_launch_d0(const GeomK& G, const SchemeK& S, const BndArgs& A, int conv, int order, cudaStream_t st)
     {
-        constexpr int D = 0, TAG = 9;
+        constexpr int D = 0, TAG = 66;
         switch (conv)
         {
         case GBNS_CONV_NONE: return run_boundary_flux<BndCfg<GBNS_CONV_NONE, 2, D, TAG>, D>(G, S, A, st);

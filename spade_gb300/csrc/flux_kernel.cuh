@@ -45,6 +45,31 @@ namespace gbns
 
     template <bool S> using YTabT = typename std::conditional<S, YTabK, YTabNone>::type;
 
+    // a*b and x*2^E of a tile configuration: the integer-pipe forms in the
+    // no-contraction FP64 units, the plain operators elsewhere
+    template <class Cfg>
+    __device__ __forceinline__ typename Cfg::Real pmul(typename Cfg::Real a, typename Cfg::Real b)
+    {
+        if constexpr (Cfg::IMUL) return dmul_int(a, b);
+        else return a*b;
+    }
+    template <class Cfg, int E>
+    __device__ __forceinline__ typename Cfg::Real ppow2(typename Cfg::Real x)
+    {
+        static_assert(E == -1 || E == -2, "x/2 or x/4");
+        using Real = typename Cfg::Real;
+        if constexpr (Cfg::IMUL) return dmul_pow2<E>(x);
+        else return (E == -1 ? Real(0.5) : Real(0.25))*x;
+    }
+    // nD*x with nD the face normal's metric factor (1 on identity grids,
+    // where the plain product folds away)
+    template <class Cfg>
+    __device__ __forceinline__ typename Cfg::Real nmul(typename Cfg::Real nD, typename Cfg::Real x)
+    {
+        if constexpr (Cfg::STRETCH) return pmul<Cfg>(x, nD);
+        else return x*nD;
+    }
+
     constexpr int cmax3(int a, int b, int c) { return a > b ? (a > c ? a : c) : (b > c ? b : c); }
     constexpr size_t align128(size_t x) { return (x + 127) & ~size_t(127); }
 
@@ -54,10 +79,19 @@ namespace gbns
     // STG_ (FP32 only): 0 = stage the FP64 box (TMA or coalesced loads) and
     // convert it; 1 = load the stencil cells straight into FP32 shared
     // memory (no FP64 staging buffer, more CTAs per SM).
+    // Translation units compiled without FMA contraction (-fmad=false): the
+    // FP64 drop-in's flux_f64x_* (tags 0-3), the batched FP64 kernel (64) and
+    // boundary_flux (66).
+    constexpr bool tag_no_fma(int tag) { return tag < 4 || tag == 64 || tag == 66; }
+
     template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_, int STG_ = 0>
     struct FluxCfg
     {
         using Real = Real_;
+        // products of the reference's FP64 arithmetic go to the integer pipes
+        // (dmul_int / dmul_pow2: the same bits) where no FMA contraction
+        // could have fused them
+        static constexpr bool IMUL = std::is_same<Real_, double>::value && tag_no_fma(TAG_);
         static constexpr int CONV = CONV_, ORDER = ORDER_;
         static constexpr bool STRETCH = STRETCH_;
         static constexpr int TX = TX_, TY = TY_, TZ = TZ_, NT = NT_;
@@ -321,28 +355,28 @@ namespace gbns
                                                   typename Cfg::Real& fl, typename Cfg::Real& ds)
     {
         using Real = typename Cfg::Real;
-        const Real un = V.q(2 + D, c)*nD;
+        const Real un = nmul<Cfg>(nD, V.q(2 + D, c));
         if (eq == 0)
         {
-            fl = un*(Real(0.5)*rho);
+            fl = pmul<Cfg>(un, ppow2<Cfg, -1>(rho));
             ds = hsr;
         }
         else if (eq == 1)
         {
             const Real engy = engy_c;
-            fl = (un*(Real(0.5)*rho))*(engy + S.R*V.q(1, c));
-            ds = hsr*engy;
+            fl = pmul<Cfg>(pmul<Cfg>(un, ppow2<Cfg, -1>(rho)), engy + pmul<Cfg>(S.R, V.q(1, c)));
+            ds = pmul<Cfg>(hsr, engy);
         }
         else
         {
             const int dr = eq - 2;
             const Real ud = V.q(2 + dr, c);
-            Real m = un*rho;
-            m *= ud;
-            if (dr == D) m += V.q(0, c)*nD;
-            m *= Real(0.5);
+            Real m = pmul<Cfg>(un, rho);
+            m = pmul<Cfg>(m, ud);
+            if (dr == D) m += nmul<Cfg>(nD, V.q(0, c));
+            m = ppow2<Cfg, -1>(m);
             fl = m;
-            ds = hsr*ud;
+            ds = pmul<Cfg>(hsr, ud);
         }
     }
 
@@ -580,10 +614,10 @@ namespace gbns
 
     __device__ __forceinline__ Weno5Side weno5_nd(double a, double b, double c, double d, double e)
     {
-        // the six independent smoothness products go to the integer pipes
-        // (dmul_int, bit-identical to a*b); the rest stay on the FP64 unit,
-        // whose latency is shorter at this kernel's 8-16 warps per SM
-        const double q0 = fma(2.0, a, fma(-7.0, b, 11.0*c));
+        // every product on the integer pipes (dmul_int, bit-identical to a*b):
+        // with 18 warps per SM their latency hides and the FP64 unit keeps
+        // the additions and FMAs
+        const double q0 = fma(2.0, a, fma(-7.0, b, dmul_int(11.0, c)));
         const double q1 = fma(5.0, c, fma(2.0, d, -b));
         const double q2 = fma(2.0, c, fma(5.0, d, -e));
         const double t0 = fma(-2.0, b, a) + c, s0 = fma(3.0, c, fma(-4.0, b, a));
@@ -593,10 +627,11 @@ namespace gbns
         const double e0 = fma(dmul_int(k, t0), t0, dmul_int(s0, s0)) + eps4;
         const double e1 = fma(dmul_int(k, t1), t1, dmul_int(s1, s1)) + eps4;
         const double e2 = fma(dmul_int(k, t2), t2, dmul_int(s2, s2)) + eps4;
-        const double E0 = e0*e0, E1 = e1*e1, E2 = e2*e2;
-        const double a0 = 0.1*(E1*E2), a1 = 0.6*(E0*E2), a2 = 0.3*(E0*E1);
+        const double E0 = dmul_int(e0, e0), E1 = dmul_int(e1, e1), E2 = dmul_int(e2, e2);
+        const double a0 = dmul_int(0.1, dmul_int(E1, E2)), a1 = dmul_int(0.6, dmul_int(E0, E2));
+        const double a2 = dmul_int(0.3, dmul_int(E0, E1));
         Weno5Side r;
-        r.N = fma(a0, q0, fma(a1, q1, a2*q2));
+        r.N = fma(a0, q0, fma(a1, q1, dmul_int(a2, q2)));
         r.D = (a0 + a1) + a2;
         return r;
     }
@@ -614,9 +649,9 @@ namespace gbns
         }
         const Weno5Side u = weno5_nd(ua, ub, uc, ud, ue);
         const Weno5Side d = weno5_nd(da, db, dc, dd, de);
-        const double den = 6.0*(u.D*d.D);
+        const double den = dmul_int(6.0, dmul_int(u.D, d.D));
         if (den < 1.0e300)
-            return fma(u.N, d.D, d.N*u.D)/den;
+            return fma(u.N, d.D, dmul_int(d.N, u.D))/den;
         return u.N/(6.0*u.D) + d.N/(6.0*d.D);
     }
 
@@ -672,26 +707,26 @@ namespace gbns
         const Real pr = V.q(0, cr), Tr = V.q(1, cr), ur = V.q(2, cr), vr = V.q(3, cr), wr = V.q(4, cr);
         const Real delta_p = pl - pr;
         const Real delta_T = Tl - Tr;
-        const Real pavg = Real(0.5)*(pl + pr);
-        const Real Tavg = Real(0.5)*(Tl + Tr);
-        const Real inv_RT = Real(1.0)/(S.R_avg*Tavg);
-        const Real p_inv_rt2 = pavg*inv_RT/Tavg;
-        const Real k = Real(0.5)*(ul*ur + vl*vr + wl*wr);
-        const Real u = Real(0.5)*(ul + ur);
-        const Real v = Real(0.5)*(vl + vr);
-        const Real w = Real(0.5)*(wl + wr);
-        const Real ap = scl*S.eps_p*delta_p;
-        const Real aT = scl*S.eps_T*delta_T*p_inv_rt2;
-        out[0] = ap*inv_RT;
-        out[1] = ap*(k*inv_RT + S.inv_gamma_avg);
-        out[2] = ap*u*inv_RT;
-        out[3] = ap*v*inv_RT;
-        out[4] = ap*w*inv_RT;
+        const Real pavg = ppow2<Cfg, -1>(pl + pr);
+        const Real Tavg = ppow2<Cfg, -1>(Tl + Tr);
+        const Real inv_RT = Real(1.0)/pmul<Cfg>(S.R_avg, Tavg);
+        const Real p_inv_rt2 = pmul<Cfg>(pavg, inv_RT)/Tavg;
+        const Real k = ppow2<Cfg, -1>(pmul<Cfg>(ul, ur) + pmul<Cfg>(vl, vr) + pmul<Cfg>(wl, wr));
+        const Real u = ppow2<Cfg, -1>(ul + ur);
+        const Real v = ppow2<Cfg, -1>(vl + vr);
+        const Real w = ppow2<Cfg, -1>(wl + wr);
+        const Real ap = pmul<Cfg>(pmul<Cfg>(scl, S.eps_p), delta_p);
+        const Real aT = pmul<Cfg>(pmul<Cfg>(pmul<Cfg>(scl, S.eps_T), delta_T), p_inv_rt2);
+        out[0] = pmul<Cfg>(ap, inv_RT);
+        out[1] = pmul<Cfg>(ap, pmul<Cfg>(k, inv_RT) + S.inv_gamma_avg);
+        out[2] = pmul<Cfg>(pmul<Cfg>(ap, u), inv_RT);
+        out[3] = pmul<Cfg>(pmul<Cfg>(ap, v), inv_RT);
+        out[4] = pmul<Cfg>(pmul<Cfg>(ap, w), inv_RT);
         out[0] -= aT;
-        out[1] -= aT*(Real(0.5)*k);
-        out[2] -= aT*u;
-        out[3] -= aT*v;
-        out[4] -= aT*w;
+        out[1] -= pmul<Cfg>(aT, ppow2<Cfg, -1>(k));
+        out[2] -= pmul<Cfg>(aT, u);
+        out[3] -= pmul<Cfg>(aT, v);
+        out[4] -= pmul<Cfg>(aT, w);
     }
 
     // info::gradient at the face (info_gradient.h:61-123): grad[a][t],
@@ -709,17 +744,19 @@ namespace gbns
         for (int t = 0; t < 4; ++t)
         {
             const int v = t + 1;
-            grad[D][t]  = (Real(-1.0)*V.q(v, cl))*inv[D];
-            grad[D1][t] = (Real(0.25)*V.q(v, cl + S1))*inv[D1];
-            grad[D1][t] += (Real(-0.25)*V.q(v, cl - S1))*inv[D1];
-            grad[D2][t] = (Real(0.25)*V.q(v, cl + S2))*inv[D2];
-            grad[D2][t] += (Real(-0.25)*V.q(v, cl - S2))*inv[D2];
-            grad[D][t]  += (Real(1.0)*V.q(v, cr))*inv[D];
-            grad[D1][t] += (Real(0.25)*V.q(v, cr + S1))*inv[D1];
-            grad[D1][t] += (Real(-0.25)*V.q(v, cr - S1))*inv[D1];
-            grad[D2][t] += (Real(0.25)*V.q(v, cr + S2))*inv[D2];
-            grad[D2][t] += (Real(-0.25)*V.q(v, cr - S2))*inv[D2];
-            if constexpr (Cfg::STRETCH) grad[1][t] *= im;
+            // (c*q)*inv with c = -1, 1, 0.25, -0.25: the +-1 products are exact
+            // sign changes, the +-0.25 ones exact exponent shifts
+            grad[D][t]  = pmul<Cfg>(-V.q(v, cl), inv[D]);
+            grad[D1][t] = pmul<Cfg>(ppow2<Cfg, -2>(V.q(v, cl + S1)), inv[D1]);
+            grad[D1][t] += pmul<Cfg>(-ppow2<Cfg, -2>(V.q(v, cl - S1)), inv[D1]);
+            grad[D2][t] = pmul<Cfg>(ppow2<Cfg, -2>(V.q(v, cl + S2)), inv[D2]);
+            grad[D2][t] += pmul<Cfg>(-ppow2<Cfg, -2>(V.q(v, cl - S2)), inv[D2]);
+            grad[D][t]  += pmul<Cfg>(V.q(v, cr), inv[D]);
+            grad[D1][t] += pmul<Cfg>(ppow2<Cfg, -2>(V.q(v, cr + S1)), inv[D1]);
+            grad[D1][t] += pmul<Cfg>(-ppow2<Cfg, -2>(V.q(v, cr - S1)), inv[D1]);
+            grad[D2][t] += pmul<Cfg>(ppow2<Cfg, -2>(V.q(v, cr + S2)), inv[D2]);
+            grad[D2][t] += pmul<Cfg>(-ppow2<Cfg, -2>(V.q(v, cr - S2)), inv[D2]);
+            if constexpr (Cfg::STRETCH) grad[1][t] = pmul<Cfg>(grad[1][t], im);
         }
     }
 
@@ -749,7 +786,7 @@ namespace gbns
         const int cl = rc - SD, cr = rc;
         Real qf[5];
         #pragma unroll
-        for (int v = 0; v < 5; ++v) { qf[v] = V.q(v, cl); qf[v] += V.q(v, cr); qf[v] *= Real(0.5); }
+        for (int v = 0; v < 5; ++v) { qf[v] = V.q(v, cl); qf[v] += V.q(v, cr); qf[v] = ppow2<Cfg, -1>(qf[v]); }
         Real visc, visc2, dfs;
         if (S.law == GBNS_LAW_CONSTANT)
         {
@@ -757,36 +794,36 @@ namespace gbns
         }
         else if (S.law == GBNS_LAW_POWER)
         {
-            visc = S.mu*dev_pow(qf[1]/S.T_ref, S.power);
-            visc2 = Real(-0.66666666667)*visc;
+            visc = pmul<Cfg>(S.mu, dev_pow(qf[1]/S.T_ref, S.power));
+            visc2 = pmul<Cfg>(Real(-0.66666666667), visc);
             dfs = visc/S.prandtl;
         }
         else
         {
             const Real x = qf[1]/S.T_ref;
-            visc = S.mu*(x*dev_sqrt(x))*(S.tref_plus_s/(qf[1] + S.S));
-            visc2 = visc*Real(-2.0/3.0);
-            dfs = visc*S.inv_pr;
+            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt(x))), S.tref_plus_s/(qf[1] + S.S));
+            visc2 = pmul<Cfg>(visc, Real(-2.0/3.0));
+            dfs = pmul<Cfg>(visc, S.inv_pr);
         }
         const Real div = grad[0][1] + grad[1][2] + grad[2][3];
-        const Real t00 = visc*(grad[0][1] + grad[0][1]) + visc2*div;
-        const Real t01 = visc*(grad[0][2] + grad[1][1]);
-        const Real t02 = visc*(grad[0][3] + grad[2][1]);
-        const Real t12 = visc*(grad[1][3] + grad[2][2]);
-        const Real t11 = visc*(grad[1][2] + grad[1][2]) + visc2*div;
-        const Real t22 = visc*(grad[2][3] + grad[2][3]) + visc2*div;
-        const Real cond = S.spec_heat*dfs;
+        const Real t00 = pmul<Cfg>(visc, grad[0][1] + grad[0][1]) + pmul<Cfg>(visc2, div);
+        const Real t01 = pmul<Cfg>(visc, grad[0][2] + grad[1][1]);
+        const Real t02 = pmul<Cfg>(visc, grad[0][3] + grad[2][1]);
+        const Real t12 = pmul<Cfg>(visc, grad[1][3] + grad[2][2]);
+        const Real t11 = pmul<Cfg>(visc, grad[1][2] + grad[1][2]) + pmul<Cfg>(visc2, div);
+        const Real t22 = pmul<Cfg>(visc, grad[2][3] + grad[2][3]) + pmul<Cfg>(visc2, div);
+        const Real cond = pmul<Cfg>(S.spec_heat, dfs);
         // only row D of tau and component D of the heat flux survive n = nD e_D
         Real tr0, tr1, tr2;
         if constexpr (D == 0) { tr0 = t00; tr1 = t01; tr2 = t02; }
         else if constexpr (D == 1) { tr0 = t01; tr1 = t11; tr2 = t12; }
         else { tr0 = t02; tr1 = t12; tr2 = t22; }
-        const Real ht = qf[2]*tr0 + qf[3]*tr1 + qf[4]*tr2 + cond*grad[D][0];
+        const Real ht = pmul<Cfg>(qf[2], tr0) + pmul<Cfg>(qf[3], tr1) + pmul<Cfg>(qf[4], tr2) + pmul<Cfg>(cond, grad[D][0]);
         out[0] = Real(0.0);
-        out[1] = -(nD*ht);
-        out[2] = -(nD*tr0);
-        out[3] = -(nD*tr1);
-        out[4] = -(nD*tr2);
+        out[1] = -nmul<Cfg>(nD, ht);
+        out[2] = -nmul<Cfg>(nD, tr0);
+        out[3] = -nmul<Cfg>(nD, tr1);
+        out[4] = -nmul<Cfg>(nD, tr2);
     }
 
     // Composite face flux conv + (diss + visc)  (omni/compose.h:19-24)

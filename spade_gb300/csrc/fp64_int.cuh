@@ -46,4 +46,18 @@ namespace gbns
         const uint64_t r = ((ua ^ ub) & SGN) | ((((uint64_t)(e - 1)) << 52) + m + up);
         return __longlong_as_double((long long)r);
     }
+
+    // x * 2^E (E < 0), the same bits as the hardware multiply by the constant:
+    // for a normal x whose product stays normal the scaling only lowers the
+    // biased exponent field (exact); zeros, subnormals, infinities, NaNs and
+    // products that would become subnormal take the hardware multiply.
+    template <int E>
+    __device__ __forceinline__ double dmul_pow2(double x)
+    {
+        static_assert(E < 0 && E > -1022, "negative power of two");
+        const uint64_t u = (uint64_t)__double_as_longlong(x);
+        const uint32_t ex = (uint32_t)(u >> 52) & 0x7ffu;
+        if (ex - uint32_t(1 - E) >= uint32_t(2046 - (1 - E) + 1)) return x*(E == -1 ? 0.5 : (E == -2 ? 0.25 : __longlong_as_double((long long)(uint64_t(1023 + E) << 52))));
+        return __longlong_as_double((long long)(u - (uint64_t(-E) << 52)));
+    }
 }

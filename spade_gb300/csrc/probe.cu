@@ -130,7 +130,11 @@ namespace gbns
             const double b = __longlong_as_double((long long)dmul_operand(k, 1));
             const double h = __dmul_rn(a, b), e = dmul_int(a, b);
             const bool same = __double_as_longlong(h) == __double_as_longlong(e) || (h != h && e != e);
-            if (!same) atomicAdd(bad, 1ull);
+            const double h1 = __dmul_rn(a, 0.5), e1 = dmul_pow2<-1>(a);
+            const double h2 = __dmul_rn(a, 0.25), e2 = dmul_pow2<-2>(a);
+            const bool same1 = __double_as_longlong(h1) == __double_as_longlong(e1) || (h1 != h1 && e1 != e1);
+            const bool same2 = __double_as_longlong(h2) == __double_as_longlong(e2) || (h2 != h2 && e2 != e2);
+            if (!same || !same1 || !same2) atomicAdd(bad, 1ull);
         }
     }
 }

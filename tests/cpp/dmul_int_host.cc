@@ -1,4 +1,5 @@
-// Host check of the integer FP64 multiply (spade_gb300/csrc/fp64_int.cuh):
+// Host check of the integer FP64 multiply and power-of-two scaling
+// (spade_gb300/csrc/fp64_int.cuh):
 // the header is compiled for the CPU with its CUDA intrinsics replaced by
 // portable equivalents and compared bit for bit with the host's IEEE
 // multiply (round to nearest even) on generated operand pairs.
@@ -52,6 +53,15 @@ int main(int argc, char** argv)
         if (__double_as_longlong(h) != __double_as_longlong(e) && !(h != h && e != e))
         {
             if (!bad) std::printf("first mismatch: a=%a b=%a hw=%a int=%a\n", a, b, h, e);
+            ++bad;
+        }
+        // exact power-of-two scalings
+        const double h1 = __dmul_rn(a, 0.5), e1 = gbns::dmul_pow2<-1>(a);
+        const double h2 = __dmul_rn(a, 0.25), e2 = gbns::dmul_pow2<-2>(a);
+        if ((__double_as_longlong(h1) != __double_as_longlong(e1) && !(h1 != h1 && e1 != e1)) ||
+            (__double_as_longlong(h2) != __double_as_longlong(e2) && !(h2 != h2 && e2 != e2)))
+        {
+            if (!bad) std::printf("first pow2 mismatch: a=%a hw=%a,%a int=%a,%a\n", a, h1, h2, e1, e2);
             ++bad;
         }
     }
