@@ -88,10 +88,14 @@ namespace gbns
     struct FluxCfg
     {
         using Real = Real_;
-        // products of the reference's FP64 arithmetic go to the integer pipes
-        // (dmul_int / dmul_pow2: the same bits) where no FMA contraction
-        // could have fused them
-        static constexpr bool IMUL = std::is_same<Real_, double>::value && tag_no_fma(TAG_);
+        // FP64 products on the integer pipes (dmul_int / dmul_pow2: the same
+        // bits) in the throughput tiles of more than 512 threads, whose 18+
+        // warps per SM hide the longer integer chains (smaller tiles, chosen
+        // for small latency-bound grids, keep the FP64 unit): every WENO5
+        // product (explicit FMAs, so in both FP64 modes), and the reference's
+        // flux products where no FMA contraction could have fused them
+        static constexpr bool IMUL_WENO = std::is_same<Real_, double>::value && NT_ > 512;
+        static constexpr bool IMUL = IMUL_WENO && tag_no_fma(TAG_);
         static constexpr int CONV = CONV_, ORDER = ORDER_;
         static constexpr bool STRETCH = STRETCH_;
         static constexpr int TX = TX_, TY = TY_, TZ = TZ_, NT = NT_;
@@ -612,30 +616,38 @@ namespace gbns
     // sides are divided separately).
     struct Weno5Side { double N, D; };
 
+    template <bool IM>
+    __device__ __forceinline__ double wmul(double a, double b)
+    {
+        if constexpr (IM) return dmul_int(a, b);
+        else return a*b;
+    }
+
+    template <bool IM>
     __device__ __forceinline__ Weno5Side weno5_nd(double a, double b, double c, double d, double e)
     {
-        // every product on the integer pipes (dmul_int, bit-identical to a*b):
-        // with 18 warps per SM their latency hides and the FP64 unit keeps
-        // the additions and FMAs
-        const double q0 = fma(2.0, a, fma(-7.0, b, dmul_int(11.0, c)));
+        // products through wmul: on the integer pipes in the throughput tiles
+        // (bit-identical to a*b), the additions and FMAs on the FP64 unit
+        const double q0 = fma(2.0, a, fma(-7.0, b, wmul<IM>(11.0, c)));
         const double q1 = fma(5.0, c, fma(2.0, d, -b));
         const double q2 = fma(2.0, c, fma(5.0, d, -e));
         const double t0 = fma(-2.0, b, a) + c, s0 = fma(3.0, c, fma(-4.0, b, a));
         const double t1 = fma(-2.0, c, b) + d, s1 = b - d;
         const double t2 = fma(-2.0, d, c) + e, s2 = fma(3.0, c, fma(-4.0, d, e));
         const double k = 13.0/3.0, eps4 = 4e-16;
-        const double e0 = fma(dmul_int(k, t0), t0, dmul_int(s0, s0)) + eps4;
-        const double e1 = fma(dmul_int(k, t1), t1, dmul_int(s1, s1)) + eps4;
-        const double e2 = fma(dmul_int(k, t2), t2, dmul_int(s2, s2)) + eps4;
-        const double E0 = dmul_int(e0, e0), E1 = dmul_int(e1, e1), E2 = dmul_int(e2, e2);
-        const double a0 = dmul_int(0.1, dmul_int(E1, E2)), a1 = dmul_int(0.6, dmul_int(E0, E2));
-        const double a2 = dmul_int(0.3, dmul_int(E0, E1));
+        const double e0 = fma(wmul<IM>(k, t0), t0, wmul<IM>(s0, s0)) + eps4;
+        const double e1 = fma(wmul<IM>(k, t1), t1, wmul<IM>(s1, s1)) + eps4;
+        const double e2 = fma(wmul<IM>(k, t2), t2, wmul<IM>(s2, s2)) + eps4;
+        const double E0 = wmul<IM>(e0, e0), E1 = wmul<IM>(e1, e1), E2 = wmul<IM>(e2, e2);
+        const double a0 = wmul<IM>(0.1, wmul<IM>(E1, E2)), a1 = wmul<IM>(0.6, wmul<IM>(E0, E2));
+        const double a2 = wmul<IM>(0.3, wmul<IM>(E0, E1));
         Weno5Side r;
-        r.N = fma(a0, q0, fma(a1, q1, dmul_int(a2, q2)));
+        r.N = fma(a0, q0, fma(a1, q1, wmul<IM>(a2, q2)));
         r.D = (a0 + a1) + a2;
         return r;
     }
 
+    template <bool IM>
     __device__ __forceinline__ double weno5_pair(double ua, double ub, double uc, double ud, double ue,
                                                  double da, double db, double dc, double dd, double de, int smooth)
     {
@@ -647,11 +659,11 @@ namespace gbns
                                   fma(0.6, fma(5.0, dc, fma(2.0, dd, -db)), 0.3*fma(2.0, dc, fma(5.0, dd, -de))));
             return (pu + pd)*(1.0/6.0);
         }
-        const Weno5Side u = weno5_nd(ua, ub, uc, ud, ue);
-        const Weno5Side d = weno5_nd(da, db, dc, dd, de);
-        const double den = dmul_int(6.0, dmul_int(u.D, d.D));
+        const Weno5Side u = weno5_nd<IM>(ua, ub, uc, ud, ue);
+        const Weno5Side d = weno5_nd<IM>(da, db, dc, dd, de);
+        const double den = wmul<IM>(6.0, wmul<IM>(u.D, d.D));
         if (den < 1.0e300)
-            return fma(u.N, d.D, dmul_int(d.N, u.D))/den;
+            return fma(u.N, d.D, wmul<IM>(d.N, u.D))/den;
         return u.N/(6.0*u.D) + d.N/(6.0*d.D);
     }
 
@@ -683,7 +695,7 @@ namespace gbns
                 }
             }
             if constexpr (sizeof(Real) == 8)
-                out[eq] = weno5_pair(up[0], up[1], up[2], up[3], up[4], dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
+                out[eq] = weno5_pair<Cfg::IMUL_WENO>(up[0], up[1], up[2], up[3], up[4], dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
             else
             {
                 const float2 f = weno5_side2(make_float2(up[0], dn[5]), make_float2(up[1], dn[4]),
