@@ -211,6 +211,12 @@ namespace gbns
         }
     };
 
+    // a/b: the correctly rounded FP64 division, and in FP32-flux arithmetic the
+    // fast quotient (within 2 ulp for |b| in [2^-126, 2^126], which holds for
+    // every divisor below: gas constants, temperatures, densities and the
+    // Ducros sensor's denominator)
+    __device__ __forceinline__ double pdiv(double a, double b) { return a/b; }
+    __device__ __forceinline__ float  pdiv(float a, float b)   { return __fdividef(a, b); }
     __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
     __device__ __forceinline__ float  dev_sqrt(float x)  { return sqrtf(x); }
     __device__ __forceinline__ double dev_pow(double x, double y) { return pow(x, y); }
@@ -231,14 +237,14 @@ namespace gbns
         h += w*w;
         h = dev_sqrt(h);
         h += dev_sqrt(r*S.gamma);
-        const Real rho = p/r;
+        const Real rho = pdiv(p, r);
         h *= rho;
         h *= Real(0.5);
         Real e = u*u;
         e += v*v;
         e += w*w;
         e *= Real(0.5);
-        e += (S.R*T)/S.gm1;
+        e += pdiv(S.R*T, S.gm1);
         rho_o = rho; h_o = h; e_o = e;
     }
 
@@ -253,9 +259,9 @@ namespace gbns
                       (Cfg::CONV == GBNS_CONV_HYBRID && Cfg::SPLIT))
         {
             // convective.h:130-131 / 80-84 (the hybrid's fweno half reads the split cache)
-            const Real rho = p/(S.R*T);
+            const Real rho = pdiv(p, S.R*T);
             der[0*Cfg::BOXN + c] = rho;
-            der[1*Cfg::BOXN + c] = p/(rho*S.gm1);
+            der[1*Cfg::BOXN + c] = pdiv(p, rho*S.gm1);
         }
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5 ||
                            Cfg::CONV == GBNS_CONV_HYBRID)
@@ -267,7 +273,7 @@ namespace gbns
             der[2*Cfg::BOXN + c] = e;
             // cent_keep's e (convective.h:131); its rho = p/(R*T) is the
             // same rounding as fweno's p/r above
-            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = p/(rho*S.gm1);
+            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv(p, rho*S.gm1);
         }
     }
 
@@ -588,8 +594,11 @@ namespace gbns
         const float2 b1 = __ffma2_rn(__fmul2_rn(k13, t1), t1, __fmul2_rn(__fmul2_rn(q4, s1), s1));
         const float2 b2 = __ffma2_rn(__fmul2_rn(k13, t2), t2, __fmul2_rn(__fmul2_rn(q4, s2), s2));
         const float eps = 1e-16f;
+        // the fast reciprocal and quotient (within 2 ulp) instead of the
+        // correctly rounded division sequence; sc is kept below 2^126, the
+        // fast reciprocal's range (no WENO5 indicator reaches it)
         const float2 sc = max2(max2(b0, b1), max2(b2, bc2(eps)));
-        const float2 is = make_float2(1.0f/sc.x, 1.0f/sc.y);
+        const float2 is = make_float2(__fdividef(1.0f, fminf(sc.x, 0x1p126f)), __fdividef(1.0f, fminf(sc.y, 0x1p126f)));
         const float2 ee = __fmul2_rn(bc2(eps), is);
         const float2 fl = bc2(1e-30f);
         const float2 u0 = __ffma2_rn(b0, is, ee), u1 = __ffma2_rn(b1, is, ee), u2 = __ffma2_rn(b2, is, ee);
@@ -601,7 +610,7 @@ namespace gbns
         const float2 a2 = __fmul2_rn(bc2(0.3f), __fmul2_rn(q0, q1));
         const float2 num = __ffma2_rn(a2, p2, __ffma2_rn(a1, p1, __fmul2_rn(a0, p0)));
         const float2 den = __fadd2_rn(__fadd2_rn(a0, a1), a2);
-        return make_float2(num.x/den.x, num.y/den.y);
+        return make_float2(__fdividef(num.x, den.x), __fdividef(num.y, den.y));
     }
 
     // FP64 WENO5-JS face flux F = F(f+ side) + F(f- side), each side a..e
@@ -721,8 +730,8 @@ namespace gbns
         const Real delta_T = Tl - Tr;
         const Real pavg = ppow2<Cfg, -1>(pl + pr);
         const Real Tavg = ppow2<Cfg, -1>(Tl + Tr);
-        const Real inv_RT = Real(1.0)/pmul<Cfg>(S.R_avg, Tavg);
-        const Real p_inv_rt2 = pmul<Cfg>(pavg, inv_RT)/Tavg;
+        const Real inv_RT = pdiv(Real(1.0), pmul<Cfg>(S.R_avg, Tavg));
+        const Real p_inv_rt2 = pdiv(pmul<Cfg>(pavg, inv_RT), Tavg);
         const Real k = ppow2<Cfg, -1>(pmul<Cfg>(ul, ur) + pmul<Cfg>(vl, vr) + pmul<Cfg>(wl, wr));
         const Real u = ppow2<Cfg, -1>(ul + ur);
         const Real v = ppow2<Cfg, -1>(vl + vr);
@@ -782,7 +791,7 @@ namespace gbns
         const Real vort1 = g[2][1] - g[0][3];
         const Real vort2 = g[0][2] - g[1][1];
         const Real vort_sq = vort0*vort0 + vort1*vort1 + vort2*vort2;
-        return theta_sq / (theta_sq + vort_sq + epsilon);
+        return pdiv(theta_sq, theta_sq + vort_sq + epsilon);
     }
 
     // visc_lr::operator() (viscous.h:39-79) with info::value / info::gradient
@@ -806,14 +815,14 @@ namespace gbns
         }
         else if (S.law == GBNS_LAW_POWER)
         {
-            visc = pmul<Cfg>(S.mu, dev_pow(qf[1]/S.T_ref, S.power));
+            visc = pmul<Cfg>(S.mu, dev_pow(pdiv(qf[1], S.T_ref), S.power));
             visc2 = pmul<Cfg>(Real(-0.66666666667), visc);
-            dfs = visc/S.prandtl;
+            dfs = pdiv(visc, S.prandtl);
         }
         else
         {
-            const Real x = qf[1]/S.T_ref;
-            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt(x))), S.tref_plus_s/(qf[1] + S.S));
+            const Real x = pdiv(qf[1], S.T_ref);
+            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt(x))), pdiv(S.tref_plus_s, qf[1] + S.S));
             visc2 = pmul<Cfg>(visc, Real(-2.0/3.0));
             dfs = pmul<Cfg>(visc, S.inv_pr);
         }
