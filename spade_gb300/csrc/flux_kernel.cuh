@@ -92,10 +92,11 @@ namespace gbns
         // bits) in the throughput tiles of more than 512 threads, whose 18+
         // warps per SM hide the longer integer chains (smaller tiles, chosen
         // for small latency-bound grids, keep the FP64 unit): every WENO5
-        // product (explicit FMAs, so in both FP64 modes), and the reference's
-        // flux products where no FMA contraction could have fused them
-        static constexpr bool IMUL_WENO = std::is_same<Real_, double>::value && NT_ > 512;
-        static constexpr bool IMUL = IMUL_WENO && tag_no_fma(TAG_);
+        // product (explicit FMAs, so in both FP64 modes) and every division
+        // (correctly rounded in both modes), and the reference's flux products
+        // where no FMA contraction could have fused them
+        static constexpr bool IEMU = std::is_same<Real_, double>::value && NT_ > 512;
+        static constexpr bool IMUL = IEMU && tag_no_fma(TAG_);
         static constexpr int CONV = CONV_, ORDER = ORDER_;
         static constexpr bool STRETCH = STRETCH_;
         static constexpr int TX = TX_, TY = TY_, TZ = TZ_, NT = NT_;
@@ -215,8 +216,15 @@ namespace gbns
     // fast quotient (within 2 ulp for |b| in [2^-126, 2^126], which holds for
     // every divisor below: gas constants, temperatures, densities and the
     // Ducros sensor's denominator)
-    __device__ __forceinline__ double pdiv(double a, double b) { return a/b; }
-    __device__ __forceinline__ float  pdiv(float a, float b)   { return __fdividef(a, b); }
+    // (IM: FP64 on the integer pipes, ddiv_int, the same bits)
+    template <bool IM = false>
+    __device__ __forceinline__ double pdiv(double a, double b)
+    {
+        if constexpr (IM) return ddiv_int(a, b);
+        else return a/b;
+    }
+    template <bool IM = false>
+    __device__ __forceinline__ float pdiv(float a, float b) { return __fdividef(a, b); }
     __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
     __device__ __forceinline__ float  dev_sqrt(float x)  { return sqrtf(x); }
     __device__ __forceinline__ double dev_pow(double x, double y) { return pow(x, y); }
@@ -227,7 +235,7 @@ namespace gbns
     // fweno_t per-point quantities (convective.h:360-376, 458-467): rho,
     // h = rho (|u| + a)/2 (the Rusanov speed times rho/2) and the total
     // specific energy e.
-    template <class Real>
+    template <class Real, bool IM = false>
     __device__ __forceinline__ void fweno_derive(const SchemeR<Real>& S, Real p, Real T, Real u, Real v, Real w,
                                                  Real& rho_o, Real& h_o, Real& e_o)
     {
@@ -237,14 +245,14 @@ namespace gbns
         h += w*w;
         h = dev_sqrt(h);
         h += dev_sqrt(r*S.gamma);
-        const Real rho = pdiv(p, r);
+        const Real rho = pdiv<IM>(p, r);
         h *= rho;
         h *= Real(0.5);
         Real e = u*u;
         e += v*v;
         e += w*w;
         e *= Real(0.5);
-        e += pdiv(S.R*T, S.gm1);
+        e += pdiv<IM>(S.R*T, S.gm1);
         rho_o = rho; h_o = h; e_o = e;
     }
 
@@ -259,21 +267,21 @@ namespace gbns
                       (Cfg::CONV == GBNS_CONV_HYBRID && Cfg::SPLIT))
         {
             // convective.h:130-131 / 80-84 (the hybrid's fweno half reads the split cache)
-            const Real rho = pdiv(p, S.R*T);
+            const Real rho = pdiv<Cfg::IEMU>(p, S.R*T);
             der[0*Cfg::BOXN + c] = rho;
-            der[1*Cfg::BOXN + c] = pdiv(p, rho*S.gm1);
+            der[1*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, rho*S.gm1);
         }
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5 ||
                            Cfg::CONV == GBNS_CONV_HYBRID)
         {
             Real rho, h, e;
-            fweno_derive<Real>(S, p, T, u, v, w, rho, h, e);
+            fweno_derive<Real, Cfg::IEMU>(S, p, T, u, v, w, rho, h, e);
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = h;
             der[2*Cfg::BOXN + c] = e;
             // cent_keep's e (convective.h:131); its rho = p/(R*T) is the
             // same rounding as fweno's p/r above
-            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv(p, rho*S.gm1);
+            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, rho*S.gm1);
         }
     }
 
@@ -525,7 +533,7 @@ namespace gbns
             const int x = lx - (D == 0 ? HC : 0), y = ly - (D == 1 ? HC : 0), z = lz - (D == 2 ? HC : 0);
             const int c = (z + H)*Cfg::SZ + (y + H)*Cfg::SY + (x + H + shift);
             double rho, hsr, engy;
-            fweno_derive<double>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
+            fweno_derive<double, Cfg::IEMU>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
             store(l, c, y, rho, hsr, engy);
         }
     }
@@ -672,8 +680,8 @@ namespace gbns
         const Weno5Side d = weno5_nd<IM>(da, db, dc, dd, de);
         const double den = wmul<IM>(6.0, wmul<IM>(u.D, d.D));
         if (den < 1.0e300)
-            return fma(u.N, d.D, wmul<IM>(d.N, u.D))/den;
-        return u.N/(6.0*u.D) + d.N/(6.0*d.D);
+            return pdiv<IM>(fma(u.N, d.D, wmul<IM>(d.N, u.D)), den);
+        return pdiv<IM>(u.N, 6.0*u.D) + pdiv<IM>(d.N, 6.0*d.D);
     }
 
     template <class Cfg, int D>
@@ -704,7 +712,7 @@ namespace gbns
                 }
             }
             if constexpr (sizeof(Real) == 8)
-                out[eq] = weno5_pair<Cfg::IMUL_WENO>(up[0], up[1], up[2], up[3], up[4], dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
+                out[eq] = weno5_pair<Cfg::IEMU>(up[0], up[1], up[2], up[3], up[4], dn[5], dn[4], dn[3], dn[2], dn[1], S.smooth);
             else
             {
                 const float2 f = weno5_side2(make_float2(up[0], dn[5]), make_float2(up[1], dn[4]),
@@ -730,8 +738,8 @@ namespace gbns
         const Real delta_T = Tl - Tr;
         const Real pavg = ppow2<Cfg, -1>(pl + pr);
         const Real Tavg = ppow2<Cfg, -1>(Tl + Tr);
-        const Real inv_RT = pdiv(Real(1.0), pmul<Cfg>(S.R_avg, Tavg));
-        const Real p_inv_rt2 = pdiv(pmul<Cfg>(pavg, inv_RT), Tavg);
+        const Real inv_RT = pdiv<Cfg::IEMU>(Real(1.0), pmul<Cfg>(S.R_avg, Tavg));
+        const Real p_inv_rt2 = pdiv<Cfg::IEMU>(pmul<Cfg>(pavg, inv_RT), Tavg);
         const Real k = ppow2<Cfg, -1>(pmul<Cfg>(ul, ur) + pmul<Cfg>(vl, vr) + pmul<Cfg>(wl, wr));
         const Real u = ppow2<Cfg, -1>(ul + ur);
         const Real v = ppow2<Cfg, -1>(vl + vr);
@@ -782,7 +790,7 @@ namespace gbns
     }
 
     // state_sensor::ducros_t::get_sensor (state_sensor.h:21-43)
-    template <class Real>
+    template <class Real, bool IM = false>
     __device__ __forceinline__ Real ducros_sensor(const Real (&g)[3][4], Real epsilon)
     {
         Real theta_sq = g[0][1] + g[1][2] + g[2][3];
@@ -791,7 +799,7 @@ namespace gbns
         const Real vort1 = g[2][1] - g[0][3];
         const Real vort2 = g[0][2] - g[1][1];
         const Real vort_sq = vort0*vort0 + vort1*vort1 + vort2*vort2;
-        return pdiv(theta_sq, theta_sq + vort_sq + epsilon);
+        return pdiv<IM>(theta_sq, theta_sq + vort_sq + epsilon);
     }
 
     // visc_lr::operator() (viscous.h:39-79) with info::value / info::gradient
@@ -815,14 +823,14 @@ namespace gbns
         }
         else if (S.law == GBNS_LAW_POWER)
         {
-            visc = pmul<Cfg>(S.mu, dev_pow(pdiv(qf[1], S.T_ref), S.power));
+            visc = pmul<Cfg>(S.mu, dev_pow(pdiv<Cfg::IEMU>(qf[1], S.T_ref), S.power));
             visc2 = pmul<Cfg>(Real(-0.66666666667), visc);
-            dfs = pdiv(visc, S.prandtl);
+            dfs = pdiv<Cfg::IEMU>(visc, S.prandtl);
         }
         else
         {
-            const Real x = pdiv(qf[1], S.T_ref);
-            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt(x))), pdiv(S.tref_plus_s, qf[1] + S.S));
+            const Real x = pdiv<Cfg::IEMU>(qf[1], S.T_ref);
+            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt(x))), pdiv<Cfg::IEMU>(S.tref_plus_s, qf[1] + S.S));
             visc2 = pmul<Cfg>(visc, Real(-2.0/3.0));
             dfs = pmul<Cfg>(visc, S.inv_pr);
         }
@@ -873,7 +881,7 @@ namespace gbns
             {
                 face_gradient<Cfg, D>(V, rc, inv, im, grad);
                 have_grad = true;
-                blend = ducros_sensor<Real>(grad, S.hyb_param);
+                blend = ducros_sensor<Real, Cfg::IEMU>(grad, S.hyb_param);
             }
             conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
             conv_fweno<Cfg, D>(V, S, rc, lr, nD, t1);
@@ -894,7 +902,7 @@ namespace gbns
         // the gradient is not live across it; ducros_t needs the gradient first.
         if (hd && !ducros) diss_pressure<Cfg, D>(V, S, rc, S.sens, t1);
         if ((hv || ducros) && !have_grad) face_gradient<Cfg, D>(V, rc, inv, im, grad);
-        if (ducros) diss_pressure<Cfg, D>(V, S, rc, ducros_sensor<Real>(grad, S.sens), t1);
+        if (ducros) diss_pressure<Cfg, D>(V, S, rc, ducros_sensor<Real, Cfg::IEMU>(grad, S.sens), t1);
         if (hv) visc_lr<Cfg, D>(V, S, rc, nD, grad, t2);
         #pragma unroll
         for (int v = 0; v < 5; ++v)
@@ -1246,7 +1254,7 @@ namespace gbns
                 if (cc >= Cfg::NCELL) break;
                 const int cx = cc % TX, cy = (cc / TX) % TY, cz = cc / (TX*TY);
                 const int c = (cz + H)*Cfg::SZ + (cy + H)*Cfg::SY + (cx + H + shift);
-                fweno_derive<double>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
+                fweno_derive<double, Cfg::IEMU>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
             }
         }
 

@@ -1,4 +1,4 @@
-// IEEE 754 binary64 multiplication computed on the integer pipes.
+// IEEE 754 binary64 multiplication and division computed on the integer pipes.
 //
 // GB300 executes FP64 at 1/64 of its FP32 rate (two FP64 lanes per SM and
 // clock) while its integer multiply-add and logic pipes are mostly idle in the
@@ -45,6 +45,68 @@ namespace gbns
         const uint32_t up = (uint32_t)(rem > 0x400u) | ((uint32_t)(rem == 0x400u) & ((uint32_t)(lo != 0) | (uint32_t)(m & 1)));
         const uint64_t r = ((ua ^ ub) & SGN) | ((((uint64_t)(e - 1)) << 52) + m + up);
         return __longlong_as_double((long long)r);
+    }
+
+    // a/b correctly rounded (to nearest even), the same bits as the hardware
+    // division, on the integer pipes: the quotient of the 53-bit significands
+    // to 54 bits plus remainder, from an FP32 reciprocal seed (the fast
+    // reciprocal of the divisor's top 24 bits, relative error ~2^-21) refined
+    // twice by the exact remainder (R = N - Q*mb in 128-bit integers,
+    // Q += R*Y/2^115 with Y ~ 2^115/mb: each step multiplies the error by the
+    // seed's), then corrected to 0 <= R < mb; round bit and sticky (R != 0)
+    // give the rounding.  The classic quotient refinement by remainders
+    // (Newton-Raphson on the reciprocal, Markstein-style final correction with
+    // the exact remainder), done in fixed point.  Operands outside the normal
+    // range and quotients near the ends of it take the hardware division.
+    __device__ __forceinline__ double ddiv_int(double a, double b)
+    {
+        constexpr uint64_t M52 = 0x000FFFFFFFFFFFFFull, H53 = 0x0010000000000000ull, SGN = 0x8000000000000000ull;
+        const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
+        const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
+        int e = (int)ea - (int)eb + 1023;
+        if (ea - 1u >= 2046u || eb - 1u >= 2046u || (unsigned)(e - 2) >= 2044u) return a/b;
+        uint64_t ma = (ua & M52) | H53;
+        const uint64_t mb = (ub & M52) | H53;
+        if (ma < mb) { ma <<= 1; e -= 1; }
+        // ma/mb in [1, 2): Q = floor(N/mb) in [2^53, 2^54) with N = ma*2^53
+        const uint64_t Nhi = ma >> 11, Nlo = ma << 53;
+        // the divisor's top 24 bits as a float in [2^23, 2^24) (biased exponent 150)
+        const float fb = __uint_as_float((150u << 23) | ((uint32_t)(mb >> 29) & 0x7fffffu));
+        const uint32_t rb = __float_as_uint(__fdividef(1.0f, fb));
+        const int rexp = (int)((rb >> 23) & 0xffu) - 127;                  // -24 or -23
+        const uint64_t Y = (uint64_t)((rb & 0x7fffffu) | 0x800000u) << (63 + rexp);   // ~2^115/mb < 2^63
+        uint64_t Q = __umul64hi(ma << 2, Y);                               // ~ma*2^53/mb
+        #pragma unroll
+        for (int it = 0; it < 2; ++it)
+        {
+            const uint64_t Plo = Q*mb, Phi = __umul64hi(Q, mb);
+            uint64_t Rlo = Nlo - Plo;
+            uint64_t Rhi = Nhi - Phi - (uint64_t)(Nlo < Plo);
+            const bool neg = (int64_t)Rhi < 0;
+            if (neg) { Rlo = ~Rlo + 1; Rhi = ~Rhi + (uint64_t)(Rlo == 0); }
+            // |R| < 2^90: its top 64 bits |R| >> 26 times Y, over 2^89
+            const uint64_t d = __umul64hi((Rhi << 38) | (Rlo >> 26), Y) >> 25;
+            Q = neg ? Q - d : Q + d;
+        }
+        const uint64_t Plo = Q*mb, Phi = __umul64hi(Q, mb);
+        uint64_t Rlo = Nlo - Plo;
+        uint64_t Rhi = Nhi - Phi - (uint64_t)(Nlo < Plo);
+        for (int k = 0; k < 4 && (int64_t)Rhi < 0; ++k)
+        {
+            Q -= 1;
+            const uint64_t t = Rlo + mb;
+            Rhi += (uint64_t)(t < Rlo);
+            Rlo = t;
+        }
+        for (int k = 0; k < 4 && (Rhi != 0 || Rlo >= mb); ++k)
+        {
+            Q += 1;
+            Rhi -= (uint64_t)(Rlo < mb);
+            Rlo -= mb;
+        }
+        const uint64_t m = Q >> 1;
+        const uint32_t up = (uint32_t)(Q & 1) & ((uint32_t)(Rlo != 0) | (uint32_t)(m & 1));
+        return __longlong_as_double((long long)(((ua ^ ub) & SGN) | ((((uint64_t)(e - 1)) << 52) + m + up)));
     }
 
     // x * 2^E (E < 0), the same bits as the hardware multiply by the constant:

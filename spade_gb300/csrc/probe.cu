@@ -134,7 +134,9 @@ namespace gbns
             const double h2 = __dmul_rn(a, 0.25), e2 = dmul_pow2<-2>(a);
             const bool same1 = __double_as_longlong(h1) == __double_as_longlong(e1) || (h1 != h1 && e1 != e1);
             const bool same2 = __double_as_longlong(h2) == __double_as_longlong(e2) || (h2 != h2 && e2 != e2);
-            if (!same || !same1 || !same2) atomicAdd(bad, 1ull);
+            const double hq = __ddiv_rn(a, b), eq = ddiv_int(a, b);
+            const bool same3 = __double_as_longlong(hq) == __double_as_longlong(eq) || (hq != hq && eq != eq);
+            if (!same || !same1 || !same2 || !same3) atomicAdd(bad, 1ull);
         }
     }
 }

@@ -1,4 +1,4 @@
-// Host check of the integer FP64 multiply and power-of-two scaling
+// Host check of the integer FP64 multiply, power-of-two scaling and division
 // (spade_gb300/csrc/fp64_int.cuh):
 // the header is compiled for the CPU with its CUDA intrinsics replaced by
 // portable equivalents and compared bit for bit with the host's IEEE
@@ -14,6 +14,13 @@ static inline long long __double_as_longlong(double d) { long long x; std::memcp
 static inline double __longlong_as_double(long long x) { double d; std::memcpy(&d, &x, 8); return d; }
 static inline uint64_t __umul64hi(uint64_t a, uint64_t b) { return (uint64_t)(((unsigned __int128)a*b) >> 64); }
 static inline double __dmul_rn(double a, double b) { volatile double r = a*b; return r; }
+static inline float __uint_as_float(uint32_t x) { float f; std::memcpy(&f, &x, 4); return f; }
+static inline uint32_t __float_as_uint(float f) { uint32_t x; std::memcpy(&x, &f, 4); return x; }
+// the device's fast quotient is within 2 ulp; the host stands in with the
+// correctly rounded one perturbed by 2^-19 both ways (the refinement must
+// absorb either)
+static float g_seed_scale = 1.0f;
+static inline float __fdividef(float a, float b) { volatile float q = (a/b)*g_seed_scale; return q; }
 #include "fp64_int.cuh"
 
 static uint64_t mix64(uint64_t x)
@@ -63,6 +70,25 @@ int main(int argc, char** argv)
         {
             if (!bad) std::printf("first pow2 mismatch: a=%a hw=%a,%a int=%a,%a\n", a, h1, h2, e1, e2);
             ++bad;
+        }
+    }
+    // division, with the reciprocal seed exact and off by 2^-19 either way
+    const float scales[3] = {1.0f, 1.0f + 0x1p-19f, 1.0f - 0x1p-19f};
+    for (float sc : scales)
+    {
+        g_seed_scale = sc;
+        for (uint64_t k = 0; k < n/4; ++k)
+        {
+            const double a = __longlong_as_double((long long)operand(k, 0));
+            double b = __longlong_as_double((long long)operand(k, 1));
+            if ((k & 15) == 5) b = __longlong_as_double(__double_as_longlong(a) ^ (long long)(mix64(k) & 0xF));
+            volatile double hv = a/b;
+            const double h = hv, e = gbns::ddiv_int(a, b);
+            if (__double_as_longlong(h) != __double_as_longlong(e) && !(h != h && e != e))
+            {
+                if (!bad) std::printf("first division mismatch: a=%a b=%a hw=%a int=%a\n", a, b, h, e);
+                ++bad;
+            }
         }
     }
     std::printf("pairs %llu mismatches %llu\n", (unsigned long long)n, (unsigned long long)bad);

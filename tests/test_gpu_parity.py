@@ -493,10 +493,10 @@ def test_fp32_flux_weno_weights_do_not_overflow(conv):
 
 @pytest.mark.gpu
 def test_integer_pipe_multiply_matches_hardware():
-    """The FP64 multiply the flux kernels run on the integer pipes returns the
-    hardware multiply's bits on 2^26 generated pairs (all bit patterns,
-    exponent bands at the normal-range edges, exact products and ties, zeros,
-    subnormals, infinities, NaNs)."""
+    """The FP64 multiply, x/2, x/4 and division the flux kernels run on the
+    integer pipes return the hardware operations' bits on 2^26 generated
+    pairs (all bit patterns, exponent bands at the normal-range edges, exact
+    products and ties, zeros, subnormals, infinities, NaNs)."""
     bad = ctypes.c_uint64(123)
     _native.check(lib().gbns_selftest_dmul_int(1 << 26, 7, ctypes.byref(bad), stream()))
     assert bad.value == 0
