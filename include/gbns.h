@@ -252,9 +252,9 @@ int gbns_measure_fma_rate(int fp64, double* flops_per_s, void* stream);
  * context stays usable.  No counterpart in the reference. */
 int gbns_selftest_wait_timeout(int* status, void* stream);
 
-/* Checks the integer-pipe FP64 multiply, power-of-two scalings (x/2, x/4)
- * and division the flux kernels use against the hardware multiply and
- * division on `npairs` generated operand
+/* Checks the integer-pipe FP64 multiply, power-of-two scalings (x/2, x/4),
+ * division and square root the flux kernels use against the hardware
+ * operations on `npairs` generated operand
  * pairs (all bit patterns, range edges, exact products and ties, zeros,
  * subnormals, infinities, NaNs); *mismatches = pairs whose bits differ (NaN
  * results compare equal).  Synchronises `stream`.  No reference counterpart. */

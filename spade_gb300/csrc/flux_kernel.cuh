@@ -225,8 +225,14 @@ namespace gbns
     }
     template <bool IM = false>
     __device__ __forceinline__ float pdiv(float a, float b) { return __fdividef(a, b); }
-    __device__ __forceinline__ double dev_sqrt(double x) { return sqrt(x); }
-    __device__ __forceinline__ float  dev_sqrt(float x)  { return sqrtf(x); }
+    template <bool IM = false>
+    __device__ __forceinline__ double dev_sqrt(double x)
+    {
+        if constexpr (IM) return dsqrt_int(x);
+        else return sqrt(x);
+    }
+    template <bool IM = false>
+    __device__ __forceinline__ float dev_sqrt(float x) { return sqrtf(x); }
     __device__ __forceinline__ double dev_pow(double x, double y) { return pow(x, y); }
     __device__ __forceinline__ float  dev_pow(float x, float y)   { return powf(x, y); }
 
@@ -243,8 +249,8 @@ namespace gbns
         Real h = u*u;
         h += v*v;
         h += w*w;
-        h = dev_sqrt(h);
-        h += dev_sqrt(r*S.gamma);
+        h = dev_sqrt<IM>(h);
+        h += dev_sqrt<IM>(r*S.gamma);
         const Real rho = pdiv<IM>(p, r);
         h *= rho;
         h *= Real(0.5);
@@ -830,7 +836,7 @@ namespace gbns
         else
         {
             const Real x = pdiv<Cfg::IEMU>(qf[1], S.T_ref);
-            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt(x))), pdiv<Cfg::IEMU>(S.tref_plus_s, qf[1] + S.S));
+            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt<Cfg::IEMU>(x))), pdiv<Cfg::IEMU>(S.tref_plus_s, qf[1] + S.S));
             visc2 = pmul<Cfg>(visc, Real(-2.0/3.0));
             dfs = pmul<Cfg>(visc, S.inv_pr);
         }

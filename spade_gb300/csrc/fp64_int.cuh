@@ -1,4 +1,5 @@
-// IEEE 754 binary64 multiplication and division computed on the integer pipes.
+// IEEE 754 binary64 multiplication, division and square root computed on the
+// integer pipes.
 //
 // GB300 executes FP64 at 1/64 of its FP32 rate (two FP64 lanes per SM and
 // clock) while its integer multiply-add and logic pipes are mostly idle in the
@@ -107,6 +108,70 @@ namespace gbns
         const uint64_t m = Q >> 1;
         const uint32_t up = (uint32_t)(Q & 1) & ((uint32_t)(Rlo != 0) | (uint32_t)(m & 1));
         return __longlong_as_double((long long)(((ua ^ ub) & SGN) | ((((uint64_t)(e - 1)) << 52) + m + up)));
+    }
+
+    // sqrt(x) correctly rounded, the same bits as the hardware square root, on
+    // the integer pipes: S = floor(sqrt(M)) to 54 bits for the significand
+    // scaled to M in [2^106, 2^108) (even exponent), from an FP32 seed (the
+    // fast reciprocal square root r of M's top 24 bits t, sqrt(t) ~ t*r)
+    // refined twice by the exact remainder (R = M - S^2, S += R/(2S) with
+    // 1/(2S) from r: Newton's iteration for the square root in fixed point),
+    // then corrected to 0 <= R <= 2S; round bit and sticky (R != 0) give the
+    // rounding.  Zero, negative, subnormal, infinite and NaN operands take
+    // the hardware square root.
+    __device__ __forceinline__ double dsqrt_int(double x)
+    {
+        constexpr uint64_t M52 = 0x000FFFFFFFFFFFFFull, H53 = 0x0010000000000000ull;
+        const uint64_t ux = (uint64_t)__double_as_longlong(x);
+        const uint32_t ex = (uint32_t)(ux >> 52);            // the sign bit makes negatives fail the range test
+        if (ex - 1u >= 2046u) return __dsqrt_rn(x);
+        const int E = (int)ex - 1023;
+        const int p = E & 1;
+        const uint64_t mx = (ux & M52) | H53;
+        const uint64_t Mhi = mx >> (10 - p), Mlo = mx << (54 + p);   // M = mx*2^(54+p)
+        // t = M >> 84 in [2^22, 2^24) as a float (exact), r ~ t^-1/2, sqrt(t) ~ t*r
+        const uint32_t t = (uint32_t)(Mhi >> 20);
+        const uint32_t tm = t >> 23;                                  // 1 if t >= 2^23
+        const float tf = __uint_as_float(((149u + tm) << 23) | ((t << (1 - tm)) & 0x7fffffu));
+        const float r = rsqrtf(tf);
+        const uint32_t sb = __float_as_uint(tf*r);
+        const uint32_t rb = __float_as_uint(r);
+        // S0 = sqrt(t)*2^42; Yr = r*2^74 ~ 2^116/S
+        uint64_t S = (uint64_t)((sb & 0x7fffffu) | 0x800000u) << ((int)((sb >> 23) & 0xffu) - 127 + 19);
+        const uint64_t Yr = (uint64_t)((rb & 0x7fffffu) | 0x800000u) << ((int)((rb >> 23) & 0xffu) - 127 + 51);
+        #pragma unroll
+        for (int it = 0; it < 2; ++it)
+        {
+            const uint64_t Plo = S*S, Phi = __umul64hi(S, S);
+            uint64_t Rlo = Mlo - Plo;
+            uint64_t Rhi = Mhi - Phi - (uint64_t)(Mlo < Plo);
+            const bool neg = (int64_t)Rhi < 0;
+            if (neg) { Rlo = ~Rlo + 1; Rhi = ~Rhi + (uint64_t)(Rlo == 0); }
+            // |R| < 2^94: |R|/(2S) ~ (|R| >> 30)*Yr/2^87
+            const uint64_t d = __umul64hi((Rhi << 34) | (Rlo >> 30), Yr) >> 23;
+            S = neg ? S - d : S + d;
+        }
+        const uint64_t Plo = S*S, Phi = __umul64hi(S, S);
+        uint64_t Rlo = Mlo - Plo;
+        uint64_t Rhi = Mhi - Phi - (uint64_t)(Mlo < Plo);
+        for (int k = 0; k < 4 && (int64_t)Rhi < 0; ++k)
+        {
+            const uint64_t add = 2*S - 1;                             // (S-1)^2 = S^2 - (2S - 1)
+            S -= 1;
+            const uint64_t t2 = Rlo + add;
+            Rhi += (uint64_t)(t2 < Rlo);
+            Rlo = t2;
+        }
+        for (int k = 0; k < 4 && (Rhi != 0 || Rlo > 2*S); ++k)
+        {
+            const uint64_t sub = 2*S + 1;                             // (S+1)^2 = S^2 + (2S + 1)
+            S += 1;
+            Rhi -= (uint64_t)(Rlo < sub);
+            Rlo -= sub;
+        }
+        const uint64_t m = S >> 1;
+        const uint32_t up = (uint32_t)(S & 1) & ((uint32_t)(Rlo != 0 || Rhi != 0) | (uint32_t)(m & 1));
+        return __longlong_as_double((long long)((((uint64_t)((E - p)/2 + 1022)) << 52) + m + up));
     }
 
     // x * 2^E (E < 0), the same bits as the hardware multiply by the constant:

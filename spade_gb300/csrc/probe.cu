@@ -136,7 +136,9 @@ namespace gbns
             const bool same2 = __double_as_longlong(h2) == __double_as_longlong(e2) || (h2 != h2 && e2 != e2);
             const double hq = __ddiv_rn(a, b), eq = ddiv_int(a, b);
             const bool same3 = __double_as_longlong(hq) == __double_as_longlong(eq) || (hq != hq && eq != eq);
-            if (!same || !same1 || !same2 || !same3) atomicAdd(bad, 1ull);
+            const double hs = __dsqrt_rn(a), es = dsqrt_int(a);
+            const bool same4 = __double_as_longlong(hs) == __double_as_longlong(es) || (hs != hs && es != es);
+            if (!same || !same1 || !same2 || !same3 || !same4) atomicAdd(bad, 1ull);
         }
     }
 }

@@ -1,4 +1,5 @@
-// Host check of the integer FP64 multiply, power-of-two scaling and division
+// Host check of the integer FP64 multiply, power-of-two scaling, division and
+// square root
 // (spade_gb300/csrc/fp64_int.cuh):
 // the header is compiled for the CPU with its CUDA intrinsics replaced by
 // portable equivalents and compared bit for bit with the host's IEEE
@@ -7,6 +8,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <cmath>
 
 #define __device__
 #define __forceinline__ inline
@@ -21,6 +23,8 @@ static inline uint32_t __float_as_uint(float f) { uint32_t x; std::memcpy(&x, &f
 // absorb either)
 static float g_seed_scale = 1.0f;
 static inline float __fdividef(float a, float b) { volatile float q = (a/b)*g_seed_scale; return q; }
+static inline float rsqrtf(float x) { volatile float r = (1.0f/std::sqrt(x))*g_seed_scale; return r; }
+static inline double __dsqrt_rn(double x) { volatile double r = std::sqrt(x); return r; }
 #include "fp64_int.cuh"
 
 static uint64_t mix64(uint64_t x)
@@ -87,6 +91,12 @@ int main(int argc, char** argv)
             if (__double_as_longlong(h) != __double_as_longlong(e) && !(h != h && e != e))
             {
                 if (!bad) std::printf("first division mismatch: a=%a b=%a hw=%a int=%a\n", a, b, h, e);
+                ++bad;
+            }
+            const double hs = __dsqrt_rn(a), es = gbns::dsqrt_int(a);
+            if (__double_as_longlong(hs) != __double_as_longlong(es) && !(hs != hs && es != es))
+            {
+                if (!bad) std::printf("first sqrt mismatch: a=%a hw=%a int=%a\n", a, hs, es);
                 ++bad;
             }
         }

@@ -493,8 +493,8 @@ def test_fp32_flux_weno_weights_do_not_overflow(conv):
 
 @pytest.mark.gpu
 def test_integer_pipe_multiply_matches_hardware():
-    """The FP64 multiply, x/2, x/4 and division the flux kernels run on the
-    integer pipes return the hardware operations' bits on 2^26 generated
+    """The FP64 multiply, x/2, x/4, division and square root the flux kernels
+    run on the integer pipes return the hardware operations' bits on 2^26 generated
     pairs (all bit patterns, exponent bands at the normal-range edges, exact
     products and ties, zeros, subnormals, infinities, NaNs)."""
     bad = ctypes.c_uint64(123)
