@@ -633,7 +633,8 @@ def main():
                      "alg_bytes_per_cell": ALG_BYTES_FUSED, "avg_launch_ms": r["flux_avg_ms"],
                      "share_of_step": r["flux_share"]},
         "fp64_roof": {"fma_rate_tflops": r["fp64_fma_flops"] / 1e12, "fp32_fma_rate_tflops": r["fp32_fma_flops"] / 1e12,
-                      "note": "measured DFMA/FFMA chains on this GPU; the FP64 kernel is bound by the FP64 pipe",
+                      "note": "measured DFMA/FFMA chains on this GPU; the FP64 kernel is bound by the FP64 unit, with its "
+                              "products, quotients and square roots computed exactly on the integer pipes",
                       "fp64_pipe_active_frac_ncu": _profile_value("fp64_pipe_active_frac"),
                       "pipe_source": "profiles/flux_div_rk_channel_fp64.md (sm__pipe_fp64_cycles_active, 2.1M-cell capture)"},
         "step_bytes": {"alg_bytes_per_cell_step": ALG_BYTES_STEP,
