@@ -178,6 +178,17 @@ int gbns_array_size(const gbns_grid_desc* grid, size_t* count);
 int gbns_flux_div(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                   const double* prims, double* rhs, int increment, void* stream);
 
+/* gbns_flux_div for prims and rhs in host memory (a grid_array on
+ * device::cpu): both arrays are staged through device buffers the library
+ * keeps per device and reuses across calls, the flux divergence runs on the
+ * GPU (the same kernels and bits as gbns_flux_div) and rhs, ghost layers
+ * included, is copied back.  Returns when rhs holds the result (synchronises
+ * `stream`); calls on the host path are serialised.  Pinned host memory
+ * copies at the full host link speed.  No reference counterpart (the
+ * reference runs device::cpu arrays on the CPU). */
+int gbns_flux_div_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                       const double* host_prims, double* host_rhs, int increment, void* stream);
+
 /* Ghost fill: periodic / inter-block exchange of interior donor cells into
  * ghost layers, then wall mirror fill on non-periodic faces.
  * Replaces arr_exchange_t::exchange (grid/make_exchange.h:111-410, single

@@ -16,9 +16,11 @@
  * it is the more constrained candidate.  It lowers the composed functor type
  * at compile time into a gbns_scheme_desc (static_assert on anything the
  * kernels do not implement: there is no CPU fallback), the grid_array into a
- * gbns_grid_desc, calls gbns_flux_div on the arrays' device storage, and then
- * synchronises and throws except::sp_exception on failure, like the
- * reference's dispatch (dispatch/execute.h:84-96).
+ * gbns_grid_desc, calls gbns_flux_div on the arrays' device storage
+ * (device::gpu) or gbns_flux_div_host on their host storage (device::cpu,
+ * staged through the GPU), and then synchronises and throws
+ * except::sp_exception on failure, like the reference's dispatch
+ * (dispatch/execute.h:84-96).
  *
  * Lowered functors: convective::cent_keep_scheme_t<gas, 2|4|6|8>,
  * convective::totani_lr, convective::fweno_t<gas, smooth>,
@@ -348,10 +350,20 @@ namespace spade::pde_algs
 #ifdef GBNS_DROPIN_HOOK
         const int rc = GBNS_DROPIN_HOOK(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0);
 #else
-        static_assert(device::is_gpu<typename sol_arr_t::device_type> && device::is_gpu<typename rhs_arr_t::device_type>,
-                      "the gb300 flux_div runs on device::gpu arrays");
-        int rc = gbns_flux_div(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0, nullptr);
-        if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+        constexpr bool on_gpu = device::is_gpu<typename sol_arr_t::device_type>;
+        static_assert(on_gpu == device::is_gpu<typename rhs_arr_t::device_type>,
+                      "the gb300 flux_div takes prims and rhs on the same device kind");
+        int rc = GBNS_OK;
+        if constexpr (on_gpu)
+        {
+            rc = gbns_flux_div(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0, nullptr);
+            if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+        }
+        else
+        {
+            // device::cpu arrays: staged through the GPU (synchronous)
+            rc = gbns_flux_div_host(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0, nullptr);
+        }
 #endif
         if (rc != GBNS_OK)
         {

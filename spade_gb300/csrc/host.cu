@@ -366,6 +366,50 @@ extern "C"
                                scheme->tile_variant);
     }
 
+    int gbns_flux_div_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                           const double* host_prims, double* host_rhs, int increment, void* stream)
+    {
+        using namespace gbns;
+        if (!host_prims || !host_rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
+        if (host_prims == host_rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
+        size_t count = 0;
+        int rc = gbns_array_size(grid, &count);
+        if (rc) return rc;
+        int dev = 0;
+        rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+        if (rc) return rc;
+        // one pair of staging arrays per device, grown on demand; the lock
+        // covers the whole call so concurrent host-path calls never share them
+        struct Staging { double* q = nullptr; double* r = nullptr; size_t count = 0; };
+        static std::mutex mu;
+        static Staging staging[64];
+        if (dev < 0 || dev >= 64) return set_error(GBNS_ERR_UNSUPPORTED, "device index above 63");
+        std::lock_guard<std::mutex> lk(mu);
+        Staging& sg = staging[dev];
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        if (sg.count < count)
+        {
+            rc = check_cuda(cudaStreamSynchronize(st), "host-path sync");
+            if (rc) return rc;
+            if (sg.q) cudaFree(sg.q);
+            if (sg.r) cudaFree(sg.r);
+            sg.q = sg.r = nullptr;
+            sg.count = 0;
+            rc = check_cuda(cudaMalloc(&sg.q, count*sizeof(double)), "host-path staging (prims)");
+            if (!rc) rc = check_cuda(cudaMalloc(&sg.r, count*sizeof(double)), "host-path staging (rhs)");
+            if (rc) return rc;
+            sg.count = count;
+        }
+        const size_t bytes = count*sizeof(double);
+        rc = check_cuda(cudaMemcpyAsync(sg.q, host_prims, bytes, cudaMemcpyHostToDevice, st), "prims to device");
+        // rhs goes down in both modes: overwrite leaves its ghost layers as they were
+        if (!rc) rc = check_cuda(cudaMemcpyAsync(sg.r, host_rhs, bytes, cudaMemcpyHostToDevice, st), "rhs to device");
+        if (!rc) rc = gbns_flux_div(grid, scheme, sg.q, sg.r, increment, stream);
+        if (!rc) rc = check_cuda(cudaMemcpyAsync(host_rhs, sg.r, bytes, cudaMemcpyDeviceToHost, st), "rhs to host");
+        if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "host-path sync");
+        return rc;
+    }
+
     int gbns_flux_div_variant(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                               const double* prims, double* rhs, int increment, int variant, void* stream)
     {

@@ -64,3 +64,14 @@ def test_dropin_overload_and_lowering():
     assert bf[0][1:7] == ["0", "0", "1", "1", "0", "0"]
     assert bf[0][bf[0].index("conv") + 1] == "1" and bf[0][bf[0].index("order") + 1] == "4"
     assert bf[0][bf[0].index("visc") + 1] == "1" and bf[0][bf[0].index("ng") + 1] == "3"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+def test_dropin_host_array_path_compiles():
+    """Without the test hooks, the gb300 flux_div overload compiles for
+    device::cpu grid_arrays (the host path through gbns_flux_div_host)."""
+    cmd = ["g++", "-std=c++20", "-fsyntax-only", "-I" + REF_SRC, "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(ROOT, "oracle", "mpi_stub"), "-I" + CUDA_INC,
+           os.path.join(ROOT, "tests", "cpp", "dropin_host_arrays.cc")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]

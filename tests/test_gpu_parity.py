@@ -108,6 +108,27 @@ def test_flux_div_fp64_fma_within_tolerance(name):
     assert normwise(interior(r, fg["ng"]), g["rhs_" + name]) <= TOL64
 
 
+@pytest.mark.parametrize("name", ["ck2_visc", "fweno_diss_visc", "totani_visc"])
+@pytest.mark.parametrize("increment", [False, True])
+def test_flux_div_host_arrays_equal_reference(name, increment):
+    """gbns_flux_div_host on numpy (host) arrays, staged through the GPU:
+    the reference's own result bit for bit, and the ghost layers of rhs kept
+    as they were."""
+    g = load("flux_div_ref.npz")
+    fg = FLUX_GRID
+    grid = _abi.grid_desc(fg["nblk"], fg["ncell"], fg["ng"], fg["bounds"])
+    q = np.ascontiguousarray(g["q"])
+    rhs = np.full_like(q, 0.0) if increment else np.full_like(q, 7.25)
+    _native.check(lib().gbns_flux_div_host(grid, P.scheme(**FLUX_CASES[name][1]), q.ctypes.data, rhs.ctypes.data,
+                                           int(increment), stream()))
+    assert np.array_equal(interior(rhs, fg["ng"]), g["rhs_" + name])
+    if not increment:
+        n = fg["ng"]
+        mask = np.ones(rhs.shape[:-1], bool)
+        mask[:, n:-n, n:-n, n:-n] = False
+        assert np.all(rhs[mask] == 7.25)
+
+
 def test_flux_div_overwrite_leaves_ghost_layers():
     g = load("flux_div_ref.npz")
     fg = FLUX_GRID
