@@ -103,6 +103,41 @@ def test_flux_div_rejects_bad_scheme_before_cuda():
     assert _native.lib().gbns_flux_div(g, s, ctypes.c_void_p(16), ctypes.c_void_p(32), 0, None) == _abi.ERR_INVALID
 
 
+def test_boundary_flux_validates_before_cuda():
+    """gbns_boundary_flux: NULL flags, stretched coordinates and too few ghost
+    layers for the ghost-row face gradients are rejected before any CUDA call."""
+    import problems as P
+    L = _native.lib()
+    flags = (ctypes.c_int * 6)(1, 1, 1, 1, 1, 1)
+    g = _abi.grid_desc((1, 1, 1), (8, 8, 8), 3, (0, 1, 0, 1, 0, 1))
+    s = P.scheme(conv=_abi.CONV_WENO5, diss=1, visc=1)
+    assert L.gbns_boundary_flux(g, s, ctypes.c_void_p(16), ctypes.c_void_p(32), None, None) == _abi.ERR_INVALID
+    gs = _abi.grid_desc((1, 1, 1), (8, 8, 8), 3, (0, 1, -1, 1, 0, 1), coords=_abi.COORDS_TANH_Y, coord_param=(2.0, 0, 0, 0))
+    assert L.gbns_boundary_flux(gs, s, ctypes.c_void_p(16), ctypes.c_void_p(32), flags, None) == _abi.ERR_UNSUPPORTED
+    g1 = _abi.grid_desc((1, 1, 1), (8, 8, 8), 1, (0, 1, 0, 1, 0, 1))
+    sv = P.scheme(conv=_abi.CONV_CENT_KEEP, order=2, visc=1)
+    assert L.gbns_boundary_flux(g1, sv, ctypes.c_void_p(16), ctypes.c_void_p(32), flags, None) == _abi.ERR_INVALID
+    assert "ghost" in _native.last_error()
+
+
+def test_host_path_graph_run_and_selftest_validate_before_cuda():
+    """gbns_flux_div_host (NULL or aliased arrays), gbns_ssprk3_run (negative
+    step count, NULL work; zero steps is a no-op) and gbns_selftest_dmul_int
+    (NULL output) fail or return before any CUDA call."""
+    import problems as P
+    L = _native.lib()
+    g = _abi.grid_desc((1, 1, 1), (8, 8, 8), 2, (0, 1, 0, 1, 0, 1))
+    s = P.scheme()
+    p = ctypes.c_void_p(64)
+    assert L.gbns_flux_div_host(g, s, None, p, 1, None) == _abi.ERR_INVALID
+    assert L.gbns_flux_div_host(g, s, p, p, 1, None) == _abi.ERR_INVALID
+    bc = _abi.BcDesc()
+    assert L.gbns_ssprk3_run(g, s, bc, p, p, ctypes.c_double(1e-3), -1, None) == _abi.ERR_INVALID
+    assert L.gbns_ssprk3_run(g, s, bc, p, None, ctypes.c_double(1e-3), 1, None) == _abi.ERR_INVALID
+    assert L.gbns_ssprk3_run(g, s, bc, p, p, ctypes.c_double(1e-3), 0, None) == _abi.OK
+    assert L.gbns_selftest_dmul_int(16, 0, None, None) == _abi.ERR_INVALID
+
+
 def test_fill_ghosts_rejects_unpaired_periodic():
     g = _abi.grid_desc((1, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
     bc = _abi.bc_desc([_abi.BC_PERIODIC, _abi.BC_NONE, 0, 0, 0, 0])
