@@ -7,13 +7,12 @@ TMA copy of the FP64 box).  tune() times each variant on the caller's own
 arrays with CUDA events and caches the winner per (scheme, block shape,
 ghosts, precision, GPU) in spade_gb300/_build/autotune.json.
 """
-import ctypes
 import json
 import os
 
 import torch
 
-from . import _abi, _native
+from . import _native
 
 CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "autotune.json")
 

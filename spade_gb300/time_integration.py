@@ -13,7 +13,7 @@ from fractions import Fraction as F
 
 import torch
 
-from . import _abi, _native
+from . import _native
 from .grid import grid_array, _stream
 
 

@@ -6,7 +6,6 @@ in FP64 (no FMA contraction anywhere); FP32-flux within 1e-6 normwise (the
 FP32 face arithmetic is FMA-contracted, and the compiler may contract the
 same source differently inside the persistent kernel)."""
 import ctypes
-import math
 
 import numpy as np
 import pytest

@@ -2,14 +2,13 @@
 up, batched together, retired at their own step counts; a request whose
 state goes non-physical is evicted as failed; every completed result equals
 the same solve run alone, bit for bit."""
-import ctypes
 
 import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")
 
-from spade_gb300 import _abi, _native, serve
+from spade_gb300 import _abi, serve
 from spade_gb300.batch import batch_t
 
 pytestmark = pytest.mark.gpu
