@@ -95,7 +95,9 @@ def flux_div(prims, rhs, flux_func, traits=None, stream=None, variant=0):
     """rhs (+)= div F(prims): pde_algs::flux_div(prims, rhs, flux_func[, traits]).
     Default increment mode like the reference; pass
     make_traits(pde_algs.overwrite) to overwrite.  Asynchronous on the
-    current torch stream."""
+    current torch stream for device arrays; arrays on the CPU are staged
+    through the GPU (gbns_flux_div_host) and the call returns with rhs
+    updated."""
     traits = traits or ()
     inc = True
     prec = _abi.PREC_FP64
@@ -112,6 +114,16 @@ def flux_div(prims, rhs, flux_func, traits=None, stream=None, variant=0):
     if prims.shape != rhs.shape or prims.grid is not rhs.grid and prims.shape != rhs.shape:
         raise ValueError("prims and rhs must live on the same grid")
     scheme = flux_func if isinstance(flux_func, _abi.SchemeDesc) else lower(flux_func, prec)
+    on_cpu = prims.data.device.type == "cpu", rhs.data.device.type == "cpu"
+    if any(on_cpu):
+        if not all(on_cpu):
+            raise ValueError("prims and rhs must both be on the CPU or both on the GPU")
+        if variant:
+            raise ValueError("tile variants select kernels for device arrays")
+        if not (prims.data.is_contiguous() and rhs.data.is_contiguous()):
+            raise ValueError("host arrays must be contiguous")
+        _native.check(_native.lib().gbns_flux_div_host(prims.desc(), scheme, prims.ptr(), rhs.ptr(), int(inc), None))
+        return
     if variant:
         rc = _native.lib().gbns_flux_div_variant(prims.desc(), scheme, prims.ptr(), rhs.ptr(), int(inc), int(variant), _stream(stream))
     else:

@@ -138,6 +138,23 @@ def test_host_path_graph_run_and_selftest_validate_before_cuda():
     assert L.gbns_selftest_dmul_int(16, 0, None, None) == _abi.ERR_INVALID
 
 
+def test_flux_div_cpu_arrays_take_the_host_path():
+    """pde_algs.flux_div with grid_arrays on the CPU goes to gbns_flux_div_host
+    (without a GPU: a CUDA error from the host path, never a device launch on
+    host pointers); mixed CPU/GPU arguments are refused."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: the host path runs (tests/test_gpu_parity.py)")
+    from spade_gb300 import grid
+    blocks = grid.cartesian_blocks_t((1, 1, 1), (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    g = grid.cartesian_grid_t((8, 8, 8), blocks)
+    q = grid.grid_array(g, 1.0, 2, device="cpu")
+    r = grid.grid_array(g, 0.0, 2, device="cpu")
+    air = fluid_state.ideal_gas_t(1.4, 287.0)
+    with pytest.raises(_native.SpadeError):
+        pde_algs.flux_div(q, r, convective.cent_keep(2, air))
+
+
 def test_fill_ghosts_rejects_unpaired_periodic():
     g = _abi.grid_desc((1, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
     bc = _abi.bc_desc([_abi.BC_PERIODIC, _abi.BC_NONE, 0, 0, 0, 0])
