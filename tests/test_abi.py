@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 import subprocess
+import sys
 import tempfile
 
 import numpy as np
@@ -272,3 +273,28 @@ def test_fill_array_and_physical_coordinates_on_cpu_tensors():
     algs.fill_array(q2, lambda x, y, z: (x, y, z, 0.0, 0.0), algs.exclude_exchanges)
     d2 = q2.data.numpy()
     assert np.all(d2[:, 0] == 7.0) and d2[0, ng, ng, ng, 3] == 0.0
+
+
+def test_missing_library_raises_instead_of_falling_back():
+    """With libgbns.so absent, the public API raises SpadeError for CPU and
+    GPU grid_arrays alike: there is no CPU or PyTorch fallback.  Run in a child
+    process so the loaded library of this session is untouched."""
+    code = r'''
+import sys
+from spade_gb300 import _native, pde_algs, convective, fluid_state, grid
+_native.LIB_PATH = "/nonexistent/libgbns.so"
+_native._LIB = None
+blocks = grid.cartesian_blocks_t((1, 1, 1), (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+g = grid.cartesian_grid_t((8, 8, 8), blocks)
+q = grid.grid_array(g, 1.0, 2, device="cpu")
+r = grid.grid_array(g, 0.0, 2, device="cpu")
+try:
+    pde_algs.flux_div(q, r, convective.cent_keep(2, fluid_state.ideal_gas_t(1.4, 287.0)))
+except _native.SpadeError as e:
+    assert "not built" in str(e), e
+    print("raised")
+    sys.exit(0)
+sys.exit(1)
+'''
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "raised" in r.stdout, r.stdout + r.stderr
