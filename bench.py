@@ -577,9 +577,11 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        warm = max(0, min(args.warmup, 1))
-        for _ in range(warm):
+        warm = 0
+        tw = time.perf_counter()
+        while warm < args.warmup and time.perf_counter() - tw < 60:
             cpu_sample(steps=1, nblk=(4, 4, 2))
+            warm += 1
         vals = []
         cb = None
         t0 = time.perf_counter()
