@@ -1,11 +1,12 @@
-"""Axis-permutation symmetry on the oracle (CPU): on a cubic periodic grid,
-permuting the coordinate axes cyclically (x <- y <- z <- x, with the velocity
+"""Axis-permutation and mirror symmetry on the oracle (CPU): on a cubic
+periodic grid, permuting the coordinate axes cyclically (x <- y <- z <- x, with the velocity
 and momentum components permuted alike) permutes the residual the same way.
 Only the order in which the three directions are accumulated changes, so the
 results agree to round-off.  This checks that every functor treats the three
 directions alike (stencils, face normals, transverse gradient terms), which
 the bitwise comparisons with the reference on fixed inputs do not by
-themselves."""
+themselves.  Reflecting one axis checks that the upwind-biased left and right
+states mirror each other."""
 import numpy as np
 import pytest
 
@@ -48,3 +49,34 @@ def test_cyclic_axis_permutation(name):
     assert np.all(np.abs(a - b).max(axis=0) <= 1e-12 * scale), np.abs(a - b).max(axis=0) / scale
     # three rotations are the identity
     assert np.array_equal(_rot(_rot(_rot(q))), q)
+
+
+def _mirror(a, axis, comp):
+    """Reflect array axis `axis` (3 = x, 2 = y, 1 = z) and negate the velocity
+    or momentum component `comp` (2, 3, 4) normal to the mirror."""
+    b = np.ascontiguousarray(np.flip(a, axis=axis))
+    b[..., comp] = -b[..., comp]
+    return b
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("axis", [1, 2, 3])
+def test_mirror_reflection(name, axis):
+    """Reflecting one axis (x -> -x with u -> -u) reflects the residual and
+    negates its normal momentum component: the upwind-biased stencils of
+    fweno_t / WENO5 and their left/right states must mirror each other."""
+    comp = {3: 2, 2: 3, 1: 4}[axis]
+    n, ng = 6, 3
+    grid = _abi.grid_desc((1, 1, 1), (n, n, n), ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    q = P.random_state((1, 1, 1), (n, n, n), ng, seed=71 + axis)
+    O.fill_ghosts(grid, P.periodic_bc(), q)
+    s = P.scheme(**CASES[name])
+    r = np.zeros_like(q)
+    O.flux_div(grid, s, q, r, increment=False)
+    qm = _mirror(q, axis, comp)
+    rm = np.zeros_like(qm)
+    O.flux_div(grid, s, qm, rm, increment=False)
+    a = rm[:, ng:-ng, ng:-ng, ng:-ng, :].reshape(-1, 5)
+    b = _mirror(r, axis, comp)[:, ng:-ng, ng:-ng, ng:-ng, :].reshape(-1, 5)
+    scale = np.abs(b).max(axis=0)
+    assert np.all(np.abs(a - b).max(axis=0) <= 1e-12 * scale), np.abs(a - b).max(axis=0) / scale
