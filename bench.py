@@ -594,7 +594,11 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": len(vals), "warmup": warm, "ms_per_step": cfg["cells"] / v * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": cfg,
+                "config": dict(cfg, reference_sample="each step: 1 SSPRK3 step of a 4x4x2-block sub-box of 32^3 cells "
+                                                     "(1,048,576 cells, same scheme, coordinates and walls); value = "
+                                                     "sub-box cells / sub-box step time, ms_per_step = the full "
+                                                     "grid's cells / value (extrapolated, per-cell cost is "
+                                                     "state-independent for these branch-free schemes)"),
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": cb["cores"], "kind": "port",
                                  "sample": "per step: 1 SSPRK3 step on a 4x4x2-block sub-box of 32^3 cells "
                                            "(1048576 cells) of the channel workload; the reference's CPU path cannot "
@@ -631,7 +635,10 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "flux_div_kernel (with the fused RK stage update)",
                      "achieved": r["achieved"], "peak": r["hbm_peak"],
                      "unit": "GB/s", "frac": r["achieved"] / r["hbm_peak"],
-                     "traffic": r["traffic"], "peak_source": r["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "traffic": r["traffic"],
+                     "traffic_source": "scaled from 2.1M-cell ncu capture (dram__bytes_read.sum + dram__bytes_write.sum "
+                                       "per cell, profiles/flux_div_rk_channel_fp64.md) to this workload's cells",
+                     "peak_source": r["peak_src"] + " (MEASURED_PEAKS.json hbm_gbs)",
                      "alg_bytes_per_cell": ALG_BYTES_FUSED, "avg_launch_ms": r["flux_avg_ms"],
                      "share_of_step": r["flux_share"]},
         "fp64_roof": {"fma_rate_tflops": r["fp64_fma_flops"] / 1e12, "fp32_fma_rate_tflops": r["fp32_fma_flops"] / 1e12,

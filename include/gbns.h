@@ -272,21 +272,21 @@ int gbns_selftest_wait_timeout(int* status, void* stream);
 int gbns_selftest_dmul_int(uint64_t npairs, uint64_t seed, uint64_t* mismatches, void* stream);
 
 /* Reduction that allocates nothing.  For callers that cannot let the
- * library call cudaMalloc: work recorded into a CUDA graph while a stream is
- * being captured (allocation is not allowed during capture) and applications
- * whose device memory all belongs to their own pool allocator.  Same
- * reductions and results as gbns_reduce; the result (1 double, 5 for
- * GBNS_RED_CONSERVED) goes to the caller's DEVICE buffer out_dev,
- * asynchronously on `stream`.  Its partial sums live in a fixed file-scope
- * device array of 6,152 doubles (about 48 KB, held by every GPU that loads
- * the library until exit); a grid whose reduction would need more scratch is
- * rejected with GBNS_ERR_CAPACITY (the current partitioning never needs more
- * than 1024 partial records).  The first call on a device looks up the
- * array's device address with that device current: make that first call
- * before any stream capture.  All calls share the one array and leave their
- * partial sums in it: calls that overlap on the GPU (several streams, or
- * several host threads on one device) race and must be serialised by the
- * caller.  No counterpart in the reference. */
+ * library call cudaMalloc: applications that hand all device memory to their
+ * own pool allocator at start-up, and solver loops that must not stall on an
+ * allocation (cudaMalloc can synchronise the device and can fail late in a
+ * run when memory is nearly full).  Same reductions and bit-identical results
+ * as gbns_reduce; the result (1 double, 5 for GBNS_RED_CONSERVED) goes to the
+ * caller's DEVICE buffer out_dev, asynchronously on `stream`.  Its partial
+ * sums live in a fixed file-scope device array of 6,152 doubles (about 48 KB,
+ * held by every GPU that loads the library until exit).  That is the most
+ * scratch any grid's reduction uses (at most 1024 partial records); a need
+ * beyond it is rejected with GBNS_ERR_CAPACITY.  The first call on a device
+ * looks up the array's device address with that device current: make that
+ * first call before any stream capture.  All calls share the one array and
+ * leave their partial sums in it: calls that overlap on the GPU (several
+ * streams, or several host threads on one device) race and must be
+ * serialised by the caller.  No counterpart in the reference. */
 int gbns_reduce_noalloc(const gbns_grid_desc* grid, const gbns_gas_desc* gas,
                         const double* prims, int kind, double* out_dev, void* stream);
 

@@ -5,7 +5,7 @@ bit-identical results; they differ in tile size, threads per CTA and, for
 FP32-flux, in how the halo is staged (straight into FP32 shared memory or a
 TMA copy of the FP64 box).  tune() times each variant on the caller's own
 arrays with CUDA events and caches the winner per (scheme, block shape,
-ghosts, precision, GPU) in spade_gb300/_build/autotune.json.
+block count, ghosts, precision, GPU) in spade_gb300/_build/autotune.json.
 """
 import json
 import os
@@ -18,10 +18,17 @@ CACHE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "auto
 
 
 def _key(grid, scheme):
+    """Everything that selects a different kernel or changes its cost: the
+    GPU, every scheme field that picks code (convective kind and order, WENO
+    smoothness switch, dissipation and its sensor, hybrid blend, viscous term
+    and law, precision), the block shape, ghosts, coordinates and the block
+    count (small grids favour small tiles)."""
     dev = torch.cuda.get_device_name()
     return "|".join(str(x) for x in (
-        dev, scheme.convective, scheme.order, scheme.weno_smooth, scheme.dissipation, scheme.viscous,
-        scheme.visc_law, scheme.precision, tuple(grid.ncell), grid.ng, grid.coords))
+        dev, scheme.convective, scheme.order, scheme.weno_smooth, scheme.dissipation, scheme.sensor,
+        scheme.hybrid_flux, scheme.hybrid_sensor, scheme.hybrid_param,
+        scheme.viscous, scheme.visc_law, scheme.precision, tuple(grid.ncell), grid.ng, grid.coords,
+        tuple(grid.nblk)))
 
 
 def _load():

@@ -17,6 +17,14 @@ namespace gbns
     constexpr int MAX_BLK_PER_DIM = 64;     // blocks per direction
     constexpr int MAX_YTAB        = 1024;   // doubles per stretched-metric table
 
+    // Interior reductions: values per partial record (up to 5 sums and a
+    // weight sum), the most partial records a reduction uses, and the result
+    // slots after them.  Scratch for one reduction is
+    // npart*RED_NVAL + RED_RESULT_SLOTS doubles.
+    constexpr int RED_NVAL         = 6;
+    constexpr int RED_MAX_PART     = 1024;
+    constexpr int RED_RESULT_SLOTS = 8;
+
     // ------------------------------------------------------------------
     // error reporting (per host thread)
     // ------------------------------------------------------------------

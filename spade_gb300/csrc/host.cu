@@ -397,7 +397,14 @@ extern "C"
             sg.count = 0;
             rc = check_cuda(cudaMalloc(&sg.q, count*sizeof(double)), "host-path staging (prims)");
             if (!rc) rc = check_cuda(cudaMalloc(&sg.r, count*sizeof(double)), "host-path staging (rhs)");
-            if (rc) return rc;
+            if (rc)
+            {
+                // never keep half a staging pair
+                if (sg.q) cudaFree(sg.q);
+                if (sg.r) cudaFree(sg.r);
+                sg.q = sg.r = nullptr;
+                return rc;
+            }
             sg.count = count;
         }
         const size_t bytes = count*sizeof(double);

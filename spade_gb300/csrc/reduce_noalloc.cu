@@ -1,12 +1,13 @@
 // Interior reduction that allocates nothing.
 //
-// Some callers cannot let a library call cudaMalloc: code that records its
-// work into a CUDA graph while the stream is being captured (allocation is
-// not allowed during capture), and applications that hand all device memory
-// to their own pool allocator up front.  gbns_reduce_noalloc serves them: the
-// partial sums of the reduction live in a file-scope device array of fixed
-// size instead of library- or caller-allocated scratch.  The arithmetic is
-// gbns_reduce_async's, so results equal gbns_reduce's.
+// Some callers cannot let a library call cudaMalloc: applications that hand
+// all device memory to their own pool allocator at start-up and must not see
+// a second allocator take memory behind its back, and solver loops that must
+// not stall, since cudaMalloc can synchronise the whole device and may fail
+// late in a run when memory is nearly full.  gbns_reduce_noalloc serves them:
+// the partial sums of the reduction live in a file-scope device array of
+// fixed size instead of library- or caller-allocated scratch.  The arithmetic
+// is gbns_reduce_async's, so results equal gbns_reduce's bit for bit.
 #include <mutex>
 #include <string>
 #include <vector>
@@ -14,10 +15,12 @@
 
 namespace gbns
 {
-    // Capacity in doubles: room for 1024 partial records of 6 doubles plus
-    // the result slots (49,216 bytes).  Every GPU that loads the library
-    // holds this array until the process exits.
-    constexpr size_t NOALLOC_SCRATCH_DOUBLES = 1024*6 + 8;
+    // Capacity in doubles: room for the most partial records a reduction
+    // uses (1024 of 6 doubles) plus the result slots, 6,152 doubles or
+    // 49,216 bytes.  Every GPU that loads the library holds this array until
+    // the process exits.
+    constexpr size_t NOALLOC_SCRATCH_DOUBLES = size_t(RED_MAX_PART)*RED_NVAL + RED_RESULT_SLOTS;
+    static_assert(NOALLOC_SCRATCH_DOUBLES == 6152, "the documented capacity of the no-alloc reduction array");
 
     static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLES];
 

@@ -363,7 +363,6 @@ namespace gbns
     };
 
     constexpr int RED_THREADS = 256;
-    constexpr int RED_NVAL = 6;   // up to 5 sums + weight sum
 
     __device__ __forceinline__ double warp_sum(double v)
     {
@@ -483,7 +482,7 @@ namespace gbns
     {
         const long long total = (long long)G.n[0]*G.n[1]*G.n[2]*G.nblk;
         long long np = (total + RED_THREADS*8 - 1)/(RED_THREADS*8);
-        if (np > 1024) np = 1024;
+        if (np > RED_MAX_PART) np = RED_MAX_PART;
         if (np < 1) np = 1;
         return int(np);
     }
@@ -564,7 +563,7 @@ extern "C"
         if (kind < GBNS_RED_MAX_WAVESPEED || kind > GBNS_RED_HEALTH) return set_error(GBNS_ERR_INVALID, "unknown reduction");
         const int npart = reduce_npart(G);
         double* scratch = nullptr;
-        rc = get_scratch(size_t(npart)*RED_NVAL + 8, &scratch);
+        rc = get_scratch(size_t(npart)*RED_NVAL + RED_RESULT_SLOTS, &scratch);
         if (rc) return rc;
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         rc = launch_reduce(grid, G, gas->gamma, gas->R, prims, kind, scratch, npart, st);
@@ -585,7 +584,7 @@ extern "C"
         int rc = make_geom(grid, G);
         if (rc) return rc;
         const int npart = reduce_npart(G);
-        if (ndouble) *ndouble = size_t(npart)*RED_NVAL + 8;
+        if (ndouble) *ndouble = size_t(npart)*RED_NVAL + RED_RESULT_SLOTS;
         if (result_offset) *result_offset = size_t(npart)*RED_NVAL;
         return GBNS_OK;
     }
@@ -599,7 +598,7 @@ extern "C"
         if (!gas || !prims || !scratch) return set_error(GBNS_ERR_INVALID, "NULL argument");
         if (kind < GBNS_RED_MAX_WAVESPEED || kind > GBNS_RED_HEALTH) return set_error(GBNS_ERR_INVALID, "unknown reduction");
         const int npart = reduce_npart(G);
-        if (scratch_len < size_t(npart)*RED_NVAL + 8) return set_error(GBNS_ERR_INVALID, "reduction scratch too small");
+        if (scratch_len < size_t(npart)*RED_NVAL + RED_RESULT_SLOTS) return set_error(GBNS_ERR_INVALID, "reduction scratch too small");
         return launch_reduce(grid, G, gas->gamma, gas->R, prims, kind, scratch, npart, static_cast<cudaStream_t>(stream));
     }
 }

@@ -10,11 +10,14 @@ import tempfile
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = "/root/reference/src"
+
+from __graft_entry__ import ref_src
+
+REF_SRC = ref_src() or ""
 CUDA_INC = "/usr/local/cuda/include"
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
 def test_dropin_overload_and_lowering():
     with tempfile.TemporaryDirectory() as d:
         exe = os.path.join(d, "dropin")
@@ -66,7 +69,7 @@ def test_dropin_overload_and_lowering():
     assert bf[0][bf[0].index("visc") + 1] == "1" and bf[0][bf[0].index("ng") + 1] == "3"
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference sources not present")
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
 def test_dropin_host_array_path_compiles():
     """Without the test hooks, the gb300 flux_div overload compiles for
     device::cpu grid_arrays (the host path through gbns_flux_div_host)."""

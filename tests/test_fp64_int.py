@@ -1,7 +1,11 @@
-"""The integer-pipe FP64 multiply of the flux kernels (fp64_int.cuh),
-compiled for the host and compared bit for bit with the CPU's IEEE multiply
-on generated operand pairs (the GPU comparison with the hardware multiply is
-tests/test_gpu_parity.py::test_integer_pipe_multiply_matches_hardware)."""
+"""The integer-pipe FP64 arithmetic of the flux kernels (fp64_int.cuh):
+multiply (dmul_int), power-of-two scaling (dmul_pow2), division (ddiv_int)
+and square root (dsqrt_int), compiled for the host and compared bit for bit
+with the CPU's IEEE operations on generated operand sets; division and square
+root also with their reciprocal seeds perturbed, to show the refinement
+absorbs a seed error well beyond the device's.  The GPU comparison with the
+hardware operations is
+tests/test_gpu_parity.py::test_integer_pipe_multiply_matches_hardware."""
 import os
 import subprocess
 import tempfile

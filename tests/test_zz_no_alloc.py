@@ -1,13 +1,17 @@
 """gbns_reduce_noalloc: the reduction entry point that allocates nothing (its
-partial sums live in a fixed device array inside the library), for callers
-that cannot let the library call cudaMalloc — work recorded into a CUDA graph
-while a stream is being captured, or applications whose device memory all
-belongs to their own pool allocator.
+partial sums live in a fixed device array inside the library).  It is for
+callers that cannot let the library call cudaMalloc: applications whose
+device memory all belongs to their own pool allocator, and solver loops that
+must not stall on an allocation.
 
-The test calls it through the C ABI twice in a row for every reduction kind
-and checks each result against gbns_reduce (which uses library-allocated
-scratch) on the same state, within the tolerance the other reduction tests
-use.  It must pass alone in a fresh process and after the other tests."""
+The GPU test calls it through the C ABI twice in a row for every reduction
+kind and checks each result against gbns_reduce (library-allocated scratch)
+on the same state.  The arithmetic and partition are gbns_reduce's, so the
+results must be bit-identical.  One grid is small (4 partial records) and one
+has 4x4x4 blocks of 32^3 cells, which uses the full 1024 partial records the
+fixed array holds.  It must pass alone in a fresh process and after the
+other tests.  The argument checks return before any CUDA call and run on the
+CPU."""
 import ctypes
 
 import numpy as np
@@ -18,15 +22,23 @@ torch = pytest.importorskip("torch")
 from spade_gb300 import _abi, _native
 import problems as P
 
-pytestmark = pytest.mark.gpu
+CASES = [
+    # (blocks, cells per block, ghosts, coordinates, partial records used)
+    ((3, 2, 2), (9, 7, 6), 2, _abi.COORDS_IDENTITY, 4),
+    ((3, 2, 2), (9, 7, 6), 2, _abi.COORDS_TANH_Y, 4),
+    ((4, 4, 4), (32, 32, 32), 3, _abi.COORDS_TANH_Y, 1024),
+]
 
 
-@pytest.mark.parametrize("coords", [_abi.COORDS_IDENTITY, _abi.COORDS_TANH_Y])
-def test_reduce_noalloc_matches_reduce_twice_in_a_row(coords):
+@pytest.mark.gpu
+@pytest.mark.parametrize("nblk,ncell,ng,coords,npart", CASES)
+def test_reduce_noalloc_matches_reduce_twice_in_a_row(nblk, ncell, ng, coords, npart):
     lib = _native.lib()
     st = int(torch.cuda.current_stream().cuda_stream)
-    nblk, ncell, ng = (3, 2, 2), (9, 7, 6), 2
     grid = _abi.grid_desc(nblk, ncell, ng, (0.0, 1.0, -1.0, 1.0, 0.0, 2.0), coords, (2.0, 0, 0, 0))
+    need, off = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    _native.check(lib.gbns_reduce_scratch_size(grid, ctypes.byref(need), ctypes.byref(off)))
+    assert off.value == 6 * npart and need.value <= 6152
     gas = P.gas_desc()
     q = np.abs(P.random_state(nblk, ncell, ng, seed=91))
     q[0, ng + 2, ng + 1, ng + 3, 1] = -5.0          # one cell the health count must see
@@ -41,7 +53,7 @@ def test_reduce_noalloc_matches_reduce_twice_in_a_row(coords):
             _native.check(lib.gbns_reduce_noalloc(grid, gas, qd.data_ptr(), kind, out_dev.data_ptr(), st))
             torch.cuda.synchronize()
             got = out_dev.cpu().numpy()[:n]
-            np.testing.assert_allclose(got, want[:n], rtol=1e-13, atol=0)
+            assert np.array_equal(got, want[:n]), (kind, got, want[:n])
 
 
 def test_reduce_noalloc_rejects_bad_arguments():
@@ -50,4 +62,8 @@ def test_reduce_noalloc_rejects_bad_arguments():
     rc = lib.gbns_reduce_noalloc(grid, P.gas_desc(), ctypes.c_void_p(16), 99, ctypes.c_void_p(32), None)
     assert rc == _abi.ERR_INVALID
     rc = lib.gbns_reduce_noalloc(grid, P.gas_desc(), ctypes.c_void_p(16), _abi.RED_KINETIC, None, None)
+    assert rc == _abi.ERR_INVALID
+    bad = _abi.grid_desc((1, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    bad.ncell[0] = 0
+    rc = lib.gbns_reduce_noalloc(bad, P.gas_desc(), ctypes.c_void_p(16), _abi.RED_KINETIC, ctypes.c_void_p(32), None)
     assert rc == _abi.ERR_INVALID
