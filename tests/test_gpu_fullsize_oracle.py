@@ -125,4 +125,6 @@ def test_channel_64_blocks_10_step_history_bitwise_vs_oracle():
         ke_o = O.reduce(g, s.gas, q, _abi.RED_KINETIC)
         out = np.zeros(5)
         _native.check(lib.gbns_reduce(g, s.gas, qd.data_ptr(), _abi.RED_KINETIC, out.ctypes.data_as(ctypes.c_void_p), _st()))
-        np.testing.assert_allclose(out[0], ke_o, rtol=1e-13)
+        # identical states; the two reductions sum 2.1M cells in different
+        # orders (device tree vs host loop), so agreement to summation error
+        np.testing.assert_allclose(out[0], ke_o, rtol=1e-11)
