@@ -49,8 +49,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-fp32", action="store_true", help="skip the FP32-flux side measurement")
     p.add_argument("--no-forms", action="store_true", help="skip the batched and serving measurements")
+    p.add_argument("--no-reference-gpu", action="store_true", help="skip the reference's own GPU flux_div leg")
+    p.add_argument("--reference-gpu-only", action="store_true",
+                   help="print only the reference-GPU comparison (the reference's own flux_div kernels beside gbns)")
     p.add_argument("--batch-instances", type=int, default=96)
-    p.add_argument("--batch-steps", type=int, default=10)
+    p.add_argument("--batch-steps", type=int, default=200)
     p.add_argument("--serve-requests", type=int, default=24)
     p.add_argument("--precision-report", type=int, default=0, metavar="STEPS",
                    help="instead of the bench line: run the channel workload STEPS steps in FP64 and in the "
@@ -384,6 +387,8 @@ def run_batch_form(args):
         b = batch_t(budget, prec, True)
         for p in probs:
             b.add(p.q.desc(), p.scheme_desc(prec), p.bc_desc(), p.dt, p.q.ptr())
+        # tile variant per kernel class, timed on the instances' own arrays
+        tuned = b.autotune(reps=3)
         b.step(2)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -393,7 +398,7 @@ def run_batch_form(args):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / args.batch_steps
         out[name] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms,
-                     "launches_per_step": 6, "graph": True}
+                     "launches_per_step": 6, "graph": True, "autotuned": tuned}
         b.close()
     # the same instances one grid at a time (one gbns_ssprk3_step per instance)
     works = [torch.zeros(3 * p.q.data.numel(), dtype=torch.float64, device="cuda") for p in probs]
@@ -406,12 +411,13 @@ def run_batch_form(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
-    for _ in range(max(1, args.batch_steps // 2)):
+    n_plain = max(1, min(args.batch_steps, 20))
+    for _ in range(n_plain):
         one_step()
     e1.record()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / max(1, args.batch_steps // 2)
-    out["fp64_one_grid_at_a_time"] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms,
+    ms = e0.elapsed_time(e1) / n_plain
+    out["fp64_one_grid_at_a_time"] = {"cell_steps_per_s": cells / (ms * 1e-3), "ms_per_step": ms, "steps": n_plain,
                                       "launches_per_step": 6 * len(probs)}
     out["fp32_batched_vs_fp64_plain"] = out["fp32_flux"]["cell_steps_per_s"] / out["fp64_one_grid_at_a_time"]["cell_steps_per_s"]
     del probs, works
@@ -436,6 +442,71 @@ def run_serve_form(args):
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle restatement on the host cores, bounded sample
 # ---------------------------------------------------------------------------
+def run_reference_gpu(args, reps=3):
+    """The reference's own GPU flux_div (basic, bfoct, longf), replayed on
+    this GPU from launch scripts recorded where its sources are
+    (oracle/refgpu.py), beside this library's flux_div on the same grid,
+    scheme and state: ms per flux_div (CUDA events on the launching stream,
+    median of `reps` after one warm-up) and cell-RHS/s."""
+    import torch
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from oracle import refgpu
+    from spade_gb300 import _abi, _native, autotune, workloads
+    if not refgpu.available():
+        return {"unavailable": "reference GPU recordings absent (recorded where the reference sources are)"}
+    lib = _native.lib()
+    out = {}
+    clocks = Clocks(torch.cuda.current_device())
+    for case in refgpu.CASE_NAMES:
+        if case == "tgv_ck2_visc":
+            prob = workloads.taylor_green(nblk=(8, 8, 8), ncell=(32, 32, 32), ng=2, rng="torch", seed=0)
+        else:
+            prob = workloads.channel(nblk=(8, 8, 8), ncell=(32, 32, 32), ng=2, beta=None, weno="fweno",
+                                     law="constant", rng="torch", seed=0)
+        cells = 8 * 8 * 8 * 32 ** 3
+        st = torch.cuda.current_stream()
+        sp = int(st.cuda_stream)
+
+        def timed(fn):
+            fn()
+            ts = []
+            for _ in range(reps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(st)
+                fn()
+                e1.record(st)
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            return statistics.median(ts)
+
+        rhs = torch.zeros_like(prob.q.data)
+        rep = refgpu.Replay(case, prob.q.data, rhs, sp)
+        row = {"cells": cells, "scheme": case, "reference": {}, "gbns": {}}
+        try:
+            for alg in ("basic", "bfoct", "longf"):
+                ms = timed(lambda: rep.run(alg, sp))
+                row["reference"][alg] = {"ms": ms, "cell_rhs_per_s": cells / (ms * 1e-3), "launches": rep.launches[alg]}
+        finally:
+            rep.close()
+        for prec, name in ((_abi.PREC_FP64, "fp64"), (_abi.PREC_FP32_FLUX, "fp32_flux")):
+            sd = prob.scheme_desc(prec)
+            best, times = autotune.tune(prob.q.desc(), sd, prob.q.ptr(), rhs.data_ptr(), use_cache=False)
+            ms = timed(lambda: _native.check(lib.gbns_flux_div_variant(prob.q.desc(), sd, prob.q.ptr(),
+                                                                        rhs.data_ptr(), 0, best, sp)))
+            row["gbns"][name] = {"ms": ms, "cell_rhs_per_s": cells / (ms * 1e-3), "variant": best}
+        best_ref = min(v["ms"] for v in row["reference"].values())
+        row["speedup_fp64_vs_best_reference"] = best_ref / row["gbns"]["fp64"]["ms"]
+        row["speedup_fp32_flux_vs_best_reference"] = best_ref / row["gbns"]["fp32_flux"]["ms"]
+        out[case] = row
+        del prob, rhs
+        torch.cuda.empty_cache()
+    out["clocks"] = clocks.stop()
+    out["note"] = ("the reference's CUDA flux_div kernels (its own source, nvcc defaults + lambda flags, sm_103a) "
+                   "run unchanged on this GPU: one flux_div in increment mode per algorithm; gbns: one flux_div "
+                   "in overwrite mode with the autotuned tile")
+    return out
+
+
 def cpu_sample(steps=1, nblk=(2, 2, 2), ncell=(32, 32, 32), threads=0):
     import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -574,6 +645,10 @@ def main():
     if args.precision_report:
         run_precision_report(args)
         return
+    if args.reference_gpu_only:
+        if rank == 0:
+            print(json.dumps({"reference_gpu": run_reference_gpu(args)}))
+        return
     if args.impl == "reference":
         if rank != 0:
             return
@@ -623,6 +698,8 @@ def main():
         forms["small_tgv"] = run_small_tgv(args)
         forms["batch_form"] = run_batch_form(args)
         forms["serve_form"] = run_serve_form(args)
+        if not args.no_reference_gpu:
+            forms["reference_gpu"] = run_reference_gpu(args)
     cpu = None
     cpu1 = None
     if world == 1 and not args.no_cpu_baseline:

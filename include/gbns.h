@@ -398,6 +398,23 @@ int gbns_batch_usage(gbns_batch* batch, size_t* bytes_used, size_t* bytes_budget
 /* Arena bytes one instance of this grid occupies (state + 3 residuals); 0 if invalid. */
 size_t gbns_batch_instance_bytes(const gbns_grid_desc* grid);
 
+/* Tile autotuner of the batched form: for every kernel class present among
+ * the active instances (the compile-time flux configuration: convective
+ * scheme x coordinates, numbered 0 .. gbns_batch_class_count()-1), times
+ * each of its tile variants (tile shape and threads per CTA) on the
+ * instances' own arrays with CUDA events, `reps` persistent launches of the
+ * first SSPRK3 stage each (which writes only scratch arrays), and keeps the
+ * fastest.  variants_out (optional, gbns_batch_class_count() ints) receives
+ * the choice per class, -1 for absent classes.  Synchronises the batch.
+ * Results do not depend on the variant (bit-identical).  No reference
+ * counterpart (the reference picks tile shapes at compile time,
+ * flux_div_*.h). */
+int gbns_batch_autotune(gbns_batch* batch, int reps, int* variants_out);
+int gbns_batch_set_variant(gbns_batch* batch, int kernel_class, int variant);
+int gbns_batch_class_count(void);
+/* Tile shape (x, y, z cells) of a class's variant at a precision. */
+int gbns_batch_class_variant_info(int kernel_class, int precision, int variant, int* tile_xyz);
+
 #ifdef __cplusplus
 }
 #endif

@@ -60,6 +60,10 @@ def lib():
     L.gbns_batch_usage.argtypes = [vp, P(ctypes.c_size_t), P(ctypes.c_size_t), P(ctypes.c_int), P(ctypes.c_longlong)]
     L.gbns_batch_instance_bytes.argtypes = [P(_abi.GridDesc)]
     L.gbns_batch_instance_bytes.restype = ctypes.c_size_t
+    L.gbns_batch_autotune.argtypes = [vp, ctypes.c_int, P(ctypes.c_int)]
+    L.gbns_batch_set_variant.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    L.gbns_batch_class_count.argtypes = []
+    L.gbns_batch_class_variant_info.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_int)]
     if L.gbns_version() != _abi.ABI_VERSION:
         raise SpadeError(_abi.ERR_UNSUPPORTED, "libgbns ABI version mismatch")
     _LIB = L

@@ -48,6 +48,28 @@ class batch_t:
     def step(self, nsteps=1):
         _native.check(self.lib.gbns_batch_step(self.handle, int(nsteps)))
 
+    CLASS_NAMES = ("cent_keep2/identity", "totani_lr/identity", "fweno/identity", "weno5/stretched-y",
+                   "weno5/identity", "hybrid(cent_keep2,fweno)/identity")
+
+    def autotune(self, reps=3):
+        """Times every tile variant of each kernel class present among the
+        active instances on their own arrays (gbns_batch_autotune) and keeps
+        the fastest.  Returns {class name: {"variant": v, "tile": (x, y, z)}}."""
+        n = int(self.lib.gbns_batch_class_count())
+        out = (ctypes.c_int * n)()
+        _native.check(self.lib.gbns_batch_autotune(self.handle, int(reps), out))
+        res = {}
+        for c in range(n):
+            if out[c] < 0:
+                continue
+            t = (ctypes.c_int * 3)()
+            _native.check(self.lib.gbns_batch_class_variant_info(c, int(self.precision), int(out[c]), t))
+            res[self.CLASS_NAMES[c]] = {"variant": int(out[c]), "tile": (t[0], t[1], t[2])}
+        return res
+
+    def set_variant(self, kernel_class, variant):
+        _native.check(self.lib.gbns_batch_set_variant(self.handle, int(kernel_class), int(variant)))
+
     def state_ptr(self, slot):
         p = ctypes.c_void_p()
         n = ctypes.c_longlong()

@@ -21,11 +21,39 @@ namespace gbns
         return -1;
     }
 
-    void batch_class_tile(int cls, int precision, int tile[3])
+    // Tile shapes of the variants in batch_flux.cuh (same order).
+    int batch_class_variants(int cls, int precision)
     {
-        tile[0] = 8; tile[1] = 8; tile[2] = 8;
-        if ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) && precision == GBNS_PREC_FP32_FLUX) tile[2] = 4;
-        if (cls == BCLASS_HYB2_ID) tile[2] = 4;
+        if (cls == BCLASS_HYB2_ID && precision == GBNS_PREC_FP32_FLUX) return 2;
+        return 3;
+    }
+
+    void batch_class_tile(int cls, int precision, int variant, int tile[3])
+    {
+        const bool fp32 = precision == GBNS_PREC_FP32_FLUX;
+        const bool weno5 = cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID;
+        // 8x8x4 tiles: variant 1 of the centred and fweno classes and of FP64
+        // WENO5, variant 0 of FP32 WENO5 and of the hybrid
+        bool thin;
+        if (cls == BCLASS_HYB2_ID) thin = variant == 0;
+        else if (weno5 && fp32) thin = variant == 0;
+        else thin = variant == 1;
+        tile[0] = 8; tile[1] = 8; tile[2] = thin ? 4 : 8;
+    }
+
+    int launch_flux_batch(int cls, int v, int precision, const TileItem* items, const int* offsets, const int* counts,
+                          const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st)
+    {
+        const int group = cls == BCLASS_HYB2_ID ? 2 : ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) ? 1 : 0);
+        if (precision == GBNS_PREC_FP32_FLUX)
+        {
+            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+        }
+        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, stage, st);
     }
 
     // First-fit allocator over one device allocation (offsets in bytes).
@@ -105,6 +133,7 @@ struct gbns_batch
     std::vector<TileItem> h_tiles;
     std::vector<BlockItem> h_blocks;
     int h_meta[2*BCLASS_COUNT + 1];
+    int variant[BCLASS_COUNT] = {0, 0, 0, 0, 0, 0};   // tile variant per class (gbns_batch_autotune)
     unsigned class_mask = 0;
     bool dirty = true;
     cudaGraph_t graph = nullptr;
@@ -186,7 +215,7 @@ namespace
         {
             b->h_meta[c] = int(b->h_tiles.size());
             int t[3];
-            batch_class_tile(c, b->precision, t);
+            batch_class_tile(c, b->precision, b->variant[c], t);
             for (size_t si = 0; si < b->slots.size(); ++si)
             {
                 const Slot& S = b->slots[si];
@@ -239,9 +268,8 @@ namespace
             for (int c = 0; c < BCLASS_COUNT; ++c)
             {
                 if (!(b->class_mask & (1u << c))) continue;
-                int rc = b->precision == GBNS_PREC_FP32_FLUX
-                    ? launch_flux_batch_f32(c, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, stage, b->stream)
-                    : launch_flux_batch_f64x(c, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, stage, b->stream);
+                int rc = launch_flux_batch(c, b->variant[c], b->precision, b->d_tiles, offs, cnts, b->d_insts,
+                                           b->d_ytabs, stage, b->stream);
                 if (rc) return rc;
             }
             // the stage update ran in the flux launch's epilogue; fill the
@@ -472,6 +500,71 @@ extern "C"
         if (bytes_budget) *bytes_budget = b->arena.size;
         if (active) *active = n;
         if (cells) *cells = c;
+        return GBNS_OK;
+    }
+
+    int gbns_batch_autotune(gbns_batch* b, int reps, int* variants_out)
+    {
+        if (!b || reps < 1) return set_error(GBNS_ERR_INVALID, "bad batch or repetition count");
+        int rc = enter(b);
+        if (rc) return rc;
+        if (b->dirty) rc = rebuild_lists(b);
+        const unsigned active = b->class_mask;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (!rc) rc = check_cuda(cudaEventCreate(&e0), "autotune event");
+        if (!rc) rc = check_cuda(cudaEventCreate(&e1), "autotune event");
+        for (int c = 0; c < BCLASS_COUNT && !rc; ++c)
+        {
+            if (!(active & (1u << c))) continue;
+            // stage 0 reads q and writes only R0 and the second state buffer,
+            // so timing it leaves every instance's state as it was
+            float best_ms = 0.0f;
+            int best = 0;
+            for (int v = 0; v < batch_class_variants(c, b->precision) && !rc; ++v)
+            {
+                b->variant[c] = v;
+                rc = rebuild_lists(b);
+                const int* offs = b->d_meta;
+                const int* cnts = b->d_meta + BCLASS_COUNT;
+                if (!rc) rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, 0, b->stream);
+                if (!rc) rc = check_cuda(cudaEventRecord(e0, b->stream), "autotune event");
+                for (int r = 0; r < reps && !rc; ++r)
+                    rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, 0, b->stream);
+                if (!rc) rc = check_cuda(cudaEventRecord(e1, b->stream), "autotune event");
+                if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "autotune sync");
+                float ms = 0.0f;
+                if (!rc) rc = check_cuda(cudaEventElapsedTime(&ms, e0, e1), "autotune elapsed");
+                if (!rc && (v == 0 || ms < best_ms)) { best_ms = ms; best = v; }
+            }
+            b->variant[c] = best;
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (!rc) rc = rebuild_lists(b);
+        b->graph_valid = false;
+        if (!rc && variants_out)
+            for (int c = 0; c < BCLASS_COUNT; ++c) variants_out[c] = (active & (1u << c)) ? b->variant[c] : -1;
+        return leave(b, rc);
+    }
+
+    int gbns_batch_set_variant(gbns_batch* b, int cls, int variant)
+    {
+        if (!b || cls < 0 || cls >= BCLASS_COUNT) return set_error(GBNS_ERR_INVALID, "bad batch or kernel class");
+        if (variant < 0 || variant >= batch_class_variants(cls, b->precision))
+            return set_error(GBNS_ERR_INVALID, "tile variant out of range for this class");
+        b->variant[cls] = variant;
+        b->dirty = true;
+        b->graph_valid = false;
+        return GBNS_OK;
+    }
+
+    int gbns_batch_class_count(void) { return BCLASS_COUNT; }
+
+    int gbns_batch_class_variant_info(int cls, int precision, int variant, int* tile_xyz)
+    {
+        if (cls < 0 || cls >= BCLASS_COUNT || variant < 0 || variant >= batch_class_variants(cls, precision))
+            return set_error(GBNS_ERR_INVALID, "bad kernel class or variant");
+        if (tile_xyz) batch_class_tile(cls, precision, variant, tile_xyz);
         return GBNS_OK;
     }
 

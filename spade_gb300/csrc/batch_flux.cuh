@@ -1,5 +1,7 @@
 // Persistent flux-divergence kernels of the batched form.  Each TU defines
-// GBNS_REAL, GBNS_TAG, GBNS_FP32 and GBNS_BATCH_FN and includes this.
+// GBNS_REAL, GBNS_TAG, GBNS_FP32, GBNS_BATCH_GROUP and GBNS_BATCH_FN and
+// includes this; a TU instantiates the tile variants of its group of kernel
+// classes (0: cent_keep<2>, totani_lr, fweno_t; 1: WENO5; 2: hybrid).
 #pragma once
 
 #include "flux_kernel.cuh"
@@ -11,9 +13,27 @@ namespace gbns
     {
         status_registrar tu_status_registrar;
 
+        // The per-item arguments live in shared memory, not in registers: a
+        // CTA copies its item's geometry and scheme constants there and the
+        // tile code reads them like the single-grid kernel's parameters, so
+        // the persistent loop adds no live state to the tile's register
+        // budget (which lets the FP64 classes run the 576-thread tiles).
+        template <class Real>
+        struct ItemArgs
+        {
+            GeomK G;
+            SchemeK S;
+            SchemeR<Real> SR;
+            FluxArgs A;
+            const YTabK* ytab;
+            int it, n, lb, tile;    // the CTA's position in its class's item range
+        };
+
         // CTAs loop over their class's range of the tile list; the arrays
         // are read through the instance descriptors (no TMA: the halo is
         // staged with coalesced loads, or straight into FP32 for FP32-flux).
+        // The loop's own state (item index, range, the item) is kept in
+        // shared memory too.
         template <class Cfg>
         __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
         flux_batch_kernel(const TileItem* __restrict__ items, const int* __restrict__ offsets,
@@ -21,47 +41,73 @@ namespace gbns
                           const YTabK* __restrict__ ytabs, const int cls, const int stage)
         {
             extern __shared__ __align__(128) unsigned char smem_raw[];
-            const int base = offsets[cls];
-            const int n = counts[cls];
-            for (int it = blockIdx.x; it < n; it += gridDim.x)
+            __shared__ __align__(16) ItemArgs<typename Cfg::Real> arg;
+            if (threadIdx.x == 0)
             {
-                const TileItem w = items[base + it];
+                arg.it = blockIdx.x;
+                arg.n = counts[cls];
+            }
+            __syncthreads();
+            while (arg.it < arg.n)
+            {
+                const TileItem w = items[offsets[cls] + arg.it];
                 const InstK& I = insts[w.inst];
-                // The SSPRK3 stage fused into the flux launch, as gbns_ssprk3_step
-                // issues it, with R[2] as the second state buffer:
-                //   stage 0: q    -> R0, q1 into R[2]
-                //   stage 1: R[2] -> R1, q2 into q
-                //   stage 2: q    -> (no store), q3 into R[2]  (copied back by the ghost pass)
-                // coefficients: ratio_diff of consecutive ssprk3_t rows times dt
-                // (advance.h:80-95).
-                const double dt = I.dt;
-                FluxArgs A;
-                A.increment = 0;
-                A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
-                A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
-                A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
-                A.use_tma = 0;
-                A.rk_nres = stage + 1;
-                A.rk_res[0] = I.R[0];
-                A.rk_res[1] = I.R[1];
-                A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
-                if (stage == 0)
                 {
-                    A.prims = I.q; A.rhs = I.R[0]; A.write_rhs = 1; A.q_out = I.R[2];
-                    A.rk_coeff[0] = (1.0/1.0)*dt;
+                    // geometry and scheme constants: word copies by the whole CTA
+                    const int* sg = reinterpret_cast<const int*>(&I.G);
+                    int* dg = reinterpret_cast<int*>(&arg.G);
+                    for (int i = threadIdx.x; i < int(sizeof(GeomK)/4); i += Cfg::NT) dg[i] = sg[i];
+                    const int* ss = reinterpret_cast<const int*>(&I.S);
+                    int* ds = reinterpret_cast<int*>(&arg.S);
+                    for (int i = threadIdx.x; i < int(sizeof(SchemeK)/4); i += Cfg::NT) ds[i] = ss[i];
                 }
-                else if (stage == 1)
+                if (threadIdx.x == 0)
                 {
-                    A.prims = I.R[2]; A.rhs = I.R[1]; A.write_rhs = 1; A.q_out = I.q;
-                    A.rk_coeff[0] = (-3.0/4.0)*dt; A.rk_coeff[1] = (1.0/4.0)*dt;
+                    // The SSPRK3 stage fused into the flux launch, as gbns_ssprk3_step
+                    // issues it, with R[2] as the second state buffer:
+                    //   stage 0: q    -> R0, q1 into R[2]
+                    //   stage 1: R[2] -> R1, q2 into q
+                    //   stage 2: q    -> (no store), q3 into R[2]  (copied back by the ghost pass)
+                    // coefficients: ratio_diff of consecutive ssprk3_t rows times dt
+                    // (advance.h:80-95).
+                    const double dt = I.dt;
+                    FluxArgs& A = arg.A;
+                    A.increment = 0;
+                    A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
+                    A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
+                    A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
+                    A.use_tma = 0;
+                    A.sh_off = 0;
+                    A.rk_nres = stage + 1;
+                    A.rk_res[0] = I.R[0];
+                    A.rk_res[1] = I.R[1];
+                    A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
+                    if (stage == 0)
+                    {
+                        A.prims = I.q; A.rhs = I.R[0]; A.write_rhs = 1; A.q_out = I.R[2];
+                        A.rk_coeff[0] = (1.0/1.0)*dt;
+                    }
+                    else if (stage == 1)
+                    {
+                        A.prims = I.R[2]; A.rhs = I.R[1]; A.write_rhs = 1; A.q_out = I.q;
+                        A.rk_coeff[0] = (-3.0/4.0)*dt; A.rk_coeff[1] = (1.0/4.0)*dt;
+                    }
+                    else
+                    {
+                        A.prims = I.q; A.rhs = nullptr; A.write_rhs = 0; A.q_out = I.R[2];
+                        A.rk_coeff[0] = (-1.0/12.0)*dt; A.rk_coeff[1] = (-1.0/12.0)*dt; A.rk_coeff[2] = (2.0/3.0)*dt;
+                    }
+                    arg.ytab = I.ytab >= 0 ? ytabs + I.ytab : nullptr;
+                    arg.lb = w.lb;
+                    arg.tile = w.tile;
                 }
-                else
-                {
-                    A.prims = I.q; A.rhs = nullptr; A.write_rhs = 0; A.q_out = I.R[2];
-                    A.rk_coeff[0] = (-1.0/12.0)*dt; A.rk_coeff[1] = (-1.0/12.0)*dt; A.rk_coeff[2] = (2.0/3.0)*dt;
-                }
-                if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, I.G, ytabs[I.ytab], I.S, A, w.lb, w.tile);
-                else flux_tile<Cfg>(smem_raw, nullptr, I.G, YTabNone{}, I.S, A, w.lb, w.tile);
+                __syncthreads();
+                if (threadIdx.x == 0) arg.SR.load(arg.S);
+                __syncthreads();
+                if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, arg.G, *arg.ytab, arg.S, arg.A, arg.lb, arg.tile, &arg.SR);
+                else flux_tile<Cfg>(smem_raw, nullptr, arg.G, YTabNone{}, arg.S, arg.A, arg.lb, arg.tile, &arg.SR);
+                __syncthreads();
+                if (threadIdx.x == 0) arg.it += gridDim.x;
                 __syncthreads();
             }
         }
@@ -82,23 +128,62 @@ namespace gbns
 #define GBNS_BRUN(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
     return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, cls, stage, st)
 
-    int GBNS_BATCH_FN(int cls, const TileItem* items, const int* offsets, const int* counts,
+    // The tile variants of each class (their shapes are listed by
+    // batch_class_tile in batch.cu, in the same order); variant 0 is the
+    // default the autotuner starts from.
+    int GBNS_BATCH_FN(int cls, int v, const TileItem* items, const int* offsets, const int* counts,
                       const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st)
     {
+#if GBNS_BATCH_GROUP == 0
         switch (cls)
         {
-            case BCLASS_CK2_ID:    GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, 256);
-            case BCLASS_TOTANI_ID: GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, 256);
-            case BCLASS_FWENO_ID:  GBNS_BRUN(GBNS_CONV_FWENO, 2, false, 8, 8, 8, 256);
-#if GBNS_FP32
-            case BCLASS_WENO5_ST:  GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 4, 256);
-            case BCLASS_WENO5_ID:  GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 4, 256);
-#else
-            case BCLASS_WENO5_ST:  GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 256);
-            case BCLASS_WENO5_ID:  GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 256);
-#endif
-            case BCLASS_HYB2_ID:   GBNS_BRUN(GBNS_CONV_HYBRID, 2, false, 8, 8, 4, 256);
+            case BCLASS_CK2_ID:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 4, 128);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, (GBNS_FP32 ? 512 : 576));
+                GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, 256);
+            case BCLASS_TOTANI_ID:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 4, 128);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, (GBNS_FP32 ? 512 : 576));
+                GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, 256);
+            case BCLASS_FWENO_ID:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_FWENO, 2, false, 8, 8, 4, 128);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_FWENO, 2, false, 8, 8, 8, (GBNS_FP32 ? 512 : 576));
+                GBNS_BRUN(GBNS_CONV_FWENO, 2, false, 8, 8, 8, 256);
         }
+#elif GBNS_BATCH_GROUP == 1
+        switch (cls)
+        {
+#if GBNS_FP32
+            case BCLASS_WENO5_ST:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 256);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 512);
+                GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 4, 256);
+            case BCLASS_WENO5_ID:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 256);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 512);
+                GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 4, 256);
+#else
+            case BCLASS_WENO5_ST:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 4, 256);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 576);
+                GBNS_BRUN(GBNS_CONV_WENO5, 2, true, 8, 8, 8, 256);
+            case BCLASS_WENO5_ID:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 4, 256);
+                if (v == 2) GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 576);
+                GBNS_BRUN(GBNS_CONV_WENO5, 2, false, 8, 8, 8, 256);
+#endif
+        }
+#else
+        switch (cls)
+        {
+            case BCLASS_HYB2_ID:
+                if (v == 1) GBNS_BRUN(GBNS_CONV_HYBRID, 2, false, 8, 8, 8, 256);
+#if !GBNS_FP32
+                if (v == 2) GBNS_BRUN(GBNS_CONV_HYBRID, 2, false, 8, 8, 8, 576);
+#endif
+                GBNS_BRUN(GBNS_CONV_HYBRID, 2, false, 8, 8, 4, 256);
+        }
+#endif
         return set_error(GBNS_ERR_UNSUPPORTED, "no batched kernel for this class");
     }
 }

@@ -1,0 +1,7 @@
+// Batched persistent flux kernels: FP32 flux arithmetic, FP64 accumulation; class group 1.
+#define GBNS_REAL float
+#define GBNS_TAG 65
+#define GBNS_FP32 1
+#define GBNS_BATCH_GROUP 1
+#define GBNS_BATCH_FN launch_flux_batch_f32_b
+#include "batch_flux.cuh"

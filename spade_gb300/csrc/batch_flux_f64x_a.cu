@@ -1,0 +1,7 @@
+// Batched persistent flux kernels: FP64, no FMA contraction (built with -fmad=false); class group 0.
+#define GBNS_REAL double
+#define GBNS_TAG 64
+#define GBNS_FP32 0
+#define GBNS_BATCH_GROUP 0
+#define GBNS_BATCH_FN launch_flux_batch_f64x_a
+#include "batch_flux.cuh"

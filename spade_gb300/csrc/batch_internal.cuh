@@ -51,15 +51,25 @@ namespace gbns
     // Returns the class of a (grid, scheme) pair or -1 if it has no batched kernel.
     int batch_class_of(const gbns_grid_desc* g, const gbns_scheme_desc* s);
 
-    // Tile shape of a class (for counting tiles per block on the host).
-    void batch_class_tile(int cls, int precision, int tile[3]);
+    // Tile variants of a class: how many, and the tile shape of one (for
+    // counting tiles per block on the host).
+    int batch_class_variants(int cls, int precision);
+    void batch_class_tile(int cls, int precision, int variant, int tile[3]);
 
-    // Persistent flux launch of one class for one SSPRK3 stage.  `offsets`
-    // and `counts` (device, BCLASS_COUNT ints) locate the class's items.
-    int launch_flux_batch_f64x(int cls, const TileItem* items, const int* offsets, const int* counts,
-                               const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
-    int launch_flux_batch_f32(int cls, const TileItem* items, const int* offsets, const int* counts,
-                              const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
+    // Persistent flux launch of one class (tile variant v) for one SSPRK3
+    // stage.  `offsets` and `counts` (device, BCLASS_COUNT ints) locate the
+    // class's items.  One function per precision and class group
+    // (a: cent_keep<2>, totani_lr, fweno_t; b: WENO5; c: hybrid).
+#define GBNS_BATCH_DECL(NAME) \
+    int NAME(int cls, int v, const TileItem* items, const int* offsets, const int* counts, \
+             const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
+    GBNS_BATCH_DECL(launch_flux_batch_f64x_a)
+    GBNS_BATCH_DECL(launch_flux_batch_f64x_b)
+    GBNS_BATCH_DECL(launch_flux_batch_f64x_c)
+    GBNS_BATCH_DECL(launch_flux_batch_f32_a)
+    GBNS_BATCH_DECL(launch_flux_batch_f32_b)
+    GBNS_BATCH_DECL(launch_flux_batch_f32_c)
+#undef GBNS_BATCH_DECL
 
     // Batched ghost fill (mode 0: q, 1: R[2], 2: copy R[2] into q and fill
     // q's ghosts); the RK stage update runs in the flux launch's epilogue.

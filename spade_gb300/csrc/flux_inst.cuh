@@ -43,33 +43,45 @@ namespace gbns
         CUtensorMap tmap;
         std::memset(&tmap, 0, sizeof(tmap));
         A.use_tma = 0;
-        const bool aligned = (G.ni % 2 == 0) && ((reinterpret_cast<uintptr_t>(c.prims) & 15) == 0);
-        if (!Cfg::DIRECT && aligned && !tma_disabled())
-        {
-            int rc = encode_prims_tmap(&tmap, c.prims, G, Cfg::BXE, Cfg::BY, Cfg::BZ);
-            if (rc) return rc;
-            A.use_tma = 1;
-        }
+        A.sh_off = 0;
         auto kern = flux_div_kernel<Cfg>;
         int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM_BYTES)),
                             "flux_div smem attribute");
         if (rc) return rc;
+        const bool aligned = (G.ni % 2 == 0) && ((reinterpret_cast<uintptr_t>(c.prims) & 15) == 0);
+        ShadowK sh{nullptr, 0, 0};
+        if constexpr (Cfg::SHADOW)
+        {
+            // FP32 copy of the state, staged by TMA (its layout is always aligned)
+            rc = shadow_begin(c.prims, G, Cfg::H, Cfg::BXE, Cfg::BY, Cfg::BZ, c.stream, sh, &tmap);
+            if (rc) return rc;
+            A.use_tma = 1;
+            A.sh_off = sh.off;
+        }
+        else if (!Cfg::DIRECT && aligned && !tma_disabled())
+        {
+            rc = encode_prims_tmap(&tmap, c.prims, G, Cfg::BXE, Cfg::BY, Cfg::BZ);
+            if (rc) return rc;
+            A.use_tma = 1;
+        }
         const dim3 grid(unsigned(ntiles), unsigned(G.nblk));
         YTabT<Cfg::STRETCH> Y;
         if constexpr (Cfg::STRETCH) Y = *c.Y;
         kern<<<grid, Cfg::NT, Cfg::SMEM_BYTES, c.stream>>>(tmap, G, Y, *c.S, A);
-        return check_cuda(cudaGetLastError(), "flux_div launch");
+        rc = check_cuda(cudaGetLastError(), "flux_div launch");
+        const int erc = shadow_end(sh, c.stream);
+        return rc ? rc : erc;
     }
     }
 }
 
 #define GBNS_RUN(CONV, ORDER, TX, TY, TZ, NT) \
     return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG, 0>>(c)
-// FP32 only: stencil cells loaded straight into FP32 shared memory
-#define GBNS_RUN_DIRECT(CONV, ORDER, TX, TY, TZ, NT) \
-    return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG, 1>>(c)
+// FP32 only: the box staged by TMA from the FP32 copy of the state
+#define GBNS_RUN_SHADOW(CONV, ORDER, TX, TY, TZ, NT) \
+    return run_flux_cfg<FluxCfg<GBNS_REAL, CONV, ORDER, GBNS_STRETCH, TX, TY, TZ, NT, GBNS_TAG, 2>>(c)
 #if GBNS_FP32
-#define GBNS_RUN_D GBNS_RUN_DIRECT
+#define GBNS_RUN_D GBNS_RUN_SHADOW
 #else
 #define GBNS_RUN_D GBNS_RUN
 #endif
@@ -77,9 +89,9 @@ namespace gbns
 namespace gbns
 {
     // Tile variants.  Variant 0 is the default; every variant computes
-    // bit-identical results.  In FP32 TUs the GBNS_RUN_D variants load the
-    // stencil straight into FP32 shared memory and the last variant stages
-    // the FP64 box through TMA.
+    // bit-identical results.  In FP32 TUs the GBNS_RUN_D variants stage their
+    // box by TMA from the FP32 copy of the state and the last variant stages
+    // the FP64 box through TMA and converts it.
     int GBNS_FN(const FluxCall& c, int conv, int order)
     {
         const int v = c.variant;

@@ -78,7 +78,9 @@ namespace gbns
     // so their kernels and launchers never share a symbol.
     // STG_ (FP32 only): 0 = stage the FP64 box (TMA or coalesced loads) and
     // convert it; 1 = load the stencil cells straight into FP32 shared
-    // memory (no FP64 staging buffer, more CTAs per SM).
+    // memory (no FP64 staging buffer, more CTAs per SM); 2 = one TMA copy of
+    // the box from the FP32 SoA copy of the state (shadow.cu), which lands
+    // in shared memory already in the kernel's SoA layout.
     // Translation units compiled without FMA contraction (-fmad=false): the
     // FP64 drop-in's flux_f64x_* (tags 0-3), the batched FP64 kernel (64) and
     // boundary_flux (66).
@@ -102,12 +104,15 @@ namespace gbns
         static constexpr int TX = TX_, TY = TY_, TZ = TZ_, NT = NT_;
         static constexpr bool FP64 = std::is_same<Real, double>::value;
         static constexpr bool DIRECT = !FP64 && STG_ == 1;
+        static constexpr bool SHADOW = !FP64 && STG_ == 2;
         static constexpr int HC = ConvTraits<CONV, ORDER>::HC;
         static constexpr int H = HC > 1 ? HC : 1;
         static constexpr int NDER = ConvTraits<CONV, ORDER>::NDER;
         // x start is rounded down to an even padded cell (TMA 16-byte rule),
         // so the box is one cell wider and its width is kept even.
-        static constexpr int BXE = ((TX + 2*H + 1) + 1) & ~1;
+        // (FP32 copy: its rows are laid out so every tile's box starts on a
+        // 16-byte boundary; the width is rounded up to whole 16-byte groups)
+        static constexpr int BXE = SHADOW ? ((TX + 2*H + 3) & ~3) : (((TX + 2*H + 1) + 1) & ~1);
         static constexpr int BY = TY + 2*H, BZ = TZ + 2*H;
         static constexpr int BOXN = BXE*BY*BZ;
         static constexpr int SX = 1, SY = BXE, SZ = BXE*BY;
@@ -115,7 +120,7 @@ namespace gbns
         static constexpr int NF0 = (TX + 1)*TY*TZ, NF1 = TX*(TY + 1)*TZ, NF2 = TX*TY*(TZ + 1);
         static constexpr int NFMAX = cmax3(NF0, NF1, NF2);
         static constexpr int CPT = (NCELL + NT - 1)/NT;
-        static constexpr size_t STAGE_BYTES = DIRECT ? 0 : align128(size_t(BOXN)*5*sizeof(double));
+        static constexpr size_t STAGE_BYTES = (DIRECT || SHADOW) ? 0 : align128(size_t(BOXN)*5*sizeof(double));
         static constexpr size_t SOA_BYTES   = FP64 ? 0 : align128(size_t(BOXN)*5*sizeof(float));
         // FP64 fweno / WENO5: the Rusanov split (f+ and f- of the 5 equations)
         // of every cell on the tile's lines along the current direction is
@@ -145,7 +150,7 @@ namespace gbns
         static constexpr size_t FLX_BYTES   = align128(size_t(5)*NFS*sizeof(double));
         // FP32 staged: the staging buffer is dead once converted, so derived
         // values and face fluxes reuse it when they fit.
-        static constexpr bool REUSE = !FP64 && !DIRECT && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
+        static constexpr bool REUSE = !FP64 && !DIRECT && !SHADOW && (DER_BYTES + FLX_BYTES <= STAGE_BYTES);
         // FP32-flux on stretched grids: the tile's rows of the y-metric
         // tables (m, 1/m at cell centres, 1/m at y-faces) as floats, converted
         // once per tile instead of once per face
@@ -930,6 +935,7 @@ namespace gbns
         int increment;
         int ntile[3];       // tiles per block per direction
         int use_tma;
+        int sh_off;         // FP32 copy: column of padded index 0 (ShadowK::off)
         // Fused RK stage (0 = none): q_out = prim(cons(q) + sum_j rk_coeff[j] R_j)
         // for the tile's cells, with R_{rk_nres-1} this launch's residual (in
         // registers) and R_0..R_{rk_nres-2} read from rk_res.
@@ -985,8 +991,14 @@ namespace gbns
             }
             face_flux<Cfg, D>(V, S, rc, SplitIdx<Cfg, D>::right(fx, fy, fz), nD, inv, im, F);
         }
+        // FP32 fluxes widen exactly on the integer pipes (f2d_int), which
+        // keeps the FP64 pipe for the accumulation
         #pragma unroll
-        for (int v = 0; v < 5; ++v) sF[v*Cfg::NFS + base + f] = double(F[v]);
+        for (int v = 0; v < 5; ++v)
+        {
+            if constexpr (Cfg::FP64) sF[v*Cfg::NFS + base + f] = F[v];
+            else sF[v*Cfg::NFS + base + f] = f2d_int(F[v]);
+        }
     }
 
     // Divergence of direction D into the cells this thread owns, in the
@@ -1013,7 +1025,8 @@ namespace gbns
             double jac = 1.0;
             if constexpr (Cfg::STRETCH) jac = Y.im_cell[b[1]*ny + j0 + cy];
             const double multL = (jac*1.0)*invd[D];
-            const double multR = (jac*(-1.0))*invd[D];
+            // (jac*(-1.0))*invd rounds to exactly -(jac*invd): RN is symmetric
+            const double multR = -multL;
             #pragma unroll
             for (int v = 0; v < 5; ++v)
             {
@@ -1073,10 +1086,15 @@ namespace gbns
     // One tile of one block: the whole per-CTA algorithm.  Called by the
     // per-grid kernel (one CTA per tile) and by the persistent batch kernel
     // (CTAs loop over a work-list of tiles of many grids).
+    // Ssh (persistent batch kernel): the scheme constants already unpacked
+    // into shared memory, read from there at each use instead of being held
+    // in registers for the whole tile (the single-grid kernel reads them from
+    // its parameters, which cost no registers).
     template <class Cfg>
     __device__ __forceinline__ void flux_tile(unsigned char* smem_raw, const CUtensorMap* tmap, const GeomK& G,
                                               const YTabT<Cfg::STRETCH>& Y, const SchemeK& SK, const FluxArgs& A,
-                                              const int lb, const int tile)
+                                              const int lb, const int tile,
+                                              const SchemeR<typename Cfg::Real>* Ssh = nullptr)
     {
         using Real = typename Cfg::Real;
         constexpr int TX = Cfg::TX, TY = Cfg::TY, TZ = Cfg::TZ, H = Cfg::H;
@@ -1096,11 +1114,29 @@ namespace gbns
         const int b[3] = {lb % G.nb[0], (lb / G.nb[0]) % G.nb[1], lb / (G.nb[0]*G.nb[1])};
         const int px = i0 - H + G.ng;
         const int xs = px & ~1;
-        const int shift = px - xs;
+        const int shift = Cfg::SHADOW ? 0 : px - xs;
         const int ys = j0 - H + G.ng, zs = k0 - H + G.ng;
 
         // ---- stage the tile + halo --------------------------------------
-        if constexpr (Cfg::DIRECT)
+        if constexpr (Cfg::SHADOW)
+        {
+            // the box's five SoA planes in one tensor copy; its x start
+            // px + sh_off is a multiple of 4 floats by the copy's layout
+            if (tid == 0) mbar_init(bar, 1);
+            __syncthreads();
+            if (tid == 0)
+            {
+                mbar_expect_tx(bar, uint32_t(Cfg::BOXN)*5u*4u);
+                tma_load_4d(soa, tmap, bar, px + A.sh_off, ys, zs, 5*lb);
+            }
+            const bool ok = mbar_wait(bar, 0, MBAR_WAIT_CYCLES);
+            if (__syncthreads_or(!ok))
+            {
+                if (tid == 0) atomicExch(&g_device_status, DEV_TMA_TIMEOUT);
+                return;
+            }
+        }
+        else if constexpr (Cfg::DIRECT)
         {
             // Only the cells some face reads: the tile, the stencil cross of
             // radius max(HC, 1), and the edge cells one step out in two
@@ -1198,7 +1234,7 @@ namespace gbns
         __syncthreads();
 
         // ---- FP32 staged: convert the box to SoA floats -------------------
-        if constexpr (!Cfg::FP64 && !Cfg::DIRECT)
+        if constexpr (!Cfg::FP64 && !Cfg::DIRECT && !Cfg::SHADOW)
         {
             for (int c = tid; c < Cfg::BOXN; c += Cfg::NT)
             {
@@ -1216,8 +1252,9 @@ namespace gbns
         if constexpr (Cfg::SPLIT)
             der = reinterpret_cast<Real*>(reinterpret_cast<unsigned char*>(der) + Cfg::SPLIT_BYTES);
         V.der = der;
-        SchemeR<Real> S;
-        S.load(SK);
+        SchemeR<Real> S_own;
+        if (!Ssh) S_own.load(SK);
+        const SchemeR<Real>& S = Ssh ? *Ssh : S_own;
 
         // ---- per-cell derived values on the stencil cross -------------------
         if constexpr (Cfg::NDERB > 0)
@@ -1308,7 +1345,7 @@ namespace gbns
                 }
                 double cs[5];
                 if constexpr (Cfg::FP64) prim_to_cons(qv, SK.R, SK.gm1, cs);
-                else prim_to_cons_fast(qv, SK.R, SK.inv_gm1, cs);
+                else prim_to_cons_fast<true>(qv, SK.R, SK.inv_gm1, cs);
                 for (int j = 0; j + 1 < A.rk_nres; ++j)
                 {
                     const double* rr = A.rk_res[j] + off;
@@ -1320,7 +1357,7 @@ namespace gbns
                 for (int v = 0; v < 5; ++v) cs[v] += cl*relem[s][v];
                 double qn[5];
                 if constexpr (Cfg::FP64) cons_to_prim(cs, SK.R, SK.gm1, qn);
-                else cons_to_prim_fast(cs, SK.inv_R, SK.gm1, qn);
+                else cons_to_prim_fast<true>(cs, SK.inv_R, SK.gm1, qn);
                 double* o = A.q_out + off;
                 #pragma unroll
                 for (int v = 0; v < 5; ++v) o[v] = qn[v];

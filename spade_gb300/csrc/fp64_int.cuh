@@ -1,5 +1,5 @@
-// IEEE 754 binary64 multiplication, division and square root computed on the
-// integer pipes.
+// IEEE 754 binary64 multiplication, division and square root, and the
+// FP32<->FP64 conversions, computed on the integer pipes.
 //
 // GB300 executes FP64 at 1/64 of its FP32 rate (two FP64 lanes per SM and
 // clock) while its integer multiply-add and logic pipes are mostly idle in the
@@ -186,5 +186,39 @@ namespace gbns
         const uint32_t ex = (uint32_t)(u >> 52) & 0x7ffu;
         if (ex - uint32_t(1 - E) >= uint32_t(2046 - (1 - E) + 1)) return x*(E == -1 ? 0.5 : (E == -2 ? 0.25 : __longlong_as_double((long long)(uint64_t(1023 + E) << 52))));
         return __longlong_as_double((long long)(u - (uint64_t(-E) << 52)));
+    }
+
+    // float -> double on the integer pipes (exact): rebias the exponent
+    // (127 -> 1023, or 255 -> 2047 for infinities and NaNs, whose payload
+    // bits move along) and widen the significand.  FP32 zeros keep their
+    // sign; FP32 subnormals (|x| < 2^-126) become zero of the same sign.
+    __device__ __forceinline__ double f2d_int(float f)
+    {
+        const uint32_t u = __float_as_uint(f);
+        const uint32_t a = u & 0x7fffffffu;
+        const uint32_t e = a >> 23;
+        uint32_t hi = (a >> 3) + (e == 255u ? (1792u << 20) : (896u << 20));
+        uint32_t lo = u << 29;
+        if (e == 0u) { hi = 0u; lo = 0u; }
+        return __hiloint2double(int(hi | (u & 0x80000000u)), int(lo));
+    }
+
+    // double -> float rounded to nearest even on the integer pipes, the same
+    // bits as the hardware conversion for every double whose float result is
+    // normal (biased float exponent 1..254 before rounding; a carry out of
+    // the rounding moves into the exponent, up to infinity as the hardware
+    // does); zeros, results in the float subnormal range, overflows,
+    // infinities and NaNs take the hardware conversion.
+    __device__ __forceinline__ float d2f_int(double x)
+    {
+        const uint64_t u = (uint64_t)__double_as_longlong(x);
+        const uint32_t hi = uint32_t(u >> 32), lo = uint32_t(u);
+        const uint32_t e = (hi >> 20) & 0x7ffu;
+        if (e - 897u > 253u) return __double2float_rn(x);
+        const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);     // 23 significand bits
+        const uint32_t rem = lo & 0x1fffffffu;                       // the 29 bits below
+        uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;
+        f += uint32_t(rem > 0x10000000u) | (uint32_t(rem == 0x10000000u) & (m & 1u));
+        return __uint_as_float(f);
     }
 }

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "gbns.h"
+#include "fp64_int.cuh"
 
 namespace gbns
 {
@@ -115,6 +116,28 @@ namespace gbns
     // Tensor-map creation through the driver entry point (no -lcuda link).
     int encode_prims_tmap(CUtensorMap* map, const double* base, const GeomK& G,
                           int box_cells_x, int box_y, int box_z);
+
+    // FP32 copy of a padded AoS5 state for the FP32-flux kernels: SoA per
+    // block, float q32[lb][v][k][j][col], col = i + ng + off, rows of ipad
+    // floats (a multiple of 4, so every row and the x start of every tile's
+    // box are 16-byte aligned for TMA).  It lives in stream-ordered memory
+    // from the library's own pool for the duration of one launch.
+    struct ShadowK
+    {
+        float* base;
+        int ipad;       // floats per row
+        int off;        // column of padded index 0
+    };
+    // Allocates the copy on `st` (cudaMallocFromPoolAsync), converts
+    // `prims` into it and encodes the tensor map of a (box_x, box_y, box_z,
+    // 5) box.  `halo` is the kernel's stencil half width H: off is chosen
+    // so that a tile starting at interior index i0 (a multiple of 4) has
+    // its box start i0 - H + ng + off on a multiple of 4.
+    int shadow_begin(const double* prims, const GeomK& G, int halo, int box_x, int box_y, int box_z,
+                     cudaStream_t st, ShadowK& S, CUtensorMap* map);
+    // Returns the copy to the pool, ordered after the kernel on `st`.
+    int shadow_end(const ShadowK& S, cudaStream_t st);
+    int encode_shadow_tmap(CUtensorMap* map, const ShadowK& S, const GeomK& G, int box_x, int box_y, int box_z);
 
     // Launchers (defined in the kernel translation units) -----------------
     struct RkFuse;
@@ -243,10 +266,12 @@ namespace gbns
     // The same conversions with two reciprocals instead of four divisions, for
     // the FP32-flux form's stage update (FP64 state; not bit-identical to the
     // reference's rounding, which only the FP64 drop-in promises).
+    // (IM: the two reciprocals on the integer pipes, ddiv_int: the same bits)
+    template <bool IM = false>
     __device__ __forceinline__ void prim_to_cons_fast(const double q[5], const double R, const double inv_gm1,
                                                       double c[5])
     {
-        const double rho = q[0]*(1.0/(R*q[1]));
+        const double rho = q[0]*(IM ? ddiv_int(1.0, R*q[1]) : 1.0/(R*q[1]));
         const double rhoU2 = rho*(q[2]*q[2] + q[3]*q[3] + q[4]*q[4]);
         c[0] = rho;
         c[1] = 0.5*rhoU2 + q[0]*inv_gm1;
@@ -255,11 +280,12 @@ namespace gbns
         c[4] = rho*q[4];
     }
 
+    template <bool IM = false>
     __device__ __forceinline__ void cons_to_prim_fast(const double c[5], const double inv_R, const double gm1,
                                                       double q[5])
     {
         const double rh = c[0];
-        const double invrho = 1.0/rh;
+        const double invrho = IM ? ddiv_int(1.0, rh) : 1.0/rh;
         const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
         const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
         const double pp = gm1*(c[1] - 0.5*ru2);

@@ -279,6 +279,24 @@ namespace gbns
         return GBNS_OK;
     }
 
+    int encode_shadow_tmap(CUtensorMap* map, const ShadowK& S, const GeomK& G, int box_x, int box_y, int box_z)
+    {
+        encode_tiled_fn fn = get_encode_fn();
+        if (!fn) return set_error(GBNS_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        // (col, j, k, v + 5*lb): one box brings all five variables of a tile
+        // box into shared memory as SoA planes
+        const cuuint64_t plane = cuuint64_t(S.ipad)*G.nj*G.nk;
+        const cuuint64_t dims[4] = {cuuint64_t(S.ipad), cuuint64_t(G.nj), cuuint64_t(G.nk), cuuint64_t(5)*G.nblk};
+        const cuuint64_t strides[3] = {cuuint64_t(S.ipad)*4, cuuint64_t(S.ipad)*G.nj*4, plane*4};
+        const cuuint32_t box[4] = {cuuint32_t(box_x), cuuint32_t(box_y), cuuint32_t(box_z), 5};
+        const cuuint32_t estr[4] = {1, 1, 1, 1};
+        CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, S.base, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return set_error(GBNS_ERR_CUDA, "cuTensorMapEncodeTiled (FP32 copy) failed (" + std::to_string(int(r)) + ")");
+        return GBNS_OK;
+    }
+
     static int validate_bc(const gbns_bc_desc* bc)
     {
         if (!bc) return set_error(GBNS_ERR_INVALID, "bc descriptor is NULL");

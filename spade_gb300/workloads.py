@@ -77,8 +77,7 @@ def taylor_green(nblk=(2, 2, 2), ncell=(16, 16, 16), ng=2, mach=0.1, reynolds=16
     positive up to Mach ~1."""
     L = 1.0
     p0 = rho0 * R * T0
-    u0 = mach * math.sqrt(gamma * R * T0)
-    mu = rho0 * u0 * L / reynolds
+    u0, mu = tgv_params(mach, reynolds, gamma, R, T0, rho0)
     air = fluid_state.ideal_gas_t(gamma, R)
     blocks = _grid.cartesian_blocks_t(nblk, (0.0, 2 * math.pi, 0.0, 2 * math.pi, 0.0, 2 * math.pi))
     g = _grid.cartesian_grid_t(ncell, blocks, coords.identity())
@@ -113,24 +112,60 @@ def taylor_green(nblk=(2, 2, 2), ncell=(16, 16, 16), ng=2, mach=0.1, reynolds=16
                    dt=dt, mu=mu, u0=u0, ng=ng)
 
 
+def channel_flux(air, mu_ref, c_w, prandtl=0.72, T_wall=300.0, sutherland_S=110.4, eps_diss=0.01,
+                 weno="weno5", law="sutherland"):
+    """The channel's flux functor: compose(WENO, pressure_diss_lr(const
+    sensor 1, eps = eps_diss * c_w), visc_lr(law))."""
+    if weno == "weno5":
+        conv = convective.weno5_t(air)
+    elif weno == "fweno":
+        conv = convective.fweno_t(air)
+    else:
+        raise ValueError(weno)
+    if law == "sutherland":
+        vlaw = viscous_laws.sutherland_t(mu_ref, T_wall, sutherland_S, prandtl)
+    elif law == "power":
+        vlaw = viscous_laws.power_law_t(mu_ref, T_wall, 0.76, prandtl)
+    else:
+        vlaw = viscous_laws.constant_viscosity_t(mu_ref, prandtl)
+    diss = convective.pressure_diss_lr(air, state_sensor.const_sensor_t(1.0), eps_diss * c_w, eps_diss * c_w)
+    return omni.compose(conv, diss, viscous.visc_lr(vlaw, air))
+
+
+def channel_params(mach_b=0.5, re_b=3000.0, gamma=1.4, R=287.0, T_wall=300.0, rho_b=1.0):
+    """(c_w, U_b, mu_ref) of the channel: wall sound speed, bulk velocity,
+    viscosity rho_b U_b h / Re_b with half-height h = 1."""
+    c_w = math.sqrt(gamma * R * T_wall)
+    U_b = mach_b * c_w
+    return c_w, U_b, rho_b * U_b * 1.0 / re_b
+
+
+def tgv_params(mach=0.1, reynolds=1600.0, gamma=1.4, R=287.0, T0=300.0, rho0=1.0):
+    """(u0, mu) of the Taylor-Green vortex with L = 1."""
+    u0 = mach * math.sqrt(gamma * R * T0)
+    return u0, rho0 * u0 * 1.0 / reynolds
+
+
 def channel(nblk=(8, 8, 8), ncell=(32, 32, 32), ng=3, beta=2.0, mach_b=0.5, re_b=3000.0, prandtl=0.72,
             gamma=1.4, R=287.0, T_wall=300.0, rho_b=1.0, sutherland_S=110.4, pert=0.05, seed=0, cfl=0.5,
             eps_diss=0.01, rng="numpy", device="cuda", weno="weno5", law="sutherland"):
-    """Wall-bounded channel 4 pi x 2 x 4 pi/3, tanh-stretched in y, periodic
-    in x and z, isothermal no-slip walls at y = +-1; laminar Poiseuille
-    profile plus Gaussian velocity perturbations."""
+    """Wall-bounded channel 4 pi x 2 x 4 pi/3, tanh-stretched in y (beta;
+    beta=None: uniform identity coordinates), periodic in x and z,
+    isothermal no-slip walls at y = +-1; laminar Poiseuille profile plus
+    Gaussian velocity perturbations."""
     air = fluid_state.ideal_gas_t(gamma, R)
-    c_w = math.sqrt(gamma * R * T_wall)
-    U_b = mach_b * c_w
+    c_w, U_b, mu_ref = channel_params(mach_b, re_b, gamma, R, T_wall, rho_b)
     p0 = rho_b * R * T_wall
-    mu_ref = rho_b * U_b * 1.0 / re_b
     blocks = _grid.cartesian_blocks_t(nblk, (0.0, 4 * math.pi, -1.0, 1.0, 0.0, 4 * math.pi / 3))
-    csys = coords.diagonal_coords(coords.identity_1D(), coords.tanh_stretch_1D(beta), coords.identity_1D())
+    if beta:
+        csys = coords.diagonal_coords(coords.identity_1D(), coords.tanh_stretch_1D(beta), coords.identity_1D())
+    else:
+        csys = coords.identity()
     g = _grid.cartesian_grid_t(ncell, blocks, csys)
     q = _grid.grid_array(g, 0.0, ng, device=device)
     nb = g.get_num_global_blocks()
     eta = _cell_centres(g, nb, ng, 1)
-    yphys = np.tanh(beta * eta) / math.tanh(beta)
+    yphys = np.tanh(beta * eta) / math.tanh(beta) if beta else eta
     y = torch.from_numpy(yphys).to(device)[:, None, :, None]
     d = q.data
     d[..., 0] = p0
@@ -145,24 +180,11 @@ def channel(nblk=(8, 8, 8), ncell=(32, 32, 32), ng=3, beta=2.0, mach_b=0.5, re_b
     wall = boundary.isothermal_wall_t(T_wall)
     walls = {2: wall, 3: wall}
     algs.boundary_fill(q, boundary.combine(boundary.ymin, boundary.ymax), wall)
-    if weno == "weno5":
-        conv = convective.weno5_t(air)
-    elif weno == "fweno":
-        conv = convective.fweno_t(air)
-    else:
-        raise ValueError(weno)
-    if law == "sutherland":
-        vlaw = viscous_laws.sutherland_t(mu_ref, T_wall, sutherland_S, prandtl)
-    elif law == "power":
-        vlaw = viscous_laws.power_law_t(mu_ref, T_wall, 0.76, prandtl)
-    else:
-        vlaw = viscous_laws.constant_viscosity_t(mu_ref, prandtl)
-    diss = convective.pressure_diss_lr(air, state_sensor.const_sensor_t(1.0), eps_diss * c_w, eps_diss * c_w)
-    flux = omni.compose(conv, diss, viscous.visc_lr(vlaw, air))
+    flux = channel_flux(air, mu_ref, c_w, prandtl, T_wall, sutherland_S, eps_diss, weno, law)
     # physical spacing: dy = deta * dy/deta, smallest at the walls
     deta = g.get_dx(1)
     s_wall = 1.0
-    dydeta_min = beta * (1.0 - math.tanh(beta * s_wall) ** 2) / math.tanh(beta)
+    dydeta_min = beta * (1.0 - math.tanh(beta * s_wall) ** 2) / math.tanh(beta) if beta else 1.0
     dmin = min(g.get_dx(0), g.get_dx(2), deta * dydeta_min)
     umax = algs.transform_reduce(q, air, algs.reduce_ops.max_wavespeed)
     dt = stable_dt(cfl, dmin, umax, mu_ref / rho_b)

@@ -1,5 +1,5 @@
-// Host check of the integer FP64 multiply, power-of-two scaling, division and
-// square root
+// Host check of the integer FP64 multiply, power-of-two scaling, division,
+// square root and FP32<->FP64 conversions
 // (spade_gb300/csrc/fp64_int.cuh):
 // the header is compiled for the CPU with its CUDA intrinsics replaced by
 // portable equivalents and compared bit for bit with the host's IEEE
@@ -25,6 +25,12 @@ static float g_seed_scale = 1.0f;
 static inline float __fdividef(float a, float b) { volatile float q = (a/b)*g_seed_scale; return q; }
 static inline float rsqrtf(float x) { volatile float r = (1.0f/std::sqrt(x))*g_seed_scale; return r; }
 static inline double __dsqrt_rn(double x) { volatile double r = std::sqrt(x); return r; }
+static inline double __hiloint2double(int hi, int lo)
+{
+    const uint64_t u = (uint64_t(uint32_t(hi)) << 32) | uint32_t(lo);
+    return __longlong_as_double((long long)u);
+}
+static inline float __double2float_rn(double x) { volatile float f = float(x); return f; }
 #include "fp64_int.cuh"
 
 static uint64_t mix64(uint64_t x)
@@ -99,6 +105,41 @@ int main(int argc, char** argv)
                 if (!bad) std::printf("first sqrt mismatch: a=%a hw=%a int=%a\n", a, hs, es);
                 ++bad;
             }
+        }
+    }
+    // float -> double: every float bit pattern whose low 7 bits are a fixed
+    // mix (2^25 patterns covering every exponent and sign); FP32 subnormals
+    // become signed zeros, everything else must equal the host conversion
+    for (uint64_t k = 0; k < (1ull << 25); ++k)
+    {
+        const uint32_t fb = uint32_t(k << 7) | uint32_t(mix64(k) & 0x7f);
+        const float f = __uint_as_float(fb);
+        const double h = double(f), e = gbns::f2d_int(f);
+        const bool sub = ((fb >> 23) & 0xff) == 0;
+        const double want = sub ? (std::signbit(f) ? -0.0 : 0.0) : h;
+        if (__double_as_longlong(want) != __double_as_longlong(e) && !(want != want && e != e))
+        {
+            if (!bad) std::printf("first f2d mismatch: f=%a hw=%a int=%a\n", double(f), h, e);
+            ++bad;
+        }
+    }
+    // double -> float (round to nearest even): the generated operands, plus
+    // doubles placed exactly on and next to float rounding ties
+    for (uint64_t k = 0; k < n/2; ++k)
+    {
+        double a = __longlong_as_double((long long)operand(k, 0));
+        if ((k & 3) == 1)
+        {
+            // exponent within the float range, low 29 bits a tie or its neighbours
+            const uint64_t r = mix64(k);
+            const uint64_t ex = 897 + r % 254, low = 0x10000000ull + (r >> 40) % 3 - 1;
+            a = __longlong_as_double((long long)((r & 0x800FFFFFE0000000ull) | (ex << 52) | low));
+        }
+        const float h = __double2float_rn(a), e = gbns::d2f_int(a);
+        if (__float_as_uint(h) != __float_as_uint(e) && !(h != h && e != e))
+        {
+            if (!bad) std::printf("first d2f mismatch: a=%a hw=%a int=%a\n", a, double(h), double(e));
+            ++bad;
         }
     }
     std::printf("pairs %llu mismatches %llu\n", (unsigned long long)n, (unsigned long long)bad);

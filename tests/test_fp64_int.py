@@ -1,7 +1,8 @@
 """The integer-pipe FP64 arithmetic of the flux kernels (fp64_int.cuh):
-multiply (dmul_int), power-of-two scaling (dmul_pow2), division (ddiv_int)
-and square root (dsqrt_int), compiled for the host and compared bit for bit
-with the CPU's IEEE operations on generated operand sets; division and square
+multiply (dmul_int), power-of-two scaling (dmul_pow2), division (ddiv_int),
+square root (dsqrt_int) and the FP32<->FP64 conversions (f2d_int, d2f_int),
+compiled for the host and compared bit for bit with the CPU's IEEE operations
+on generated operand sets; division and square
 root also with their reciprocal seeds perturbed, to show the refinement
 absorbs a seed error well beyond the device's.  The GPU comparison with the
 hardware operations is

@@ -7,7 +7,7 @@ must not stall on an allocation.
 The GPU test calls it through the C ABI twice in a row for every reduction
 kind and checks each result against gbns_reduce (library-allocated scratch)
 on the same state.  The arithmetic and partition are gbns_reduce's, so the
-results must be bit-identical.  One grid is small (4 partial records) and one
+results must be bit-identical.  One grid is small (3 partial records) and one
 has 4x4x4 blocks of 32^3 cells, which uses the full 1024 partial records the
 fixed array holds.  It must pass alone in a fresh process and after the
 other tests.  The argument checks return before any CUDA call and run on the
@@ -24,8 +24,8 @@ import problems as P
 
 CASES = [
     # (blocks, cells per block, ghosts, coordinates, partial records used)
-    ((3, 2, 2), (9, 7, 6), 2, _abi.COORDS_IDENTITY, 4),
-    ((3, 2, 2), (9, 7, 6), 2, _abi.COORDS_TANH_Y, 4),
+    ((3, 2, 2), (9, 7, 6), 2, _abi.COORDS_IDENTITY, 3),
+    ((3, 2, 2), (9, 7, 6), 2, _abi.COORDS_TANH_Y, 3),
     ((4, 4, 4), (32, 32, 32), 3, _abi.COORDS_TANH_Y, 1024),
 ]
 
