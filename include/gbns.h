@@ -386,8 +386,18 @@ int gbns_batch_add(gbns_batch* batch, const gbns_grid_desc* grid, const gbns_sch
                    const gbns_bc_desc* bc, double dt, const double* prims, int* slot);
 int gbns_batch_remove(gbns_batch* batch, int slot);
 
-/* Advances every active instance by nsteps SSPRK3 steps (asynchronous). */
+/* Advances every active instance by nsteps SSPRK3 steps (asynchronous); an
+ * instance with a step limit (gbns_batch_set_steps) stops when it reaches
+ * it and idles (its tiles are skipped on the device) until removed. */
 int gbns_batch_step(gbns_batch* batch, int nsteps);
+
+/* Step limit of an instance: it does at most nsteps more steps, counted on
+ * the device, so a request can finish inside a chunk of steps without the
+ * chunk being cut to it (nsteps < 0: no limit, the default).  Results are
+ * those of exactly that many steps.  No reference counterpart. */
+int gbns_batch_set_steps(gbns_batch* batch, int slot, long long nsteps);
+/* Steps the instance still has to do (-1: no limit), as of the work enqueued. */
+int gbns_batch_steps_left(gbns_batch* batch, int slot, long long* left);
 
 /* Device pointer to an instance's AoS5 state (owned by the batch) and its step count. */
 int gbns_batch_state(gbns_batch* batch, int slot, double** prims, long long* steps_done);

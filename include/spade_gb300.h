@@ -24,11 +24,13 @@
  *
  * Lowered functors: convective::cent_keep_scheme_t<gas, 2|4|6|8>,
  * convective::totani_lr, convective::fweno_t<gas, smooth>,
+ * spade::gb300::weno5_t<gas> (5th-order WENO, no reference counterpart),
  * convective::pressure_diss_lr<gas, state_sensor::const_sensor_t | ducros_t>,
  * convective::hybrid_scheme_t<cent_keep_scheme_t<gas, 2|4>, fweno_t, const_sensor_t | ducros_t, full_flux | diss_flux>,
- * viscous::visc_lr<viscous_laws::constant_viscosity_t | power_law_t, gas>,
+ * viscous::visc_lr<viscous_laws::constant_viscosity_t | power_law_t | spade::gb300::sutherland_t, gas>,
  * and omni::compose of one of each (convective, dissipation, viscous).
- * Coordinates: coords::identity.
+ * Coordinates: coords::identity, and coords::diagonal_coords(identity_1D, y, identity_1D)
+ * with y = spade::gb300::tanh_stretch_1D (beta) or coords::integrated_tanh_1D.
  *
  * source_term: spade::gb300::const_source_t / body_force_t / body_accel_t
  * passed to spade::pde_algs::source_term run on the GPU (gbns_source_term).
@@ -50,6 +52,7 @@
  */
 #pragma once
 
+#include <cmath>
 #include <string>
 #include <type_traits>
 #include <cuda_runtime_api.h>
@@ -64,6 +67,93 @@ namespace spade::pde_algs
 
 namespace spade::gb300
 {
+    // ------------------------------------------------------------------
+    // Functors and coordinate maps of the GB300 path with no counterpart in
+    // the reference; they compose with the reference's own types
+    // (omni::compose, coords::diagonal_coords) and lower like them.
+    // ------------------------------------------------------------------
+
+    // 5th-order WENO-JS with the Rusanov flux splitting of fweno_t
+    // (navier-stokes/convective.h:335-497 is the 3rd-order model): six cells
+    // per face, linear weights 0.1/0.6/0.3, epsilon 1e-16.  Evaluated by the
+    // GB300 kernels only (flux_div with the gb300 traits); calling it on the
+    // CPU throws.
+    template <typename gas_t>
+    struct weno5_t
+    {
+        using float_t     = typename gas_t::value_type;
+        using output_type = fluid_state::flux_t<float_t>;
+        using m_info_type = omni::info_list_t<omni::info::value, omni::info::metric>;
+        using g_info_type = typename gas_t::info_type;
+        using info_type   = omni::info_union<m_info_type, g_info_type>;
+        using omni_type   = omni::stencil_t<
+                grid::face_centered,
+                omni::elem_t<omni::offset_t<-5, 0, 0>, info_type>,
+                omni::elem_t<omni::offset_t<-3, 0, 0>, info_type>,
+                omni::elem_t<omni::offset_t<-1, 0, 0>, info_type>,
+                omni::elem_t<omni::offset_t< 1, 0, 0>, info_type>,
+                omni::elem_t<omni::offset_t< 3, 0, 0>, info_type>,
+                omni::elem_t<omni::offset_t< 5, 0, 0>, info_type>
+            >;
+        const gas_t gas;
+        weno5_t(const gas_t& gas_in) : gas{gas_in} {}
+        output_type operator()(const auto&) const
+        {
+            throw except::sp_exception("gb300::weno5_t is evaluated by the GB300 kernels: use flux_div with the gb300 traits");
+        }
+    };
+
+    // Sutherland's law mu = mu_ref (T/T_ref)^(3/2) (T_ref + S)/(T + S) at the
+    // face state, beta = -2/3 mu, conductivity mu/Pr (the constant law's
+    // conventions, navier-stokes/viscous_laws.h:62-100).  State-dependent, in
+    // the form of power_law_t (viscous_laws.h:102-135).
+    template <typename dtype>
+    struct sutherland_t
+    : public viscous_laws::visc_law_interface_t<sutherland_t<dtype>, omni::info_list_t<omni::info::value>>
+    {
+        using value_type = dtype;
+        using base_t = viscous_laws::visc_law_interface_t<sutherland_t<dtype>, omni::info_list_t<omni::info::value>>;
+        using base_t::get_visc;
+        using base_t::get_beta;
+        using base_t::get_diffuse;
+        using base_t::info_type;
+        dtype mu_ref, T_ref, S, prandtl;
+        sutherland_t(const dtype& mu_ref_in, const dtype& T_ref_in, const dtype& S_in, const dtype& prandtl_in)
+        : mu_ref{mu_ref_in}, T_ref{T_ref_in}, S{S_in}, prandtl{prandtl_in} {}
+        template <fluid_state::is_state_type state_t> dtype get_visc(const state_t& q) const
+        {
+            const dtype x = q.T()/T_ref;
+            return (mu_ref*(x*std::sqrt(x)))*((T_ref + S)/(q.T() + S));
+        }
+        template <fluid_state::is_state_type state_t> dtype get_beta(const state_t& q) const
+        {
+            return this->get_visc(q)*dtype(-2.0/3.0);
+        }
+        template <fluid_state::is_state_type state_t> dtype get_diffuse(const state_t& q) const
+        {
+            return this->get_visc(q)/prandtl;
+        }
+    };
+
+    // Wall-normal tanh stretching y = tanh(beta eta)/tanh(beta) for eta in the
+    // grid's y bounds, usable as the y map of coords::diagonal_coords
+    // (core/coord_system.h:65-90; the reference parametrises its own tanh map,
+    // integrated_tanh_1D, by y0, y1, inflation and rate instead).
+    template <typename dtype>
+    struct tanh_stretch_1D
+    {
+        typedef dtype coord_type;
+        dtype beta = dtype(1.0);
+        tanh_stretch_1D() {}
+        tanh_stretch_1D(const dtype& beta_in) : beta{beta_in} {}
+        dtype map(const dtype& eta) const { return std::tanh(beta*eta)/std::tanh(beta); }
+        dtype coord_deriv(const dtype& eta) const
+        {
+            const dtype th = std::tanh(beta*eta);
+            return beta*(dtype(1.0) - th*th)/std::tanh(beta);
+        }
+    };
+
     // flux arithmetic precision trait
     struct flux_precision_base_t
     {
@@ -103,6 +193,17 @@ namespace spade::gb300
                 static_assert(order == 2 || order == 4 || order == 6 || order == 8, "cent_keep order 2, 4, 6 or 8");
                 s.convective = GBNS_CONV_CENT_KEEP;
                 s.order = order;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        template <typename gas_t>
+        struct lower<weno5_t<gas_t>>
+        {
+            static constexpr int slot = 0;
+            static void apply(gbns_scheme_desc& s, const weno5_t<gas_t>& f, bool& g)
+            {
+                s.convective = GBNS_CONV_WENO5;
                 set_gas(s, f.gas, g);
             }
         };
@@ -228,6 +329,64 @@ namespace spade::gb300
             }
         };
 
+        template <typename dt, typename gas_t>
+        struct lower<viscous::visc_lr<sutherland_t<dt>, gas_t>>
+        {
+            static constexpr int slot = 2;
+            static void apply(gbns_scheme_desc& s, const viscous::visc_lr<sutherland_t<dt>, gas_t>& f, bool& g)
+            {
+                s.viscous = GBNS_VISC_LR;
+                s.visc_law = GBNS_LAW_SUTHERLAND;
+                s.mu = f.vlaw.mu_ref;
+                s.T_ref = f.vlaw.T_ref;
+                s.S = f.vlaw.S;
+                s.power = 1.5;
+                s.prandtl = f.vlaw.prandtl;
+                set_gas(s, f.gas, g);
+            }
+        };
+
+        // coordinate systems: identity, or diagonal_coords with identity x
+        // and z and a tanh-stretched y (gbns_grid_desc coords, coord_param)
+        template <typename T> struct lower_coords
+        {
+            static_assert(always_false<T>::value,
+                          "the GB300 drop-in lowers coords::identity and diagonal_coords(identity_1D, "
+                          "tanh_stretch_1D | integrated_tanh_1D, identity_1D)");
+        };
+        template <> struct lower_coords<coords::identity<double>>
+        {
+            static void apply(gbns_grid_desc& g, const coords::identity<double>&) { g.coords = GBNS_COORDS_IDENTITY; }
+        };
+        template <> struct lower_coords<coords::diagonal_coords<coords::identity_1D<double>, tanh_stretch_1D<double>,
+                                                                coords::identity_1D<double>>>
+        {
+            template <typename c_t>
+            static void apply(gbns_grid_desc& g, const c_t& c)
+            {
+                g.coords = GBNS_COORDS_TANH_Y;
+                g.coord_param[0] = c.ycoord.beta;
+            }
+        };
+        template <> struct lower_coords<coords::diagonal_coords<coords::identity_1D<double>, coords::integrated_tanh_1D<double>,
+                                                                coords::identity_1D<double>>>
+        {
+            // integrated_tanh_1D keeps (eta1 = y0, eta0 = y1, deta, alpha0 =
+            // rate/deta, beta0 = alpha0 (inflation deta - eta0), ...)
+            // (core/coord_system.h:107-125); its constructor arguments are
+            // recovered from them (rate and inflation to rounding)
+            template <typename c_t>
+            static void apply(gbns_grid_desc& g, const c_t& c)
+            {
+                const auto& y = c.ycoord;
+                g.coords = GBNS_COORDS_INTEGRATED_TANH_Y;
+                g.coord_param[0] = y.eta1;
+                g.coord_param[1] = y.eta0;
+                g.coord_param[2] = (y.beta0/y.alpha0 + y.eta0)/y.deta;
+                g.coord_param[3] = y.alpha0*y.deta;
+            }
+        };
+
         template <typename k0_t, typename... ks_t>
         struct lower<omni::composite_kernel_t<k0_t, ks_t...>>
         {
@@ -290,7 +449,6 @@ namespace spade::gb300
     {
         const auto& grid = arr.get_grid();
         using coord_t = typename utils::remove_all<decltype(grid.get_coord_sys())>::type;
-        static_assert(std::is_same_v<coord_t, coords::identity<double>>, "the GB300 drop-in lowers coords::identity grids");
         static_assert(std::is_same_v<typename arr_t::value_type, double>, "the GB300 path works on double arrays");
         gbns_grid_desc g{};
         const auto& blocks = grid.get_blocks();
@@ -308,7 +466,7 @@ namespace spade::gb300
         if (arr.get_num_exchange(1) != ng || arr.get_num_exchange(2) != ng)
             throw except::sp_exception("gb300 flux_div: equal ghost depth in every direction required");
         g.ng = ng;
-        g.coords = GBNS_COORDS_IDENTITY;
+        detail::lower_coords<coord_t>::apply(g, grid.get_coord_sys());
         return g;
     }
 

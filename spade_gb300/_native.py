@@ -61,6 +61,8 @@ def lib():
     L.gbns_batch_instance_bytes.argtypes = [P(_abi.GridDesc)]
     L.gbns_batch_instance_bytes.restype = ctypes.c_size_t
     L.gbns_batch_autotune.argtypes = [vp, ctypes.c_int, P(ctypes.c_int)]
+    L.gbns_batch_set_steps.argtypes = [vp, ctypes.c_int, ctypes.c_longlong]
+    L.gbns_batch_steps_left.argtypes = [vp, ctypes.c_int, P(ctypes.c_longlong)]
     L.gbns_batch_set_variant.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     L.gbns_batch_class_count.argtypes = []
     L.gbns_batch_class_variant_info.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P(ctypes.c_int)]

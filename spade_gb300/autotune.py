@@ -1,9 +1,10 @@
 """Autotuner for the flux_div tile shape.
 
-Every tile variant of a scheme (gbns_flux_variant_count) computes
-bit-identical results; they differ in tile size, threads per CTA and, for
-FP32-flux, in how the halo is staged (straight into FP32 shared memory or a
-TMA copy of the FP64 box).  tune() times each variant on the caller's own
+Every tile variant of a scheme (gbns_flux_variant_count) computes the same
+results (bit for bit in FP64; in FP32-flux to single-precision rounding,
+since each instantiation's FP32 arithmetic is FMA-contracted on its own);
+they differ in tile size, threads per CTA and, for FP32-flux, in how the halo
+is staged (a TMA copy from the FP32 copy of the state, or of the FP64 box).  tune() times each variant on the caller's own
 arrays with CUDA events and caches the winner per (scheme, block shape,
 block count, ghosts, precision, GPU) in spade_gb300/_build/autotune.json.
 """

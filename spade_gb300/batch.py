@@ -67,6 +67,16 @@ class batch_t:
             res[self.CLASS_NAMES[c]] = {"variant": int(out[c]), "tile": (t[0], t[1], t[2])}
         return res
 
+    def set_steps(self, slot, nsteps):
+        """The instance does at most `nsteps` more steps (counted on the
+        device), then idles until removed; nsteps < 0 lifts the limit."""
+        _native.check(self.lib.gbns_batch_set_steps(self.handle, int(slot), int(nsteps)))
+
+    def steps_left(self, slot):
+        n = ctypes.c_longlong()
+        _native.check(self.lib.gbns_batch_steps_left(self.handle, int(slot), ctypes.byref(n)))
+        return n.value
+
     def set_variant(self, kernel_class, variant):
         _native.check(self.lib.gbns_batch_set_variant(self.handle, int(kernel_class), int(variant)))
 

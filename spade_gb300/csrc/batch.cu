@@ -42,18 +42,18 @@ namespace gbns
     }
 
     int launch_flux_batch(int cls, int v, int precision, const TileItem* items, const int* offsets, const int* counts,
-                          const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st)
+                          const InstK* insts, const YTabK* ytabs, const long long* left, int stage, cudaStream_t st)
     {
         const int group = cls == BCLASS_HYB2_ID ? 2 : ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) ? 1 : 0);
         if (precision == GBNS_PREC_FP32_FLUX)
         {
-            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, stage, st);
-            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, stage, st);
-            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
+            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
+            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
         }
-        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, stage, st);
-        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, stage, st);
-        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, stage, st);
+        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
+        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
+        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
     }
 
     // First-fit allocator over one device allocation (offsets in bytes).
@@ -106,6 +106,7 @@ namespace gbns
         int cls = -1;
         long long steps = 0;
         long long cells = 0;
+        long long left = -1;     // steps still to do before it idles (-1: no limit); mirrors d_left
     };
 }
 
@@ -123,6 +124,7 @@ struct gbns_batch
     Arena arena;
     std::vector<Slot> slots;
     InstK* d_insts = nullptr;
+    long long* d_left = nullptr;        // per-slot step counters (device)
     int inst_cap = 0;
     YTabK* d_ytabs = nullptr;
     TileItem* d_tiles = nullptr;
@@ -167,20 +169,29 @@ namespace
         while (cap < need) cap *= 2;
         InstK* ni = nullptr;
         YTabK* ny = nullptr;
+        long long* nl = nullptr;
         int rc = check_cuda(cudaMalloc(&ni, sizeof(InstK)*cap), "batch instance table");
         if (rc) return rc;
         rc = check_cuda(cudaMalloc(&ny, sizeof(YTabK)*cap), "batch metric tables");
         if (rc) { cudaFree(ni); return rc; }
+        rc = check_cuda(cudaMalloc(&nl, sizeof(long long)*cap), "batch step counters");
+        if (rc) { cudaFree(ni); cudaFree(ny); return rc; }
+        // new slots start idle (0) until an instance takes them
+        rc = check_cuda(cudaMemsetAsync(nl, 0, sizeof(long long)*cap, b->stream), "batch step counters");
+        if (rc) { cudaFree(ni); cudaFree(ny); cudaFree(nl); return rc; }
         if (b->d_insts)
         {
             cudaMemcpyAsync(ni, b->d_insts, sizeof(InstK)*b->inst_cap, cudaMemcpyDeviceToDevice, b->stream);
             cudaMemcpyAsync(ny, b->d_ytabs, sizeof(YTabK)*b->inst_cap, cudaMemcpyDeviceToDevice, b->stream);
+            cudaMemcpyAsync(nl, b->d_left, sizeof(long long)*b->inst_cap, cudaMemcpyDeviceToDevice, b->stream);
             cudaStreamSynchronize(b->stream);
             cudaFree(b->d_insts);
             cudaFree(b->d_ytabs);
+            cudaFree(b->d_left);
         }
         b->d_insts = ni;
         b->d_ytabs = ny;
+        b->d_left = nl;
         b->inst_cap = cap;
         b->graph_valid = false;
         return GBNS_OK;
@@ -269,15 +280,17 @@ namespace
             {
                 if (!(b->class_mask & (1u << c))) continue;
                 int rc = launch_flux_batch(c, b->variant[c], b->precision, b->d_tiles, offs, cnts, b->d_insts,
-                                           b->d_ytabs, stage, b->stream);
+                                           b->d_ytabs, b->d_left, stage, b->stream);
                 if (rc) return rc;
             }
             // the stage update ran in the flux launch's epilogue; fill the
             // ghosts of the state it wrote (stage 2: copy it back into q)
-            int rc = launch_ghost_batch(b->d_blocks, nblk, b->d_insts, stage == 0 ? 1 : (stage == 1 ? 0 : 2), b->stream);
+            int rc = launch_ghost_batch(b->d_blocks, nblk, b->d_insts, b->d_left, stage == 0 ? 1 : (stage == 1 ? 0 : 2),
+                                        b->stream);
             if (rc) return rc;
         }
-        return GBNS_OK;
+        // one step done by every instance that still had steps to do
+        return launch_steps_tick(b->d_left, b->inst_cap, b->stream);
     }
 
     int capture(gbns_batch* b)
@@ -342,6 +355,7 @@ extern "C"
         cudaFree(b->arena_base);
         cudaFree(b->d_insts);
         cudaFree(b->d_ytabs);
+        cudaFree(b->d_left);
         cudaFree(b->d_tiles);
         cudaFree(b->d_blocks);
         cudaFree(b->d_meta);
@@ -422,6 +436,8 @@ extern "C"
         }
         if (!rc) rc = check_cuda(cudaMemcpyAsync(I.q, prims, arr, cudaMemcpyDefault, b->stream), "copy initial state");
         if (!rc) rc = check_cuda(cudaMemcpyAsync(b->d_insts + si, &I, sizeof(InstK), cudaMemcpyHostToDevice, b->stream), "upload instance");
+        if (!rc) rc = launch_steps_set(b->d_left, si, -1, b->stream);
+        sl.left = -1;
         if (!rc) rc = launch_fill_ghosts(G, bc, I.q, b->stream);
         if (!rc) rc = check_cuda(cudaStreamSynchronize(b->stream), "batch add");
         if (rc) { sl.active = false; b->arena.release(off, 4*per); return rc; }
@@ -439,10 +455,13 @@ extern "C"
         if (!rc) rc = check_cuda(cudaStreamSynchronize(b->stream), "batch remove");
         if (rc) return rc;
         Slot& sl = b->slots[slot];
+        rc = launch_steps_set(b->d_left, slot, 0, b->stream);
+        if (rc) return rc;
         b->arena.release(sl.off, 4*sl.arr_bytes);
         sl.active = false;
+        sl.left = 0;
         b->dirty = true;
-        return GBNS_OK;
+        return leave(b, GBNS_OK);
     }
 
     static int batch_step_impl(gbns_batch* b, int nsteps);
@@ -476,7 +495,34 @@ extern "C"
             for (int n = 0; n < nsteps && !rc; ++n) rc = launch_step(b);
             if (rc) return rc;
         }
-        for (auto& sl : b->slots) if (sl.active) sl.steps += nsteps;
+        for (auto& sl : b->slots)
+        {
+            if (!sl.active) continue;
+            if (sl.left < 0) { sl.steps += nsteps; continue; }
+            const long long done = sl.left < nsteps ? sl.left : nsteps;
+            sl.steps += done;
+            sl.left -= done;
+        }
+        return GBNS_OK;
+    }
+
+    int gbns_batch_set_steps(gbns_batch* b, int slot, long long nsteps)
+    {
+        if (!b || slot < 0 || slot >= int(b->slots.size()) || !b->slots[slot].active)
+            return set_error(GBNS_ERR_INVALID, "no active instance in that slot");
+        int rc = enter(b);
+        if (rc) return rc;
+        const long long v = nsteps < 0 ? -1 : nsteps;
+        rc = launch_steps_set(b->d_left, slot, v, b->stream);
+        if (!rc) b->slots[slot].left = v;
+        return leave(b, rc);
+    }
+
+    int gbns_batch_steps_left(gbns_batch* b, int slot, long long* left)
+    {
+        if (!b || !left || slot < 0 || slot >= int(b->slots.size()) || !b->slots[slot].active)
+            return set_error(GBNS_ERR_INVALID, "no active instance in that slot");
+        *left = b->slots[slot].left;
         return GBNS_OK;
     }
 
@@ -526,10 +572,12 @@ extern "C"
                 rc = rebuild_lists(b);
                 const int* offs = b->d_meta;
                 const int* cnts = b->d_meta + BCLASS_COUNT;
-                if (!rc) rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, 0, b->stream);
+                if (!rc) rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs,
+                                                b->d_left, 0, b->stream);
                 if (!rc) rc = check_cuda(cudaEventRecord(e0, b->stream), "autotune event");
                 for (int r = 0; r < reps && !rc; ++r)
-                    rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs, 0, b->stream);
+                    rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs,
+                                           b->d_left, 0, b->stream);
                 if (!rc) rc = check_cuda(cudaEventRecord(e1, b->stream), "autotune event");
                 if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "autotune sync");
                 float ms = 0.0f;

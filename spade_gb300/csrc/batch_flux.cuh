@@ -38,7 +38,8 @@ namespace gbns
         __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
         flux_batch_kernel(const TileItem* __restrict__ items, const int* __restrict__ offsets,
                           const int* __restrict__ counts, const InstK* __restrict__ insts,
-                          const YTabK* __restrict__ ytabs, const int cls, const int stage)
+                          const YTabK* __restrict__ ytabs, const long long* __restrict__ left,
+                          const int cls, const int stage)
         {
             extern __shared__ __align__(128) unsigned char smem_raw[];
             __shared__ __align__(16) ItemArgs<typename Cfg::Real> arg;
@@ -51,6 +52,14 @@ namespace gbns
             while (arg.it < arg.n)
             {
                 const TileItem w = items[offsets[cls] + arg.it];
+                if (left[w.inst] == 0)
+                {
+                    // the instance has done its steps and idles until it is retired
+                    __syncthreads();
+                    if (threadIdx.x == 0) arg.it += gridDim.x;
+                    __syncthreads();
+                    continue;
+                }
                 const InstK& I = insts[w.inst];
                 {
                     // geometry and scheme constants: word copies by the whole CTA
@@ -114,25 +123,26 @@ namespace gbns
 
         template <class Cfg>
         int run_batch(const TileItem* items, const int* offsets, const int* counts, const InstK* insts,
-                      const YTabK* ytabs, int cls, int stage, cudaStream_t st)
+                      const YTabK* ytabs, const long long* left, int cls, int stage, cudaStream_t st)
         {
             auto kern = flux_batch_kernel<Cfg>;
             int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM_BYTES)),
                                 "flux_batch smem attribute");
             if (rc) return rc;
-            kern<<<persistent_grid(Cfg::MINB), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, cls, stage);
+            kern<<<persistent_grid(Cfg::MINB), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, left,
+                                                                               cls, stage);
             return check_cuda(cudaGetLastError(), "flux_batch launch");
         }
     }
 
 #define GBNS_BRUN(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
-    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, cls, stage, st)
+    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, left, cls, stage, st)
 
     // The tile variants of each class (their shapes are listed by
     // batch_class_tile in batch.cu, in the same order); variant 0 is the
     // default the autotuner starts from.
     int GBNS_BATCH_FN(int cls, int v, const TileItem* items, const int* offsets, const int* counts,
-                      const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st)
+                      const InstK* insts, const YTabK* ytabs, const long long* left, int stage, cudaStream_t st)
     {
 #if GBNS_BATCH_GROUP == 0
         switch (cls)

@@ -60,9 +60,11 @@ namespace gbns
     // stage.  `offsets` and `counts` (device, BCLASS_COUNT ints) locate the
     // class's items.  One function per precision and class group
     // (a: cent_keep<2>, totani_lr, fweno_t; b: WENO5; c: hybrid).
+    // `left` (device, one per slot): steps an instance still has to do before
+    // it idles (-1: no limit); items of instances at 0 are skipped.
 #define GBNS_BATCH_DECL(NAME) \
     int NAME(int cls, int v, const TileItem* items, const int* offsets, const int* counts, \
-             const InstK* insts, const YTabK* ytabs, int stage, cudaStream_t st);
+             const InstK* insts, const YTabK* ytabs, const long long* left, int stage, cudaStream_t st);
     GBNS_BATCH_DECL(launch_flux_batch_f64x_a)
     GBNS_BATCH_DECL(launch_flux_batch_f64x_b)
     GBNS_BATCH_DECL(launch_flux_batch_f64x_c)
@@ -73,7 +75,11 @@ namespace gbns
 
     // Batched ghost fill (mode 0: q, 1: R[2], 2: copy R[2] into q and fill
     // q's ghosts); the RK stage update runs in the flux launch's epilogue.
-    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, int mode, cudaStream_t st);
+    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, const long long* left,
+                           int mode, cudaStream_t st);
+    // per-slot step counters: one step done by every limited instance; set one
+    int launch_steps_tick(long long* left, int n, cudaStream_t st);
+    int launch_steps_set(long long* left, int slot, long long value, cudaStream_t st);
 
     int persistent_grid(int ctas_per_sm);
 }

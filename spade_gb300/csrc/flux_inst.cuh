@@ -88,8 +88,10 @@ namespace gbns
 
 namespace gbns
 {
-    // Tile variants.  Variant 0 is the default; every variant computes
-    // bit-identical results.  In FP32 TUs the GBNS_RUN_D variants stage their
+    // Tile variants.  Variant 0 is the default; every variant computes the
+    // same results (bit for bit in FP64, to single-precision rounding in
+    // FP32-flux, whose FP32 arithmetic each instantiation contracts on its
+    // own).  In FP32 TUs the GBNS_RUN_D variants stage their
     // box by TMA from the FP32 copy of the state and the last variant stages
     // the FP64 box through TMA and converts it.
     int GBNS_FN(const FluxCall& c, int conv, int order)

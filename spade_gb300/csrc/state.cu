@@ -310,7 +310,7 @@ namespace gbns
 
     __global__ void __launch_bounds__(256)
     ghost_batch_kernel(const BlockItem* __restrict__ items, const int* __restrict__ count, const InstK* __restrict__ insts,
-                       const int mode)
+                       const long long* __restrict__ left, const int mode)
     {
         // mode 0: ghosts of q; 1: ghosts of R[2] (the fused stage's second
         // state buffer); 2: q = R[2] on the interior with q's ghosts filled
@@ -319,6 +319,7 @@ namespace gbns
         for (int it = blockIdx.x; it < n; it += gridDim.x)
         {
             const BlockItem w = items[it];
+            if (left[w.inst] == 0) continue;      // the instance has done its steps: it idles
             const InstK& I = insts[w.inst];
             const GeomK& G = I.G;
             double* dst = mode == 1 ? I.R[2] : I.q;
@@ -343,10 +344,37 @@ namespace gbns
         }
     }
 
-    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, int mode, cudaStream_t st)
+    int launch_ghost_batch(const BlockItem* items, const int* count, const InstK* insts, const long long* left,
+                           int mode, cudaStream_t st)
     {
-        ghost_batch_kernel<<<persistent_grid(8), 256, 0, st>>>(items, count, insts, mode);
+        ghost_batch_kernel<<<persistent_grid(8), 256, 0, st>>>(items, count, insts, left, mode);
         return check_cuda(cudaGetLastError(), "ghost_batch launch");
+    }
+
+    // End of a batched step: every limited instance that still had steps to
+    // do has done one more (unlimited ones hold -1, finished ones 0).
+    __global__ void steps_tick_kernel(long long* left, const int n)
+    {
+        for (int i = blockIdx.x*blockDim.x + threadIdx.x; i < n; i += gridDim.x*blockDim.x)
+            if (left[i] > 0) left[i] -= 1;
+    }
+
+    __global__ void steps_set_kernel(long long* left, const int slot, const long long value)
+    {
+        left[slot] = value;
+    }
+
+    int launch_steps_tick(long long* left, int n, cudaStream_t st)
+    {
+        if (n <= 0) return GBNS_OK;
+        steps_tick_kernel<<<(n + 255)/256, 256, 0, st>>>(left, n);
+        return check_cuda(cudaGetLastError(), "batch step counters");
+    }
+
+    int launch_steps_set(long long* left, int slot, long long value, cudaStream_t st)
+    {
+        steps_set_kernel<<<1, 1, 0, st>>>(left, slot, value);
+        return check_cuda(cudaGetLastError(), "batch step limit");
     }
 
     // ------------------------------------------------------------------

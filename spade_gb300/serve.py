@@ -85,14 +85,29 @@ def build_instance(req, precision, seed):
 
 
 class server_t:
+    """Continuous batching server.  Between chunks of steps (one chunk in
+    flight on the GPU at a time) it retires the requests that reached their
+    step counts, admits arrived requests whose arrays fit the HBM budget
+    (first come, first served) and launches the next chunk.  While a chunk
+    runs, the host builds the initial states of arrived requests on a side
+    stream and polls the chunk's completion event instead of synchronising.
+    Each instance carries a device-side step limit (gbns_batch_set_steps), so
+    a request that finishes inside a chunk idles there at exactly its step
+    count and chunks keep their length (`chunk_ms` of GPU time, adapted from
+    the measured step time)."""
+
     def __init__(self, precision=_abi.PREC_FP32_FLUX, hbm_budget=150 << 30, chunk=16, use_graph=True,
-                 health_every=4):
+                 health_every=4, chunk_ms=60.0, prepare_ahead=4):
         self.precision = precision
         self.batch = batch_t(hbm_budget, precision, use_graph)
-        self.chunk = int(chunk)
+        self.chunk = int(chunk)               # steps of the first chunk (the cap is 4x this)
+        self.chunk_ms = float(chunk_ms)
         self.health_every = int(health_every)
+        self.prepare_ahead = int(prepare_ahead)
         self.lib = _native.lib()
-        self.st = int(torch.cuda.current_stream().cuda_stream)
+        self.stream = self.batch.stream
+        self.st = int(self.stream.cuda_stream)
+        self.side = torch.cuda.Stream()
 
     def _healthy(self, req):
         ptr, _ = self.batch.state_ptr(req.slot)
@@ -101,98 +116,140 @@ class server_t:
                                            ctypes.byref(out), self.st))
         return out.value == 0.0
 
-    def _admit(self, req, now):
-        prob = build_instance(req, self.precision, seed=req.id)
+    def _prepare(self, req):
+        """Builds the request's initial state on the side stream."""
+        with torch.cuda.stream(self.side):
+            prob = build_instance(req, self.precision, seed=req.id)
+            ev = torch.cuda.Event()
+            ev.record(self.side)
         req.grid = prob.q.desc()
         req.scheme = prob.scheme_desc(self.precision)
         req.bc = prob.bc_desc()
         req.dt = prob.dt
+        return prob, ev
+
+    def _admit(self, req, prob, ev, now):
+        ev.synchronize()
         req.slot = self.batch.add(req.grid, req.scheme, req.bc, req.dt, prob.q.ptr(), shape=prob.q.shape)
+        self.batch.set_steps(req.slot, req.steps)
         req.admitted = now
         req.status = "running"
-        torch.cuda.synchronize()
-        del prob
+
+    @staticmethod
+    def _need(req):
+        nb = req.edge // req.block
+        return batch_t.instance_bytes(_abi.grid_desc((nb,) * 3, (req.block,) * 3, 3, (0, 1, 0, 1, 0, 1)))
 
     def run(self, requests, collect=None, time_limit=None):
-        """Serves `requests` (sorted by arrival) to completion.  `collect`, if
-        given, is called as collect(req, state_tensor) on every completed
-        request before its slot is freed.  Returns statistics."""
+        """Serves `requests` (sorted by arrival) to completion, or until
+        `time_limit` seconds.  `collect`, if given, is called as
+        collect(req, state_tensor) on every completed request before its slot
+        is freed.  Returns statistics."""
         queue = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        prepared = collections.deque()
         active = {}
         done = []
         t0 = time.perf_counter()
         cell_steps = 0
         chunks = 0
-        while queue or active:
+        busy_ms = 0.0
+        k = max(1, self.chunk)
+        inflight = None          # (start event, end event, steps)
+        stopping = False
+        while queue or prepared or active or inflight is not None:
             now = time.perf_counter() - t0
             if time_limit is not None and now > time_limit:
-                break
-            # admission: everything that has arrived and fits, first come first served
-            while queue and queue[0].arrival <= now:
-                need = batch_t.instance_bytes(_abi.grid_desc((queue[0].edge // queue[0].block,) * 3,
-                                                             (queue[0].block,) * 3, 3, (0, 1, 0, 1, 0, 1)))
-                use = self.batch.usage()
-                if need > use["bytes_budget"]:
-                    r = queue.popleft()
+                stopping = True
+            # build the initial states of arrived requests while the GPU works
+            while not stopping and queue and queue[0].arrival <= now and len(prepared) < self.prepare_ahead:
+                r = queue.popleft()
+                if self._need(r) > self.batch.usage()["bytes_budget"]:
                     r.status = "rejected"
                     r.done = now
                     done.append(r)
                     continue
-                if use["bytes_used"] + need > use["bytes_budget"]:
+                prob, ev = self._prepare(r)
+                prepared.append((r, prob, ev))
+            if inflight is not None:
+                if not inflight[1].query():
+                    time.sleep(0.0002)
+                    continue
+                # the chunk has finished: account it, retire, check health
+                e0, e1, kk = inflight
+                inflight = None
+                ms = e0.elapsed_time(e1)
+                busy_ms += ms
+                chunks += 1
+                now = time.perf_counter() - t0
+                k = int(min(self.chunk * 4, max(1, round(self.chunk_ms * kk / max(ms, 1e-3)))))
+                finished = []
+                periodic = self.health_every and chunks % self.health_every == 0
+                for slot, r in active.items():
+                    left = self.batch.steps_left(slot)
+                    if (left == 0 or periodic) and not self._healthy(r):
+                        r.status = "failed"
+                        finished.append(slot)
+                    elif left == 0:
+                        r.status = "ok"
+                        finished.append(slot)
+                for slot in finished:
+                    r = active.pop(slot)
+                    r.done = now
+                    if collect is not None and r.status == "ok":
+                        collect(r, self.batch.state(slot))
+                    self.batch.remove(slot)
+                    done.append(r)
+            if stopping:
+                break
+            # admission between chunks: nothing of this batch is in flight
+            while prepared:
+                r, prob, ev = prepared[0]
+                use = self.batch.usage()
+                if use["bytes_used"] + self._need(r) > use["bytes_budget"]:
                     break
-                r = queue.popleft()
+                prepared.popleft()
                 try:
-                    self._admit(r, now)
+                    self._admit(r, prob, ev, time.perf_counter() - t0)
                 except _native.SpadeError as e:
                     if e.code == _abi.ERR_CAPACITY:
-                        queue.appendleft(r)
+                        prepared.appendleft((r, prob, ev))
                         break
                     r.status = "failed"
                     r.done = time.perf_counter() - t0
                     done.append(r)
                     continue
                 active[r.slot] = r
+                del prob
             if not active:
-                if queue:
+                if queue and not prepared:
                     wait = queue[0].arrival - (time.perf_counter() - t0)
                     if wait > 0:
-                        time.sleep(min(wait, 0.05))
+                        time.sleep(min(wait, 0.01))
                 continue
-            k = min(self.chunk, min(r.remaining for r in active.values()))
-            self.batch.step(k)
-            torch.cuda.synchronize()
-            chunks += 1
-            now = time.perf_counter() - t0
-            finished = []
+            # launch the next chunk; the cell-steps it does are known now
             for slot, r in active.items():
-                r.remaining -= k
-                cell_steps += r.cells * k
-                check = r.remaining == 0 or (self.health_every and chunks % self.health_every == 0)
-                if check and not self._healthy(r):
-                    r.status = "failed"
-                    finished.append(slot)
-                elif r.remaining == 0:
-                    r.status = "ok"
-                    finished.append(slot)
-            for slot in finished:
-                r = active.pop(slot)
-                r.done = now
-                if collect is not None and r.status == "ok":
-                    collect(r, self.batch.state(slot))
-                self.batch.remove(slot)
-                done.append(r)
+                left = self.batch.steps_left(slot)
+                cell_steps += r.cells * (k if left < 0 else min(k, left))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            self.batch.step(k)
+            e1.record(self.stream)
+            inflight = (e0, e1, k)
+        torch.cuda.synchronize()
         makespan = time.perf_counter() - t0
         lat = [r.latency() for r in done if r.status == "ok"]
         return {
+            "offered": len(requests),
             "completed": sum(r.status == "ok" for r in done),
             "failed": sum(r.status == "failed" for r in done),
             "rejected": sum(r.status == "rejected" for r in done),
-            "unfinished": len(queue) + len(active),
+            "unfinished": len(queue) + len(prepared) + len(active),
             "p50_latency_s": float(np.percentile(lat, 50)) if lat else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if lat else None,
             "cell_steps": cell_steps,
             "makespan_s": makespan,
             "cell_steps_per_s": cell_steps / makespan if makespan > 0 else None,
+            "gpu_busy_frac": busy_ms * 1e-3 / makespan if makespan > 0 else None,
             "chunks": chunks,
         }
 

@@ -16,6 +16,8 @@ static int record(const gbns_grid_desc* g, const gbns_scheme_desc* s, const doub
                 s->convective, s->order, s->weno_smooth, s->dissipation, s->viscous, s->visc_law, s->precision,
                 s->eps_p, s->eps_T, s->sensor_alpha, s->mu, s->prandtl_inv, s->gas.gamma, s->gas.R, s->T_ref,
                 incr, int(q != nullptr && r != nullptr), s->sensor, s->hybrid_flux, s->hybrid_sensor, s->hybrid_param);
+    std::printf("coords %d %.17g %.17g %.17g %.17g law %d S %.17g Tref %.17g pr %.17g\n", g->coords, g->coord_param[0],
+                g->coord_param[1], g->coord_param[2], g->coord_param[3], s->visc_law, s->S, s->T_ref, s->prandtl);
     return 0;
 }
 #define GBNS_DROPIN_HOOK record
@@ -93,7 +95,25 @@ int main(int argc, char** argv)
         walls.max(1) = true;
         spade::pde_algs::boundary_flux(q, rhs, walls, spade::omni::compose(spade::convective::cent_keep<4>(air), visc),
                                        spade::algs::make_traits(spade::pde_algs::gb300));
+        // 9, 10: the channel at scale's scheme, compose(weno5_t, pressure_diss_lr,
+        // visc_lr(sutherland_t)), on tanh-stretched and integrated-tanh y grids
+        spade::gb300::sutherland_t<real_t> suth(1.8e-5, 300.0, 110.4, 0.72);
+        spade::viscous::visc_lr svisc(suth, air);
+        const auto channel_flux = spade::omni::compose(spade::gb300::weno5_t<decltype(air)>(air), diss, svisc);
+        spade::coords::diagonal_coords scoords(spade::coords::identity_1D<real_t>(), spade::gb300::tanh_stretch_1D<real_t>(2.0),
+                                               spade::coords::identity_1D<real_t>());
+        spade::grid::cartesian_grid_t sgrid(cells, blocks, scoords, group);
+        spade::grid::grid_array sq  (sgrid, spade::fluid_state::prim_t<real_t>(0.0), nexch, spade::device::cpu);
+        spade::grid::grid_array srhs(sgrid, spade::fluid_state::flux_t<real_t>(0.0), nexch, spade::device::cpu);
+        spade::pde_algs::flux_div(sq, srhs, channel_flux, spade::algs::make_traits(spade::pde_algs::gb300, spade::pde_algs::overwrite));
+        spade::coords::diagonal_coords icoords(spade::coords::identity_1D<real_t>(),
+                                               spade::coords::integrated_tanh_1D<real_t>(-1.0, 1.0, 0.3, 2.5),
+                                               spade::coords::identity_1D<real_t>());
+        spade::grid::cartesian_grid_t igrid(cells, blocks, icoords, group);
+        spade::grid::grid_array iq  (igrid, spade::fluid_state::prim_t<real_t>(0.0), nexch, spade::device::cpu);
+        spade::grid::grid_array irhs(igrid, spade::fluid_state::flux_t<real_t>(0.0), nexch, spade::device::cpu);
+        spade::pde_algs::flux_div(iq, irhs, channel_flux, spade::algs::make_traits(spade::pde_algs::gb300));
     });
     std::printf("calls %d sources %d bflux %d\n", g_calls, g_src_calls, g_bf_calls);
-    return (g_calls == 5 && g_src_calls == 2 && g_bf_calls == 1) ? 0 : 1;
+    return (g_calls == 7 && g_src_calls == 2 && g_bf_calls == 1) ? 0 : 1;
 }

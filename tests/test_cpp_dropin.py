@@ -31,7 +31,19 @@ def test_dropin_overload_and_lowering():
     lines = out.stdout.strip().splitlines()
     grids = [l.split() for l in lines if l.startswith("grid")]
     schemes = [l.split() for l in lines if l.startswith("scheme")]
-    assert len(grids) == 5 and len(schemes) == 5
+    coords = [l.split() for l in lines if l.startswith("coords")]
+    assert len(grids) == 7 and len(schemes) == 7 and len(coords) == 7
+    assert all(c[1] == "0" for c in coords[:5])
+    # weno5_t + pressure_diss + visc_lr(sutherland_t) on the tanh-stretched grid
+    s, c = schemes[5], coords[5]
+    assert s[1] == "4" and s[4] == "1" and s[5] == "1" and s[6] == "2"
+    assert c[1] == "1" and float(c[2]) == 2.0
+    assert float(c[c.index("S") + 1]) == 110.4 and float(c[c.index("Tref") + 1]) == 300.0
+    assert float(c[c.index("pr") + 1]) == 0.72 and float(s[11]) == 1.8e-5
+    # ... and on the integrated-tanh grid: its (y0, y1, inflation, rate) recovered
+    c = coords[6]
+    assert c[1] == "2" and float(c[2]) == -1.0 and float(c[3]) == 1.0
+    assert abs(float(c[4]) - 0.3) < 1e-14 and abs(float(c[5]) - 2.5) < 1e-14
     assert grids[0][1:8] == ["2", "3", "1", "8", "6", "4", "3"]
     assert [float(x) for x in grids[0][8:14]] == [0.0, 2.0, -1.0, 1.0, 0.0, 0.5]
     # cent_keep<2> + visc_lr(constant), FP64, increment

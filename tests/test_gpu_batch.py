@@ -182,3 +182,79 @@ def test_batch_rejects_mismatched_precision_and_unbatched_scheme():
         b.add(grid, s2, bc, dt, qd.data_ptr())
     assert e.value.code in (_abi.ERR_UNSUPPORTED, _abi.ERR_INVALID)
     b.close()
+
+
+@pytest.mark.parametrize("precision", [_abi.PREC_FP64, _abi.PREC_FP32_FLUX])
+def test_batch_step_limits_inside_one_chunk_equal_alone(precision):
+    """Instances with different step limits advanced by one chunk of 6
+    steps: each stops at exactly its own count (counted on the device) and
+    idles, and its state is bit-identical to advancing it alone that many
+    steps; the host's count of steps done and left agrees."""
+    insts = [tgv_instance((2, 1, 1), 71, precision, mach=0.2), channel_instance(72, precision),
+             tgv_instance((1, 1, 1), 73, precision, re=400.0)]
+    limits = [2, 5, -1]
+    b = batch_t(512 << 20, precision, True)
+    keep, slots = [], []
+    for (grid, s, bc, q, dt), n in zip(insts, limits):
+        qd = torch.from_numpy(q).cuda()
+        keep.append(qd)
+        sl = b.add(grid, s, bc, dt, qd.data_ptr())
+        if n >= 0:
+            b.set_steps(sl, n)
+        slots.append(sl)
+    b.step(6)
+    torch.cuda.synchronize()
+    for inst, sl, n in zip(insts, slots, limits):
+        done = 6 if n < 0 else n
+        assert b.steps_done(sl) == done
+        assert b.steps_left(sl) == (-1 if n < 0 else 0)
+        assert np.array_equal(b.state(sl).cpu().numpy(), alone_in_batch(inst, precision, done)), sl
+    b.close()
+
+
+def _close32(a, r):
+    """FP32-flux states of two tile variants: the FP32 face arithmetic is
+    FMA-contracted per kernel instantiation, so variants agree to single
+    precision (velocities against the largest velocity)."""
+    w = np.abs(r).reshape(-1, 5).max(axis=0)
+    scale = np.array([w[0], w[1], w[2:].max(), w[2:].max(), w[2:].max()])
+    err = np.abs(a - r).reshape(-1, 5).max(axis=0) / scale
+    return np.all(err < 1e-6), err
+
+
+@pytest.mark.parametrize("precision", [_abi.PREC_FP64, _abi.PREC_FP32_FLUX])
+def test_batch_tile_variants_identical_and_autotune(precision):
+    """Every tile variant of every class gives the same states: bit for bit
+    in FP64, to single-precision rounding in FP32-flux; the autotuner
+    reports a valid variant for each class present."""
+    insts = [tgv_instance((2, 1, 1), 81, precision), channel_instance(82, precision), hybrid_instance(83, precision)]
+    ref = None
+    ncls = int(lib().gbns_batch_class_count())
+    for v in range(3):
+        b = batch_t(512 << 20, precision, True)
+        keep, slots = [], []
+        for grid, s, bc, q, dt in insts:
+            qd = torch.from_numpy(q).cuda()
+            keep.append(qd)
+            slots.append(b.add(grid, s, bc, dt, qd.data_ptr()))
+        for c in range(ncls):
+            try:
+                b.set_variant(c, v)
+            except _native.SpadeError:
+                pass                                      # class with fewer variants
+        b.step(2)
+        torch.cuda.synchronize()
+        states = [b.state(sl).cpu().numpy() for sl in slots]
+        if ref is None:
+            ref = states
+            tuned = b.autotune(reps=1)
+            assert set(tuned) == {"cent_keep2/identity", "weno5/stretched-y", "hybrid(cent_keep2,fweno)/identity"}
+            assert all(t["variant"] >= 0 and t["tile"][0] == 8 for t in tuned.values())
+        else:
+            for a, r in zip(states, ref):
+                if precision == _abi.PREC_FP64:
+                    assert np.array_equal(a, r), v
+                else:
+                    ok, err = _close32(a, r)
+                    assert ok, (v, err)
+        b.close()
