@@ -303,6 +303,46 @@ int gbns_flux_div_rk(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                      double* rhs, int write_rhs, int nres, const double* const* earlier,
                      const double* coeffs, double* q_out, void* stream);
 
+/* ---- exchange plans (AMR coarse/fine ghost fill) -------------------------
+ * The ghost fill of a block layout with refinement levels, executed from the
+ * plan the reference's make_exchange builds (grid/make_exchange.h:98-421,
+ * grid/get_transaction.h:10-263): one record per transaction, either an
+ * injection (same level: the destination box is a copy of an equally sized
+ * donor box) or an interpolation (levels differ: every destination cell is
+ * (1/8) x the sum of 8 donor cells, visited in the order
+ * d = (0,0,0), (1,0,0), (0,1,0), (1,1,0), (0,0,1), ... with donor index
+ * ((i << (i_coeff + 1)) >> 1) + d*i_incr per direction: i_coeff -1 takes the
+ * coarse cell i/2 eight times, 1 averages the fine cells 2i and 2i+1).
+ * Cell indices are block-local with the interior at [0, n); blocks are
+ * numbered as the grid enumerates them (all of equal cell count). */
+#define GBNS_PATCH_INJECT  0
+#define GBNS_PATCH_INTERP  1
+typedef struct gbns_patch
+{
+    int32_t kind;          /* GBNS_PATCH_INJECT or GBNS_PATCH_INTERP */
+    int32_t src_block;     /* donor block */
+    int32_t dst_block;     /* receiving block */
+    int32_t src_lo[3];     /* donor box origin (i, j, k) */
+    int32_t dst_lo[3];     /* receiving box [dst_lo, dst_hi) */
+    int32_t dst_hi[3];
+    int32_t i_coeff[3];    /* interpolation: -1, 0 or 1 per direction */
+    int32_t i_incr[3];     /* interpolation: 0 or 1 per direction */
+} gbns_patch;
+
+typedef struct gbns_exchange_plan gbns_exchange_plan;
+
+/* Validates a plan for blocks of nx*ny*nz cells with ng ghost layers and
+ * nblocks blocks (every destination cell a ghost cell written once, every
+ * donor inside its block's padded array), uploads it once and returns a
+ * handle (the reference's exchange handle, make_exchange).  Injections run
+ * before interpolations, as in the reference.  Synchronises `stream`. */
+int gbns_exchange_plan_create(gbns_exchange_plan** plan, int nx, int ny, int nz, int ng, int nblocks,
+                              const gbns_patch* patches, int npatch, void* stream);
+/* One exchange on the AoS5 array `prims` (arr_exchange_t::exchange,
+ * grid/make_exchange.h:111-410): two launches, asynchronous on `stream`. */
+int gbns_exchange_plan_run(gbns_exchange_plan* plan, double* prims, void* stream);
+int gbns_exchange_plan_destroy(gbns_exchange_plan* plan);
+
 /* dst = src on interior cells, dst's ghost layers filled from src's interior
  * donors (gbns_fill_ghosts of src, written into dst).  Asynchronous. */
 int gbns_copy_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc, double* dst,

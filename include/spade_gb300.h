@@ -32,6 +32,11 @@
  * Coordinates: coords::identity, and coords::diagonal_coords(identity_1D, y, identity_1D)
  * with y = spade::gb300::tanh_stretch_1D (beta) or coords::integrated_tanh_1D.
  *
+ * Exchange on refined (AMR) block layouts: spade::gb300::exchange_plan_t built
+ * from the reference's own exchange handle (grid::make_exchange) runs its
+ * injections and coarse/fine interpolations on the GPU (gbns_exchange_plan_*);
+ * spade::gb300::lower_exchange gives the plan as gbns_patch records.
+ *
  * source_term: spade::gb300::const_source_t / body_force_t / body_accel_t
  * passed to spade::pde_algs::source_term run on the GPU (gbns_source_term).
  *
@@ -55,6 +60,7 @@
 #include <cmath>
 #include <string>
 #include <type_traits>
+#include <vector>
 #include <cuda_runtime_api.h>
 
 #include "gbns.h"
@@ -536,6 +542,104 @@ namespace spade::pde_algs
 
 namespace spade::gb300
 {
+    // The exchange plan of a reference exchange handle
+    // (grid::make_exchange(q, periodic), grid/make_exchange.h:98-421): its
+    // same-level injections and coarse/fine interpolations, in the
+    // reference's order, as gbns_patch records for gbns_exchange_plan_create.
+    // Single-rank grids (every block on this device).
+    template <typename handle_t>
+    std::vector<gbns_patch> lower_exchange(const handle_t& h)
+    {
+        using namespace sym::literals;
+        const auto& inj = h.config.send_data[0_c];
+        const auto& itp = h.config.send_data[1_c];
+        std::vector<gbns_patch> out;
+        out.reserve(inj.size() + itp.size());
+        for (std::size_t i = 0; i < inj.size(); ++i)
+        {
+            const auto& t = inj[i];
+            gbns_patch p{};
+            p.kind = GBNS_PATCH_INJECT;
+            p.src_block = t.source.min(3);
+            p.dst_block = t.dest.min(3);
+            for (int d = 0; d < 3; ++d)
+            {
+                p.src_lo[d] = t.source.min(d);
+                p.dst_lo[d] = t.dest.min(d);
+                p.dst_hi[d] = t.dest.max(d);
+            }
+            out.push_back(p);
+        }
+        for (std::size_t i = 0; i < itp.size(); ++i)
+        {
+            const auto& t = itp[i];
+            gbns_patch p{};
+            p.kind = GBNS_PATCH_INTERP;
+            p.src_block = t.patches.source.min(3);
+            p.dst_block = t.patches.dest.min(3);
+            for (int d = 0; d < 3; ++d)
+            {
+                p.src_lo[d] = t.patches.source.min(d);
+                p.dst_lo[d] = t.patches.dest.min(d);
+                p.dst_hi[d] = t.patches.dest.max(d);
+                p.i_coeff[d] = t.i_coeff[d];
+                p.i_incr[d] = t.i_incr[d];
+            }
+            out.push_back(p);
+        }
+        return out;
+    }
+
+    // A reference exchange handle run on the GPU: build it once from the
+    // handle and the array (blocks, cells, ghosts), then exchange(q) on
+    // device::gpu grid_arrays replaces handle.exchange(q, group).
+    struct exchange_plan_t
+    {
+        gbns_exchange_plan* plan = nullptr;
+        template <typename handle_t, typename arr_t>
+        exchange_plan_t(const handle_t& h, const arr_t& q)
+        {
+            const auto& grid = q.get_grid();
+            if (grid.get_num_local_blocks() != grid.get_num_global_blocks())
+                throw except::sp_exception("gb300 exchange: the grid must hold every block on this device");
+            const auto patches = lower_exchange(h);
+#ifndef GBNS_DROPIN_HOOK
+            const int rc = gbns_exchange_plan_create(&plan, grid.get_num_cells(0), grid.get_num_cells(1), grid.get_num_cells(2),
+                                                     q.get_num_exchange(0), int(grid.get_num_global_blocks()),
+                                                     patches.data(), int(patches.size()), nullptr);
+            if (rc != GBNS_OK)
+            {
+                char msg[512];
+                gbns_last_error(msg, sizeof(msg));
+                throw except::sp_exception(std::string("gb300 exchange plan: ") + msg);
+            }
+#endif
+        }
+        exchange_plan_t(const exchange_plan_t&) = delete;
+        exchange_plan_t& operator=(const exchange_plan_t&) = delete;
+        ~exchange_plan_t()
+        {
+#ifndef GBNS_DROPIN_HOOK
+            gbns_exchange_plan_destroy(plan);
+#endif
+        }
+        template <typename arr_t>
+        void exchange(arr_t& q) const
+        {
+#ifndef GBNS_DROPIN_HOOK
+            static_assert(device::is_gpu<typename arr_t::device_type>, "the gb300 exchange runs on device::gpu arrays");
+            int rc = gbns_exchange_plan_run(plan, q.image().base, nullptr);
+            if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+            if (rc != GBNS_OK)
+            {
+                char msg[512];
+                gbns_last_error(msg, sizeof(msg));
+                throw except::sp_exception(std::string("gb300 exchange failed: ") + msg);
+            }
+#endif
+        }
+    };
+
     // Point sources with a GB300 kernel (gbns_source_desc).  Passing one of
     // these instead of a lambda to spade::pde_algs::source_term selects the
     // overload below (a non-template parameter beats the reference's

@@ -1071,3 +1071,56 @@ int oracle_max_threads(void)
     return 1;
 #endif
 }
+
+
+/* Exchange plan of a refined block layout (the reference's transactions,
+ * grid/make_exchange.h:111-410 with grid/get_transaction.h:10-263): records
+ * of 18 ints (gbns_patch: kind, source block, dest block, source box min,
+ * dest box [min, max), i_coeff, i_incr), injections run first, then
+ * interpolations, each in plan order.  An injection copies an equally sized
+ * donor box; an interpolation sets each destination cell to
+ * (0 + sum of 8 donors in order d = (0,0,0), (1,0,0), (0,1,0), ...) * 0.125,
+ * donor index ((i << (c + 1)) >> 1) + d*incr per direction. */
+int oracle_exchange_patches(int nx, int ny, int nz, int ng, int nblocks, const int* plan, int nplan, double* prims)
+{
+    const long long ni = nx + 2*ng, nj = ny + 2*ng, nk = nz + 2*ng;
+    const long long bstride = 5*ni*nj*nk;
+    (void)nblocks;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int t = 0; t < nplan; ++t)
+        {
+            const int* r = plan + 18*(long long)t;
+            if (r[0] != pass) continue;
+            const int sb = r[1], db = r[2];
+            const int* slo = r + 3;
+            const int* dlo = r + 6;
+            const int* dhi = r + 9;
+            const int* c = r + 12;
+            const int* inc = r + 15;
+            for (int dk = 0; dk < dhi[2] - dlo[2]; ++dk)
+            for (int dj = 0; dj < dhi[1] - dlo[1]; ++dj)
+            for (int di = 0; di < dhi[0] - dlo[0]; ++di)
+            {
+                double* dst = prims + db*bstride + (((dlo[2] + dk + ng)*nj + (dlo[1] + dj + ng))*ni + (dlo[0] + di + ng))*5;
+                if (pass == 0)
+                {
+                    const double* src = prims + sb*bstride + (((slo[2] + dk + ng)*nj + (slo[1] + dj + ng))*ni + (slo[0] + di + ng))*5;
+                    for (int v = 0; v < 5; ++v) dst[v] = src[v];
+                }
+                else
+                {
+                    const int i0 = (di << (c[0] + 1)) >> 1, j0 = (dj << (c[1] + 1)) >> 1, k0 = (dk << (c[2] + 1)) >> 1;
+                    double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+                    for (int iv = 0; iv < 8; ++iv)
+                    {
+                        const int d0 = iv & 1, d1 = (iv >> 1) & 1, d2 = (iv >> 2) & 1;
+                        const long long ii = slo[0] + i0 + d0*inc[0], jj = slo[1] + j0 + d1*inc[1], kk = slo[2] + k0 + d2*inc[2];
+                        const double* src = prims + sb*bstride + (((kk + ng)*nj + (jj + ng))*ni + (ii + ng))*5;
+                        for (int v = 0; v < 5; ++v) acc[v] += src[v];
+                    }
+                    for (int v = 0; v < 5; ++v) dst[v] = acc[v]*0.125;
+                }
+            }
+        }
+    return 0;
+}

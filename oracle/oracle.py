@@ -47,6 +47,7 @@ def port():
         lib.oracle_max_threads.restype = ctypes.c_int
         lib.oracle_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), ctypes.c_void_p, ctypes.c_void_p]
         lib.oracle_boundary_flux.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_int)]
+        lib.oracle_exchange_patches.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         _port = lib
     return _port
 
@@ -65,6 +66,9 @@ def ref():
         lib.spade_ref_fill_ghosts.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.spade_ref_ssprk3.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         lib.spade_ref_source_term.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        lib.spade_ref_amr_exchange.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -109,6 +113,13 @@ def boundary_flux(grid, scheme, prims, rhs, apply):
     flags = (ctypes.c_int * 6)(*[int(bool(a)) for a in apply])
     _check(port().oracle_boundary_flux(ctypes.byref(grid), ctypes.byref(scheme), _ptr(prims), _ptr(rhs), flags),
            "oracle_boundary_flux")
+
+
+def exchange_patches(ncell, ng, nblocks, plan, prims):
+    """Executes an exchange plan ((n, 18) int32 gbns_patch records) on prims in place."""
+    plan = np.ascontiguousarray(plan, dtype=np.int32)
+    _check(port().oracle_exchange_patches(int(ncell[0]), int(ncell[1]), int(ncell[2]), int(ng), int(nblocks),
+                                          plan.ctypes.data, int(plan.shape[0]), _ptr(prims)), "oracle_exchange_patches")
 
 
 def max_threads():
@@ -179,3 +190,33 @@ def ref_source_term(grid, scheme, src, prims, rhs):
     c = np.ascontiguousarray(np.array(list(src.c), dtype=np.float64))
     _check(ref().spade_ref_source_term(int(src.kind), ints.ctypes.data, reals.ctypes.data, c.ctypes.data, _ptr(prims), _ptr(rhs)),
            "spade_ref_source_term")
+
+
+def ref_amr_exchange(nb, nc, ng, periodic, passes, bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), cap_blocks=512, cap_plan=1 << 16):
+    """The reference's AMR exchange on a grid refined in place pass by pass
+    (oracle/ref_harness.cc spade_ref_amr_exchange).  Returns the array before
+    and after the exchange (nblocks, nz+2ng, ny+2ng, nx+2ng, 5), the block
+    boxes (nblocks, 6) and levels, and the plan: (ntransactions, 18) int32
+    records, injections first (count `ninject`)."""
+    ints = [nb[0], nb[1], nb[2], nc[0], nc[1], nc[2], ng] + [int(bool(p)) for p in periodic] + [len(passes)]
+    for ps in passes:
+        ints += [len(ps)] + list(ps)
+    ints = np.array(ints, dtype=np.int32)
+    b = np.array(bounds, dtype=np.float64)
+    per_block = (nc[0] + 2 * ng) * (nc[1] + 2 * ng) * (nc[2] + 2 * ng) * 5
+    cap = per_block * cap_blocks
+    before = np.zeros(cap)
+    after = np.zeros(cap)
+    boxes = np.zeros(6 * cap_blocks)
+    levels = np.zeros(cap_blocks, dtype=np.int32)
+    plan = np.zeros(18 * cap_plan, dtype=np.int32)
+    nblk, nplan, ninj = ctypes.c_int(0), ctypes.c_int(0), ctypes.c_int(0)
+    _check(ref().spade_ref_amr_exchange(ints.ctypes.data, b.ctypes.data, cap, before.ctypes.data, after.ctypes.data,
+                                        ctypes.byref(nblk), boxes.ctypes.data, levels.ctypes.data, cap_blocks,
+                                        plan.ctypes.data, cap_plan, ctypes.byref(nplan), ctypes.byref(ninj)),
+           "spade_ref_amr_exchange")
+    n = nblk.value
+    shape = (n, nc[2] + 2 * ng, nc[1] + 2 * ng, nc[0] + 2 * ng, 5)
+    return {"before": before[:n * per_block].reshape(shape), "after": after[:n * per_block].reshape(shape),
+            "boxes": boxes[:6 * n].reshape(n, 6), "levels": levels[:n].copy(),
+            "plan": plan[:18 * nplan.value].reshape(-1, 18).copy(), "ninject": ninj.value}

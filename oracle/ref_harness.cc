@@ -21,6 +21,7 @@
 
 namespace
 {
+    template <typename grid_t> struct utils_grid_point { using type = typename grid_t::coord_point_type; };
     using real_t = double;
     using prim_t = spade::fluid_state::prim_t<real_t>;
     using flux_t = spade::fluid_state::flux_t<real_t>;
@@ -392,5 +393,112 @@ extern "C"
         }
         catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_ssprk3: %s\n", e.what()); return -1; }
         return 0;
+    }
+
+    // AMR coarse/fine exchange through the reference's current API: an
+    // amr_blocks_t grid built unrefined, refined in place pass by pass with
+    // cartesian_grid_t::refine_blocks (grid/cartesian_grid.h:331-367; the
+    // factor-2 constraint refines neighbours as needed), then make_exchange
+    // and one exchange (grid/make_exchange.h:98-421).
+    //   ints: nb[3], nc[3], ng, periodic[3], npass, then per pass its block
+    //         count and the global block indices refined in it
+    //   bounds: 6 doubles
+    // The interior is filled with p = 3 + x, T = 1 + y^2, u = z, v = x*y,
+    // w = 2 at cell centres (exact in binary floating point for power-of-two
+    // geometry), ghosts start at 0.  Outputs: the array before and after the
+    // exchange (cap doubles each), per block its box (6 doubles) and level,
+    // and the exchange plan the reference built: one record of 18 ints per
+    // transaction, injections first, each list in the reference's order:
+    //   kind (0 injection, 1 interpolation), source block, dest block,
+    //   source box min (3), dest box min (3), dest box max (3),
+    //   i_coeff (3), i_incr (3).
+    int spade_ref_amr_exchange(const int* ints, const double* bounds, long long cap, double* before, double* after,
+                               int* nblk_out, double* boxes, int* levels, int box_cap,
+                               int* plan, int plan_cap, int* nplan_out, int* ninject_out)
+    {
+        try
+        {
+            const int nb[3] = {ints[0], ints[1], ints[2]};
+            const int nc[3] = {ints[3], ints[4], ints[5]};
+            const int ng = ints[6];
+            spade::ctrs::array<bool, 3> per(ints[7] != 0, ints[8] != 0, ints[9] != 0);
+            int argc = 0;
+            char** argv = nullptr;
+            spade::parallel::compute_env_t env(&argc, &argv, {0});
+            int rc = 0;
+            env.exec([&](spade::parallel::pool_t& group)
+            {
+                spade::bound_box_t<real_t, 3> bbx;
+                for (int d = 0; d < 3; ++d) { bbx.min(d) = bounds[2*d]; bbx.max(d) = bounds[2*d + 1]; }
+                spade::coords::identity<real_t> coords;
+                spade::ctrs::array<int, 3> num_blocks(nb[0], nb[1], nb[2]), cells(nc[0], nc[1], nc[2]);
+                spade::amr::amr_blocks_t blocks(num_blocks, bbx);
+                spade::grid::cartesian_grid_t grid(cells, blocks, coords, group);
+                const int npass = ints[10];
+                int pos = 11;
+                for (int pss = 0; pss < npass; ++pss)
+                {
+                    const int cnt = ints[pos++];
+                    std::vector<std::size_t> list;
+                    for (int i = 0; i < cnt; ++i) list.push_back(std::size_t(ints[pos++]));
+                    grid.refine_blocks(list, per);
+                }
+                spade::ctrs::array<int, 3> nexch(ng, ng, ng);
+                spade::grid::grid_array q(grid, prim_t(0.0), nexch, spade::device::cpu);
+                auto handle = spade::grid::make_exchange(q, per);
+                using point_t = typename utils_grid_point<decltype(grid)>::type;
+                spade::algs::fill_array(q, [](const point_t& x)
+                {
+                    prim_t o;
+                    o.p() = 3.0 + x[0];
+                    o.T() = 1.0 + x[1]*x[1];
+                    o.u() = x[2];
+                    o.v() = x[0]*x[1];
+                    o.w() = 2.0;
+                    return o;
+                }, spade::grid::exclude_exchanges);
+                const int nblk = int(grid.get_num_global_blocks());
+                *nblk_out = nblk;
+                if ((long long)q.data.size() > cap || nblk > box_cap) { rc = -2; return; }
+                copy_out(q, before);
+                handle.exchange(q, group);
+                copy_out(q, after);
+                for (int lb = 0; lb < nblk; ++lb)
+                {
+                    const auto b = grid.get_bounding_box(spade::utils::tag[spade::partition::global](std::size_t(lb)));
+                    for (int d = 0; d < 3; ++d) { boxes[6*lb + 2*d] = b.min(d); boxes[6*lb + 2*d + 1] = b.max(d); }
+                    levels[lb] = grid.get_blocks().get_amr_node(lb).level[0];
+                }
+                using namespace spade::sym::literals;
+                const auto& inj = handle.config.send_data[0_c];
+                const auto& itp = handle.config.send_data[1_c];
+                *ninject_out = int(inj.size());
+                *nplan_out = int(inj.size() + itp.size());
+                if (*nplan_out > plan_cap) { rc = -3; return; }
+                int* r = plan;
+                for (std::size_t i = 0; i < inj.size(); ++i, r += 18)
+                {
+                    const auto& t = inj[i];
+                    const int rec[18] = {0, t.source.min(3), t.dest.min(3),
+                                         t.source.min(0), t.source.min(1), t.source.min(2),
+                                         t.dest.min(0), t.dest.min(1), t.dest.min(2),
+                                         t.dest.max(0), t.dest.max(1), t.dest.max(2), 0, 0, 0, 0, 0, 0};
+                    std::memcpy(r, rec, sizeof(rec));
+                }
+                for (std::size_t i = 0; i < itp.size(); ++i, r += 18)
+                {
+                    const auto& t = itp[i];
+                    const auto& pt = t.patches;
+                    const int rec[18] = {1, pt.source.min(3), pt.dest.min(3),
+                                         pt.source.min(0), pt.source.min(1), pt.source.min(2),
+                                         pt.dest.min(0), pt.dest.min(1), pt.dest.min(2),
+                                         pt.dest.max(0), pt.dest.max(1), pt.dest.max(2),
+                                         t.i_coeff[0], t.i_coeff[1], t.i_coeff[2], t.i_incr[0], t.i_incr[1], t.i_incr[2]};
+                    std::memcpy(r, rec, sizeof(rec));
+                }
+            });
+            return rc;
+        }
+        catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_amr_exchange: %s\n", e.what()); return -1; }
     }
 }

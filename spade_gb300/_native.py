@@ -35,6 +35,10 @@ def lib():
     L.gbns_flux_div_variant.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, ctypes.c_int, vp]
     L.gbns_flux_variant_count.argtypes = [P(_abi.SchemeDesc)]
     L.gbns_fill_ghosts.argtypes = [P(_abi.GridDesc), P(_abi.BcDesc), vp, vp]
+    L.gbns_exchange_plan_create.argtypes = [P(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            vp, ctypes.c_int, vp]
+    L.gbns_exchange_plan_run.argtypes = [vp, vp, vp]
+    L.gbns_exchange_plan_destroy.argtypes = [vp]
     L.gbns_rk_stage.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, vp, vp, ctypes.c_int, vp]
     L.gbns_reduce.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, vp]
     L.gbns_reduce_scratch_size.argtypes = [P(_abi.GridDesc), P(ctypes.c_size_t), P(ctypes.c_size_t)]

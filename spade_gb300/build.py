@@ -43,7 +43,7 @@ def up_to_date():
 
 # Translation units whose FP64 arithmetic must round exactly like the
 # reference's CPU code: no fused multiply-add contraction.
-NO_FMA = ("flux_f64x_", "state.cu", "batch_flux_f64x", "source.cu", "bflux_")
+NO_FMA = ("flux_f64x_", "state.cu", "batch_flux_f64x", "source.cu", "bflux_", "exchange.cu")
 
 
 def _compile(src):

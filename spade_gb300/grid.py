@@ -6,6 +6,8 @@ A grid_array owns one torch float64 tensor on the GPU of shape
 linear_t<5> map: variables fastest, then i, j, k, block.  torch is used only
 for device memory and streams.
 """
+import ctypes
+
 import numpy as np
 import torch
 
@@ -187,6 +189,48 @@ class arr_exchange_t:
     def exchange(self, q, group=None, stream=None):
         bc = self.bc_desc()
         _native.check(_native.lib().gbns_fill_ghosts(q.desc(), bc, q.ptr(), _stream(stream)))
+
+
+class exchange_plan_t:
+    """The ghost fill of a block layout with refinement levels (AMR), run from
+    an exchange plan: the reference's own transaction list for that layout
+    (its make_exchange on an amr_blocks_t grid, grid/make_exchange.h:98-421),
+    as an (n, 18) int32 array of gbns_patch records (kind, source block,
+    destination block, source box origin, destination box [lo, hi),
+    i_coeff, i_incr).  The C++ drop-in lowers a reference exchange handle into
+    such a plan (spade::gb300::lower_exchange).  exchange(q) runs it on a
+    grid_array-shaped float64 tensor (nblocks, nz+2ng, ny+2ng, nx+2ng, 5) on
+    the GPU: injections, then interpolations, bit-identical to the
+    reference's exchange."""
+
+    def __init__(self, ncell, ng, nblocks, plan, stream=None):
+        self.plan = np.ascontiguousarray(plan, dtype=np.int32)
+        assert self.plan.ndim == 2 and self.plan.shape[1] == 18
+        self.ncell, self.ng, self.nblocks = tuple(int(n) for n in ncell), int(ng), int(nblocks)
+        h = ctypes.c_void_p()
+        _native.check(_native.lib().gbns_exchange_plan_create(ctypes.byref(h), self.ncell[0], self.ncell[1], self.ncell[2],
+                                                              self.ng, self.nblocks,
+                                                              ctypes.c_void_p(self.plan.ctypes.data),
+                                                              int(self.plan.shape[0]), _stream(stream)))
+        self.handle = h
+
+    def exchange(self, q, stream=None):
+        data = q.data if hasattr(q, "data") and not isinstance(q, torch.Tensor) else q
+        want = (self.nblocks, self.ncell[2] + 2 * self.ng, self.ncell[1] + 2 * self.ng, self.ncell[0] + 2 * self.ng, 5)
+        if tuple(data.shape) != want or data.dtype != torch.float64 or not data.is_cuda:
+            raise ValueError("exchange_plan_t.exchange: expected a CUDA float64 array of shape %s" % (want,))
+        _native.check(_native.lib().gbns_exchange_plan_run(self.handle, ctypes.c_void_p(data.data_ptr()), _stream(stream)))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            _native.lib().gbns_exchange_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def make_exchange(q, periodic):

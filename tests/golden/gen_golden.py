@@ -182,6 +182,50 @@ def gen_channel():
                         mu=U_b / 3000.0, eps=0.01 * c_w)
 
 
+# AMR layouts refined in place (cartesian_grid_t::refine_blocks), one refinement
+# pass per inner list of global block indices: (base blocks, cells per block,
+# ghosts, periodic flags, passes)
+AMR_CASES = {
+    "one_level_periodic": ((2, 2, 2), (4, 4, 4), 2, (1, 1, 1), [[0]]),
+    "two_levels_walls_y": ((2, 2, 2), (4, 4, 4), 3, (1, 0, 1), [[0], [0]]),
+    "anisotropic_blocks": ((2, 2, 1), (8, 4, 4), 2, (1, 1, 1), [[0, 3]]),
+}
+
+
+def amr_fill(boxes, ncell, ng):
+    """The harness's interior field at cell centres (exact in binary floating
+    point for these power-of-two boxes), ghosts 0."""
+    nb = boxes.shape[0]
+    q = np.zeros((nb, ncell[2] + 2 * ng, ncell[1] + 2 * ng, ncell[0] + 2 * ng, 5))
+    for lb in range(nb):
+        c = [boxes[lb, 2 * d] + (np.arange(ncell[d]) + 0.5) * ((boxes[lb, 2 * d + 1] - boxes[lb, 2 * d]) / ncell[d])
+             for d in range(3)]
+        z, y, x = np.meshgrid(c[2], c[1], c[0], indexing="ij")
+        inner = q[lb, ng:-ng, ng:-ng, ng:-ng]
+        inner[..., 0] = 3.0 + x
+        inner[..., 1] = 1.0 + y * y
+        inner[..., 2] = z
+        inner[..., 3] = x * y
+        inner[..., 4] = 2.0
+    return q
+
+
+def gen_amr():
+    out = {}
+    for name, (nb, nc, ng, per, passes) in AMR_CASES.items():
+        r = O.ref_amr_exchange(nb, nc, ng, per, passes)
+        before = amr_fill(r["boxes"], nc, ng)
+        assert np.array_equal(before, r["before"]), name        # the fill is rebuilt exactly
+        out[name + "_plan"] = r["plan"]
+        out[name + "_ninject"] = np.int32(r["ninject"])
+        out[name + "_boxes"] = r["boxes"]
+        out[name + "_levels"] = r["levels"]
+        out[name + "_after"] = r["after"]
+        out[name + "_ncell"] = np.array(nc, dtype=np.int32)
+        out[name + "_ng"] = np.int32(ng)
+    np.savez_compressed(os.path.join(OUT, "amr_ref.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("reference harness not built: make -C oracle ref")
@@ -190,6 +234,7 @@ if __name__ == "__main__":
     gen_ghosts()
     gen_tgv()
     gen_channel()
+    gen_amr()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))
