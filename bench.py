@@ -452,10 +452,11 @@ def run_serve_form(args):
         # a stream the GPU sustains: 70 % of the measured capacity
         mean_work = sum(work) / len(work)
         rate = 0.7 * full["cell_steps_per_s"] / mean_work
-        n = 30 if prec == _abi.PREC_FP32_FLUX else 10
+        n = 30 if prec == _abi.PREC_FP32_FLUX else 6
         sreqs = serve.poisson_requests(n, rate=rate, seed=5)
         srv = serve.server_t(prec, hbm_budget=150 << 30, chunk=16, health_every=8)
-        sus = srv.run(sreqs, time_limit=2.0 * args.serve_time_limit)
+        # served until every request has arrived plus the configured window
+        sus = srv.run(sreqs, time_limit=sreqs[-1].arrival + args.serve_time_limit)
         srv.close()
         torch.cuda.empty_cache()
         sus["rate_req_per_s"] = rate
