@@ -226,6 +226,57 @@ def gen_amr():
     np.savez_compressed(os.path.join(OUT, "amr_ref.npz"), **out)
 
 
+def read_dropin_records(path):
+    """Parses the calls tests/cpp/gbns_record_stub.c recorded."""
+    import struct
+    d = open(path, "rb").read()
+    i, out = 0, []
+    while i < len(d):
+        gs = struct.unpack_from("<Q", d, i)[0]; i += 8
+        gb = d[i:i + gs]; i += gs
+        ss = struct.unpack_from("<Q", d, i)[0]; i += 8
+        sb = d[i:i + ss]; i += ss
+        incr = struct.unpack_from("<i", d, i)[0]; i += 4
+        n = struct.unpack_from("<Q", d, i)[0]; i += 8
+        q = np.frombuffer(d, dtype=np.float64, count=n, offset=i).copy(); i += 8 * n
+        r = np.frombuffer(d, dtype=np.float64, count=n, offset=i).copy(); i += 8 * n
+        out.append((gb, sb, incr, q, r))
+    return out
+
+
+def gen_dropin():
+    """Runs the C++ drop-in at a SPADE call site with no test hook
+    (tests/cpp/dropin_record.cc), linked with the recording stand-in for
+    libgbns.so, and stores the C-ABI calls it made with the reference's own
+    CPU results for the two schemes the reference runs."""
+    import subprocess
+    import tempfile
+    from __graft_entry__ import ref_src
+    src = ref_src()
+    with tempfile.TemporaryDirectory() as d:
+        stub = os.path.join(d, "stub.o")
+        exe = os.path.join(d, "dropin_record")
+        subprocess.run(["gcc", "-O1", "-c", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "gbns_record_stub.c"), "-o", stub], check=True)
+        subprocess.run(["g++", "-std=c++20", "-O1", "-I" + src, "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(ROOT, "oracle", "mpi_stub"), "-I/usr/local/cuda/include",
+                        os.path.join(ROOT, "tests", "cpp", "dropin_record.cc"), stub, "-o", exe], check=True)
+        rec, res = os.path.join(d, "calls.bin"), os.path.join(d, "ref.bin")
+        subprocess.run([exe, res], check=True, env=dict(os.environ, GBNS_RECORD=rec))
+        calls = read_dropin_records(rec)
+        refs = np.fromfile(res)
+    assert len(calls) == 3
+    n = calls[0][3].size
+    out = {"q": calls[0][3], "ref": refs.reshape(2, n)}
+    for k, (gb, sb, incr, q, r) in enumerate(calls):
+        assert np.array_equal(q, calls[0][3])              # one state for all three calls
+        out["grid%d" % k] = np.frombuffer(gb, dtype=np.uint8)
+        out["scheme%d" % k] = np.frombuffer(sb, dtype=np.uint8)
+        out["incr%d" % k] = np.int32(incr)
+        out["rhs_in%d" % k] = r
+    np.savez_compressed(os.path.join(OUT, "dropin_ref.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("reference harness not built: make -C oracle ref")
@@ -235,6 +286,7 @@ if __name__ == "__main__":
     gen_tgv()
     gen_channel()
     gen_amr()
+    gen_dropin()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -90,3 +90,24 @@ def test_dropin_host_array_path_compiles():
            os.path.join(ROOT, "tests", "cpp", "dropin_host_arrays.cc")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_recorded_dropin_calls_reproduce_the_reference_on_the_oracle():
+    """The C-ABI calls the drop-in made at a SPADE call site
+    (tests/golden/dropin_ref.npz, recorded by tests/cpp/dropin_record.cc):
+    run by the oracle, the two schemes the reference has give its own CPU
+    result bit for bit, so the recorded descriptors carry the reference's
+    scheme and grid exactly (the GPU replay is tests/test_gpu_dropin_replay.py)."""
+    import numpy as np
+    from spade_gb300 import _abi
+    from oracle import oracle as O
+    g = np.load(os.path.join(ROOT, "tests", "golden", "dropin_ref.npz"))
+    for k in range(2):
+        grid = _abi.GridDesc.from_buffer_copy(g["grid%d" % k].tobytes())
+        s = _abi.SchemeDesc.from_buffer_copy(g["scheme%d" % k].tobytes())
+        shape = (grid.nblk[0] * grid.nblk[1] * grid.nblk[2], grid.ncell[2] + 2 * grid.ng,
+                 grid.ncell[1] + 2 * grid.ng, grid.ncell[0] + 2 * grid.ng, 5)
+        q = g["q"].reshape(shape).copy()
+        r = g["rhs_in%d" % k].reshape(shape).copy()
+        O.flux_div(grid, s, q, r, increment=bool(g["incr%d" % k]))
+        assert np.array_equal(r.ravel(), g["ref"][k]), k
