@@ -334,12 +334,20 @@ typedef struct gbns_exchange_plan gbns_exchange_plan;
 /* Validates a plan for blocks of nx*ny*nz cells with ng ghost layers and
  * nblocks blocks (every destination cell a ghost cell written once, every
  * donor inside its block's padded array), uploads it once and returns a
- * handle (the reference's exchange handle, make_exchange).  Injections run
- * before interpolations, as in the reference.  Synchronises `stream`. */
+ * handle (the reference's exchange handle, make_exchange).  The result is
+ * the reference's: its transactions executed one after the other in plan
+ * order, injections before interpolations.  A donor that is a ghost cell
+ * written by another transaction of the same kind therefore holds the new
+ * value when its writer comes earlier in the plan and the old value when it
+ * comes later; the plan is split into waves (one launch each) that keep this
+ * order.  A transaction that reads a cell it writes itself is rejected
+ * (GBNS_ERR_UNSUPPORTED).  Synchronises `stream`. */
 int gbns_exchange_plan_create(gbns_exchange_plan** plan, int nx, int ny, int nz, int ng, int nblocks,
                               const gbns_patch* patches, int npatch, void* stream);
 /* One exchange on the AoS5 array `prims` (arr_exchange_t::exchange,
- * grid/make_exchange.h:111-410): two launches, asynchronous on `stream`. */
+ * grid/make_exchange.h:111-410): one launch per wave (one injection wave and
+ * one interpolation wave when no donor is a ghost cell), asynchronous on
+ * `stream`. */
 int gbns_exchange_plan_run(gbns_exchange_plan* plan, double* prims, void* stream);
 int gbns_exchange_plan_destroy(gbns_exchange_plan* plan);
 
@@ -373,6 +381,29 @@ int gbns_ssprk3_step(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
 int gbns_ssprk3_run(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                     const gbns_bc_desc* bc, double* prims, double* work,
                     double dt, int nsteps, void* stream);
+
+/* One gbns_ssprk3_step of a state held in host memory, with the copies
+ * overlapped with the stages.  The blocks are split into `ngroups`
+ * contiguous groups (0: the library's choice, min(8, blocks)).  Group g is
+ * copied to the device on `copy_stream` while stage 1 runs on the groups
+ * already there; after stage 3 each group's ghost fill and copy back run as
+ * soon as the groups holding its ghost donors are done, while stage 3 goes
+ * on with the later groups.
+ *   host_prims  padded AoS5 state with valid ghosts (gbns_array_size
+ *               doubles), page-locked (cudaHostAlloc / cudaHostRegister) for
+ *               the copies to overlap; it receives the new state
+ *   prims       device array of the same size (overwritten)
+ *   work        as for gbns_ssprk3_step
+ *   copy_stream a stream other than `stream`; NULL: a non-blocking stream the
+ *               library keeps per device and host thread
+ * Asynchronous: host_prims holds the new state once the work issued on
+ * `stream` so far has finished (the call makes `stream` wait for its
+ * copies).  Bit-identical to copying in, gbns_ssprk3_step, copying out: the
+ * copies a reference caller makes around advance() on device-resident
+ * state (time-integration/advance.h:234-280). */
+int gbns_ssprk3_step_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                          const gbns_bc_desc* bc, double* host_prims, double* prims, double* work,
+                          double dt, int ngroups, void* stream, void* copy_stream);
 
 /* ---- source terms ----------------------------------------------------
  * Lowered forms of the point source a caller passes to

@@ -49,6 +49,8 @@ def lib():
     L.gbns_ssprk3_step.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double, vp]
     L.gbns_ssprk3_run.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, ctypes.c_double,
                                   ctypes.c_int, vp]
+    L.gbns_ssprk3_step_host.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), P(_abi.BcDesc), vp, vp, vp,
+                                        ctypes.c_double, ctypes.c_int, vp, vp]
     L.gbns_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), vp, vp, vp]
     L.gbns_flux_div_host.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, vp]
     L.gbns_boundary_flux.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, P(ctypes.c_int), vp]

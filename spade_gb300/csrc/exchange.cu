@@ -10,10 +10,17 @@
 // grid-stride loop over the cells of all injections, then over the cells of
 // all interpolations (the reference's order).  A thread finds its
 // transaction by binary search over the prefix sums of the transactions'
-// cell counts.  Every destination is a ghost cell written once and every
-// donor an interior cell (checked when the plan is created), so the threads
-// of a launch are independent.  HBM-bound gather: 80 bytes per injected cell,
-// 40 x 9 per interpolated one.  The arithmetic follows the reference's:
+// cell counts.  Every destination is a ghost cell written once (checked when
+// the plan is created).  A donor may be a ghost cell that another
+// transaction of the same kind writes (a coarse block's ghost layer feeding
+// the interpolation into a finer neighbour): the reference executes the
+// transactions one after the other, so such a donor holds the new value if
+// its writer comes earlier in the plan and the old one if it comes later.
+// The plan is therefore split into waves: a transaction runs in a later wave
+// than every earlier writer of its donors, and in an earlier wave than every
+// later writer; the transactions of one wave are independent and each wave
+// is one launch.  HBM-bound gather: 80 bytes per injected cell, 40 x 9 per
+// interpolated one.  The arithmetic follows the reference's:
 // +0.0, eight additions in donor order, then x 0.125 (compiled without FMA
 // contraction).
 #include <algorithm>
@@ -105,9 +112,17 @@ struct gbns_exchange_plan
     PlanGeom G;
     int nx, ny, nz, nblocks;
     int n_inj = 0, n_int = 0;
-    PatchK* d_patches = nullptr;        // injections, then interpolations
-    long long* d_first = nullptr;       // prefix sums: injections (n_inj+1), then interpolations (n_int+1)
-    long long cells_inj = 0, cells_int = 0;
+    // one launch per wave: injection waves, then interpolation waves
+    struct Wave
+    {
+        bool interp;
+        int p0, np;             // its transactions in d_patches
+        long long f0;           // its np+1 prefix sums in d_first
+        long long cells;
+    };
+    std::vector<Wave> waves;
+    PatchK* d_patches = nullptr;
+    long long* d_first = nullptr;
 };
 
 namespace
@@ -116,7 +131,29 @@ namespace
     // interpolation's two donors: base and base + i_incr)
     int donor_base(int d, int coeff) { return (d << (coeff + 1)) >> 1; }
 
-    int validate_patch(const gbns_exchange_plan& P, const gbns_patch& p, std::vector<bool>& written,
+    // Visits the donor cells of every destination cell of patch p (padded
+    // indices relative to the donor block's interior origin).
+    template <class F>
+    void for_each_donor(const gbns_patch& p, F&& f)
+    {
+        const int ext[3] = {p.dst_hi[0] - p.dst_lo[0], p.dst_hi[1] - p.dst_lo[1], p.dst_hi[2] - p.dst_lo[2]};
+        for (int dk = 0; dk < ext[2]; ++dk)
+            for (int dj = 0; dj < ext[1]; ++dj)
+                for (int di = 0; di < ext[0]; ++di)
+                {
+                    if (p.kind == GBNS_PATCH_INJECT)
+                    {
+                        f(p.src_lo[0] + di, p.src_lo[1] + dj, p.src_lo[2] + dk);
+                        continue;
+                    }
+                    const int b[3] = {donor_base(di, p.i_coeff[0]), donor_base(dj, p.i_coeff[1]), donor_base(dk, p.i_coeff[2])};
+                    for (int iv = 0; iv < 8; ++iv)
+                        f(p.src_lo[0] + b[0] + (iv & 1)*p.i_incr[0], p.src_lo[1] + b[1] + ((iv >> 1) & 1)*p.i_incr[1],
+                          p.src_lo[2] + b[2] + ((iv >> 2) & 1)*p.i_incr[2]);
+                }
+    }
+
+    int validate_patch(const gbns_exchange_plan& P, const gbns_patch& p, int index, std::vector<int>& writer,
                        std::string& why)
     {
         const int n[3] = {P.nx, P.ny, P.nz};
@@ -138,7 +175,7 @@ namespace
                 lo = p.src_lo[d] + donor_base(0, p.i_coeff[d]);
                 hi = p.src_lo[d] + donor_base(ext - 1, p.i_coeff[d]) + p.i_incr[d];
             }
-            if (lo < 0 || hi >= n[d]) { why = "donor box not inside the donor block's interior"; return 1; }
+            if (lo < -ng || hi >= n[d] + ng) { why = "donor box not inside the donor block's padded array"; return 1; }
         }
         // every destination cell: a ghost cell, written by no other patch
         const long long ni = P.G.ni, nj = P.G.nj, nk = P.G.nk;
@@ -149,9 +186,43 @@ namespace
                     if (i >= 0 && i < n[0] && j >= 0 && j < n[1] && k >= 0 && k < n[2])
                     { why = "destination box covers interior cells"; return 1; }
                     const long long c = (long long)p.dst_block*ni*nj*nk + ((k + ng)*nj + (j + ng))*ni + (i + ng);
-                    if (written[c]) { why = "two patches write the same ghost cell"; return 1; }
-                    written[c] = true;
+                    if (writer[c] >= 0) { why = "two patches write the same ghost cell"; return 1; }
+                    writer[c] = index;
                 }
+        return 0;
+    }
+
+    // Wave of every patch of one kind, in plan order (see the file comment):
+    // wave(t) > wave(w) for an earlier writer w of one of t's donors, and
+    // wave(w) > wave(t) for a later one.  Returns 1 (why set) if a patch
+    // reads a cell it writes itself.
+    int assign_waves(const gbns_exchange_plan& P, const gbns_patch* patches, int npatch, int kind,
+                     const std::vector<int>& writer, std::vector<int>& wave, std::string& why)
+    {
+        const long long ni = P.G.ni, nj = P.G.nj, nk = P.G.nk;
+        const int ng = P.G.ng;
+        std::vector<int> pending(npatch, 0);
+        std::vector<int> later;
+        for (int t = 0; t < npatch; ++t)
+        {
+            const gbns_patch& p = patches[t];
+            if (p.kind != kind) continue;
+            int w0 = pending[t];
+            bool self = false;
+            later.clear();
+            for_each_donor(p, [&](int i, int j, int k) {
+                const long long c = (long long)p.src_block*ni*nj*nk + ((k + ng)*nj + (j + ng))*ni + (i + ng);
+                const int w = writer[c];
+                if (w < 0 || patches[w].kind != kind) return;
+                if (w == t) self = true;
+                else if (w < t) { if (wave[w] + 1 > w0) w0 = wave[w] + 1; }
+                else later.push_back(w);
+            });
+            if (self) { why = "patch " + std::to_string(t) + " reads a ghost cell it writes"; return 1; }
+            wave[t] = w0;
+            for (int w : later)
+                if (pending[w] < w0 + 1) pending[w] = w0 + 1;
+        }
         return 0;
     }
 }
@@ -169,17 +240,48 @@ extern "C"
         P->G.ng = ng;
         P->G.ni = nx + 2*ng; P->G.nj = ny + 2*ng; P->G.nk = nz + 2*ng;
         P->G.bstride = 5ll*P->G.ni*P->G.nj*P->G.nk;
-        std::vector<bool> written(size_t(nblocks)*P->G.ni*P->G.nj*P->G.nk, false);
-        std::vector<PatchK> inj, itp;
+        std::vector<int> writer(size_t(nblocks)*P->G.ni*P->G.nj*P->G.nk, -1);
         for (int i = 0; i < npatch; ++i)
         {
             std::string why;
-            if (validate_patch(*P, patches[i], written, why))
+            if (validate_patch(*P, patches[i], i, writer, why))
             {
                 delete P;
                 return set_error(GBNS_ERR_INVALID, "exchange plan, patch " + std::to_string(i) + ": " + why);
             }
+        }
+        std::vector<int> wave(npatch, 0);
+        for (int kind : {GBNS_PATCH_INJECT, GBNS_PATCH_INTERP})
+        {
+            std::string why;
+            if (assign_waves(*P, patches, npatch, kind, writer, wave, why))
+            {
+                delete P;
+                return set_error(GBNS_ERR_UNSUPPORTED, "exchange plan: " + why);
+            }
+        }
+        // injection waves, then interpolation waves; plan order within a wave
+        std::vector<int> order(npatch);
+        for (int i = 0; i < npatch; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            const int ka = patches[a].kind == GBNS_PATCH_INTERP, kb = patches[b].kind == GBNS_PATCH_INTERP;
+            if (ka != kb) return ka < kb;
+            return wave[a] < wave[b];
+        });
+        std::vector<PatchK> all;
+        std::vector<long long> first;
+        all.reserve(npatch);
+        for (int oi = 0; oi < npatch; ++oi)
+        {
+            const int i = order[oi];
             const gbns_patch& p = patches[i];
+            const bool interp = p.kind == GBNS_PATCH_INTERP;
+            if (P->waves.empty() || P->waves.back().interp != interp || wave[order[oi - 1]] != wave[i])
+            {
+                if (!P->waves.empty()) first.push_back(P->waves.back().cells);
+                P->waves.push_back({interp, int(all.size()), 0, (long long)first.size(), 0});
+            }
+            gbns_exchange_plan::Wave& W = P->waves.back();
             PatchK k;
             std::memset(&k, 0, sizeof(k));
             k.src_block = p.src_block;
@@ -189,24 +291,17 @@ extern "C"
                 k.src_lo[d] = p.src_lo[d];
                 k.dst_lo[d] = p.dst_lo[d];
                 k.ext[d] = p.dst_hi[d] - p.dst_lo[d];
-                k.i_coeff[d] = p.kind == GBNS_PATCH_INTERP ? p.i_coeff[d] : 0;
-                k.i_incr[d] = p.kind == GBNS_PATCH_INTERP ? p.i_incr[d] : 0;
+                k.i_coeff[d] = interp ? p.i_coeff[d] : 0;
+                k.i_incr[d] = interp ? p.i_incr[d] : 0;
             }
-            (p.kind == GBNS_PATCH_INJECT ? inj : itp).push_back(k);
+            all.push_back(k);
+            first.push_back(W.cells);
+            W.np += 1;
+            W.cells += (long long)k.ext[0]*k.ext[1]*k.ext[2];
+            (interp ? P->n_int : P->n_inj) += 1;
         }
-        P->n_inj = int(inj.size());
-        P->n_int = int(itp.size());
-        std::vector<long long> first;
-        long long acc = 0;
-        for (const auto& k : inj) { first.push_back(acc); acc += (long long)k.ext[0]*k.ext[1]*k.ext[2]; }
-        first.push_back(acc);
-        P->cells_inj = acc;
-        acc = 0;
-        for (const auto& k : itp) { first.push_back(acc); acc += (long long)k.ext[0]*k.ext[1]*k.ext[2]; }
-        first.push_back(acc);
-        P->cells_int = acc;
-        std::vector<PatchK> all(inj);
-        all.insert(all.end(), itp.begin(), itp.end());
+        if (!P->waves.empty()) first.push_back(P->waves.back().cells);
+        if (first.empty()) first.push_back(0);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         int rc = check_cuda(cudaMalloc(&P->d_patches, sizeof(PatchK)*(all.size() ? all.size() : 1)), "exchange plan");
         if (!rc) rc = check_cuda(cudaMalloc(&P->d_first, sizeof(long long)*first.size()), "exchange plan offsets");
@@ -232,21 +327,19 @@ extern "C"
         if (!P || !prims) return set_error(GBNS_ERR_INVALID, "NULL argument");
         cudaStream_t st = static_cast<cudaStream_t>(stream);
         const long long cap = (long long)sm_count()*8;
-        if (P->cells_inj > 0)
+        for (const auto& W : P->waves)
         {
-            long long nb = (P->cells_inj + 255)/256;
+            if (W.cells <= 0) continue;
+            long long nb = (W.cells + 255)/256;
             if (nb > cap) nb = cap;
-            exchange_plan_kernel<false><<<unsigned(nb), 256, 0, st>>>(prims, P->d_patches, P->d_first, P->n_inj, P->G);
-            int rc = check_cuda(cudaGetLastError(), "exchange plan launch (injections)");
-            if (rc) return rc;
-        }
-        if (P->cells_int > 0)
-        {
-            long long nb = (P->cells_int + 255)/256;
-            if (nb > cap) nb = cap;
-            exchange_plan_kernel<true><<<unsigned(nb), 256, 0, st>>>(prims, P->d_patches + P->n_inj,
-                                                                    P->d_first + P->n_inj + 1, P->n_int, P->G);
-            int rc = check_cuda(cudaGetLastError(), "exchange plan launch (interpolations)");
+            if (W.interp)
+                exchange_plan_kernel<true><<<unsigned(nb), 256, 0, st>>>(prims, P->d_patches + W.p0, P->d_first + W.f0,
+                                                                        W.np, P->G);
+            else
+                exchange_plan_kernel<false><<<unsigned(nb), 256, 0, st>>>(prims, P->d_patches + W.p0, P->d_first + W.f0,
+                                                                         W.np, P->G);
+            int rc = check_cuda(cudaGetLastError(), W.interp ? "exchange plan launch (interpolations)"
+                                                             : "exchange plan launch (injections)");
             if (rc) return rc;
         }
         return GBNS_OK;

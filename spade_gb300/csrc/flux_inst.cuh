@@ -38,7 +38,9 @@ namespace gbns
         A.ntile[1] = (G.n[1] + Cfg::TY - 1)/Cfg::TY;
         A.ntile[2] = (G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
         const long long ntiles = (long long)A.ntile[0]*A.ntile[1]*A.ntile[2];
-        if (ntiles > 2147483647ll || G.nblk > 65535)
+        const int nrun = c.blk1 - c.blk0;
+        if (nrun < 1) return GBNS_OK;
+        if (ntiles > 2147483647ll || nrun > 65535)
             return set_error(GBNS_ERR_UNSUPPORTED, "grid too large for one flux_div launch (blocks > 65535)");
         CUtensorMap tmap;
         std::memset(&tmap, 0, sizeof(tmap));
@@ -53,7 +55,7 @@ namespace gbns
         if constexpr (Cfg::SHADOW)
         {
             // FP32 copy of the state, staged by TMA (its layout is always aligned)
-            rc = shadow_begin(c.prims, G, Cfg::H, Cfg::BXE, Cfg::BY, Cfg::BZ, c.stream, sh, &tmap);
+            rc = shadow_begin(c.prims, G, c.blk0, c.blk1, Cfg::H, Cfg::BXE, Cfg::BY, Cfg::BZ, c.stream, sh, &tmap);
             if (rc) return rc;
             A.use_tma = 1;
             A.sh_off = sh.off;
@@ -64,10 +66,10 @@ namespace gbns
             if (rc) return rc;
             A.use_tma = 1;
         }
-        const dim3 grid(unsigned(ntiles), unsigned(G.nblk));
+        const dim3 grid{unsigned(ntiles), unsigned(nrun)};
         YTabT<Cfg::STRETCH> Y;
         if constexpr (Cfg::STRETCH) Y = *c.Y;
-        kern<<<grid, Cfg::NT, Cfg::SMEM_BYTES, c.stream>>>(tmap, G, Y, *c.S, A);
+        kern<<<grid, Cfg::NT, Cfg::SMEM_BYTES, c.stream>>>(tmap, G, Y, *c.S, A, c.blk0);
         rc = check_cuda(cudaGetLastError(), "flux_div launch");
         const int erc = shadow_end(sh, c.stream);
         return rc ? rc : erc;

@@ -1369,9 +1369,11 @@ namespace gbns
     template <class Cfg>
     __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
     flux_div_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ GeomK G,
-                    const __grid_constant__ YTabT<Cfg::STRETCH> Y, const __grid_constant__ SchemeK SK, const FluxArgs A)
+                    const __grid_constant__ YTabT<Cfg::STRETCH> Y, const __grid_constant__ SchemeK SK, const FluxArgs A,
+                    const int blk0)
     {
+        // blockIdx.y: the block within the launch's range blk0 .. blk0 + gridDim.y - 1
         extern __shared__ __align__(128) unsigned char smem_raw[];
-        flux_tile<Cfg>(smem_raw, &tmap, G, Y, SK, A, int(blockIdx.y), int(blockIdx.x));
+        flux_tile<Cfg>(smem_raw, &tmap, G, Y, SK, A, int(blockIdx.y) + blk0, int(blockIdx.x));
     }
 }

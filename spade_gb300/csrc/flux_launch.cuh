@@ -27,6 +27,7 @@ namespace gbns
         cudaStream_t stream;
         int variant;
         const RkFuse* fuse;
+        int blk0, blk1;     // the blocks this launch covers: blk0 .. blk1 - 1
     };
 
     // f64x: FP64 without FMA contraction (-fmad=false): the kernels follow the

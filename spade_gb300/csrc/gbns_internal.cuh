@@ -133,8 +133,8 @@ namespace gbns
     // 5) box.  `halo` is the kernel's stencil half width H: off is chosen
     // so that a tile starting at interior index i0 (a multiple of 4) has
     // its box start i0 - H + ng + off on a multiple of 4.
-    int shadow_begin(const double* prims, const GeomK& G, int halo, int box_x, int box_y, int box_z,
-                     cudaStream_t st, ShadowK& S, CUtensorMap* map);
+    int shadow_begin(const double* prims, const GeomK& G, int blk0, int blk1, int halo, int box_x, int box_y,
+                     int box_z, cudaStream_t st, ShadowK& S, CUtensorMap* map);
     // Returns the copy to the pool, ordered after the kernel on `st`.
     int shadow_end(const ShadowK& S, cudaStream_t st);
     int encode_shadow_tmap(CUtensorMap* map, const ShadowK& S, const GeomK& G, int box_x, int box_y, int box_z);
@@ -143,9 +143,17 @@ namespace gbns
     struct RkFuse;
     int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
                         const gbns_scheme_desc* desc, const double* prims, double* rhs,
-                        int increment, cudaStream_t stream, int variant, const RkFuse* fuse = nullptr);
-    int launch_copy_fill(const GeomK& G, const gbns_bc_desc* bc, double* dst, const double* src, cudaStream_t stream);
-    int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream);
+                        int increment, cudaStream_t stream, int variant, const RkFuse* fuse = nullptr,
+                        int blk0 = 0, int blk1 = -1);
+    // gbns_flux_div_rk over the blocks blk0 .. blk1 - 1 (host.cu)
+    int flux_div_rk_range(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
+                          double* rhs, int write_rhs, int nres, const double* const* earlier,
+                          const double* coeffs, double* q_out, void* stream, int blk0, int blk1);
+    // blk0 .. blk1 - 1: the blocks whose cells the launch writes (blk1 = -1: to the last block)
+    int launch_copy_fill(const GeomK& G, const gbns_bc_desc* bc, double* dst, const double* src, cudaStream_t stream,
+                         int blk0 = 0, int blk1 = -1);
+    int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream,
+                           int blk0 = 0, int blk1 = -1);
     int launch_rk_stage(const GeomK& G, double gamma, double R, double* prims,
                         const double* const* res, const double* coeffs, int nres, cudaStream_t stream);
     int launch_reduce(const gbns_grid_desc* g, const GeomK& G, double gamma, double R, const double* prims,

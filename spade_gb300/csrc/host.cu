@@ -490,6 +490,17 @@ extern "C"
                          double* rhs, int write_rhs, int nres, const double* const* earlier,
                          const double* coeffs, double* q_out, void* stream)
     {
+        return gbns::flux_div_rk_range(grid, scheme, prims, rhs, write_rhs, nres, earlier, coeffs, q_out, stream, 0, -1);
+    }
+}
+
+namespace gbns
+{
+    // gbns_flux_div_rk over the blocks blk0 .. blk1 - 1 (blk1 = -1: to the last)
+    int flux_div_rk_range(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
+                          double* rhs, int write_rhs, int nres, const double* const* earlier,
+                          const double* coeffs, double* q_out, void* stream, int blk0, int blk1)
+    {
         GeomK G;
         SchemeK S;
         int rc = make_geom(grid, G);
@@ -521,8 +532,107 @@ extern "C"
             Y = &ytab;
         }
         return launch_flux_div(grid, G, Y, S, scheme, prims, write_rhs ? rhs : q_out, 0,
-                               static_cast<cudaStream_t>(stream), scheme->tile_variant, &f);
+                               static_cast<cudaStream_t>(stream), scheme->tile_variant, &f, blk0, blk1);
     }
+
+    namespace
+    {
+        // Non-blocking copy streams the library keeps, one per device and host thread.
+        struct ThreadCopyStreams
+        {
+            std::vector<cudaStream_t> st;
+            ~ThreadCopyStreams()
+            {
+                for (cudaStream_t s : st)
+                    if (s) cudaStreamDestroy(s);
+            }
+        };
+        thread_local ThreadCopyStreams t_copy_streams;
+
+        int thread_copy_stream(cudaStream_t* out)
+        {
+            int dev = 0;
+            int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+            if (rc) return rc;
+            auto& v = t_copy_streams.st;
+            if (v.size() <= size_t(dev)) v.resize(dev + 1, nullptr);
+            if (!v[dev])
+            {
+                rc = check_cuda(cudaStreamCreateWithFlags(&v[dev], cudaStreamNonBlocking), "copy stream");
+                if (rc) return rc;
+            }
+            *out = v[dev];
+            return GBNS_OK;
+        }
+
+        // Events of one gbns_ssprk3_step_host call; destroyed when the call
+        // returns (their resources go once the recorded work has finished).
+        struct EventSet
+        {
+            std::vector<cudaEvent_t> ev;
+            ~EventSet()
+            {
+                for (cudaEvent_t e : ev)
+                    if (e) cudaEventDestroy(e);
+            }
+            int make(int n)
+            {
+                ev.assign(n, nullptr);
+                for (int i = 0; i < n; ++i)
+                {
+                    int rc = check_cuda(cudaEventCreateWithFlags(&ev[i], cudaEventDisableTiming), "copy event");
+                    if (rc) return rc;
+                }
+                return GBNS_OK;
+            }
+        };
+
+        // The last group (in issue order 0, 1, ...) holding a ghost donor of a
+        // block of group g: the block itself and its 26 neighbours, wrapped
+        // across periodic faces and dropped across the others (the donors
+        // fill_one_ghost_from can read).
+        int last_donor_group(const GeomK& G, const gbns_bc_desc* bc, const std::vector<int>& start, int g)
+        {
+            const int ngroup = int(start.size()) - 1;
+            int last = g;
+            for (int lb = start[g]; lb < start[g + 1]; ++lb)
+            {
+                const int b[3] = {lb % G.nb[0], (lb / G.nb[0]) % G.nb[1], lb / (G.nb[0]*G.nb[1])};
+                for (int dz = -1; dz <= 1; ++dz)
+                    for (int dy = -1; dy <= 1; ++dy)
+                        for (int dx = -1; dx <= 1; ++dx)
+                        {
+                            const int d[3] = {dx, dy, dz};
+                            int nb[3];
+                            bool skip = false;
+                            for (int a = 0; a < 3; ++a)
+                            {
+                                nb[a] = b[a] + d[a];
+                                if (nb[a] < 0)
+                                {
+                                    if (bc->kind[2*a] != GBNS_BC_PERIODIC) skip = true;
+                                    nb[a] += G.nb[a];
+                                }
+                                else if (nb[a] >= G.nb[a])
+                                {
+                                    if (bc->kind[2*a + 1] != GBNS_BC_PERIODIC) skip = true;
+                                    nb[a] -= G.nb[a];
+                                }
+                            }
+                            if (skip) continue;
+                            const int lbs = nb[0] + G.nb[0]*(nb[1] + G.nb[1]*nb[2]);
+                            int h = 0;
+                            while (h + 1 < ngroup && start[h + 1] <= lbs) ++h;
+                            if (h > last) last = h;
+                        }
+            }
+            return last;
+        }
+    }
+}
+
+extern "C"
+{
 
     int gbns_copy_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc, double* dst,
                               const double* src, void* stream)
@@ -562,6 +672,87 @@ extern "C"
         if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
         if ((rc = gbns_flux_div_rk(grid, scheme, prims, nullptr, 0, 3, e2, c3, B, stream))) return rc;
         return gbns_copy_fill_ghosts(grid, bc, prims, B, stream);
+    }
+
+    int gbns_ssprk3_step_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                              const gbns_bc_desc* bc, double* host_prims, double* prims, double* work,
+                              double dt, int ngroups, void* stream, void* copy_stream)
+    {
+        using namespace gbns;
+        GeomK G;
+        int rc = make_geom(grid, G);
+        if (rc) return rc;
+        if (!scheme) return set_error(GBNS_ERR_INVALID, "scheme descriptor is NULL");
+        if (!work || !prims || !host_prims) return set_error(GBNS_ERR_INVALID, "NULL pointer");
+        if (host_prims == prims) return set_error(GBNS_ERR_INVALID, "host_prims and prims must be distinct arrays");
+        rc = validate_bc(bc);
+        if (rc) return rc;
+        if (ngroups < 0) return set_error(GBNS_ERR_INVALID, "ngroups must be >= 0");
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        cudaStream_t cs = static_cast<cudaStream_t>(copy_stream);
+        if (!cs && (rc = thread_copy_stream(&cs))) return rc;
+        if (cs == st) return set_error(GBNS_ERR_INVALID, "copy_stream must differ from stream");
+        const int ng = ngroups == 0 ? (G.nblk < 8 ? G.nblk : 8) : (ngroups < G.nblk ? ngroups : G.nblk);
+        std::vector<int> start(ng + 1);
+        for (int g = 0; g <= ng; ++g) start[g] = int((long long)g*G.nblk/ng);
+        const size_t bstride = size_t(G.bstride);
+        const size_t n = bstride*G.nblk;
+        double* R0 = work;
+        double* R1 = work + n;
+        double* B = work + 2*n;
+        const double c1[1] = {(1.0/1.0)*dt};
+        const double c2[2] = {(-3.0/4.0)*dt, (1.0/4.0)*dt};
+        const double c3[3] = {(-1.0/12.0)*dt, (-1.0/12.0)*dt, (2.0/3.0)*dt};
+        const double* e1[2] = {R0, nullptr};
+        const double* e2[2] = {R0, R1};
+        // events: 0 = work issued on `stream` before the call, 1..ng = group
+        // copied in, ng+1..2ng = group final, 2ng+1 = every copy out issued
+        EventSet E;
+        if ((rc = E.make(2*ng + 2))) return rc;
+        cudaEvent_t* ev = E.ev.data();
+        if ((rc = check_cuda(cudaEventRecord(ev[0], st), "event record"))) return rc;
+        if ((rc = check_cuda(cudaStreamWaitEvent(cs, ev[0], 0), "stream wait"))) return rc;
+        for (int g = 0; g < ng; ++g)
+        {
+            const size_t off = bstride*start[g], cnt = bstride*(start[g + 1] - start[g]);
+            if ((rc = check_cuda(cudaMemcpyAsync(prims + off, host_prims + off, cnt*sizeof(double),
+                                                 cudaMemcpyHostToDevice, cs), "state copy to the device")))
+                return rc;
+            if ((rc = check_cuda(cudaEventRecord(ev[1 + g], cs), "event record"))) return rc;
+        }
+        // stage 1 group by group as the groups arrive (a block's stencil reads
+        // only its own padded array, whose ghosts are valid on entry)
+        for (int g = 0; g < ng; ++g)
+        {
+            if ((rc = check_cuda(cudaStreamWaitEvent(st, ev[1 + g], 0), "stream wait"))) return rc;
+            if ((rc = flux_div_rk_range(grid, scheme, prims, R0, 1, 1, e1, c1, B, stream, start[g], start[g + 1])))
+                return rc;
+        }
+        if ((rc = gbns_fill_ghosts(grid, bc, B, stream))) return rc;
+        if ((rc = gbns_flux_div_rk(grid, scheme, B, R1, 1, 2, e1, c2, prims, stream))) return rc;
+        if ((rc = gbns_fill_ghosts(grid, bc, prims, stream))) return rc;
+        // stage 3 group by group; a group's ghost fill and copy out follow the
+        // stage-3 launch of the last group holding one of its ghost donors
+        std::vector<int> ready(ng);
+        for (int g = 0; g < ng; ++g) ready[g] = last_donor_group(G, bc, start, g);
+        for (int h = 0; h < ng; ++h)
+        {
+            if ((rc = flux_div_rk_range(grid, scheme, prims, nullptr, 0, 3, e2, c3, B, stream, start[h], start[h + 1])))
+                return rc;
+            for (int g = 0; g < ng; ++g)
+            {
+                if (ready[g] != h) continue;
+                if ((rc = launch_copy_fill(G, bc, prims, B, st, start[g], start[g + 1]))) return rc;
+                if ((rc = check_cuda(cudaEventRecord(ev[1 + ng + g], st), "event record"))) return rc;
+                if ((rc = check_cuda(cudaStreamWaitEvent(cs, ev[1 + ng + g], 0), "stream wait"))) return rc;
+                const size_t off = bstride*start[g], cnt = bstride*(start[g + 1] - start[g]);
+                if ((rc = check_cuda(cudaMemcpyAsync(host_prims + off, prims + off, cnt*sizeof(double),
+                                                     cudaMemcpyDeviceToHost, cs), "state copy to the host")))
+                    return rc;
+            }
+        }
+        if ((rc = check_cuda(cudaEventRecord(ev[2*ng + 1], cs), "event record"))) return rc;
+        return check_cuda(cudaStreamWaitEvent(st, ev[2*ng + 1], 0), "stream wait");
     }
 
     int gbns_boundary_flux(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,

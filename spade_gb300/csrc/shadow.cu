@@ -25,16 +25,17 @@ namespace gbns
         // box never reads uninitialised memory
         __global__ void __launch_bounds__(256)
         to_shadow_kernel(const double* __restrict__ prims, float* __restrict__ out, const int ni, const int nj,
-                         const int nk, const int nblk, const int ipad, const int off)
+                         const int nk, const int blk0, const int nrun, const int ipad, const int off)
         {
-            const long long rows = (long long)nj*nk*nblk;
+            const long long rows = (long long)nj*nk*nrun;
             const long long total = rows*ipad;
             const long long plane = (long long)ipad*nj*nk;
+            const long long row0 = (long long)blk0*nj*nk;
             for (long long t = blockIdx.x*(long long)blockDim.x + threadIdx.x; t < total;
                  t += (long long)gridDim.x*blockDim.x)
             {
                 const int col = int(t % ipad);
-                const long long row = t / ipad;               // (lb*nk + k)*nj + j
+                const long long row = row0 + t / ipad;        // (lb*nk + k)*nj + j
                 const long long lb = row / ((long long)nj*nk);
                 const long long jk = row - lb*nj*nk;          // k*nj + j
                 const int i = col - off;
@@ -84,8 +85,8 @@ namespace gbns
         }
     }
 
-    int shadow_begin(const double* prims, const GeomK& G, int halo, int box_x, int box_y, int box_z,
-                     cudaStream_t st, ShadowK& S, CUtensorMap* map)
+    int shadow_begin(const double* prims, const GeomK& G, int blk0, int blk1, int halo, int box_x, int box_y,
+                     int box_z, cudaStream_t st, ShadowK& S, CUtensorMap* map)
     {
         S.base = nullptr;
         // box start column i0 - halo + ng + off with i0 a multiple of 4
@@ -99,11 +100,12 @@ namespace gbns
         rc = check_cuda(cudaMallocFromPoolAsync(&p, bytes, pool, st), "FP32 copy of the state (pool allocation)");
         if (rc) return rc;
         S.base = static_cast<float*>(p);
-        const long long total = (long long)S.ipad*G.nj*G.nk*G.nblk;
+        // only the launch's blocks are converted (the copy is laid out for the whole grid)
+        const long long total = (long long)S.ipad*G.nj*G.nk*(blk1 - blk0);
         long long nb = (total + 255)/256;
         const long long cap = (long long)sm_count()*16;
         if (nb > cap) nb = cap;
-        to_shadow_kernel<<<unsigned(nb), 256, 0, st>>>(prims, S.base, G.ni, G.nj, G.nk, G.nblk, S.ipad, S.off);
+        to_shadow_kernel<<<unsigned(nb), 256, 0, st>>>(prims, S.base, G.ni, G.nj, G.nk, blk0, blk1 - blk0, S.ipad, S.off);
         rc = check_cuda(cudaGetLastError(), "FP32 copy launch");
         if (!rc) rc = encode_shadow_tmap(map, S, G, box_x, box_y, box_z);
         if (rc)

@@ -145,17 +145,18 @@ namespace gbns
 
     // One thread per ghost cell.
     __global__ void __launch_bounds__(256)
-    fill_ghosts_kernel(double* __restrict__ q, const __grid_constant__ GeomK G, const BcK bc)
+    fill_ghosts_kernel(double* __restrict__ q, const __grid_constant__ GeomK G, const BcK bc, const int blk0,
+                       const int nrun)
     {
         const long long per_block = ghosts_per_block(G);
-        const long long total = per_block*G.nblk;
+        const long long total = per_block*nrun;
         for (long long idx = blockIdx.x*(long long)blockDim.x + threadIdx.x; idx < total;
              idx += (long long)gridDim.x*blockDim.x)
         {
-            const int lb = int(idx / per_block);
+            const int r = int(idx / per_block);
             int ii, jj, kk;
-            ghost_cell(idx - lb*per_block, G, ii, jj, kk);
-            fill_one_ghost(q, G, bc, lb, ii, jj, kk);
+            ghost_cell(idx - r*per_block, G, ii, jj, kk);
+            fill_one_ghost(q, G, bc, blk0 + r, ii, jj, kk);
         }
     }
 
@@ -164,27 +165,28 @@ namespace gbns
     // the scratch buffer, landing in the caller's array).  Ghost cells first,
     // then the interior copy, in one grid-stride range.
     __global__ void __launch_bounds__(256)
-    copy_fill_kernel(double* __restrict__ dst, const double* __restrict__ src, const __grid_constant__ GeomK G, const BcK bc)
+    copy_fill_kernel(double* __restrict__ dst, const double* __restrict__ src, const __grid_constant__ GeomK G, const BcK bc,
+                     const int blk0, const int nrun)
     {
         const long long gpb = ghosts_per_block(G);
         const long long ipb = (long long)G.n[0]*G.n[1]*G.n[2];
-        const long long ng_total = gpb*G.nblk;
-        const long long total = ng_total + ipb*G.nblk;
+        const long long ng_total = gpb*nrun;
+        const long long total = ng_total + ipb*nrun;
         for (long long idx = blockIdx.x*(long long)blockDim.x + threadIdx.x; idx < total;
              idx += (long long)gridDim.x*blockDim.x)
         {
             if (idx < ng_total)
             {
-                const int lb = int(idx / gpb);
+                const int r = int(idx / gpb);
                 int ii, jj, kk;
-                ghost_cell(idx - lb*gpb, G, ii, jj, kk);
-                fill_one_ghost_from(dst, src, G, bc, lb, ii, jj, kk);
+                ghost_cell(idx - r*gpb, G, ii, jj, kk);
+                fill_one_ghost_from(dst, src, G, bc, blk0 + r, ii, jj, kk);
             }
             else
             {
                 const long long c = idx - ng_total;
-                const int lb = int(c / ipb);
-                const long long off = interior_offset(c - lb*ipb, G, lb);
+                const int r = int(c / ipb);
+                const long long off = interior_offset(c - r*ipb, G, blk0 + r);
                 #pragma unroll
                 for (int v = 0; v < 5; ++v) dst[off + v] = src[off + v];
             }
@@ -206,21 +208,34 @@ namespace gbns
         return unsigned(want < cap ? (want > 0 ? want : 1) : cap);
     }
 
-    int launch_copy_fill(const GeomK& G, const gbns_bc_desc* bc, double* dst, const double* src, cudaStream_t stream)
+    static int block_range(const GeomK& G, int& blk0, int& blk1)
     {
+        if (blk1 < 0) blk1 = G.nblk;
+        if (blk0 < 0 || blk1 > G.nblk || blk0 > blk1) return set_error(GBNS_ERR_INVALID, "block range out of the grid");
+        return GBNS_OK;
+    }
+
+    int launch_copy_fill(const GeomK& G, const gbns_bc_desc* bc, double* dst, const double* src, cudaStream_t stream,
+                         int blk0, int blk1)
+    {
+        int rc = block_range(G, blk0, blk1);
+        if (rc || blk1 == blk0) return rc;
         BcK k;
         for (int i = 0; i < 6; ++i) { k.kind[i] = bc->kind[i]; k.t_wall[i] = bc->t_wall[i]; }
-        const long long total = (long long)G.ni*G.nj*G.nk*G.nblk;   // ghosts + interior
-        copy_fill_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(dst, src, G, k);
+        const long long total = (long long)G.ni*G.nj*G.nk*(blk1 - blk0);   // ghosts + interior
+        copy_fill_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(dst, src, G, k, blk0, blk1 - blk0);
         return check_cuda(cudaGetLastError(), "copy_fill launch");
     }
 
-    int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream)
+    int launch_fill_ghosts(const GeomK& G, const gbns_bc_desc* bc, double* prims, cudaStream_t stream,
+                           int blk0, int blk1)
     {
+        int rc = block_range(G, blk0, blk1);
+        if (rc || blk1 == blk0) return rc;
         BcK k;
         for (int i = 0; i < 6; ++i) { k.kind[i] = bc->kind[i]; k.t_wall[i] = bc->t_wall[i]; }
-        const long long total = ((long long)G.ni*G.nj*G.nk - (long long)G.n[0]*G.n[1]*G.n[2])*G.nblk;
-        fill_ghosts_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(prims, G, k);
+        const long long total = ((long long)G.ni*G.nj*G.nk - (long long)G.n[0]*G.n[1]*G.n[2])*(blk1 - blk0);
+        fill_ghosts_kernel<<<grid_for(total, 256, 16), 256, 0, stream>>>(prims, G, k, blk0, blk1 - blk0);
         return check_cuda(cudaGetLastError(), "fill_ghosts launch");
     }
 

@@ -152,3 +152,18 @@ class ssprk3_stepper:
         for _ in range(nsteps):
             _native.check(L.gbns_ssprk3_step(self.q.desc(), self.scheme, self.bc, self.q.ptr(), self.work.data_ptr(),
                                              ctypes.c_double(self.dt), st))
+
+    def step_host(self, host_q, ngroups=0, stream=None, copy_stream=None):
+        """One step of the state in `host_q` (a page-locked CPU tensor of
+        q's shape, float64) through gbns_ssprk3_step_host: copied in block
+        groups while stage 1 runs, copied back as stage 3 finishes each group;
+        q's device array is the staging copy.  Asynchronous on `stream`."""
+        if host_q.device.type != "cpu" or host_q.dtype != torch.float64 or tuple(host_q.shape) != tuple(self.q.shape):
+            raise ValueError("host_q must be a float64 CPU tensor of the state's shape")
+        if not host_q.is_contiguous():
+            raise ValueError("host_q must be contiguous")
+        st = _stream(stream)
+        cs = None if copy_stream is None else _stream(copy_stream)
+        _native.check(_native.lib().gbns_ssprk3_step_host(self.q.desc(), self.scheme, self.bc, host_q.data_ptr(),
+                                                          self.q.ptr(), self.work.data_ptr(), ctypes.c_double(self.dt),
+                                                          int(ngroups), st, cs))

@@ -110,8 +110,12 @@ def test_plan_validation_rejects_malformed_plans():
     bad[0, 9:12] = [1, 1, 1]
     assert _create(bad) == _abi.ERR_INVALID
     bad = plan.copy()
-    bad[0, 3] = 3                                                   # donor box past the interior
+    bad[0, 3] = 5                                                   # donor box past the padded array
     assert _create(bad) == _abi.ERR_INVALID
+    # an injection whose donors are its own destination ghost cells
+    selfread = np.zeros((1, 18), dtype=np.int32)
+    selfread[0, :12] = [0, 0, 0, -2, 0, 0, -2, 0, 0, 0, 1, 1]
+    assert _create(selfread) == _abi.ERR_UNSUPPORTED
     bad = plan.copy()
     bad[-1, 12] = 2                                                 # interpolation coefficient out of range
     assert _create(bad) == _abi.ERR_INVALID
