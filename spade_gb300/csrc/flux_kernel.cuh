@@ -61,6 +61,15 @@ namespace gbns
         if constexpr (Cfg::IMUL) return dmul_pow2<E>(x);
         else return (E == -1 ? Real(0.5) : Real(0.25))*x;
     }
+    // 2*x (exact): an exponent increment on the integer pipes in the IMUL tiles
+    // (in the others a DMUL by 2 measured faster than the integer sequence)
+    template <class Cfg>
+    __device__ __forceinline__ typename Cfg::Real ptwice(typename Cfg::Real x)
+    {
+        using Real = typename Cfg::Real;
+        if constexpr (Cfg::IMUL) return dmul_2(x);
+        else return Real(2.0)*x;
+    }
     // nD*x with nD the face normal's metric factor (1 on identity grids,
     // where the plain product folds away)
     template <class Cfg>
@@ -86,7 +95,12 @@ namespace gbns
     // boundary_flux (66).
     constexpr bool tag_no_fma(int tag) { return tag < 4 || tag == 64 || tag == 66; }
 
-    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_, int STG_ = 0>
+    // MINB_ > 0 fixes the launch bound's CTAs per SM (0: from the shared
+    // memory the tile takes); 1 leaves a 256-thread tile the whole register
+    // file, which the batched kernels use to keep their per-item loop out of
+    // local memory.
+    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_, int STG_ = 0,
+              int MINB_ = 0>
     struct FluxCfg
     {
         using Real = Real_;
@@ -162,7 +176,7 @@ namespace gbns
         static constexpr int MINB_RAW = int((227*1024) / (SMEM_BYTES + 1024));
         // (tiles of more than 512 threads run one CTA per SM: two would leave
         // fewer than 57 registers per thread)
-        static constexpr int MINB = NT > 512 ? 1 : (MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW));
+        static constexpr int MINB = MINB_ > 0 ? MINB_ : (NT > 512 ? 1 : (MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW)));
         static_assert(5*BXE <= 256, "TMA box inner extent exceeds 256 elements");
     };
 
@@ -246,24 +260,34 @@ namespace gbns
     // fweno_t per-point quantities (convective.h:360-376, 458-467): rho,
     // h = rho (|u| + a)/2 (the Rusanov speed times rho/2) and the total
     // specific energy e.
-    template <class Real, bool IM = false>
+    // (IM: quotients and square roots on the integer pipes; IMUL: the
+    // products too, dmul_int / dmul_pow2; the same bits either way)
+    template <class Real, bool IM = false, bool IMUL = false>
     __device__ __forceinline__ void fweno_derive(const SchemeR<Real>& S, Real p, Real T, Real u, Real v, Real w,
                                                  Real& rho_o, Real& h_o, Real& e_o)
     {
-        Real r = S.R*T;
-        Real h = u*u;
-        h += v*v;
-        h += w*w;
+        auto mul = [](Real a, Real b) -> Real {
+            if constexpr (IMUL) return dmul_int(a, b);
+            else return a*b;
+        };
+        auto half = [](Real x) -> Real {
+            if constexpr (IMUL) return dmul_pow2<-1>(x);
+            else return x*Real(0.5);
+        };
+        Real r = mul(S.R, T);
+        Real h = mul(u, u);
+        h += mul(v, v);
+        h += mul(w, w);
         h = dev_sqrt<IM>(h);
-        h += dev_sqrt<IM>(r*S.gamma);
+        h += dev_sqrt<IM>(mul(r, S.gamma));
         const Real rho = pdiv<IM>(p, r);
-        h *= rho;
-        h *= Real(0.5);
-        Real e = u*u;
-        e += v*v;
-        e += w*w;
-        e *= Real(0.5);
-        e += pdiv<IM>(S.R*T, S.gm1);
+        h = mul(h, rho);
+        h = half(h);
+        Real e = mul(u, u);
+        e += mul(v, v);
+        e += mul(w, w);
+        e = half(e);
+        e += pdiv<IM>(mul(S.R, T), S.gm1);
         rho_o = rho; h_o = h; e_o = e;
     }
 
@@ -278,21 +302,21 @@ namespace gbns
                       (Cfg::CONV == GBNS_CONV_HYBRID && Cfg::SPLIT))
         {
             // convective.h:130-131 / 80-84 (the hybrid's fweno half reads the split cache)
-            const Real rho = pdiv<Cfg::IEMU>(p, S.R*T);
+            const Real rho = pdiv<Cfg::IEMU>(p, pmul<Cfg>(S.R, T));
             der[0*Cfg::BOXN + c] = rho;
-            der[1*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, rho*S.gm1);
+            der[1*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, pmul<Cfg>(rho, S.gm1));
         }
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5 ||
                            Cfg::CONV == GBNS_CONV_HYBRID)
         {
             Real rho, h, e;
-            fweno_derive<Real, Cfg::IEMU>(S, p, T, u, v, w, rho, h, e);
+            fweno_derive<Real, Cfg::IEMU, Cfg::IMUL>(S, p, T, u, v, w, rho, h, e);
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = h;
             der[2*Cfg::BOXN + c] = e;
             // cent_keep's e (convective.h:131); its rho = p/(R*T) is the
             // same rounding as fweno's p/r above
-            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, rho*S.gm1);
+            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, pmul<Cfg>(rho, S.gm1));
         }
     }
 
@@ -319,10 +343,12 @@ namespace gbns
         for (int m = 0; m < W; ++m)
         {
             const int c = rc + (m - hw)*SD;
-            un[m]  = V.q(2 + D, c)*nD;
+            un[m]  = nmul<Cfg>(nD, V.q(2 + D, c));
             rho[m] = V.d(0, c);
             eng[m] = V.d(Cfg::CK_E, c);
         }
+        // the reference's products in its order; pmul / ppow2 / ptwice are the
+        // plain operators except in the IMUL tiles (integer pipes, same bits)
         Real cc = 0, mx = 0, my = 0, mz = 0, g = 0, k = 0, ie = 0, pp = 0;
         #pragma unroll
         for (int ii = 1; ii < hw + 1; ++ii)
@@ -335,22 +361,22 @@ namespace gbns
                 const int c0 = rc + (i0 - hw)*SD, c1 = rc + (i1 - hw)*SD;
                 const Real u0 = V.q(2, c0), v0 = V.q(3, c0), w0 = V.q(4, c0), p0 = V.q(0, c0);
                 const Real u1 = V.q(2, c1), v1 = V.q(3, c1), w1 = V.q(4, c1), p1 = V.q(0, c1);
-                const Real c_loc = a*(Real(0.25)*(rho[i0] + rho[i1])*(un[i1] + un[i0]));
+                const Real c_loc = pmul<Cfg>(a, pmul<Cfg>(ppow2<Cfg, -2>(rho[i0] + rho[i1]), un[i1] + un[i0]));
                 cc += c_loc;
-                mx += c_loc*(Real(0.5)*(u0 + u1));
-                my += c_loc*(Real(0.5)*(v0 + v1));
-                mz += c_loc*(Real(0.5)*(w0 + w1));
-                g  += a*(Real(0.5)*(p0 + p1));
-                k  += Real(0.5)*c_loc*(u0*u1 + v0*v1 + w0*w1);
-                ie += c_loc*(Real(0.5)*(eng[i0] + eng[i1]));
-                pp += a*(Real(0.5)*(un[i0]*p1 + un[i1]*p0));
+                mx += pmul<Cfg>(c_loc, ppow2<Cfg, -1>(u0 + u1));
+                my += pmul<Cfg>(c_loc, ppow2<Cfg, -1>(v0 + v1));
+                mz += pmul<Cfg>(c_loc, ppow2<Cfg, -1>(w0 + w1));
+                g  += pmul<Cfg>(a, ppow2<Cfg, -1>(p0 + p1));
+                k  += pmul<Cfg>(ppow2<Cfg, -1>(c_loc), pmul<Cfg>(u0, u1) + pmul<Cfg>(v0, v1) + pmul<Cfg>(w0, w1));
+                ie += pmul<Cfg>(c_loc, ppow2<Cfg, -1>(eng[i0] + eng[i1]));
+                pp += pmul<Cfg>(a, ppow2<Cfg, -1>(pmul<Cfg>(un[i0], p1) + pmul<Cfg>(un[i1], p0)));
             }
         }
-        out[0] = Real(2.0)*cc;
-        out[1] = Real(2.0)*(k + ie + pp);
-        out[2] = Real(2.0)*(D == 0 ? mx + g*nD : mx);
-        out[3] = Real(2.0)*(D == 1 ? my + g*nD : my);
-        out[4] = Real(2.0)*(D == 2 ? mz + g*nD : mz);
+        out[0] = ptwice<Cfg>(cc);
+        out[1] = ptwice<Cfg>(k + ie + pp);
+        out[2] = ptwice<Cfg>(D == 0 ? mx + nmul<Cfg>(nD, g) : mx);
+        out[3] = ptwice<Cfg>(D == 1 ? my + nmul<Cfg>(nD, g) : my);
+        out[4] = ptwice<Cfg>(D == 2 ? mz + nmul<Cfg>(nD, g) : mz);
     }
 
     // totani_lr::operator() (convective.h:68-93)
@@ -363,16 +389,18 @@ namespace gbns
         const int cl = rc - SD, cr = rc;
         const Real pl = V.q(0, cl), ul = V.q(2, cl), vl = V.q(3, cl), wl = V.q(4, cl);
         const Real pr = V.q(0, cr), ur = V.q(2, cr), vr = V.q(3, cr), wr = V.q(4, cr);
-        const Real un_l = V.q(2 + D, cl)*nD, un_r = V.q(2 + D, cr)*nD;
+        const Real un_l = nmul<Cfg>(nD, V.q(2 + D, cl)), un_r = nmul<Cfg>(nD, V.q(2 + D, cr));
         const Real rho_l = V.d(0, cl), rho_r = V.d(0, cr);
         const Real e_l = V.d(1, cl), e_r = V.d(1, cr);
-        const Real c = Real(0.25)*(rho_l + rho_r)*(un_l + un_r);
+        const Real c = pmul<Cfg>(ppow2<Cfg, -2>(rho_l + rho_r), un_l + un_r);
+        const Real hc = ppow2<Cfg, -1>(c);
         out[0] = c;
-        out[1] = Real(0.5)*c*(e_l + e_r + ul*ur + vl*vr + wl*wr) + Real(0.5)*(un_l*pr + un_r*pl);
-        const Real pn = Real(0.5)*(nD*pl + nD*pr);
-        out[2] = Real(0.5)*c*(ul + ur) + (D == 0 ? pn : Real(0));
-        out[3] = Real(0.5)*c*(vl + vr) + (D == 1 ? pn : Real(0));
-        out[4] = Real(0.5)*c*(wl + wr) + (D == 2 ? pn : Real(0));
+        out[1] = pmul<Cfg>(hc, e_l + e_r + pmul<Cfg>(ul, ur) + pmul<Cfg>(vl, vr) + pmul<Cfg>(wl, wr)) +
+                 ppow2<Cfg, -1>(pmul<Cfg>(un_l, pr) + pmul<Cfg>(un_r, pl));
+        const Real pn = ppow2<Cfg, -1>(nmul<Cfg>(nD, pl) + nmul<Cfg>(nD, pr));
+        out[2] = pmul<Cfg>(hc, ul + ur) + (D == 0 ? pn : Real(0));
+        out[3] = pmul<Cfg>(hc, vl + vr) + (D == 1 ? pn : Real(0));
+        out[4] = pmul<Cfg>(hc, wl + wr) + (D == 2 ? pn : Real(0));
     }
 
     // fweno_t flux/dissipation of equation `eq` at one stencil point
@@ -417,20 +445,35 @@ namespace gbns
         fweno_point_v<Cfg, D>(V, S, c, V.d(0, c), V.d(1, c), V.d(2, c), eq, nD, fl, ds);
     }
 
-    // apply_weno of fweno_t (convective.h:378-427)
-    template <class Real>
+    // apply_weno of fweno_t (convective.h:378-427).  FP64 with IMUL: the
+    // products on the integer pipes (dmul_int; x/2 as dmul_pow2 and -x/2 as
+    // its negation, exact since rounding is sign-symmetric), with IM the two
+    // divisions too (ddiv_int): the same bits as the FP64 unit's.
+    template <class Real, bool IMUL = false, bool IM = false>
     __device__ __forceinline__ Real fweno_apply_ud(const Real fu[4], const Real fd[4], int smooth)
     {
+        auto mul = [](Real a, Real b) -> Real {
+            if constexpr (IMUL) return dmul_int(a, b);
+            else return a*b;
+        };
+        auto half = [](Real x) -> Real {
+            if constexpr (IMUL) return dmul_pow2<-1>(x);
+            else return Real(0.5)*x;
+        };
+        auto mhalf = [](Real x) -> Real {
+            if constexpr (IMUL) return -dmul_pow2<-1>(x);
+            else return Real(-0.5)*x;
+        };
         const Real f0uk = fu[0], f0dk = fd[0];
         const Real f1uk = fu[1], f1dk = fd[1];
         const Real f2uk = fu[2], f2dk = fd[2];
         const Real f3uk = fu[3], f3dk = fd[3];
-        const Real r0 = Real(-0.5)*(f0uk) + Real(1.5)*(f1uk);
-        const Real r1 = Real( 0.5)*(f1uk) + Real(0.5)*(f2uk);
-        const Real r2 = Real( 0.5)*(f1dk) + Real(0.5)*(f2dk);
-        const Real r3 = Real( 1.5)*(f2dk) - Real(0.5)*(f3dk);
+        const Real r0 = mhalf(f0uk) + mul(Real(1.5), f1uk);
+        const Real r1 = half(f1uk) + half(f2uk);
+        const Real r2 = half(f1dk) + half(f2dk);
+        const Real r3 = mul(Real(1.5), f2dk) - half(f3dk);
         if (!smooth)
-            return Real(1.0/3.0)*r0 + Real(2.0/3.0)*r1 + Real(2.0/3.0)*r2 + Real(1.0/3.0)*r3;
+            return mul(Real(1.0/3.0), r0) + mul(Real(2.0/3.0), r1) + mul(Real(2.0/3.0), r2) + mul(Real(1.0/3.0), r3);
         const Real eps = Real(1e-16);
         if constexpr (sizeof(Real) == 4)
         {
@@ -455,15 +498,15 @@ namespace gbns
             return w0*r0 + (Real(1.0) - w0)*r1 + (Real(1.0) - w3)*r2 + w3*r3;
         }
         Real a0 = (f0uk) - (f1uk), a1 = (f1uk) - (f2uk), a2 = (f1dk) - (f2dk), a3 = (f2dk) - (f3dk);
-        a0 *= a0; a0 += eps; a0 *= a0;
-        a1 *= a1; a1 += eps; a1 *= a1;
-        a2 *= a2; a2 += eps; a2 *= a2;
-        a3 *= a3; a3 += eps; a3 *= a3;
-        a0 += a0; a0 += a1; a0 = a1/a0;
-        a3 += a3; a3 += a2; a3 = a2/a3;
+        a0 = mul(a0, a0); a0 += eps; a0 = mul(a0, a0);
+        a1 = mul(a1, a1); a1 += eps; a1 = mul(a1, a1);
+        a2 = mul(a2, a2); a2 += eps; a2 = mul(a2, a2);
+        a3 = mul(a3, a3); a3 += eps; a3 = mul(a3, a3);
+        a0 += a0; a0 += a1; a0 = pdiv<IM>(a1, a0);
+        a3 += a3; a3 += a2; a3 = pdiv<IM>(a2, a3);
         a1 = Real(1.0) - a0;
         a2 = Real(1.0) - a3;
-        return a0*r0 + a1*r1 + a2*r2 + a3*r3;
+        return mul(a0, r0) + mul(a1, r1) + mul(a2, r2) + mul(a3, r3);
     }
 
     template <class Real>
@@ -544,7 +587,7 @@ namespace gbns
             const int x = lx - (D == 0 ? HC : 0), y = ly - (D == 1 ? HC : 0), z = lz - (D == 2 ? HC : 0);
             const int c = (z + H)*Cfg::SZ + (y + H)*Cfg::SY + (x + H + shift);
             double rho, hsr, engy;
-            fweno_derive<double, Cfg::IEMU>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
+            fweno_derive<double, Cfg::IEMU, Cfg::IMUL>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
             store(l, c, y, rho, hsr, engy);
         }
     }
@@ -568,7 +611,7 @@ namespace gbns
                     fu[m] = V.split[(2*eq)*Cfg::NLMAX + lr + (m - 2)*LS];
                     fd[m] = V.split[(2*eq + 1)*Cfg::NLMAX + lr + (m - 2)*LS];
                 }
-                out[eq] = fweno_apply_ud<Real>(fu, fd, S.smooth);
+                out[eq] = fweno_apply_ud<Real, Cfg::IMUL, Cfg::IEMU>(fu, fd, S.smooth);
             }
             else
             {
@@ -900,8 +943,8 @@ namespace gbns
             #pragma unroll
             for (int v = 0; v < 5; ++v)
             {
-                t0[v] *= c0;
-                t1[v] *= blend;
+                t0[v] = pmul<Cfg>(t0[v], c0);
+                t1[v] = pmul<Cfg>(t1[v], blend);
                 t0[v] += t1[v];
             }
         }
@@ -1024,14 +1067,29 @@ namespace gbns
             else { fL = cx + TX*(cy + TY*cz); fR = fL + TX*TY; }
             double jac = 1.0;
             if constexpr (Cfg::STRETCH) jac = Y.im_cell[b[1]*ny + j0 + cy];
-            const double multL = (jac*1.0)*invd[D];
-            // (jac*(-1.0))*invd rounds to exactly -(jac*invd): RN is symmetric
-            const double multR = -multL;
-            #pragma unroll
-            for (int v = 0; v < 5; ++v)
+            // (jac*(-1.0))*invd rounds to exactly -(jac*invd): RN is symmetric;
+            // the products on the integer pipes in the IMUL tiles (same bits)
+            if constexpr (Cfg::IMUL)
             {
-                relem[s][v] += sF[v*Cfg::NFS + base + fL]*multL;
-                relem[s][v] += sF[v*Cfg::NFS + base + fR]*multR;
+                const double multL = dmul_int(jac, invd[D]);
+                const double multR = -multL;
+                #pragma unroll
+                for (int v = 0; v < 5; ++v)
+                {
+                    relem[s][v] += dmul_int(sF[v*Cfg::NFS + base + fL], multL);
+                    relem[s][v] += dmul_int(sF[v*Cfg::NFS + base + fR], multR);
+                }
+            }
+            else
+            {
+                const double multL = (jac*1.0)*invd[D];
+                const double multR = -multL;
+                #pragma unroll
+                for (int v = 0; v < 5; ++v)
+                {
+                    relem[s][v] += sF[v*Cfg::NFS + base + fL]*multL;
+                    relem[s][v] += sF[v*Cfg::NFS + base + fR]*multR;
+                }
             }
         }
     }
@@ -1297,7 +1355,7 @@ namespace gbns
                 if (cc >= Cfg::NCELL) break;
                 const int cx = cc % TX, cy = (cc / TX) % TY, cz = cc / (TX*TY);
                 const int c = (cz + H)*Cfg::SZ + (cy + H)*Cfg::SY + (cx + H + shift);
-                fweno_derive<double, Cfg::IEMU>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
+                fweno_derive<double, Cfg::IEMU, Cfg::IMUL>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
             }
         }
 
@@ -1344,19 +1402,19 @@ namespace gbns
                     for (int v = 0; v < 5; ++v) qv[v] = __ldg(A.prims + off + v);
                 }
                 double cs[5];
-                if constexpr (Cfg::FP64) prim_to_cons(qv, SK.R, SK.gm1, cs);
+                if constexpr (Cfg::FP64) prim_to_cons<Cfg::IMUL>(qv, SK.R, SK.gm1, cs);
                 else prim_to_cons_fast<true>(qv, SK.R, SK.inv_gm1, cs);
                 for (int j = 0; j + 1 < A.rk_nres; ++j)
                 {
                     const double* rr = A.rk_res[j] + off;
                     #pragma unroll
-                    for (int v = 0; v < 5; ++v) cs[v] += A.rk_coeff[j]*rr[v];
+                    for (int v = 0; v < 5; ++v) cs[v] += pmul64<Cfg::IMUL>(A.rk_coeff[j], rr[v]);
                 }
                 const double cl = A.rk_coeff[A.rk_nres - 1];
                 #pragma unroll
-                for (int v = 0; v < 5; ++v) cs[v] += cl*relem[s][v];
+                for (int v = 0; v < 5; ++v) cs[v] += pmul64<Cfg::IMUL>(cl, relem[s][v]);
                 double qn[5];
-                if constexpr (Cfg::FP64) cons_to_prim(cs, SK.R, SK.gm1, qn);
+                if constexpr (Cfg::FP64) cons_to_prim<Cfg::IMUL>(cs, SK.R, SK.gm1, qn);
                 else cons_to_prim_fast<true>(cs, SK.inv_R, SK.gm1, qn);
                 double* o = A.q_out + off;
                 #pragma unroll

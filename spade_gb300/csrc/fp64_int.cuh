@@ -188,6 +188,18 @@ namespace gbns
         return __longlong_as_double((long long)(u - (uint64_t(-E) << 52)));
     }
 
+    // 2*x, the same bits as the hardware multiply: for a normal x whose
+    // double stays finite the exponent field goes up by one (exact); zeros,
+    // subnormals, infinities, NaNs and doubles that would overflow take the
+    // hardware multiply.
+    __device__ __forceinline__ double dmul_2(double x)
+    {
+        const uint64_t u = (uint64_t)__double_as_longlong(x);
+        const uint32_t ex = (uint32_t)(u >> 52) & 0x7ffu;
+        if (ex - 1u >= 2045u) return x*2.0;
+        return __longlong_as_double((long long)(u + (uint64_t(1) << 52)));
+    }
+
     // float -> double on the integer pipes (exact): rebias the exponent
     // (127 -> 1023, or 255 -> 2047 for infinities and NaNs, whose payload
     // bits move along) and widen the significand.  FP32 zeros keep their

@@ -246,26 +246,49 @@ namespace gbns
 
     // fluid_state::convert_state prim -> cons and cons -> prim
     // (navier-stokes/fluid_state.h:151-184), in the reference's operation order.
-    __device__ __forceinline__ void prim_to_cons(const double q[5], const double R, const double gm1, double c[5])
+    // a*b, a/b and x/2 in FP64: with IM on the integer pipes (dmul_int,
+    // ddiv_int, dmul_pow2), the same bits as the FP64 unit's
+    template <bool IM>
+    __device__ __forceinline__ double pmul64(double a, double b)
     {
-        const double rho = q[0]/(R*q[1]);
-        const double rhoU2 = rho*(q[2]*q[2] + q[3]*q[3] + q[4]*q[4]);
-        c[0] = rho;
-        c[1] = 0.5*rhoU2 + (q[0]/(gm1));
-        c[2] = rho*q[2];
-        c[3] = rho*q[3];
-        c[4] = rho*q[4];
+        if constexpr (IM) return dmul_int(a, b);
+        else return a*b;
+    }
+    template <bool IM>
+    __device__ __forceinline__ double pdiv64(double a, double b)
+    {
+        if constexpr (IM) return ddiv_int(a, b);
+        else return a/b;
+    }
+    template <bool IM>
+    __device__ __forceinline__ double phalf64(double x)
+    {
+        if constexpr (IM) return dmul_pow2<-1>(x);
+        else return 0.5*x;
     }
 
+    template <bool IM = false>
+    __device__ __forceinline__ void prim_to_cons(const double q[5], const double R, const double gm1, double c[5])
+    {
+        const double rho = pdiv64<IM>(q[0], pmul64<IM>(R, q[1]));
+        const double rhoU2 = pmul64<IM>(rho, (pmul64<IM>(q[2], q[2]) + pmul64<IM>(q[3], q[3]) + pmul64<IM>(q[4], q[4])));
+        c[0] = rho;
+        c[1] = phalf64<IM>(rhoU2) + pdiv64<IM>(q[0], gm1);
+        c[2] = pmul64<IM>(rho, q[2]);
+        c[3] = pmul64<IM>(rho, q[3]);
+        c[4] = pmul64<IM>(rho, q[4]);
+    }
+
+    template <bool IM = false>
     __device__ __forceinline__ void cons_to_prim(const double c[5], const double R, const double gm1, double q[5])
     {
         const double rh = c[0];
-        const double invrho = 1.0/rh;
-        const double uu = invrho*c[2], vv = invrho*c[3], ww = invrho*c[4];
-        const double ru2 = rh*(uu*uu + vv*vv + ww*ww);
-        const double pp = gm1*(c[1] - 0.5*ru2);
+        const double invrho = pdiv64<IM>(1.0, rh);
+        const double uu = pmul64<IM>(invrho, c[2]), vv = pmul64<IM>(invrho, c[3]), ww = pmul64<IM>(invrho, c[4]);
+        const double ru2 = pmul64<IM>(rh, (pmul64<IM>(uu, uu) + pmul64<IM>(vv, vv) + pmul64<IM>(ww, ww)));
+        const double pp = pmul64<IM>(gm1, (c[1] - phalf64<IM>(ru2)));
         q[0] = pp;
-        q[1] = pp/(R*rh);
+        q[1] = pdiv64<IM>(pp, pmul64<IM>(R, rh));
         q[2] = uu;
         q[3] = vv;
         q[4] = ww;
