@@ -25,8 +25,6 @@ namespace gbns
     int batch_class_variants(int cls, int precision)
     {
         if (cls == BCLASS_HYB2_ID && precision == GBNS_PREC_FP32_FLUX) return 2;
-        // FP64 centred classes: a fourth, 8x8x8 / 256 threads at one CTA per SM
-        if ((cls == BCLASS_CK2_ID || cls == BCLASS_TOTANI_ID) && precision != GBNS_PREC_FP32_FLUX) return 4;
         return 3;
     }
 

@@ -137,9 +137,6 @@ namespace gbns
 
 #define GBNS_BRUN(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
     return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, left, cls, stage, st)
-// one CTA per SM with the whole register file (no local-memory spills)
-#define GBNS_BRUN1(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
-    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32, 1>>(items, offsets, counts, insts, ytabs, left, cls, stage, st)
 
     // The tile variants of each class (their shapes are listed by
     // batch_class_tile in batch.cu, in the same order); variant 0 is the
@@ -153,16 +150,10 @@ namespace gbns
             case BCLASS_CK2_ID:
                 if (v == 1) GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 4, 128);
                 if (v == 2) GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, (GBNS_FP32 ? 512 : 576));
-#if !GBNS_FP32
-                if (v == 3) GBNS_BRUN1(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, 256);
-#endif
                 GBNS_BRUN(GBNS_CONV_CENT_KEEP, 2, false, 8, 8, 8, 256);
             case BCLASS_TOTANI_ID:
                 if (v == 1) GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 4, 128);
                 if (v == 2) GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, (GBNS_FP32 ? 512 : 576));
-#if !GBNS_FP32
-                if (v == 3) GBNS_BRUN1(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, 256);
-#endif
                 GBNS_BRUN(GBNS_CONV_TOTANI, 2, false, 8, 8, 8, 256);
             case BCLASS_FWENO_ID:
                 if (v == 1) GBNS_BRUN(GBNS_CONV_FWENO, 2, false, 8, 8, 4, 128);

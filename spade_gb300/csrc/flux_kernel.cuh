@@ -95,12 +95,7 @@ namespace gbns
     // boundary_flux (66).
     constexpr bool tag_no_fma(int tag) { return tag < 4 || tag == 64 || tag == 66; }
 
-    // MINB_ > 0 fixes the launch bound's CTAs per SM (0: from the shared
-    // memory the tile takes); 1 leaves a 256-thread tile the whole register
-    // file, which the batched kernels use to keep their per-item loop out of
-    // local memory.
-    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_, int STG_ = 0,
-              int MINB_ = 0>
+    template <class Real_, int CONV_, int ORDER_, bool STRETCH_, int TX_, int TY_, int TZ_, int NT_, int TAG_, int STG_ = 0>
     struct FluxCfg
     {
         using Real = Real_;
@@ -176,7 +171,7 @@ namespace gbns
         static constexpr int MINB_RAW = int((227*1024) / (SMEM_BYTES + 1024));
         // (tiles of more than 512 threads run one CTA per SM: two would leave
         // fewer than 57 registers per thread)
-        static constexpr int MINB = MINB_ > 0 ? MINB_ : (NT > 512 ? 1 : (MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW)));
+        static constexpr int MINB = NT > 512 ? 1 : (MINB_RAW < 1 ? 1 : (MINB_RAW > 4 ? 4 : MINB_RAW));
         static_assert(5*BXE <= 256, "TMA box inner extent exceeds 256 elements");
     };
 
