@@ -57,6 +57,11 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=200)
     p.add_argument("--serve-time-limit", type=float, default=30.0,
                    help="seconds each precision serves the configured stream")
+    p.add_argument("--flux-variants", choices=["taylor_green", "channel", "channel_fweno"], default=None,
+                   help="instead of the bench line: time one plain flux_div launch of every tile variant on the named "
+                        "workload (--nblk blocks of --ncell cells; --precision) and print the times; with --steps 1 it "
+                        "is the short, fixed launch sequence (one warm-up and one timed launch per variant) the ncu "
+                        "summaries capture")
     p.add_argument("--precision-report", type=int, default=0, metavar="STEPS",
                    help="instead of the bench line: run the channel workload STEPS steps in FP64 and in the "
                         "FP32-flux form from the same state and print their per-variable errors and drifts")
@@ -682,6 +687,47 @@ def run_precision_report(args):
     print(json.dumps(out))
 
 
+def run_flux_variants(args):
+    """One plain flux_div (overwrite mode) per tile variant, CUDA events on
+    the launching stream: one warm-up launch and --steps timed launches each
+    (median).  Workloads: taylor_green (cent_keep<2> + visc_lr(constant),
+    identity, ng 2), channel (the bench's WENO5 + pressure dissipation +
+    Sutherland on tanh-y, ng 3), channel_fweno (fweno_t + pressure dissipation
+    + constant viscosity, uniform, ng 2: the reference-GPU comparison's)."""
+    import torch
+    from spade_gb300 import _abi, _native, workloads
+    lib = _native.lib()
+    nb, nc = tuple(args.nblk), tuple(args.ncell)
+    if args.flux_variants == "taylor_green":
+        prob = workloads.taylor_green(nblk=nb, ncell=nc, ng=2, rng="torch", seed=0)
+    elif args.flux_variants == "channel":
+        prob = workloads.channel(nblk=nb, ncell=nc, ng=3, rng="torch", seed=0)
+    else:
+        prob = workloads.channel(nblk=nb, ncell=nc, ng=2, beta=None, weno="fweno", law="constant", rng="torch", seed=0)
+    prec = _abi.PREC_FP32_FLUX if args.precision == "fp32_flux" else _abi.PREC_FP64
+    g, s = prob.q.desc(), prob.scheme_desc(prec)
+    rhs = torch.zeros_like(prob.q.data)
+    st = torch.cuda.current_stream()
+    sp = int(st.cuda_stream)
+    times = {}
+    for v in range(lib.gbns_flux_variant_count(s)):
+        launch = lambda: _native.check(lib.gbns_flux_div_variant(g, s, prob.q.ptr(), rhs.data_ptr(), 0, v, sp))
+        launch()
+        ts = []
+        for _ in range(max(1, args.steps)):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            launch()
+            e1.record(st)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        times[v] = statistics.median(ts)
+    cells = int(math.prod(nb) * math.prod(nc))
+    print(json.dumps({"flux_variants": args.flux_variants, "precision": args.precision, "cells": cells,
+                      "ms_per_variant": times, "best": min(times, key=times.get),
+                      "cell_rhs_per_s": {v: cells / (t * 1e-3) for v, t in times.items()}}))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -689,6 +735,10 @@ def main():
     cfg = config(args)
     if args.precision_report:
         run_precision_report(args)
+        return
+    if args.flux_variants:
+        if rank == 0:
+            run_flux_variants(args)
         return
     if args.reference_gpu_only:
         if rank == 0:

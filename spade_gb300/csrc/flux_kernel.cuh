@@ -107,6 +107,9 @@ namespace gbns
         // (correctly rounded in both modes), and the reference's flux products
         // where no FMA contraction could have fused them
         static constexpr bool IEMU = std::is_same<Real_, double>::value && NT_ > 512;
+        // FP64 quotients and square roots on the integer pipes (ddiv_int,
+        // dsqrt_int: correctly rounded, the same bits) in every FP64 tile
+        static constexpr bool IDIV = std::is_same<Real_, double>::value;
         static constexpr bool IMUL = IEMU && tag_no_fma(TAG_);
         static constexpr int CONV = CONV_, ORDER = ORDER_;
         static constexpr bool STRETCH = STRETCH_;
@@ -297,21 +300,21 @@ namespace gbns
                       (Cfg::CONV == GBNS_CONV_HYBRID && Cfg::SPLIT))
         {
             // convective.h:130-131 / 80-84 (the hybrid's fweno half reads the split cache)
-            const Real rho = pdiv<Cfg::IEMU>(p, pmul<Cfg>(S.R, T));
+            const Real rho = pdiv<Cfg::IDIV>(p, pmul<Cfg>(S.R, T));
             der[0*Cfg::BOXN + c] = rho;
-            der[1*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, pmul<Cfg>(rho, S.gm1));
+            der[1*Cfg::BOXN + c] = pdiv<Cfg::IDIV>(p, pmul<Cfg>(rho, S.gm1));
         }
         else if constexpr (Cfg::CONV == GBNS_CONV_FWENO || Cfg::CONV == GBNS_CONV_WENO5 ||
                            Cfg::CONV == GBNS_CONV_HYBRID)
         {
             Real rho, h, e;
-            fweno_derive<Real, Cfg::IEMU, Cfg::IMUL>(S, p, T, u, v, w, rho, h, e);
+            fweno_derive<Real, Cfg::IDIV, Cfg::IMUL>(S, p, T, u, v, w, rho, h, e);
             der[0*Cfg::BOXN + c] = rho;
             der[1*Cfg::BOXN + c] = h;
             der[2*Cfg::BOXN + c] = e;
             // cent_keep's e (convective.h:131); its rho = p/(R*T) is the
             // same rounding as fweno's p/r above
-            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv<Cfg::IEMU>(p, pmul<Cfg>(rho, S.gm1));
+            if constexpr (Cfg::CONV == GBNS_CONV_HYBRID) der[3*Cfg::BOXN + c] = pdiv<Cfg::IDIV>(p, pmul<Cfg>(rho, S.gm1));
         }
     }
 
@@ -582,7 +585,7 @@ namespace gbns
             const int x = lx - (D == 0 ? HC : 0), y = ly - (D == 1 ? HC : 0), z = lz - (D == 2 ? HC : 0);
             const int c = (z + H)*Cfg::SZ + (y + H)*Cfg::SY + (x + H + shift);
             double rho, hsr, engy;
-            fweno_derive<double, Cfg::IEMU, Cfg::IMUL>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
+            fweno_derive<double, Cfg::IDIV, Cfg::IMUL>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), rho, hsr, engy);
             store(l, c, y, rho, hsr, engy);
         }
     }
@@ -606,7 +609,7 @@ namespace gbns
                     fu[m] = V.split[(2*eq)*Cfg::NLMAX + lr + (m - 2)*LS];
                     fd[m] = V.split[(2*eq + 1)*Cfg::NLMAX + lr + (m - 2)*LS];
                 }
-                out[eq] = fweno_apply_ud<Real, Cfg::IMUL, Cfg::IEMU>(fu, fd, S.smooth);
+                out[eq] = fweno_apply_ud<Real, Cfg::IMUL, Cfg::IDIV>(fu, fd, S.smooth);
             }
             else
             {
@@ -787,8 +790,8 @@ namespace gbns
         const Real delta_T = Tl - Tr;
         const Real pavg = ppow2<Cfg, -1>(pl + pr);
         const Real Tavg = ppow2<Cfg, -1>(Tl + Tr);
-        const Real inv_RT = pdiv<Cfg::IEMU>(Real(1.0), pmul<Cfg>(S.R_avg, Tavg));
-        const Real p_inv_rt2 = pdiv<Cfg::IEMU>(pmul<Cfg>(pavg, inv_RT), Tavg);
+        const Real inv_RT = pdiv<Cfg::IDIV>(Real(1.0), pmul<Cfg>(S.R_avg, Tavg));
+        const Real p_inv_rt2 = pdiv<Cfg::IDIV>(pmul<Cfg>(pavg, inv_RT), Tavg);
         const Real k = ppow2<Cfg, -1>(pmul<Cfg>(ul, ur) + pmul<Cfg>(vl, vr) + pmul<Cfg>(wl, wr));
         const Real u = ppow2<Cfg, -1>(ul + ur);
         const Real v = ppow2<Cfg, -1>(vl + vr);
@@ -872,14 +875,14 @@ namespace gbns
         }
         else if (S.law == GBNS_LAW_POWER)
         {
-            visc = pmul<Cfg>(S.mu, dev_pow(pdiv<Cfg::IEMU>(qf[1], S.T_ref), S.power));
+            visc = pmul<Cfg>(S.mu, dev_pow(pdiv<Cfg::IDIV>(qf[1], S.T_ref), S.power));
             visc2 = pmul<Cfg>(Real(-0.66666666667), visc);
-            dfs = pdiv<Cfg::IEMU>(visc, S.prandtl);
+            dfs = pdiv<Cfg::IDIV>(visc, S.prandtl);
         }
         else
         {
-            const Real x = pdiv<Cfg::IEMU>(qf[1], S.T_ref);
-            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt<Cfg::IEMU>(x))), pdiv<Cfg::IEMU>(S.tref_plus_s, qf[1] + S.S));
+            const Real x = pdiv<Cfg::IDIV>(qf[1], S.T_ref);
+            visc = pmul<Cfg>(pmul<Cfg>(S.mu, pmul<Cfg>(x, dev_sqrt<Cfg::IDIV>(x))), pdiv<Cfg::IDIV>(S.tref_plus_s, qf[1] + S.S));
             visc2 = pmul<Cfg>(visc, Real(-2.0/3.0));
             dfs = pmul<Cfg>(visc, S.inv_pr);
         }
@@ -930,7 +933,7 @@ namespace gbns
             {
                 face_gradient<Cfg, D>(V, rc, inv, im, grad);
                 have_grad = true;
-                blend = ducros_sensor<Real, Cfg::IEMU>(grad, S.hyb_param);
+                blend = ducros_sensor<Real, Cfg::IDIV>(grad, S.hyb_param);
             }
             conv_cent_keep<Cfg, D>(V, S, rc, nD, t0);
             conv_fweno<Cfg, D>(V, S, rc, lr, nD, t1);
@@ -951,7 +954,7 @@ namespace gbns
         // the gradient is not live across it; ducros_t needs the gradient first.
         if (hd && !ducros) diss_pressure<Cfg, D>(V, S, rc, S.sens, t1);
         if ((hv || ducros) && !have_grad) face_gradient<Cfg, D>(V, rc, inv, im, grad);
-        if (ducros) diss_pressure<Cfg, D>(V, S, rc, ducros_sensor<Real, Cfg::IEMU>(grad, S.sens), t1);
+        if (ducros) diss_pressure<Cfg, D>(V, S, rc, ducros_sensor<Real, Cfg::IDIV>(grad, S.sens), t1);
         if (hv) visc_lr<Cfg, D>(V, S, rc, nD, grad, t2);
         #pragma unroll
         for (int v = 0; v < 5; ++v)
@@ -1350,7 +1353,7 @@ namespace gbns
                 if (cc >= Cfg::NCELL) break;
                 const int cx = cc % TX, cy = (cc / TX) % TY, cz = cc / (TX*TY);
                 const int c = (cz + H)*Cfg::SZ + (cy + H)*Cfg::SY + (cx + H + shift);
-                fweno_derive<double, Cfg::IEMU, Cfg::IMUL>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
+                fweno_derive<double, Cfg::IDIV, Cfg::IMUL>(S, V.q(0, c), V.q(1, c), V.q(2, c), V.q(3, c), V.q(4, c), dc[s][0], dc[s][1], dc[s][2]);
             }
         }
 
@@ -1397,7 +1400,7 @@ namespace gbns
                     for (int v = 0; v < 5; ++v) qv[v] = __ldg(A.prims + off + v);
                 }
                 double cs[5];
-                if constexpr (Cfg::FP64) prim_to_cons<Cfg::IMUL>(qv, SK.R, SK.gm1, cs);
+                if constexpr (Cfg::FP64) prim_to_cons<Cfg::IMUL, Cfg::IDIV>(qv, SK.R, SK.gm1, cs);
                 else prim_to_cons_fast<true>(qv, SK.R, SK.inv_gm1, cs);
                 for (int j = 0; j + 1 < A.rk_nres; ++j)
                 {
@@ -1409,7 +1412,7 @@ namespace gbns
                 #pragma unroll
                 for (int v = 0; v < 5; ++v) cs[v] += pmul64<Cfg::IMUL>(cl, relem[s][v]);
                 double qn[5];
-                if constexpr (Cfg::FP64) cons_to_prim<Cfg::IMUL>(cs, SK.R, SK.gm1, qn);
+                if constexpr (Cfg::FP64) cons_to_prim<Cfg::IMUL, Cfg::IDIV>(cs, SK.R, SK.gm1, qn);
                 else cons_to_prim_fast<true>(cs, SK.inv_R, SK.gm1, qn);
                 double* o = A.q_out + off;
                 #pragma unroll

@@ -267,28 +267,29 @@ namespace gbns
         else return 0.5*x;
     }
 
-    template <bool IM = false>
+    // (IM: products on the integer pipes; ID: quotients there)
+    template <bool IM = false, bool ID = IM>
     __device__ __forceinline__ void prim_to_cons(const double q[5], const double R, const double gm1, double c[5])
     {
-        const double rho = pdiv64<IM>(q[0], pmul64<IM>(R, q[1]));
+        const double rho = pdiv64<ID>(q[0], pmul64<IM>(R, q[1]));
         const double rhoU2 = pmul64<IM>(rho, (pmul64<IM>(q[2], q[2]) + pmul64<IM>(q[3], q[3]) + pmul64<IM>(q[4], q[4])));
         c[0] = rho;
-        c[1] = phalf64<IM>(rhoU2) + pdiv64<IM>(q[0], gm1);
+        c[1] = phalf64<IM>(rhoU2) + pdiv64<ID>(q[0], gm1);
         c[2] = pmul64<IM>(rho, q[2]);
         c[3] = pmul64<IM>(rho, q[3]);
         c[4] = pmul64<IM>(rho, q[4]);
     }
 
-    template <bool IM = false>
+    template <bool IM = false, bool ID = IM>
     __device__ __forceinline__ void cons_to_prim(const double c[5], const double R, const double gm1, double q[5])
     {
         const double rh = c[0];
-        const double invrho = pdiv64<IM>(1.0, rh);
+        const double invrho = pdiv64<ID>(1.0, rh);
         const double uu = pmul64<IM>(invrho, c[2]), vv = pmul64<IM>(invrho, c[3]), ww = pmul64<IM>(invrho, c[4]);
         const double ru2 = pmul64<IM>(rh, (pmul64<IM>(uu, uu) + pmul64<IM>(vv, vv) + pmul64<IM>(ww, ww)));
         const double pp = pmul64<IM>(gm1, (c[1] - phalf64<IM>(ru2)));
         q[0] = pp;
-        q[1] = pdiv64<IM>(pp, pmul64<IM>(R, rh));
+        q[1] = pdiv64<ID>(pp, pmul64<IM>(R, rh));
         q[2] = uu;
         q[3] = vv;
         q[4] = ww;
