@@ -42,18 +42,19 @@ namespace gbns
     }
 
     int launch_flux_batch(int cls, int v, int precision, const TileItem* items, const int* offsets, const int* counts,
-                          const InstK* insts, const YTabK* ytabs, const long long* left, int stage, cudaStream_t st)
+                          const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems,
+                          cudaStream_t st)
     {
         const int group = cls == BCLASS_HYB2_ID ? 2 : ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) ? 1 : 0);
         if (precision == GBNS_PREC_FP32_FLUX)
         {
-            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
-            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
-            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
+            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
+            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
+            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
         }
-        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
-        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
-        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, st);
+        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
+        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
+        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
     }
 
     // First-fit allocator over one device allocation (offsets in bytes).
@@ -141,6 +142,7 @@ struct gbns_batch
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     unsigned graph_mask = 0;
+    int graph_counts[BCLASS_COUNT] = {0, 0, 0, 0, 0, 0};   // items per class the graph's launch grids cover
     bool graph_valid = false;
 };
 
@@ -280,7 +282,7 @@ namespace
             {
                 if (!(b->class_mask & (1u << c))) continue;
                 int rc = launch_flux_batch(c, b->variant[c], b->precision, b->d_tiles, offs, cnts, b->d_insts,
-                                           b->d_ytabs, b->d_left, stage, b->stream);
+                                           b->d_ytabs, b->d_left, stage, b->h_meta[BCLASS_COUNT + c], b->stream);
                 if (rc) return rc;
             }
             // the stage update ran in the flux launch's epilogue; fill the
@@ -308,8 +310,19 @@ namespace
         if (rc) { cudaGraphDestroy(g); return rc; }
         b->graph = g;
         b->graph_mask = b->class_mask;
+        for (int c = 0; c < BCLASS_COUNT; ++c) b->graph_counts[c] = b->h_meta[BCLASS_COUNT + c];
         b->graph_valid = true;
         return GBNS_OK;
+    }
+
+    // The flux launches' grids are the classes' item counts: a graph captured
+    // for other counts is captured again.
+    bool graph_current(const gbns_batch* b)
+    {
+        if (!b->graph_valid || b->graph_mask != b->class_mask) return false;
+        for (int c = 0; c < BCLASS_COUNT; ++c)
+            if (b->graph_counts[c] != b->h_meta[BCLASS_COUNT + c]) return false;
+        return true;
     }
 }
 
@@ -482,7 +495,7 @@ extern "C"
         if (b->h_blocks.empty() || nsteps == 0) return GBNS_OK;
         if (b->use_graph)
         {
-            if (!b->graph_valid || b->graph_mask != b->class_mask) rc = capture(b);
+            if (!graph_current(b)) rc = capture(b);
             if (rc) return rc;
             for (int n = 0; n < nsteps; ++n)
             {
@@ -573,11 +586,11 @@ extern "C"
                 const int* offs = b->d_meta;
                 const int* cnts = b->d_meta + BCLASS_COUNT;
                 if (!rc) rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs,
-                                                b->d_left, 0, b->stream);
+                                                b->d_left, 0, b->h_meta[BCLASS_COUNT + c], b->stream);
                 if (!rc) rc = check_cuda(cudaEventRecord(e0, b->stream), "autotune event");
                 for (int r = 0; r < reps && !rc; ++r)
                     rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs,
-                                           b->d_left, 0, b->stream);
+                                           b->d_left, 0, b->h_meta[BCLASS_COUNT + c], b->stream);
                 if (!rc) rc = check_cuda(cudaEventRecord(e1, b->stream), "autotune event");
                 if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "autotune sync");
                 float ms = 0.0f;

@@ -13,27 +13,25 @@ namespace gbns
     {
         status_registrar tu_status_registrar;
 
-        // The per-item arguments live in shared memory, not in registers: a
-        // CTA copies its item's geometry and scheme constants there and the
-        // tile code reads them like the single-grid kernel's parameters, so
-        // the persistent loop adds no live state to the tile's register
-        // budget (which lets the FP64 classes run the 576-thread tiles).
-        template <class Real>
+        // The per-item arguments live in shared memory: a CTA copies its
+        // item's geometry and scheme constants there and the tile code reads
+        // them like the single-grid kernel's parameters (unpacking the scheme
+        // constants itself, as the single-grid kernel does).
         struct ItemArgs
         {
             GeomK G;
             SchemeK S;
-            SchemeR<Real> SR;
             FluxArgs A;
             const YTabK* ytab;
-            int it, n, lb, tile;    // the CTA's position in its class's item range
+            int lb, tile;
         };
 
-        // CTAs loop over their class's range of the tile list; the arrays
-        // are read through the instance descriptors (no TMA: the halo is
-        // staged with coalesced loads, or straight into FP32 for FP32-flux).
-        // The loop's own state (item index, range, the item) is kept in
-        // shared memory too.
+        // One CTA per item of the class's range of the tile list (no
+        // persistent loop: a loop around the tile lets the compiler keep
+        // values live across items, which spilled the 256-thread FP64 tiles).
+        // The arrays are read through the instance descriptors (no TMA: the
+        // halo is staged with coalesced loads, or straight into FP32 for
+        // FP32-flux).
         template <class Cfg>
         __global__ void __launch_bounds__(Cfg::NT, Cfg::MINB)
         flux_batch_kernel(const TileItem* __restrict__ items, const int* __restrict__ offsets,
@@ -42,107 +40,89 @@ namespace gbns
                           const int cls, const int stage)
         {
             extern __shared__ __align__(128) unsigned char smem_raw[];
-            __shared__ __align__(16) ItemArgs<typename Cfg::Real> arg;
+            __shared__ __align__(16) ItemArgs arg;
+            if (int(blockIdx.x) >= counts[cls]) return;
+            const TileItem w = items[offsets[cls] + int(blockIdx.x)];
+            // an instance that has done its steps idles until it is retired
+            if (left[w.inst] == 0) return;
+            const InstK& I = insts[w.inst];
+            {
+                // geometry and scheme constants: word copies by the whole CTA
+                const int* sg = reinterpret_cast<const int*>(&I.G);
+                int* dg = reinterpret_cast<int*>(&arg.G);
+                for (int i = threadIdx.x; i < int(sizeof(GeomK)/4); i += Cfg::NT) dg[i] = sg[i];
+                const int* ss = reinterpret_cast<const int*>(&I.S);
+                int* ds = reinterpret_cast<int*>(&arg.S);
+                for (int i = threadIdx.x; i < int(sizeof(SchemeK)/4); i += Cfg::NT) ds[i] = ss[i];
+            }
             if (threadIdx.x == 0)
             {
-                arg.it = blockIdx.x;
-                arg.n = counts[cls];
+                // The SSPRK3 stage fused into the flux launch, as gbns_ssprk3_step
+                // issues it, with R[2] as the second state buffer:
+                //   stage 0: q    -> R0, q1 into R[2]
+                //   stage 1: R[2] -> R1, q2 into q
+                //   stage 2: q    -> (no store), q3 into R[2]  (copied back by the ghost pass)
+                // coefficients: ratio_diff of consecutive ssprk3_t rows times dt
+                // (advance.h:80-95).
+                const double dt = I.dt;
+                FluxArgs& A = arg.A;
+                A.increment = 0;
+                A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
+                A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
+                A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
+                A.use_tma = 0;
+                A.sh_off = 0;
+                A.rk_nres = stage + 1;
+                A.rk_res[0] = I.R[0];
+                A.rk_res[1] = I.R[1];
+                A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
+                if (stage == 0)
+                {
+                    A.prims = I.q; A.rhs = I.R[0]; A.write_rhs = 1; A.q_out = I.R[2];
+                    A.rk_coeff[0] = (1.0/1.0)*dt;
+                }
+                else if (stage == 1)
+                {
+                    A.prims = I.R[2]; A.rhs = I.R[1]; A.write_rhs = 1; A.q_out = I.q;
+                    A.rk_coeff[0] = (-3.0/4.0)*dt; A.rk_coeff[1] = (1.0/4.0)*dt;
+                }
+                else
+                {
+                    A.prims = I.q; A.rhs = nullptr; A.write_rhs = 0; A.q_out = I.R[2];
+                    A.rk_coeff[0] = (-1.0/12.0)*dt; A.rk_coeff[1] = (-1.0/12.0)*dt; A.rk_coeff[2] = (2.0/3.0)*dt;
+                }
+                arg.ytab = I.ytab >= 0 ? ytabs + I.ytab : nullptr;
+                arg.lb = w.lb;
+                arg.tile = w.tile;
             }
             __syncthreads();
-            while (arg.it < arg.n)
-            {
-                const TileItem w = items[offsets[cls] + arg.it];
-                if (left[w.inst] == 0)
-                {
-                    // the instance has done its steps and idles until it is retired
-                    __syncthreads();
-                    if (threadIdx.x == 0) arg.it += gridDim.x;
-                    __syncthreads();
-                    continue;
-                }
-                const InstK& I = insts[w.inst];
-                {
-                    // geometry and scheme constants: word copies by the whole CTA
-                    const int* sg = reinterpret_cast<const int*>(&I.G);
-                    int* dg = reinterpret_cast<int*>(&arg.G);
-                    for (int i = threadIdx.x; i < int(sizeof(GeomK)/4); i += Cfg::NT) dg[i] = sg[i];
-                    const int* ss = reinterpret_cast<const int*>(&I.S);
-                    int* ds = reinterpret_cast<int*>(&arg.S);
-                    for (int i = threadIdx.x; i < int(sizeof(SchemeK)/4); i += Cfg::NT) ds[i] = ss[i];
-                }
-                if (threadIdx.x == 0)
-                {
-                    // The SSPRK3 stage fused into the flux launch, as gbns_ssprk3_step
-                    // issues it, with R[2] as the second state buffer:
-                    //   stage 0: q    -> R0, q1 into R[2]
-                    //   stage 1: R[2] -> R1, q2 into q
-                    //   stage 2: q    -> (no store), q3 into R[2]  (copied back by the ghost pass)
-                    // coefficients: ratio_diff of consecutive ssprk3_t rows times dt
-                    // (advance.h:80-95).
-                    const double dt = I.dt;
-                    FluxArgs& A = arg.A;
-                    A.increment = 0;
-                    A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
-                    A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
-                    A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
-                    A.use_tma = 0;
-                    A.sh_off = 0;
-                    A.rk_nres = stage + 1;
-                    A.rk_res[0] = I.R[0];
-                    A.rk_res[1] = I.R[1];
-                    A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
-                    if (stage == 0)
-                    {
-                        A.prims = I.q; A.rhs = I.R[0]; A.write_rhs = 1; A.q_out = I.R[2];
-                        A.rk_coeff[0] = (1.0/1.0)*dt;
-                    }
-                    else if (stage == 1)
-                    {
-                        A.prims = I.R[2]; A.rhs = I.R[1]; A.write_rhs = 1; A.q_out = I.q;
-                        A.rk_coeff[0] = (-3.0/4.0)*dt; A.rk_coeff[1] = (1.0/4.0)*dt;
-                    }
-                    else
-                    {
-                        A.prims = I.q; A.rhs = nullptr; A.write_rhs = 0; A.q_out = I.R[2];
-                        A.rk_coeff[0] = (-1.0/12.0)*dt; A.rk_coeff[1] = (-1.0/12.0)*dt; A.rk_coeff[2] = (2.0/3.0)*dt;
-                    }
-                    arg.ytab = I.ytab >= 0 ? ytabs + I.ytab : nullptr;
-                    arg.lb = w.lb;
-                    arg.tile = w.tile;
-                }
-                __syncthreads();
-                if (threadIdx.x == 0) arg.SR.load(arg.S);
-                __syncthreads();
-                if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, arg.G, *arg.ytab, arg.S, arg.A, arg.lb, arg.tile, &arg.SR);
-                else flux_tile<Cfg>(smem_raw, nullptr, arg.G, YTabNone{}, arg.S, arg.A, arg.lb, arg.tile, &arg.SR);
-                __syncthreads();
-                if (threadIdx.x == 0) arg.it += gridDim.x;
-                __syncthreads();
-            }
+            if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, arg.G, *arg.ytab, arg.S, arg.A, arg.lb, arg.tile);
+            else flux_tile<Cfg>(smem_raw, nullptr, arg.G, YTabNone{}, arg.S, arg.A, arg.lb, arg.tile);
         }
 
         template <class Cfg>
         int run_batch(const TileItem* items, const int* offsets, const int* counts, const InstK* insts,
-                      const YTabK* ytabs, const long long* left, int cls, int stage, cudaStream_t st)
+                      const YTabK* ytabs, const long long* left, int cls, int stage, int nitems, cudaStream_t st)
         {
+            if (nitems <= 0) return GBNS_OK;
             auto kern = flux_batch_kernel<Cfg>;
             int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM_BYTES)),
                                 "flux_batch smem attribute");
             if (rc) return rc;
-            kern<<<persistent_grid(Cfg::MINB), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, left,
-                                                                               cls, stage);
+            kern<<<unsigned(nitems), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, left, cls, stage);
             return check_cuda(cudaGetLastError(), "flux_batch launch");
         }
     }
 
 #define GBNS_BRUN(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
-    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, left, cls, stage, st)
+    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, left, cls, stage, nitems, st)
 
     // The tile variants of each class (their shapes are listed by
     // batch_class_tile in batch.cu, in the same order); variant 0 is the
     // default the autotuner starts from.
     int GBNS_BATCH_FN(int cls, int v, const TileItem* items, const int* offsets, const int* counts,
-                      const InstK* insts, const YTabK* ytabs, const long long* left, int stage, cudaStream_t st)
+                      const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems,
+                      cudaStream_t st)
     {
 #if GBNS_BATCH_GROUP == 0
         switch (cls)

@@ -56,15 +56,16 @@ namespace gbns
     int batch_class_variants(int cls, int precision);
     void batch_class_tile(int cls, int precision, int variant, int tile[3]);
 
-    // Persistent flux launch of one class (tile variant v) for one SSPRK3
-    // stage.  `offsets` and `counts` (device, BCLASS_COUNT ints) locate the
-    // class's items.  One function per precision and class group
-    // (a: cent_keep<2>, totani_lr, fweno_t; b: WENO5; c: hybrid).
-    // `left` (device, one per slot): steps an instance still has to do before
-    // it idles (-1: no limit); items of instances at 0 are skipped.
+    // Flux launch of one class (tile variant v) for one SSPRK3 stage: one
+    // CTA per item.  `offsets` and `counts` (device, BCLASS_COUNT ints) locate
+    // the class's items; `nitems` is the host's copy of its count (the grid).
+    // One function per precision and class group (a: cent_keep<2>,
+    // totani_lr, fweno_t; b: WENO5; c: hybrid).  `left` (device, one per
+    // slot): steps an instance still has to do before it idles (-1: no
+    // limit); items of instances at 0 are skipped.
 #define GBNS_BATCH_DECL(NAME) \
     int NAME(int cls, int v, const TileItem* items, const int* offsets, const int* counts, \
-             const InstK* insts, const YTabK* ytabs, const long long* left, int stage, cudaStream_t st);
+             const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems, cudaStream_t st);
     GBNS_BATCH_DECL(launch_flux_batch_f64x_a)
     GBNS_BATCH_DECL(launch_flux_batch_f64x_b)
     GBNS_BATCH_DECL(launch_flux_batch_f64x_c)
