@@ -433,8 +433,8 @@ int gbns_source_term(const gbns_grid_desc* grid, const gbns_source_desc* source,
 
 /* ---- batched form ----------------------------------------------------
  * Many independent grids ("instances") of uneven size advanced together:
- * each SSPRK3 stage is one persistent flux launch per kernel class (walking a
- * device work-list of tiles of every instance, with the stage update fused
+ * each SSPRK3 stage is one flux launch per kernel class (one CTA per item of
+ * a device work-list of tiles of every instance, with the stage update fused
  * into its epilogue) and one batched ghost fill; with use_graph the step
  * (six launches for one kernel class) is captured
  * once in a CUDA graph and replayed.  Instance state stays resident in an
@@ -483,7 +483,7 @@ size_t gbns_batch_instance_bytes(const gbns_grid_desc* grid);
  * the active instances (the compile-time flux configuration: convective
  * scheme x coordinates, numbered 0 .. gbns_batch_class_count()-1), times
  * each of its tile variants (tile shape and threads per CTA) on the
- * instances' own arrays with CUDA events, `reps` persistent launches of the
+ * instances' own arrays with CUDA events, `reps` launches of the
  * first SSPRK3 stage each (which writes only scratch arrays), and keeps the
  * fastest.  variants_out (optional, gbns_batch_class_count() ints) receives
  * the choice per class, -1 for absent classes.  Synchronises the batch.

@@ -1,5 +1,5 @@
 """Batched form: many independent grids of uneven size advanced together by
-persistent launches driven by device work-lists, one CUDA graph per step
+flux launches over device work-lists of tiles, one CUDA graph per step
 (gbns_batch_* in include/gbns.h).  Instance state stays resident in an arena
 sized by an HBM budget; every instance's result is bit-identical to
 advancing it alone."""

@@ -1,4 +1,4 @@
-// Persistent flux-divergence kernels of the batched form.  Each TU defines
+// Flux-divergence kernels of the batched form (one CTA per tile item).  Each TU defines
 // GBNS_REAL, GBNS_TAG, GBNS_FP32, GBNS_BATCH_GROUP and GBNS_BATCH_FN and
 // includes this; a TU instantiates the tile variants of its group of kernel
 // classes (0: cent_keep<2>, totani_lr, fweno_t; 1: WENO5; 2: hybrid).

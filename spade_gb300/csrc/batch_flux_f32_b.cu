@@ -1,4 +1,4 @@
-// Batched persistent flux kernels: FP32 flux arithmetic, FP64 accumulation; class group 1.
+// Batched flux kernels: FP32 flux arithmetic, FP64 accumulation; class group 1.
 #define GBNS_REAL float
 #define GBNS_TAG 65
 #define GBNS_FP32 1

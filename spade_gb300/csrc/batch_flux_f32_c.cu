@@ -1,4 +1,4 @@
-// Batched persistent flux kernels: FP32 flux arithmetic, FP64 accumulation; class group 2.
+// Batched flux kernels: FP32 flux arithmetic, FP64 accumulation; class group 2.
 #define GBNS_REAL float
 #define GBNS_TAG 65
 #define GBNS_FP32 1

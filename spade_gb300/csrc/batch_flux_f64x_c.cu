@@ -1,4 +1,4 @@
-// Batched persistent flux kernels: FP64, no FMA contraction (built with -fmad=false); class group 2.
+// Batched flux kernels: FP64, no FMA contraction (built with -fmad=false); class group 2.
 #define GBNS_REAL double
 #define GBNS_TAG 64
 #define GBNS_FP32 0

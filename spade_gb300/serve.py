@@ -1,7 +1,7 @@
 """Serving form: continuous batching of independent solves.
 
 Requests (a grid, a scheme, a step count) arrive over time.  The server keeps
-one resident batch (spade_gb300.batch.batch_t, one persistent launch per
+one resident batch (spade_gb300.batch.batch_t, one flux launch per
 kernel class per RK stage, replayed from a CUDA graph).  Between chunks of
 steps it admits every request that has arrived and fits the HBM budget
 (first come, first served), advances all active instances together, and
