@@ -108,8 +108,12 @@ namespace gbns
         // where no FMA contraction could have fused them
         static constexpr bool IEMU = std::is_same<Real_, double>::value && NT_ > 512;
         // FP64 quotients and square roots on the integer pipes (ddiv_int,
-        // dsqrt_int: correctly rounded, the same bits) in every FP64 tile
-        static constexpr bool IDIV = std::is_same<Real_, double>::value;
+        // dsqrt_int: correctly rounded, the same bits) in the FP64 tiles of
+        // 256 threads and more (Taylor-Green, 2.1M cells: 2.48 -> 2.40 ms at
+        // 256 threads); the 128-thread tiles the autotuner picks for small,
+        // latency-bound grids keep the FP64 unit's (the 32K-cell step measured
+        // 0.222 vs 0.237 ms)
+        static constexpr bool IDIV = std::is_same<Real_, double>::value && NT_ >= 256;
         static constexpr bool IMUL = IEMU && tag_no_fma(TAG_);
         static constexpr int CONV = CONV_, ORDER = ORDER_;
         static constexpr bool STRETCH = STRETCH_;
