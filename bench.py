@@ -308,6 +308,20 @@ def run_gpu(args, rank, world):
     }
 
 
+def fp64_ops_roof(r):
+    """The fused FP64 launch against the FP64 unit's roof: FP64-pipe thread
+    operations per cell and stage (ncu, mean of the three stages of the
+    committed channel capture) x cells / the launch's CUDA-event time, over
+    the measured DFMA lane rate (one operation per lane and DFMA)."""
+    per_cell = _profile_value("fp64_ops_per_cell")
+    if not per_cell or not r.get("fp64_fma_flops"):
+        return {}
+    achieved = per_cell * r["cells"] / (r["flux_avg_ms"] * 1e-3)
+    peak = r["fp64_fma_flops"] / 2.0
+    return {"fp64_ops_per_cell_ncu": per_cell, "achieved_fp64_ops_per_s": achieved, "peak_fp64_ops_per_s": peak,
+            "frac_of_fp64_peak": achieved / peak}
+
+
 def _profile_value(key):
     """A `key: value` line of the committed ncu summary of the fused FP64
     flux kernel (2.1M-cell capture of the channel scheme)."""
@@ -817,7 +831,8 @@ def main():
                       "note": "measured DFMA/FFMA chains on this GPU; the FP64 kernel is bound by the FP64 unit, with its "
                               "products, quotients and square roots computed exactly on the integer pipes",
                       "fp64_pipe_active_frac_ncu": _profile_value("fp64_pipe_active_frac"),
-                      "pipe_source": "profiles/flux_div_rk_channel_fp64.md (sm__pipe_fp64_cycles_active, 2.1M-cell capture)"},
+                      "pipe_source": "profiles/flux_div_rk_channel_fp64.md (sm__pipe_fp64_cycles_active, 2.1M-cell capture)",
+                      **fp64_ops_roof(r)},
         "step_bytes": {"alg_bytes_per_cell_step": ALG_BYTES_STEP,
                        "achieved_gbs": ALG_BYTES_STEP * cells_all * args.steps / (r["ms"] * 1e-3) / 1e9},
         "clocks": r["clocks"],
