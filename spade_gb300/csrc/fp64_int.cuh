@@ -21,6 +21,19 @@
 
 namespace gbns
 {
+    // The hardware operations the integer routines below fall back to for
+    // special operands (zeros, subnormals, infinities, NaNs, results outside
+    // the normal range), as calls the compiler cannot if-convert.  Inlined,
+    // the fallback became an FP64 instruction predicated off in the lanes that
+    // do not need it, which every warp still issues to the FP64 unit (about a
+    // fifth of that unit's issue in the integer-pipe tiles, measured); as a
+    // call it sits behind a branch that warps with no special lane skip.
+    static __device__ __noinline__ double dmul_hw(double a, double b) { return __dmul_rn(a, b); }
+    static __device__ __noinline__ double ddiv_hw(double a, double b) { return a/b; }
+    static __device__ __noinline__ double dsqrt_hw(double x) { return __dsqrt_rn(x); }
+    static __device__ __noinline__ double dscale_hw(double x, double c) { return x*c; }
+    static __device__ __noinline__ float d2f_hw(double x) { return __double2float_rn(x); }
+
     __device__ __forceinline__ double dmul_int(double a, double b)
     {
         constexpr uint64_t M52 = 0x000FFFFFFFFFFFFFull, H53 = 0x0010000000000000ull, SGN = 0x8000000000000000ull;
@@ -28,7 +41,7 @@ namespace gbns
         const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
         // biased exponent of the product when the significand product is in [1, 2)
         int e = (int)ea + (int)eb - 1023;
-        if (ea - 1u >= 2046u || eb - 1u >= 2046u || (unsigned)(e - 1) >= 2045u) return __dmul_rn(a, b);
+        if (ea - 1u >= 2046u || eb - 1u >= 2046u || (unsigned)(e - 1) >= 2045u) return dmul_hw(a, b);
         // significands with the hidden bit at bit 63: the product is in [2^126, 2^128)
         const uint64_t ma = ((ua & M52) | H53) << 11, mb = ((ub & M52) | H53) << 11;
         uint64_t hi = __umul64hi(ma, mb);
@@ -65,7 +78,7 @@ namespace gbns
         const uint64_t ua = (uint64_t)__double_as_longlong(a), ub = (uint64_t)__double_as_longlong(b);
         const uint32_t ea = (uint32_t)(ua >> 52) & 0x7ffu, eb = (uint32_t)(ub >> 52) & 0x7ffu;
         int e = (int)ea - (int)eb + 1023;
-        if (ea - 1u >= 2046u || eb - 1u >= 2046u || (unsigned)(e - 2) >= 2044u) return a/b;
+        if (ea - 1u >= 2046u || eb - 1u >= 2046u || (unsigned)(e - 2) >= 2044u) return ddiv_hw(a, b);
         uint64_t ma = (ua & M52) | H53;
         const uint64_t mb = (ub & M52) | H53;
         if (ma < mb) { ma <<= 1; e -= 1; }
@@ -124,7 +137,7 @@ namespace gbns
         constexpr uint64_t M52 = 0x000FFFFFFFFFFFFFull, H53 = 0x0010000000000000ull;
         const uint64_t ux = (uint64_t)__double_as_longlong(x);
         const uint32_t ex = (uint32_t)(ux >> 52);            // the sign bit makes negatives fail the range test
-        if (ex - 1u >= 2046u) return __dsqrt_rn(x);
+        if (ex - 1u >= 2046u) return dsqrt_hw(x);
         const int E = (int)ex - 1023;
         const int p = E & 1;
         const uint64_t mx = (ux & M52) | H53;
@@ -184,7 +197,8 @@ namespace gbns
         static_assert(E < 0 && E > -1022, "negative power of two");
         const uint64_t u = (uint64_t)__double_as_longlong(x);
         const uint32_t ex = (uint32_t)(u >> 52) & 0x7ffu;
-        if (ex - uint32_t(1 - E) >= uint32_t(2046 - (1 - E) + 1)) return x*(E == -1 ? 0.5 : (E == -2 ? 0.25 : __longlong_as_double((long long)(uint64_t(1023 + E) << 52))));
+        if (ex - uint32_t(1 - E) >= uint32_t(2046 - (1 - E) + 1))
+            return dscale_hw(x, E == -1 ? 0.5 : (E == -2 ? 0.25 : __longlong_as_double((long long)(uint64_t(1023 + E) << 52))));
         return __longlong_as_double((long long)(u - (uint64_t(-E) << 52)));
     }
 
@@ -196,7 +210,7 @@ namespace gbns
     {
         const uint64_t u = (uint64_t)__double_as_longlong(x);
         const uint32_t ex = (uint32_t)(u >> 52) & 0x7ffu;
-        if (ex - 1u >= 2045u) return x*2.0;
+        if (ex - 1u >= 2045u) return dscale_hw(x, 2.0);
         return __longlong_as_double((long long)(u + (uint64_t(1) << 52)));
     }
 
@@ -226,7 +240,7 @@ namespace gbns
         const uint64_t u = (uint64_t)__double_as_longlong(x);
         const uint32_t hi = uint32_t(u >> 32), lo = uint32_t(u);
         const uint32_t e = (hi >> 20) & 0x7ffu;
-        if (e - 897u > 253u) return __double2float_rn(x);
+        if (e - 897u > 253u) return d2f_hw(x);
         const uint32_t m = ((hi & 0xfffffu) << 3) | (lo >> 29);     // 23 significand bits
         const uint32_t rem = lo & 0x1fffffffu;                       // the 29 bits below
         uint32_t f = (hi & 0x80000000u) | ((e - 896u) << 23) | m;

@@ -12,6 +12,7 @@
 
 #define __device__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 static inline long long __double_as_longlong(double d) { long long x; std::memcpy(&x, &d, 8); return x; }
 static inline double __longlong_as_double(long long x) { double d; std::memcpy(&d, &x, 8); return d; }
 static inline uint64_t __umul64hi(uint64_t a, uint64_t b) { return (uint64_t)(((unsigned __int128)a*b) >> 64); }
