@@ -355,6 +355,11 @@ extern "C"
         }
         b->arena.init(hbm_budget_bytes);
         std::memset(b->h_meta, 0, sizeof(b->h_meta));
+        // FP64 starts every class on its 8x8x8 / 576-thread tile (variant 2:
+        // products and quotients on the integer pipes), the fastest on the
+        // measured mixes; gbns_batch_autotune re-times them on the instances
+        if (precision == GBNS_PREC_FP64)
+            for (int c = 0; c < BCLASS_COUNT; ++c) b->variant[c] = 2;
         *out = b;
         return GBNS_OK;
     }

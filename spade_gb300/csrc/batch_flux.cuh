@@ -4,6 +4,7 @@
 // classes (0: cent_keep<2>, totani_lr, fweno_t; 1: WENO5; 2: hybrid).
 #pragma once
 
+#include <cstddef>
 #include "flux_kernel.cuh"
 #include "batch_internal.cuh"
 
@@ -47,13 +48,24 @@ namespace gbns
             if (left[w.inst] == 0) return;
             const InstK& I = insts[w.inst];
             {
-                // geometry and scheme constants: word copies by the whole CTA
+                // geometry and scheme constants: word copies by the whole CTA.
+                // Of the per-block spacing tables only the item's block's
+                // entries are copied (the tile reads no other).
+                constexpr int GHEAD = int(offsetof(GeomK, inv_dx))/4;
                 const int* sg = reinterpret_cast<const int*>(&I.G);
                 int* dg = reinterpret_cast<int*>(&arg.G);
-                for (int i = threadIdx.x; i < int(sizeof(GeomK)/4); i += Cfg::NT) dg[i] = sg[i];
+                for (int i = threadIdx.x; i < GHEAD; i += Cfg::NT) dg[i] = sg[i];
                 const int* ss = reinterpret_cast<const int*>(&I.S);
                 int* ds = reinterpret_cast<int*>(&arg.S);
                 for (int i = threadIdx.x; i < int(sizeof(SchemeK)/4); i += Cfg::NT) ds[i] = ss[i];
+                if (threadIdx.x < 3)
+                {
+                    const int d = threadIdx.x;
+                    const int nb0 = I.G.nb[0], nb1 = I.G.nb[1];
+                    const int bd = d == 0 ? w.lb % nb0 : (d == 1 ? (w.lb / nb0) % nb1 : w.lb / (nb0*nb1));
+                    arg.G.inv_dx[d][bd] = I.G.inv_dx[d][bd];
+                    arg.G.inv_dx_f[d][bd] = I.G.inv_dx_f[d][bd];
+                }
             }
             if (threadIdx.x == 0)
             {
@@ -118,8 +130,8 @@ namespace gbns
     return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, left, cls, stage, nitems, st)
 
     // The tile variants of each class (their shapes are listed by
-    // batch_class_tile in batch.cu, in the same order); variant 0 is the
-    // default the autotuner starts from.
+    // batch_class_tile in batch.cu, in the same order); a new batch starts
+    // on variant 0 in FP32-flux and on variant 2 (576 threads) in FP64.
     int GBNS_BATCH_FN(int cls, int v, const TileItem* items, const int* offsets, const int* counts,
                       const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems,
                       cudaStream_t st)
