@@ -42,19 +42,30 @@ namespace gbns
     }
 
     int launch_flux_batch(int cls, int v, int precision, const TileItem* items, const int* offsets, const int* counts,
-                          const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems,
-                          cudaStream_t st)
+                          const InstK* insts, const YTabK* ytabs, const long long* left, const CUtensorMap* tmaps,
+                          int stage, int nitems, cudaStream_t st)
     {
         const int group = cls == BCLASS_HYB2_ID ? 2 : ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) ? 1 : 0);
         if (precision == GBNS_PREC_FP32_FLUX)
         {
-            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
-            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
-            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
+            if (group == 0) return launch_flux_batch_f32_a(cls, v, items, offsets, counts, insts, ytabs, left, nullptr, stage, nitems, st);
+            if (group == 1) return launch_flux_batch_f32_b(cls, v, items, offsets, counts, insts, ytabs, left, nullptr, stage, nitems, st);
+            return launch_flux_batch_f32_c(cls, v, items, offsets, counts, insts, ytabs, left, nullptr, stage, nitems, st);
         }
-        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
-        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
-        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, left, stage, nitems, st);
+        if (group == 0) return launch_flux_batch_f64x_a(cls, v, items, offsets, counts, insts, ytabs, left, tmaps, stage, nitems, st);
+        if (group == 1) return launch_flux_batch_f64x_b(cls, v, items, offsets, counts, insts, ytabs, left, tmaps, stage, nitems, st);
+        return launch_flux_batch_f64x_c(cls, v, items, offsets, counts, insts, ytabs, left, tmaps, stage, nitems, st);
+    }
+
+    // The FP64 TMA box of a class's variant (zeros: no TMA staging).
+    int batch_box(int cls, int v, int precision, int box[3])
+    {
+        box[0] = box[1] = box[2] = 0;
+        if (precision == GBNS_PREC_FP32_FLUX) return GBNS_OK;
+        const int group = cls == BCLASS_HYB2_ID ? 2 : ((cls == BCLASS_WENO5_ST || cls == BCLASS_WENO5_ID) ? 1 : 0);
+        if (group == 0) return launch_flux_batch_f64x_a_box(cls, v, box);
+        if (group == 1) return launch_flux_batch_f64x_b_box(cls, v, box);
+        return launch_flux_batch_f64x_c_box(cls, v, box);
     }
 
     // First-fit allocator over one device allocation (offsets in bytes).
@@ -133,6 +144,11 @@ struct gbns_batch
     BlockItem* d_blocks = nullptr;
     size_t block_cap = 0;
     int* d_meta = nullptr;     // offsets[BCLASS_COUNT], counts[BCLASS_COUNT], nblocks
+    // FP64: per slot the tensor maps of q and R[2] for the TMA staging of its
+    // class's current tile variant (rebuilt with the lists)
+    CUtensorMap* d_tmaps = nullptr;
+    size_t tmap_cap = 0;
+    std::vector<CUtensorMap> h_tmaps;
     std::vector<TileItem> h_tiles;
     std::vector<BlockItem> h_blocks;
     int h_meta[2*BCLASS_COUNT + 1];
@@ -219,11 +235,32 @@ namespace
         return GBNS_OK;
     }
 
+    // Encodes slot si's tensor maps (q and R[2]) for the TMA box of its
+    // class's current variant; false when that variant stages no FP64 box by
+    // TMA or the layout does not allow it (padded rows must hold an even
+    // number of cells for the 16-byte rule; the arena keeps the arrays
+    // 256-byte aligned).
+    bool slot_tma(gbns_batch* b, size_t si)
+    {
+        const Slot& S = b->slots[si];
+        if (b->h_tmaps.size() < 2*(si + 1)) b->h_tmaps.resize(2*(si + 1));
+        int box[3];
+        if (batch_box(S.cls, b->variant[S.cls], b->precision, box) || box[0] == 0) return false;
+        GeomK G;
+        if (make_geom(&S.g, G) || G.ni % 2 != 0) return false;
+        double* q = reinterpret_cast<double*>(b->arena_base + S.off);
+        double* r2 = reinterpret_cast<double*>(b->arena_base + S.off + 3*S.arr_bytes);
+        if (encode_prims_tmap(&b->h_tmaps[2*si], q, G, box[0], box[1], box[2])) return false;
+        if (encode_prims_tmap(&b->h_tmaps[2*si + 1], r2, G, box[0], box[1], box[2])) return false;
+        return true;
+    }
+
     int rebuild_lists(gbns_batch* b)
     {
         b->h_tiles.clear();
         b->h_blocks.clear();
         b->class_mask = 0;
+        b->h_tmaps.assign(2*b->slots.size(), CUtensorMap{});
         for (int c = 0; c < BCLASS_COUNT; ++c)
         {
             b->h_meta[c] = int(b->h_tiles.size());
@@ -235,9 +272,10 @@ namespace
                 if (!S.active || S.cls != c) continue;
                 const int nt = ((S.g.ncell[0] + t[0] - 1)/t[0])*((S.g.ncell[1] + t[1] - 1)/t[1])*((S.g.ncell[2] + t[2] - 1)/t[2]);
                 const int nblk = S.g.nblk[0]*S.g.nblk[1]*S.g.nblk[2];
+                const int tma = slot_tma(b, si) ? 1 : 0;
                 for (int lb = 0; lb < nblk; ++lb)
                     for (int tile = 0; tile < nt; ++tile)
-                        b->h_tiles.push_back(TileItem{int(si), lb, tile, 0});
+                        b->h_tiles.push_back(TileItem{int(si), lb, tile, tma});
             }
             b->h_meta[BCLASS_COUNT + c] = int(b->h_tiles.size()) - b->h_meta[c];
             if (b->h_meta[BCLASS_COUNT + c]) b->class_mask |= 1u << c;
@@ -262,6 +300,14 @@ namespace
             rc = check_cuda(cudaMemcpyAsync(b->d_blocks, b->h_blocks.data(), sizeof(BlockItem)*b->h_blocks.size(),
                                             cudaMemcpyHostToDevice, b->stream), "upload block list");
         if (rc) return rc;
+        if (b->precision != GBNS_PREC_FP32_FLUX && !b->h_tmaps.empty())
+        {
+            rc = grow_list(&b->d_tmaps, &b->tmap_cap, b->h_tmaps.size(), b, "batch tensor maps");
+            if (rc) return rc;
+            rc = check_cuda(cudaMemcpyAsync(b->d_tmaps, b->h_tmaps.data(), sizeof(CUtensorMap)*b->h_tmaps.size(),
+                                            cudaMemcpyHostToDevice, b->stream), "upload tensor maps");
+            if (rc) return rc;
+        }
         rc = check_cuda(cudaMemcpyAsync(b->d_meta, b->h_meta, sizeof(b->h_meta), cudaMemcpyHostToDevice, b->stream),
                         "upload list counts");
         if (rc) return rc;
@@ -282,7 +328,8 @@ namespace
             {
                 if (!(b->class_mask & (1u << c))) continue;
                 int rc = launch_flux_batch(c, b->variant[c], b->precision, b->d_tiles, offs, cnts, b->d_insts,
-                                           b->d_ytabs, b->d_left, stage, b->h_meta[BCLASS_COUNT + c], b->stream);
+                                           b->d_ytabs, b->d_left, b->d_tmaps, stage, b->h_meta[BCLASS_COUNT + c],
+                                           b->stream);
                 if (rc) return rc;
             }
             // the stage update ran in the flux launch's epilogue; fill the
@@ -376,6 +423,7 @@ extern "C"
         cudaFree(b->d_left);
         cudaFree(b->d_tiles);
         cudaFree(b->d_blocks);
+        cudaFree(b->d_tmaps);
         cudaFree(b->d_meta);
         cudaEventDestroy(b->ev_in);
         cudaEventDestroy(b->ev_out);
@@ -591,11 +639,11 @@ extern "C"
                 const int* offs = b->d_meta;
                 const int* cnts = b->d_meta + BCLASS_COUNT;
                 if (!rc) rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs,
-                                                b->d_left, 0, b->h_meta[BCLASS_COUNT + c], b->stream);
+                                                b->d_left, b->d_tmaps, 0, b->h_meta[BCLASS_COUNT + c], b->stream);
                 if (!rc) rc = check_cuda(cudaEventRecord(e0, b->stream), "autotune event");
                 for (int r = 0; r < reps && !rc; ++r)
                     rc = launch_flux_batch(c, v, b->precision, b->d_tiles, offs, cnts, b->d_insts, b->d_ytabs,
-                                           b->d_left, 0, b->h_meta[BCLASS_COUNT + c], b->stream);
+                                           b->d_left, b->d_tmaps, 0, b->h_meta[BCLASS_COUNT + c], b->stream);
                 if (!rc) rc = check_cuda(cudaEventRecord(e1, b->stream), "autotune event");
                 if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "autotune sync");
                 float ms = 0.0f;

@@ -24,6 +24,7 @@ namespace gbns
             SchemeK S;
             FluxArgs A;
             const YTabK* ytab;
+            const CUtensorMap* tmap;
             int lb, tile;
         };
 
@@ -38,7 +39,7 @@ namespace gbns
         flux_batch_kernel(const TileItem* __restrict__ items, const int* __restrict__ offsets,
                           const int* __restrict__ counts, const InstK* __restrict__ insts,
                           const YTabK* __restrict__ ytabs, const long long* __restrict__ left,
-                          const int cls, const int stage)
+                          const CUtensorMap* __restrict__ tmaps, const int cls, const int stage)
         {
             extern __shared__ __align__(128) unsigned char smem_raw[];
             __shared__ __align__(16) ItemArgs arg;
@@ -82,8 +83,12 @@ namespace gbns
                 A.ntile[0] = (I.G.n[0] + Cfg::TX - 1)/Cfg::TX;
                 A.ntile[1] = (I.G.n[1] + Cfg::TY - 1)/Cfg::TY;
                 A.ntile[2] = (I.G.n[2] + Cfg::TZ - 1)/Cfg::TZ;
-                A.use_tma = 0;
+                // FP64 tiles stage their box by TMA from the instance's tensor
+                // map of the array this stage reads (tmaps[2 inst]: q,
+                // tmaps[2 inst + 1]: R[2]); items the host marked (w.pad) only
+                A.use_tma = (!Cfg::DIRECT && tmaps != nullptr && w.pad) ? 1 : 0;
                 A.sh_off = 0;
+                arg.tmap = A.use_tma ? tmaps + 2*w.inst + (stage == 1 ? 1 : 0) : nullptr;
                 A.rk_nres = stage + 1;
                 A.rk_res[0] = I.R[0];
                 A.rk_res[1] = I.R[1];
@@ -108,33 +113,59 @@ namespace gbns
                 arg.tile = w.tile;
             }
             __syncthreads();
-            if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, nullptr, arg.G, *arg.ytab, arg.S, arg.A, arg.lb, arg.tile);
-            else flux_tile<Cfg>(smem_raw, nullptr, arg.G, YTabNone{}, arg.S, arg.A, arg.lb, arg.tile);
+            // the map was written to global memory by a host copy: acquire it
+            // for the tensor proxy before the thread that issues the copy uses it
+            if (threadIdx.x == 0 && arg.tmap) tensormap_acquire(arg.tmap);
+            if constexpr (Cfg::STRETCH) flux_tile<Cfg>(smem_raw, arg.tmap, arg.G, *arg.ytab, arg.S, arg.A, arg.lb, arg.tile);
+            else flux_tile<Cfg>(smem_raw, arg.tmap, arg.G, YTabNone{}, arg.S, arg.A, arg.lb, arg.tile);
         }
 
-        template <class Cfg>
-        int run_batch(const TileItem* items, const int* offsets, const int* counts, const InstK* insts,
-                      const YTabK* ytabs, const long long* left, int cls, int stage, int nitems, cudaStream_t st)
+        // The launch of one class and stage (an action of batch_dispatch).
+        struct LaunchAction
         {
-            if (nitems <= 0) return GBNS_OK;
-            auto kern = flux_batch_kernel<Cfg>;
-            int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::SMEM_BYTES)),
-                                "flux_batch smem attribute");
-            if (rc) return rc;
-            kern<<<unsigned(nitems), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, left, cls, stage);
-            return check_cuda(cudaGetLastError(), "flux_batch launch");
-        }
+            const TileItem* items; const int* offsets; const int* counts; const InstK* insts;
+            const YTabK* ytabs; const long long* left; const CUtensorMap* tmaps;
+            int cls, stage, nitems; cudaStream_t st;
+            template <class Cfg> int run() const
+            {
+                if (nitems <= 0) return GBNS_OK;
+                auto kern = flux_batch_kernel<Cfg>;
+                int rc = check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                         int(Cfg::SMEM_BYTES)), "flux_batch smem attribute");
+                if (rc) return rc;
+                kern<<<unsigned(nitems), Cfg::NT, Cfg::SMEM_BYTES, st>>>(items, offsets, counts, insts, ytabs, left,
+                                                                         tmaps, cls, stage);
+                return check_cuda(cudaGetLastError(), "flux_batch launch");
+            }
+        };
+        // The TMA box of a variant's FP64 staging (cells along x, y, z), for
+        // the tensor maps the host encodes; 0 when the variant stages no FP64
+        // box by TMA.
+        struct BoxAction
+        {
+            int* box;
+            template <class Cfg> int run() const
+            {
+                const bool tma = !Cfg::DIRECT && !Cfg::SHADOW && Cfg::FP64;
+                box[0] = tma ? Cfg::BXE : 0;
+                box[1] = tma ? Cfg::BY : 0;
+                box[2] = tma ? Cfg::BZ : 0;
+                return GBNS_OK;
+            }
+        };
     }
 
 #define GBNS_BRUN(CONV, ORDER, STRETCH, TX, TY, TZ, NT) \
-    return run_batch<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>(items, offsets, counts, insts, ytabs, left, cls, stage, nitems, st)
+    return act.template run<FluxCfg<GBNS_REAL, CONV, ORDER, STRETCH, TX, TY, TZ, NT, GBNS_TAG, GBNS_FP32>>()
 
+    namespace
+    {
     // The tile variants of each class (their shapes are listed by
     // batch_class_tile in batch.cu, in the same order); a new batch starts
     // on variant 0 in FP32-flux and on variant 2 (576 threads) in FP64.
-    int GBNS_BATCH_FN(int cls, int v, const TileItem* items, const int* offsets, const int* counts,
-                      const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems,
-                      cudaStream_t st)
+    // Runs the action with the variant's tile configuration.
+    template <class Act>
+    int batch_dispatch(int cls, int v, const Act& act)
     {
 #if GBNS_BATCH_GROUP == 0
         switch (cls)
@@ -187,5 +218,19 @@ namespace gbns
         }
 #endif
         return set_error(GBNS_ERR_UNSUPPORTED, "no batched kernel for this class");
+    }
+    }
+#undef GBNS_BRUN
+
+    int GBNS_BATCH_FN(int cls, int v, const TileItem* items, const int* offsets, const int* counts,
+                      const InstK* insts, const YTabK* ytabs, const long long* left, const CUtensorMap* tmaps,
+                      int stage, int nitems, cudaStream_t st)
+    {
+        return batch_dispatch(cls, v, LaunchAction{items, offsets, counts, insts, ytabs, left, tmaps, cls, stage, nitems, st});
+    }
+
+    int GBNS_BATCH_BOX_FN(int cls, int v, int box[3])
+    {
+        return batch_dispatch(cls, v, BoxAction{box});
     }
 }

@@ -4,4 +4,5 @@
 #define GBNS_FP32 1
 #define GBNS_BATCH_GROUP 1
 #define GBNS_BATCH_FN launch_flux_batch_f32_b
+#define GBNS_BATCH_BOX_FN launch_flux_batch_f32_b_box
 #include "batch_flux.cuh"

@@ -4,4 +4,5 @@
 #define GBNS_FP32 0
 #define GBNS_BATCH_GROUP 0
 #define GBNS_BATCH_FN launch_flux_batch_f64x_a
+#define GBNS_BATCH_BOX_FN launch_flux_batch_f64x_a_box
 #include "batch_flux.cuh"

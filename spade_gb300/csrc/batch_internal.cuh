@@ -63,9 +63,15 @@ namespace gbns
     // totani_lr, fweno_t; b: WENO5; c: hybrid).  `left` (device, one per
     // slot): steps an instance still has to do before it idles (-1: no
     // limit); items of instances at 0 are skipped.
+    // `tmaps` (device, two per slot: q and R[2]; may be NULL): tensor maps
+    // the FP64 tiles stage their box from, for the items whose `pad` is set.
+    // The *_box functions give a variant's TMA box (cells along x, y, z; zeros
+    // when the variant stages no FP64 box by TMA), which the maps must use.
 #define GBNS_BATCH_DECL(NAME) \
     int NAME(int cls, int v, const TileItem* items, const int* offsets, const int* counts, \
-             const InstK* insts, const YTabK* ytabs, const long long* left, int stage, int nitems, cudaStream_t st);
+             const InstK* insts, const YTabK* ytabs, const long long* left, const CUtensorMap* tmaps, \
+             int stage, int nitems, cudaStream_t st); \
+    int NAME##_box(int cls, int v, int box[3]);
     GBNS_BATCH_DECL(launch_flux_batch_f64x_a)
     GBNS_BATCH_DECL(launch_flux_batch_f64x_b)
     GBNS_BATCH_DECL(launch_flux_batch_f64x_c)

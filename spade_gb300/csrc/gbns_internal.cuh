@@ -242,6 +242,14 @@ namespace gbns
             : "memory");
     }
 
+    // A tensor map that a host copy wrote to global memory, made visible to
+    // the tensor proxy (the TMA unit) before this thread's first copy with it.
+    __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map)
+    {
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;"
+                     :: "l"(reinterpret_cast<uint64_t>(map)) : "memory");
+    }
+
     constexpr long long MBAR_WAIT_CYCLES = 2000000000ll;   // ~1 s at 2 GHz
 
     // fluid_state::convert_state prim -> cons and cons -> prim
