@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=200)
     p.add_argument("--serve-time-limit", type=float, default=30.0,
                    help="seconds each precision serves the configured stream")
+    p.add_argument("--batch-only", action="store_true",
+                   help="instead of the bench line: run only the batched form (--batch-instances, --batch-steps) "
+                        "and print its block")
     p.add_argument("--flux-variants", choices=["taylor_green", "channel", "channel_fweno"], default=None,
                    help="instead of the bench line: time one plain flux_div launch of every tile variant on the named "
                         "workload (--nblk blocks of --ncell cells; --precision) and print the times; with --steps 1 it "
@@ -753,6 +756,10 @@ def main():
     if args.flux_variants:
         if rank == 0:
             run_flux_variants(args)
+        return
+    if args.batch_only:
+        if rank == 0:
+            print(json.dumps({"batch_form": run_batch_form(args)}))
         return
     if args.reference_gpu_only:
         if rank == 0:
