@@ -420,9 +420,9 @@ def run_batch_form(args):
         probs.append(workloads.taylor_green(nblk=nb, ncell=(16, 16, 16), ng=2, mach=ma, reynolds=re, seed=i, rng="torch",
                                             p_factor=1.0 / 16.0))
     cells = sum(p.grid.get_grid_size() for p in probs)
-    out = {"workload": "96 Taylor-Green instances (textbook pressure field), 16^3 blocks, blocks per instance from "
-                       "{1,...,64}, Re log-uniform [100,3000], Mach uniform [0.05,0.4]", "instances": len(probs), "cells": cells,
-           "steps": args.batch_steps}
+    out = {"workload": "%d Taylor-Green instances (textbook pressure field), 16^3 blocks, blocks per instance from "
+                       "{1,...,64}, Re log-uniform [100,3000], Mach uniform [0.05,0.4]" % len(probs),
+           "instances": len(probs), "cells": cells, "steps": args.batch_steps}
     for name, prec in (("fp64", _abi.PREC_FP64), ("fp32_flux", _abi.PREC_FP32_FLUX)):
         budget = sum(batch_t.instance_bytes(p.q.desc()) for p in probs) + (256 << 20)
         b = batch_t(budget, prec, True)

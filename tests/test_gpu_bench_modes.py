@@ -1,7 +1,8 @@
-"""bench.py's side modes on a small grid: `--flux-variants` (one plain
+"""bench.py's side modes on small inputs: `--flux-variants` (one plain
 flux_div per tile variant, the launch sequence the ncu summaries capture)
 prints one JSON line with a time and a rate for every variant the library
-reports, for each workload and both precisions."""
+reports, for each workload and both precisions; `--batch-only` prints the
+batched form's block."""
 import json
 import os
 import subprocess
@@ -26,3 +27,16 @@ def test_flux_variants_mode(workload, precision):
     times = line["ms_per_variant"]
     assert len(times) >= 2 and all(t > 0 for t in times.values())
     assert str(line["best"]) in times
+
+
+def test_batch_only_mode():
+    """`--batch-only` prints the batched form's block: both precisions, the
+    autotuned variant per class and a positive rate."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--batch-only", "--batch-instances", "4", "--batch-steps", "2"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    block = json.loads(r.stdout.strip().splitlines()[-1])["batch_form"]
+    assert block["instances"] == 4 and block["steps"] == 2
+    for prec in ("fp64", "fp32_flux"):
+        assert block[prec]["cell_steps_per_s"] > 0
+        assert all(t["variant"] >= 0 for t in block[prec]["autotuned"].values())
