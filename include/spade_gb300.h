@@ -46,6 +46,14 @@
  * runs gbns_boundary_flux (the overload below is more specialised than the
  * reference's variadic template, pde-algs/boundary_flux.h:10-20).
  *
+ * Ghost fill and time integration: spade::gb300::fill_ghosts(q, periodic,
+ * walls, wall) stands for the exchange + boundary_fill pair the reference's
+ * drivers call (one launch, gbns_fill_ghosts), with the wall kernel
+ * spade::gb300::isothermal_wall_t or slip_wall_t (also usable as the
+ * reference's own boundary_fill kernel); spade::gb300::ssprk3_integrator_t
+ * is integrator_t with ssprk3_t, flux_div of the lowered functor and that
+ * ghost fill, fused (advance() is gbns_ssprk3_step).
+ *
  * Define GBNS_DROPIN_HOOK before including to route the lowered call to a
  * user function `int GBNS_DROPIN_HOOK(const gbns_grid_desc*, const
  * gbns_scheme_desc*, const double*, double*, int)` instead of the library
@@ -53,7 +61,9 @@
  * `int (const gbns_grid_desc*, const gbns_source_desc*, const double*, double*)`,
  * does the same for source_term, and GBNS_DROPIN_BFLUX_HOOK, `int (const
  * gbns_grid_desc*, const gbns_scheme_desc*, const double*, double*, const int*)`,
- * for boundary_flux.
+ * for boundary_flux, and GBNS_DROPIN_BC_HOOK, `int (const gbns_grid_desc*,
+ * const gbns_bc_desc*, const gbns_scheme_desc*, double*, double dt)`, for the
+ * ghost fill (scheme NULL) and the SSPRK3 integrator's step.
  */
 #pragma once
 
@@ -766,4 +776,169 @@ namespace spade::pde_algs
             throw except::sp_exception(std::string("gb300 boundary_flux failed: ") + msg);
         }
     }
+}
+
+namespace spade::gb300
+{
+    // Wall kernels for the domain-boundary ghost fill.  Each is also the
+    // reference's boundary_fill kernel form (ghost = kern(domain value, dir),
+    // grid/boundary_fill.h:31-133), so the same object serves a CPU
+    // spade::algs::boundary_fill and the gb300 fill below:
+    //   isothermal_wall_t: no-slip, T_ghost = 2 T_wall - T, u, v, w negated;
+    //   slip_wall_t:       adiabatic slip, the wall-normal velocity negated.
+    template <typename dtype>
+    struct isothermal_wall_t
+    {
+        using value_type = dtype;
+        dtype t_wall;
+        template <typename state_t> state_t operator()(const state_t& q, const int) const
+        {
+            state_t g = q;
+            g.T() = dtype(2.0)*t_wall - q.T();
+            g.u() = -q.u();
+            g.v() = -q.v();
+            g.w() = -q.w();
+            return g;
+        }
+    };
+    template <typename dtype>
+    struct slip_wall_t
+    {
+        using value_type = dtype;
+        template <typename state_t> state_t operator()(const state_t& q, const int dir) const
+        {
+            state_t g = q;
+            g.u(dir) = -q.u(dir);
+            return g;
+        }
+    };
+
+    template <typename T> struct is_wall_kernel : std::false_type {};
+    template <typename dtype> struct is_wall_kernel<isothermal_wall_t<dtype>> : std::true_type {};
+    template <typename dtype> struct is_wall_kernel<slip_wall_t<dtype>> : std::true_type {};
+    template <typename T> concept lowered_wall = is_wall_kernel<T>::value;
+
+    // The boundary descriptor of one ghost fill: per face min(0), max(0), ...,
+    // max(2): a wall where `walls` selects it, periodic where `periodic`
+    // does (the flags the reference passes to make_exchange), else left alone.
+    template <typename wall_t>
+    requires lowered_wall<wall_t>
+    gbns_bc_desc lower_bc(const ctrs::array<bool, 3>& periodic, const bound_box_t<bool, 3>& walls, const wall_t& wall)
+    {
+        gbns_bc_desc bc{};
+        for (int d = 0; d < 3; ++d)
+            for (int pm = 0; pm < 2; ++pm)
+            {
+                const int f = 2*d + pm;
+                const bool is_wall = pm == 0 ? walls.min(d) : walls.max(d);
+                if (is_wall && periodic[d])
+                    throw except::sp_exception("gb300 ghost fill: a face cannot be both periodic and a wall");
+                if (is_wall)
+                {
+                    if constexpr (std::same_as<wall_t, slip_wall_t<typename wall_t::value_type>>) bc.kind[f] = GBNS_BC_SLIP_ADIABATIC;
+                    else
+                    {
+                        bc.kind[f] = GBNS_BC_ISOTHERMAL_NOSLIP;
+                        bc.t_wall[f] = double(wall.t_wall);
+                    }
+                }
+                else bc.kind[f] = periodic[d] ? GBNS_BC_PERIODIC : GBNS_BC_NONE;
+            }
+        return bc;
+    }
+
+    namespace detail
+    {
+        inline void check_call(int rc, const char* what)
+        {
+            if (rc == GBNS_OK) return;
+            char msg[512] = "drop-in hook failed";
+#ifndef GBNS_DROPIN_BC_HOOK
+            gbns_last_error(msg, sizeof(msg));
+#endif
+            throw except::sp_exception(std::string(what) + msg);
+        }
+    }
+
+    // Every ghost layer of a device::gpu grid_array in one launch: the
+    // reference's `make_exchange(q, periodic)` handle's exchange followed by
+    // `algs::boundary_fill(q, walls, wall)` (grid/make_exchange.h:98-421,
+    // grid/boundary_fill.h:31-133), the pair its drivers call after each
+    // stage; each ghost resolved to an interior donor, bit-identical to that
+    // pair (gbns_fill_ghosts).
+    template <grid::multiblock_array arr_t, typename wall_t>
+    requires lowered_wall<wall_t> && grid::has_centering_type<arr_t, grid::cell_centered>
+    void fill_ghosts(arr_t& q, const ctrs::array<bool, 3>& periodic, const bound_box_t<bool, 3>& walls, const wall_t& wall)
+    {
+        const gbns_grid_desc g = lower_grid(q);
+        const gbns_bc_desc bc = lower_bc(periodic, walls, wall);
+        double* p = q.image().base;
+#ifdef GBNS_DROPIN_BC_HOOK
+        const int rc = GBNS_DROPIN_BC_HOOK(&g, &bc, nullptr, p, 0.0);
+#else
+        static_assert(device::is_gpu<typename arr_t::device_type>, "the gb300 ghost fill runs on device::gpu arrays");
+        int rc = gbns_fill_ghosts(&g, &bc, p, nullptr);
+        if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+#endif
+        detail::check_call(rc, "gb300 fill_ghosts failed: ");
+    }
+
+    // The reference's time integration of these flows, fused:
+    // integrator_t with ssprk3_t and state_transform_t
+    // (time-integration/integrator.h:18-59, advance.h:234-280, explicit.h:80-88)
+    // whose rhs_calc is flux_div of `flux` and whose boundary_cond is the
+    // exchange + boundary_fill pair above.  advance() is gbns_ssprk3_step:
+    // three launches of flux_div with the stage update fused in, three ghost
+    // fills, bit-identical to the reference in FP64.  The stepper owns the
+    // scratch (two residuals and the intermediate state, 3 arrays of q's size).
+    template <grid::multiblock_array arr_t, typename flux_func_t, typename wall_t>
+    requires lowered_wall<wall_t> && grid::has_centering_type<arr_t, grid::cell_centered>
+    struct ssprk3_integrator_t
+    {
+        arr_t& q;
+        gbns_grid_desc grid;
+        gbns_scheme_desc scheme;
+        gbns_bc_desc bc;
+        double dt;
+        double t;
+        double* work = nullptr;
+
+        ssprk3_integrator_t(arr_t& q_in, const flux_func_t& flux, const ctrs::array<bool, 3>& periodic,
+                            const bound_box_t<bool, 3>& walls, const wall_t& wall, double dt_in, double t0 = 0.0,
+                            int precision = GBNS_PREC_FP64)
+            : q{q_in}, grid{lower_grid(q_in)}, scheme{lower_scheme(flux, precision)},
+              bc{lower_bc(periodic, walls, wall)}, dt{dt_in}, t{t0}
+        {
+#ifndef GBNS_DROPIN_BC_HOOK
+            static_assert(device::is_gpu<typename arr_t::device_type>, "the gb300 integrator runs on device::gpu arrays");
+            size_t n = 0;
+            if (gbns_array_size(&grid, &n) != GBNS_OK || cudaMalloc(&work, 3*n*sizeof(double)) != cudaSuccess)
+                throw except::sp_exception("gb300 integrator: cannot allocate its scratch arrays");
+#endif
+        }
+        ssprk3_integrator_t(const ssprk3_integrator_t&) = delete;
+        ssprk3_integrator_t& operator=(const ssprk3_integrator_t&) = delete;
+        ~ssprk3_integrator_t()
+        {
+#ifndef GBNS_DROPIN_BC_HOOK
+            if (work) cudaFree(work);
+#endif
+        }
+
+        void advance()
+        {
+            double* p = q.image().base;
+#ifdef GBNS_DROPIN_BC_HOOK
+            const int rc = GBNS_DROPIN_BC_HOOK(&grid, &bc, &scheme, p, dt);
+#else
+            int rc = gbns_ssprk3_step(&grid, &scheme, &bc, p, work, dt, nullptr);
+            if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+#endif
+            detail::check_call(rc, "gb300 ssprk3 step failed: ");
+            t += dt;
+        }
+
+        arr_t& solution() { return q; }
+        double time() const { return t; }
+    };
 }

@@ -42,6 +42,17 @@ static int record_bflux(const gbns_grid_desc* g, const gbns_scheme_desc* s, cons
 }
 #define GBNS_DROPIN_BFLUX_HOOK record_bflux
 
+static int g_bc_calls = 0;
+static int record_bc(const gbns_grid_desc* g, const gbns_bc_desc* bc, const gbns_scheme_desc* s, double* q, double dt)
+{
+    ++g_bc_calls;
+    std::printf("bc %d %d %d %d %d %d tw %.17g %.17g step %d conv %d dt %.17g ng %d ptr %d\n", bc->kind[0], bc->kind[1],
+                bc->kind[2], bc->kind[3], bc->kind[4], bc->kind[5], bc->t_wall[2], bc->t_wall[3], int(s != nullptr),
+                s ? s->convective : -1, dt, g->ng, int(q != nullptr));
+    return 0;
+}
+#define GBNS_DROPIN_BC_HOOK record_bc
+
 #include "spade.h"
 #include "spade_gb300.h"
 
@@ -113,7 +124,39 @@ int main(int argc, char** argv)
         spade::grid::grid_array iq  (igrid, spade::fluid_state::prim_t<real_t>(0.0), nexch, spade::device::cpu);
         spade::grid::grid_array irhs(igrid, spade::fluid_state::flux_t<real_t>(0.0), nexch, spade::device::cpu);
         spade::pde_algs::flux_div(iq, irhs, channel_flux, spade::algs::make_traits(spade::pde_algs::gb300));
+        // 11, 12: the channel's ghost fill (periodic x and z, isothermal walls
+        // in y) and its fused SSPRK3 integrator on the stretched grid
+        const spade::ctrs::array<bool, 3> periodic(true, false, true);
+        spade::bound_box_t<bool, 3> ywalls = false;
+        ywalls.min(1) = true;
+        ywalls.max(1) = true;
+        const spade::gb300::isothermal_wall_t<real_t> wall{300.0};
+        spade::gb300::fill_ghosts(sq, periodic, ywalls, wall);
+        spade::gb300::ssprk3_integrator_t step(sq, channel_flux, periodic, ywalls, wall, 2.5e-4);
+        step.advance();
+        step.advance();
+        std::printf("integrator t %.17g\n", step.time());
+        // 13: a slip wall on z-min only
+        spade::bound_box_t<bool, 3> zwall = false;
+        zwall.min(2) = true;
+        spade::gb300::fill_ghosts(q, spade::ctrs::array<bool, 3>(true, true, false), zwall, spade::gb300::slip_wall_t<real_t>{});
+        // the same wall kernel through the reference's own CPU boundary_fill:
+        // a ghost below y-min takes T = 2 T_wall - T and negated velocities
+        spade::fluid_state::prim_t<real_t> inside;
+        inside.p() = 1.0e5; inside.T() = 310.0; inside.u() = 2.0; inside.v() = -1.0; inside.w() = 0.5;
+        spade::grid::cartesian_blocks_t wblocks(spade::ctrs::array<int, 3>(1, 1, 1), bounds);
+        spade::grid::cartesian_grid_t wgrid(spade::ctrs::array<int, 3>(4, 4, 4), wblocks, coords, group);
+        // (the reference's fill_array tiles the padded range in fours: 4 + 2*2 cells)
+        spade::grid::grid_array wq(wgrid, spade::fluid_state::prim_t<real_t>(0.0), spade::ctrs::array<int, 3>(2, 2, 2),
+                                   spade::device::cpu);
+        using point_t = spade::coords::point_t<real_t>;
+        spade::algs::fill_array(wq, [=](const point_t&) { return inside; });
+        spade::algs::boundary_fill(wq, spade::boundary::ymin, wall);
+        const auto img = wq.image();
+        spade::grid::cell_idx_t gi(0, -1, 0, 0);
+        const auto ghost = img.get_elem(gi);
+        std::printf("cpu_wall %.17g %.17g %.17g %.17g %.17g\n", ghost.p(), ghost.T(), ghost.u(), ghost.v(), ghost.w());
     });
-    std::printf("calls %d sources %d bflux %d\n", g_calls, g_src_calls, g_bf_calls);
-    return (g_calls == 7 && g_src_calls == 2 && g_bf_calls == 1) ? 0 : 1;
+    std::printf("calls %d sources %d bflux %d bc %d\n", g_calls, g_src_calls, g_bf_calls, g_bc_calls);
+    return (g_calls == 7 && g_src_calls == 2 && g_bf_calls == 1 && g_bc_calls == 4) ? 0 : 1;
 }

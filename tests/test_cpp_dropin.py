@@ -1,7 +1,9 @@
 """The C++ drop-in header (include/spade_gb300.h) compiled against the
 reference's own headers: the gb300 trait selects the GB300 overload of
 spade::pde_algs::flux_div and the functor / grid lowering produces the
-expected C-ABI descriptors.  Host only (the GPU call goes to a hook); runs
+expected C-ABI descriptors; the ghost fill and the fused SSPRK3 integrator
+lower the periodic flags and wall kernels, and the wall kernels also work as
+the kernel of the reference's own CPU boundary_fill.  Host only (the GPU call goes to a hook); runs
 only where the reference sources exist."""
 import os
 import subprocess
@@ -79,6 +81,22 @@ def test_dropin_overload_and_lowering():
     assert bf[0][1:7] == ["0", "0", "1", "1", "0", "0"]
     assert bf[0][bf[0].index("conv") + 1] == "1" and bf[0][bf[0].index("order") + 1] == "4"
     assert bf[0][bf[0].index("visc") + 1] == "1" and bf[0][bf[0].index("ng") + 1] == "3"
+    # ghost fill and fused SSPRK3 integrator: periodic x/z, isothermal walls
+    # (300 K) in y; then a slip wall on z-min only, x and y periodic
+    bcs = [l.split() for l in lines if l.startswith("bc")]
+    assert len(bcs) == 4
+    assert bcs[0][1:7] == ["0", "0", "2", "2", "0", "0"] and [float(x) for x in bcs[0][8:10]] == [300.0, 300.0]
+    assert bcs[0][bcs[0].index("step") + 1] == "0"
+    for b in bcs[1:3]:
+        assert b[1:7] == bcs[0][1:7] and b[b.index("step") + 1] == "1" and b[b.index("conv") + 1] == "4"
+        assert float(b[b.index("dt") + 1]) == 2.5e-4
+    assert bcs[3][1:7] == ["0", "0", "0", "0", "3", "1"]
+    t = [l.split() for l in lines if l.startswith("integrator")][0]
+    assert float(t[2]) == 5e-4
+    # the wall kernel through the reference's own CPU boundary_fill: the
+    # ghost below y-min of a uniform (1e5, 310, 2, -1, 0.5) state
+    w = [l.split() for l in lines if l.startswith("cpu_wall")][0]
+    assert [float(x) for x in w[1:6]] == [1.0e5, 290.0, -2.0, 1.0, -0.5]
 
 
 @pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
@@ -90,6 +108,20 @@ def test_dropin_host_array_path_compiles():
            os.path.join(ROOT, "tests", "cpp", "dropin_host_arrays.cc")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
+def test_dropin_gpu_array_path_compiles():
+    """Without the test hooks, the gb300 flux_div overload, the ghost fill
+    and the fused SSPRK3 integrator instantiate for device::gpu grid_arrays
+    under nvcc with the reference's CUDA build options (compile only)."""
+    with tempfile.TemporaryDirectory() as d:
+        cmd = ["nvcc", "-x", "cu", "-std=c++20", "--extended-lambda", "--expt-relaxed-constexpr", "-w",
+               "-gencode", "arch=compute_103a,code=sm_103a", "-I" + REF_SRC, "-I" + os.path.join(ROOT, "include"),
+               "-I" + os.path.join(ROOT, "oracle", "mpi_stub"), "-c",
+               os.path.join(ROOT, "tests", "cpp", "dropin_gpu_arrays.cu"), "-o", os.path.join(d, "dropin_gpu.o")]
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=1200)
+        assert r.returncode == 0, r.stderr[-3000:]
 
 
 def test_recorded_dropin_calls_reproduce_the_reference_on_the_oracle():
