@@ -735,7 +735,11 @@ namespace gbns
         const Weno5Side u = weno5_nd<IM>(ua, ub, uc, ud, ue);
         const Weno5Side d = weno5_nd<IM>(da, db, dc, dd, de);
         const double den = wmul<IM>(6.0, wmul<IM>(u.D, d.D));
-        if (den < 1.0e300)
+        // den < 1e300 as an unsigned compare of the bits (den is +0, positive,
+        // +inf or a NaN here: a product of 6 and two sums of non-negative
+        // weights; NaNs of either sign compare false as before), which keeps
+        // the test off the FP64 unit
+        if ((unsigned long long)__double_as_longlong(den) < 0x7E37E43C8800759Cull)
             return pdiv<IM>(fma(u.N, d.D, wmul<IM>(d.N, u.D)), den);
         return pdiv<IM>(u.N, 6.0*u.D) + pdiv<IM>(d.N, 6.0*d.D);
     }
