@@ -349,6 +349,11 @@ int gbns_exchange_plan_create(gbns_exchange_plan** plan, int nx, int ny, int nz,
  * one interpolation wave when no donor is a ghost cell), asynchronous on
  * `stream`. */
 int gbns_exchange_plan_run(gbns_exchange_plan* plan, double* prims, void* stream);
+/* The wave of each transaction that gbns_exchange_plan_create would run it in
+ * (injection waves, then interpolation waves, each wave one launch), after the
+ * same validation; host only, no CUDA call.  waves: npatch ints. */
+int gbns_exchange_plan_waves(int nx, int ny, int nz, int ng, int nblocks, const gbns_patch* patches, int npatch,
+                             int* waves);
 int gbns_exchange_plan_destroy(gbns_exchange_plan* plan);
 
 /* dst = src on interior cells, dst's ghost layers filled from src's interior

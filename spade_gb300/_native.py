@@ -38,6 +38,8 @@ def lib():
     L.gbns_exchange_plan_create.argtypes = [P(vp), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                             vp, ctypes.c_int, vp]
     L.gbns_exchange_plan_run.argtypes = [vp, vp, vp]
+    L.gbns_exchange_plan_waves.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, vp,
+                                           ctypes.c_int, vp]
     L.gbns_exchange_plan_destroy.argtypes = [vp]
     L.gbns_rk_stage.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, vp, vp, ctypes.c_int, vp]
     L.gbns_reduce.argtypes = [P(_abi.GridDesc), P(_abi.GasDesc), vp, ctypes.c_int, vp, vp]

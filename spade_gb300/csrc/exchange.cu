@@ -225,6 +225,34 @@ namespace
         }
         return 0;
     }
+
+    // Validates a plan and assigns every patch its wave (host only).
+    int plan_waves(gbns_exchange_plan& P, int nx, int ny, int nz, int ng, int nblocks, const gbns_patch* patches,
+                   int npatch, std::vector<int>& wave)
+    {
+        if (npatch > 0 && !patches) return set_error(GBNS_ERR_INVALID, "NULL argument");
+        if (nx < 1 || ny < 1 || nz < 1 || ng < 1 || ng > 8 || nblocks < 1 || npatch < 0)
+            return set_error(GBNS_ERR_INVALID, "exchange plan: bad block shape, ghost depth or counts");
+        P.nx = nx; P.ny = ny; P.nz = nz; P.nblocks = nblocks;
+        P.G.ng = ng;
+        P.G.ni = nx + 2*ng; P.G.nj = ny + 2*ng; P.G.nk = nz + 2*ng;
+        P.G.bstride = 5ll*P.G.ni*P.G.nj*P.G.nk;
+        std::vector<int> writer(size_t(nblocks)*P.G.ni*P.G.nj*P.G.nk, -1);
+        for (int i = 0; i < npatch; ++i)
+        {
+            std::string why;
+            if (validate_patch(P, patches[i], i, writer, why))
+                return set_error(GBNS_ERR_INVALID, "exchange plan, patch " + std::to_string(i) + ": " + why);
+        }
+        wave.assign(npatch, 0);
+        for (int kind : {GBNS_PATCH_INJECT, GBNS_PATCH_INTERP})
+        {
+            std::string why;
+            if (assign_waves(P, patches, npatch, kind, writer, wave, why))
+                return set_error(GBNS_ERR_UNSUPPORTED, "exchange plan: " + why);
+        }
+        return GBNS_OK;
+    }
 }
 
 extern "C"
@@ -233,33 +261,10 @@ extern "C"
                                   const gbns_patch* patches, int npatch, void* stream)
     {
         if (!out || (npatch > 0 && !patches)) return set_error(GBNS_ERR_INVALID, "NULL argument");
-        if (nx < 1 || ny < 1 || nz < 1 || ng < 1 || ng > 8 || nblocks < 1 || npatch < 0)
-            return set_error(GBNS_ERR_INVALID, "exchange plan: bad block shape, ghost depth or counts");
         auto* P = new gbns_exchange_plan();
-        P->nx = nx; P->ny = ny; P->nz = nz; P->nblocks = nblocks;
-        P->G.ng = ng;
-        P->G.ni = nx + 2*ng; P->G.nj = ny + 2*ng; P->G.nk = nz + 2*ng;
-        P->G.bstride = 5ll*P->G.ni*P->G.nj*P->G.nk;
-        std::vector<int> writer(size_t(nblocks)*P->G.ni*P->G.nj*P->G.nk, -1);
-        for (int i = 0; i < npatch; ++i)
-        {
-            std::string why;
-            if (validate_patch(*P, patches[i], i, writer, why))
-            {
-                delete P;
-                return set_error(GBNS_ERR_INVALID, "exchange plan, patch " + std::to_string(i) + ": " + why);
-            }
-        }
-        std::vector<int> wave(npatch, 0);
-        for (int kind : {GBNS_PATCH_INJECT, GBNS_PATCH_INTERP})
-        {
-            std::string why;
-            if (assign_waves(*P, patches, npatch, kind, writer, wave, why))
-            {
-                delete P;
-                return set_error(GBNS_ERR_UNSUPPORTED, "exchange plan: " + why);
-            }
-        }
+        std::vector<int> wave;
+        int rc = plan_waves(*P, nx, ny, nz, ng, nblocks, patches, npatch, wave);
+        if (rc) { delete P; return rc; }
         // injection waves, then interpolation waves; plan order within a wave
         std::vector<int> order(npatch);
         for (int i = 0; i < npatch; ++i) order[i] = i;
@@ -303,7 +308,7 @@ extern "C"
         if (!P->waves.empty()) first.push_back(P->waves.back().cells);
         if (first.empty()) first.push_back(0);
         cudaStream_t st = static_cast<cudaStream_t>(stream);
-        int rc = check_cuda(cudaMalloc(&P->d_patches, sizeof(PatchK)*(all.size() ? all.size() : 1)), "exchange plan");
+        rc = check_cuda(cudaMalloc(&P->d_patches, sizeof(PatchK)*(all.size() ? all.size() : 1)), "exchange plan");
         if (!rc) rc = check_cuda(cudaMalloc(&P->d_first, sizeof(long long)*first.size()), "exchange plan offsets");
         if (!rc && !all.empty())
             rc = check_cuda(cudaMemcpyAsync(P->d_patches, all.data(), sizeof(PatchK)*all.size(), cudaMemcpyHostToDevice, st),
@@ -319,6 +324,18 @@ extern "C"
             return rc;
         }
         *out = P;
+        return GBNS_OK;
+    }
+
+    int gbns_exchange_plan_waves(int nx, int ny, int nz, int ng, int nblocks, const gbns_patch* patches, int npatch,
+                                 int* waves)
+    {
+        if (!waves && npatch > 0) return set_error(GBNS_ERR_INVALID, "NULL argument");
+        gbns_exchange_plan P;
+        std::vector<int> wave;
+        const int rc = plan_waves(P, nx, ny, nz, ng, nblocks, patches, npatch, wave);
+        if (rc) return rc;
+        for (int i = 0; i < npatch; ++i) waves[i] = wave[i];
         return GBNS_OK;
     }
 

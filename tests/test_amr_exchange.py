@@ -123,3 +123,64 @@ def test_plan_validation_rejects_malformed_plans():
     bad[0, 1] = 99                                                  # block index out of range
     assert _create(bad) == _abi.ERR_INVALID
     assert _create(plan, ng=0) == _abi.ERR_INVALID
+
+
+def _waves(g):
+    plan = np.ascontiguousarray(g["plan"], dtype=np.int32)
+    waves = np.zeros(plan.shape[0], dtype=np.int32)
+    nc, ng = g["ncell"], int(g["ng"])
+    rc = _native.lib().gbns_exchange_plan_waves(int(nc[0]), int(nc[1]), int(nc[2]), ng, int(g["boxes"].shape[0]),
+                                                ctypes.c_void_p(plan.ctypes.data), int(plan.shape[0]),
+                                                ctypes.c_void_p(waves.ctypes.data))
+    assert rc == _abi.OK
+    return plan, waves
+
+
+def _run_in_waves(g, plan, waves, q):
+    """Executes the plan wave by wave, every transaction of a wave reading
+    before any of them writes (what one launch per wave guarantees)."""
+    ng = int(g["ng"])
+    for kind in (0, 1):
+        for w in sorted(set(int(x) for x, r in zip(waves, plan) if r[0] == kind)):
+            pending = []
+            for r, wr in zip(plan, waves):
+                if r[0] != kind or wr != w:
+                    continue
+                sb, db, slo, dlo, dhi, c, inc = r[1], r[2], r[3:6], r[6:9], r[9:12], r[12:15], r[15:18]
+                for dk in range(dhi[2] - dlo[2]):
+                    for dj in range(dhi[1] - dlo[1]):
+                        for di in range(dhi[0] - dlo[0]):
+                            if kind == 0:
+                                v = q[sb, slo[2] + dk + ng, slo[1] + dj + ng, slo[0] + di + ng].copy()
+                            else:
+                                b = [(d << (cc + 1)) >> 1 for d, cc in zip((di, dj, dk), c)]
+                                acc = np.zeros(5)
+                                for iv in range(8):
+                                    ii = slo[0] + b[0] + (iv & 1) * inc[0]
+                                    jj = slo[1] + b[1] + ((iv >> 1) & 1) * inc[1]
+                                    kk = slo[2] + b[2] + ((iv >> 2) & 1) * inc[2]
+                                    acc = acc + q[sb, kk + ng, jj + ng, ii + ng]
+                                v = acc * 0.125
+                            pending.append(((db, dlo[2] + dk + ng, dlo[1] + dj + ng, dlo[0] + di + ng), v))
+            for idx, v in pending:
+                q[idx] = v
+
+
+def test_plan_waves_reproduce_the_reference_order():
+    """gbns_exchange_plan_waves (the launches gbns_exchange_plan_create would
+    issue, host only): executing each wave as one gather (all reads before
+    any write) reproduces the reference's transaction-by-transaction exchange
+    bit for bit.  With y walls some interpolation donors are ghost cells
+    other interpolations write: one injection wave and three interpolation
+    waves; without such donors one of each."""
+    for case in CASES:
+        g = golden(case)
+        plan, waves = _waves(g)
+        q = amr_fill(g["boxes"], g["ncell"], int(g["ng"]))
+        _run_in_waves(g, plan, waves, q)
+        assert np.array_equal(q, g["after"]), case
+        nw = {k: len(set(int(w) for w, r in zip(waves, plan) if r[0] == k)) for k in (0, 1)}
+        if case == "two_levels_walls_y":
+            assert nw == {0: 1, 1: 3}
+        else:
+            assert nw[0] <= 1 and nw[1] <= 1
