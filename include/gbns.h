@@ -178,6 +178,22 @@ int gbns_array_size(const gbns_grid_desc* grid, size_t* count);
 int gbns_flux_div(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                   const double* prims, double* rhs, int increment, void* stream);
 
+/* gbns_flux_div on a refined (AMR) block layout: grid->nblk = (blocks, 1, 1)
+ * (1..65535 blocks, each of grid->ncell cells and grid->ng ghost layers, in
+ * the caller's global block order), identity coordinates (grid->bounds is
+ * not used), and block_bounds (host memory, 6 doubles per block: min and max
+ * along x, y, z) each block's bounding box.  Every block takes
+ * inv_dx[d] = 1.0/((max_d - min_d)/ncell[d]), as the reference's flux_div
+ * does from its own box (flux_div_basic.h:55, grid/grid_geometry.h:85-89) on
+ * grids refined with cartesian_grid_t::refine_blocks
+ * (grid/cartesian_grid.h:331-367).  prims carries the ghost values the
+ * coarse/fine exchange wrote (gbns_exchange_plan).  The per-block table is
+ * copied to stream-ordered device memory of the library's pool on `stream`
+ * (from pageable memory: not for stream capture).  Asynchronous on
+ * `stream`.  Stretched coordinates: GBNS_ERR_UNSUPPORTED. */
+int gbns_flux_div_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                         const double* prims, double* rhs, int increment, void* stream);
+
 /* gbns_flux_div for prims and rhs in host memory (a grid_array on
  * device::cpu): both arrays are staged through device buffers the library
  * keeps per device and reuses across calls, the flux divergence runs on the

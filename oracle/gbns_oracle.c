@@ -49,6 +49,7 @@ typedef struct
     int coords;
     double bounds[6];
     double cp[4];
+    const double* boxes;    /* refined layouts: per block min/max per direction (6 doubles), else NULL */
 } geom_t;
 
 static int geom_init(const gbns_grid_desc* g, geom_t* G)
@@ -69,6 +70,7 @@ static int geom_init(const gbns_grid_desc* g, geom_t* G)
     G->coords = g->coords;
     for (int i = 0; i < 6; ++i) G->bounds[i] = g->bounds[i];
     for (int i = 0; i < 4; ++i) G->cp[i] = g->coord_param[i];
+    G->boxes = NULL;
     return 0;
 }
 
@@ -84,9 +86,21 @@ static inline void block_pos(const geom_t* G, int lb, int b[3])
     b[2] = lb / (G->nb[0]*G->nb[1]);
 }
 
-/* cartesian_blocks.h:49,69-70 and cartesian_grid.h:130-136 / grid_geometry.h:85-89 */
+/* cartesian_blocks.h:49,69-70 and cartesian_grid.h:130-136 / grid_geometry.h:85-89;
+ * a refined layout's block takes its own bounding box (grid_geometry.h:85-89:
+ * dx = box size / cells) */
 static void block_box(const geom_t* G, int lb, double bmin[3], double dx[3])
 {
+    if (G->boxes)
+    {
+        for (int d = 0; d < 3; ++d)
+        {
+            const double mn = G->boxes[6*lb + 2*d], mx = G->boxes[6*lb + 2*d + 1];
+            bmin[d] = mn;
+            dx[d] = (mx - mn) / G->n[d];
+        }
+        return;
+    }
     int b[3];
     block_pos(G, lb, b);
     for (int d = 0; d < 3; ++d)
@@ -682,11 +696,33 @@ static int stencil_halo(const gbns_scheme_desc* S)
 /* public oracle entry points                                          */
 /* ------------------------------------------------------------------ */
 
+static int flux_div_geom(const geom_t* Gp, const gbns_scheme_desc* S,
+                         const double* prims, double* rhs, int increment, int nthreads);
+
 int oracle_flux_div(const gbns_grid_desc* g, const gbns_scheme_desc* S,
                     const double* prims, double* rhs, int increment, int nthreads)
 {
     geom_t G;
     if (geom_init(g, &G)) return -1;
+    return flux_div_geom(&G, S, prims, rhs, increment, nthreads);
+}
+
+/* flux_div on a refined layout: grid->nblk = (blocks, 1, 1), identity
+ * coordinates, each block's box from `boxes` (6 doubles per block). */
+int oracle_flux_div_blocks(const gbns_grid_desc* g, const gbns_scheme_desc* S, const double* boxes,
+                           const double* prims, double* rhs, int increment, int nthreads)
+{
+    geom_t G;
+    if (geom_init(g, &G)) return -1;
+    if (G.coords != GBNS_COORDS_IDENTITY || G.nb[1] != 1 || G.nb[2] != 1) return -1;
+    G.boxes = boxes;
+    return flux_div_geom(&G, S, prims, rhs, increment, nthreads);
+}
+
+static int flux_div_geom(const geom_t* Gp, const gbns_scheme_desc* S,
+                         const double* prims, double* rhs, int increment, int nthreads)
+{
+    const geom_t G = *Gp;
     if (stencil_halo(S) > G.ng) return -2;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);

@@ -48,6 +48,8 @@ def port():
         lib.oracle_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), ctypes.c_void_p, ctypes.c_void_p]
         lib.oracle_boundary_flux.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_int)]
         lib.oracle_exchange_patches.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        lib.oracle_flux_div_blocks.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
         _port = lib
     return _port
 
@@ -69,6 +71,8 @@ def ref():
         lib.spade_ref_amr_exchange.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p,
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.spade_ref_amr_flux_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -82,6 +86,14 @@ def _check(rc, what):
 
 def flux_div(grid, scheme, prims, rhs, increment=True, nthreads=0):
     _check(port().oracle_flux_div(ctypes.byref(grid), ctypes.byref(scheme), _ptr(prims), _ptr(rhs), int(increment), int(nthreads)), "oracle_flux_div")
+
+
+def flux_div_blocks(grid, scheme, boxes, prims, rhs, increment=True, nthreads=0):
+    """flux_div on a refined layout: grid.nblk = (blocks, 1, 1), identity
+    coordinates, boxes (blocks, 6) the per-block min/max per direction."""
+    b = np.ascontiguousarray(boxes, dtype=np.float64)
+    _check(port().oracle_flux_div_blocks(ctypes.byref(grid), ctypes.byref(scheme), _ptr(b), _ptr(prims), _ptr(rhs),
+                                         int(increment), int(nthreads)), "oracle_flux_div_blocks")
 
 
 def fill_ghosts(grid, bc, prims):
@@ -220,3 +232,24 @@ def ref_amr_exchange(nb, nc, ng, periodic, passes, bounds=(0.0, 1.0, 0.0, 1.0, 0
     return {"before": before[:n * per_block].reshape(shape), "after": after[:n * per_block].reshape(shape),
             "boxes": boxes[:6 * n].reshape(n, 6), "levels": levels[:n].copy(),
             "plan": plan[:18 * nplan.value].reshape(-1, 18).copy(), "ninject": ninj.value}
+
+
+def ref_amr_flux_div(ref_scheme, nb, nc, ng, periodic, passes, scheme, prims, bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    """The reference's flux_div (overwrite mode) on the refined layout of
+    ref_amr_exchange(nb, nc, ng, periodic, passes, bounds), with the state
+    `prims` (its full array, ghosts included) copied in
+    (oracle/ref_harness.cc spade_ref_amr_flux_div).  The scheme constants
+    come from `scheme` as for ref_flux_div.  Returns the residual array."""
+    ints = [nb[0], nb[1], nb[2], nc[0], nc[1], nc[2], ng] + [int(bool(p)) for p in periodic] + [len(passes)]
+    for ps in passes:
+        ints += [len(ps)] + list(ps)
+    ints = np.array(ints, dtype=np.int32)
+    grid = _abi.grid_desc(nb, nc, ng, bounds)
+    _, reals = _ref_problem(grid, scheme)
+    q = np.ascontiguousarray(prims, dtype=np.float64)
+    rhs = np.zeros_like(q)
+    nblk = ctypes.c_int(0)
+    _check(ref().spade_ref_amr_flux_div(int(ref_scheme), ints.ctypes.data, reals.ctypes.data, q.size, _ptr(q), _ptr(rhs),
+                                        ctypes.byref(nblk)), "spade_ref_amr_flux_div")
+    assert nblk.value == q.shape[0]
+    return rhs

@@ -231,6 +231,16 @@ extern "C"
         return pb;
     }
 
+    // The same from the refined-layout ints of spade_ref_amr_exchange (no
+    // wall flag: index 10 there is the pass count).
+    static problem_t make_problem_amr(const int* ints, const double* reals)
+    {
+        int flat[11];
+        for (int i = 0; i < 10; ++i) flat[i] = ints[i];
+        flat[10] = 0;
+        return make_problem(flat, reals);
+    }
+
     // One flux_div call.  `prims` is the full AoS5 array including ghosts,
     // used as given; `rhs` is the full AoS5 array including ghosts.  With
     // overwrite != 0 the reference's `overwrite` trait zeroes rhs first,
@@ -500,5 +510,58 @@ extern "C"
             return rc;
         }
         catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_amr_exchange: %s\n", e.what()); return -1; }
+    }
+
+    // flux_div on a refined layout: the grid of spade_ref_amr_exchange (same
+    // `ints` and bounds = reals[0..5]), the given state copied in (ghosts
+    // included, as the exchange left them) and one flux_div of `scheme` in
+    // overwrite mode (pde-algs/flux-div/flux_div_basic.h:17-76; each block
+    // takes 1/dx from its own bounding box, grid/grid_geometry.h:85-89).
+    //   reals: the problem layout of make_problem (bounds, gas, viscosity,
+    //          dissipation and sensor constants)
+    // `prims` and `rhs` hold cap doubles; nblk_out receives the block count.
+    int spade_ref_amr_flux_div(int scheme, const int* ints, const double* reals, long long cap,
+                               const double* prims, double* rhs, int* nblk_out)
+    {
+        try
+        {
+            const problem_t pb = make_problem_amr(ints, reals);
+            int argc = 0;
+            char** argv = nullptr;
+            spade::parallel::compute_env_t env(&argc, &argv, {0});
+            int rc = 0;
+            env.exec([&](spade::parallel::pool_t& group)
+            {
+                spade::ctrs::array<bool, 3> per(ints[7] != 0, ints[8] != 0, ints[9] != 0);
+                spade::bound_box_t<real_t, 3> bbx;
+                for (int d = 0; d < 3; ++d) { bbx.min(d) = pb.bounds[2*d]; bbx.max(d) = pb.bounds[2*d + 1]; }
+                spade::coords::identity<real_t> coords;
+                spade::ctrs::array<int, 3> num_blocks(pb.nb[0], pb.nb[1], pb.nb[2]), cells(pb.nc[0], pb.nc[1], pb.nc[2]);
+                spade::amr::amr_blocks_t blocks(num_blocks, bbx);
+                spade::grid::cartesian_grid_t grid(cells, blocks, coords, group);
+                const int npass = ints[10];
+                int pos = 11;
+                for (int pss = 0; pss < npass; ++pss)
+                {
+                    const int cnt = ints[pos++];
+                    std::vector<std::size_t> list;
+                    for (int i = 0; i < cnt; ++i) list.push_back(std::size_t(ints[pos++]));
+                    grid.refine_blocks(list, per);
+                }
+                spade::ctrs::array<int, 3> nexch(pb.ng, pb.ng, pb.ng);
+                spade::grid::grid_array q(grid, prim_t(0.0), nexch, spade::device::cpu);
+                spade::grid::grid_array r(grid, flux_t(0.0), nexch, spade::device::cpu);
+                *nblk_out = int(grid.get_num_global_blocks());
+                if ((long long)q.data.size() > cap) { rc = -2; return; }
+                copy_in(q, prims);
+                with_flux(pb, scheme, [&](const auto& flx)
+                {
+                    spade::pde_algs::flux_div(q, r, flx, spade::algs::make_traits(spade::pde_algs::basic, spade::pde_algs::overwrite));
+                });
+                copy_out(r, rhs);
+            });
+            return rc;
+        }
+        catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_amr_flux_div: %s\n", e.what()); return -1; }
     }
 }

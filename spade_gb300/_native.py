@@ -55,6 +55,7 @@ def lib():
                                         ctypes.c_double, ctypes.c_int, vp, vp]
     L.gbns_source_term.argtypes = [P(_abi.GridDesc), P(_abi.SourceDesc), vp, vp, vp]
     L.gbns_flux_div_host.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, vp]
+    L.gbns_flux_div_blocks.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, vp, ctypes.c_int, vp]
     L.gbns_boundary_flux.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, P(ctypes.c_int), vp]
     L.gbns_selftest_wait_timeout.argtypes = [P(ctypes.c_int), vp]
     L.gbns_selftest_dmul_int.argtypes = [ctypes.c_uint64, ctypes.c_uint64, P(ctypes.c_uint64), vp]

@@ -88,6 +88,7 @@ namespace gbns
                 // tmaps[2 inst + 1]: R[2]); items the host marked (w.pad) only
                 A.use_tma = (!Cfg::DIRECT && tmaps != nullptr && w.pad) ? 1 : 0;
                 A.sh_off = 0;
+                A.blk_inv_dx = nullptr;
                 arg.tmap = A.use_tma ? tmaps + 2*w.inst + (stage == 1 ? 1 : 0) : nullptr;
                 A.rk_nres = stage + 1;
                 A.rk_res[0] = I.R[0];

@@ -31,13 +31,13 @@ namespace gbns
     int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
                         const gbns_scheme_desc* desc, const double* prims, double* rhs,
                         int increment, cudaStream_t stream, int variant, const RkFuse* fuse,
-                        int blk0, int blk1)
+                        int blk0, int blk1, const double* blk_inv_dx)
     {
         if (variant < 0 || variant >= flux_variant_count(desc))
             return set_error(GBNS_ERR_INVALID, "flux_div tile variant out of range");
         if (blk1 < 0) blk1 = G.nblk;
         if (blk0 < 0 || blk1 > G.nblk || blk0 > blk1) return set_error(GBNS_ERR_INVALID, "block range out of the grid");
-        FluxCall c{g, &G, Y, &S, prims, rhs, increment, stream, variant, fuse, blk0, blk1};
+        FluxCall c{g, &G, Y, &S, prims, rhs, increment, stream, variant, fuse, blk0, blk1, blk_inv_dx};
         const bool stretch = g->coords != GBNS_COORDS_IDENTITY;
         const bool upwind = desc->convective == GBNS_CONV_FWENO || desc->convective == GBNS_CONV_WENO5;
         const int conv = desc->convective, order = desc->order;

@@ -23,6 +23,7 @@ namespace gbns
         A.rk_nres = 0;
         A.write_rhs = 1;
         A.q_out = nullptr;
+        A.blk_inv_dx = c.blk_inv_dx;
         A.rk_res[0] = A.rk_res[1] = nullptr;
         A.rk_coeff[0] = A.rk_coeff[1] = A.rk_coeff[2] = 0.0;
         if (c.fuse)

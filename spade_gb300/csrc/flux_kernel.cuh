@@ -993,6 +993,9 @@ namespace gbns
         const double* rk_res[2];
         double rk_coeff[3];
         double* q_out;
+        // Refined layouts: 1/dx of every block (3 per block, device memory);
+        // nullptr: the uniform layout's table in GeomK
+        const double* blk_inv_dx;
     };
 
     // One face of direction D (tile-local face index f) into the face buffer
@@ -1342,8 +1345,8 @@ namespace gbns
         #pragma unroll
         for (int d = 0; d < 3; ++d)
         {
-            invd[d] = G.inv_dx[d][b[d]];
-            if constexpr (sizeof(Real) == 4) inv[d] = G.inv_dx_f[d][b[d]];
+            invd[d] = A.blk_inv_dx ? A.blk_inv_dx[3*lb + d] : G.inv_dx[d][b[d]];
+            if constexpr (sizeof(Real) == 4) inv[d] = A.blk_inv_dx ? float(invd[d]) : G.inv_dx_f[d][b[d]];
             else inv[d] = invd[d];
         }
 

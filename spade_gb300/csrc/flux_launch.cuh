@@ -28,6 +28,7 @@ namespace gbns
         int variant;
         const RkFuse* fuse;
         int blk0, blk1;     // the blocks this launch covers: blk0 .. blk1 - 1
+        const double* blk_inv_dx;   // refined layouts: per-block 1/dx (device), else nullptr
     };
 
     // f64x: FP64 without FMA contraction (-fmad=false): the kernels follow the

@@ -144,7 +144,10 @@ namespace gbns
     int launch_flux_div(const gbns_grid_desc* g, const GeomK& G, const YTabK* Y, const SchemeK& S,
                         const gbns_scheme_desc* desc, const double* prims, double* rhs,
                         int increment, cudaStream_t stream, int variant, const RkFuse* fuse = nullptr,
-                        int blk0 = 0, int blk1 = -1);
+                        int blk0 = 0, int blk1 = -1, const double* blk_inv_dx = nullptr);
+    // Stream-ordered device memory from the library's own pool (released
+    // with cudaFreeAsync on the same stream).
+    int pool_alloc(void** p, size_t bytes, cudaStream_t st);
     // gbns_flux_div_rk over the blocks blk0 .. blk1 - 1 (host.cu)
     int flux_div_rk_range(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
                           double* rhs, int write_rhs, int nres, const double* const* earlier,

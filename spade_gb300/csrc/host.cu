@@ -384,6 +384,58 @@ extern "C"
                                scheme->tile_variant);
     }
 
+    int gbns_flux_div_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                             const double* prims, double* rhs, int increment, void* stream)
+    {
+        using namespace gbns;
+        if (!grid) return set_error(GBNS_ERR_INVALID, "grid descriptor is NULL");
+        const int nblk = grid->nblk[0];
+        if (nblk < 1 || nblk > 65535 || grid->nblk[1] != 1 || grid->nblk[2] != 1)
+            return set_error(GBNS_ERR_INVALID, "a refined layout's blocks are given as nblk = (1..65535, 1, 1)");
+        if (grid->coords != GBNS_COORDS_IDENTITY)
+            return set_error(GBNS_ERR_UNSUPPORTED, "flux_div on refined layouts takes identity coordinates");
+        if (!block_bounds) return set_error(GBNS_ERR_INVALID, "block_bounds is NULL");
+        // the descriptor checks of one block, then the whole layout
+        gbns_grid_desc one = *grid;
+        one.nblk[0] = 1;
+        GeomK G;
+        SchemeK S;
+        int rc = make_geom(&one, G);
+        if (rc) return rc;
+        G.nb[0] = nblk;
+        G.nblk = nblk;
+        if (double(nblk)*double(G.bstride) > 9.0e18) return set_error(GBNS_ERR_INVALID, "grid too large");
+        rc = make_scheme(scheme, S);
+        if (rc) return rc;
+        if (!prims || !rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
+        if (prims == rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
+        if (scheme_halo(scheme) > G.ng)
+            return set_error(GBNS_ERR_INVALID, "scheme stencil needs " + std::to_string(scheme_halo(scheme)) +
+                             " ghost layers, grid has " + std::to_string(G.ng));
+        // per-block 1/dx as the reference forms it: dx = box size / cells
+        std::vector<double> inv(3*size_t(nblk));
+        for (int lb = 0; lb < nblk; ++lb)
+            for (int d = 0; d < 3; ++d)
+            {
+                const double mn = block_bounds[6*lb + 2*d], mx = block_bounds[6*lb + 2*d + 1];
+                if (!(mx > mn) || !std::isfinite(mn) || !std::isfinite(mx))
+                    return set_error(GBNS_ERR_INVALID, "block " + std::to_string(lb) + ": bounds must be finite with min < max");
+                const double dx = (mx - mn)/G.n[d];
+                inv[3*lb + d] = 1.0/dx;
+            }
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        void* dinv = nullptr;
+        rc = pool_alloc(&dinv, inv.size()*sizeof(double), st);
+        if (rc) return rc;
+        rc = check_cuda(cudaMemcpyAsync(dinv, inv.data(), inv.size()*sizeof(double), cudaMemcpyHostToDevice, st),
+                        "per-block spacing to the device");
+        if (!rc)
+            rc = launch_flux_div(grid, G, nullptr, S, scheme, prims, rhs, increment, st, scheme->tile_variant, nullptr,
+                                 0, nblk, static_cast<const double*>(dinv));
+        const int frc = check_cuda(cudaFreeAsync(dinv, st), "per-block spacing (pool free)");
+        return rc ? rc : frc;
+    }
+
     int gbns_flux_div_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
                            const double* host_prims, double* host_rhs, int increment, void* stream)
     {

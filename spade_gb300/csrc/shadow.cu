@@ -116,6 +116,14 @@ namespace gbns
         return rc;
     }
 
+    int pool_alloc(void** p, size_t bytes, cudaStream_t st)
+    {
+        cudaMemPool_t pool = nullptr;
+        const int rc = shadow_pool(&pool);
+        if (rc) return rc;
+        return check_cuda(cudaMallocFromPoolAsync(p, bytes, pool, st), "library pool allocation");
+    }
+
     int shadow_end(const ShadowK& S, cudaStream_t st)
     {
         if (!S.base) return GBNS_OK;

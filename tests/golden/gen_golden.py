@@ -226,6 +226,36 @@ def gen_amr():
     np.savez_compressed(os.path.join(OUT, "amr_ref.npz"), **out)
 
 
+# flux_div on the refined layouts of AMR_CASES, the reference's own
+# (pde_algs::flux_div, overwrite mode, each block's 1/dx from its own box) on
+# the exchanged array, with ghost cells the exchange leaves at 0 (walls, not
+# filled by it) set to a valid state first: (reference scheme id, scheme fields)
+AMR_FLUX_SCHEMES = {
+    "ck2_visc": (O.REF_CK2_VISC, dict(conv=_abi.CONV_CENT_KEEP, visc=1)),
+    "fweno_diss_visc": (O.REF_FWENO_DISS_VISC, dict(conv=_abi.CONV_FWENO, diss=1, visc=1)),
+}
+
+
+def amr_flux_input(after):
+    q = after.copy()
+    hole = q[..., 1] == 0.0
+    q[hole] = (3.0, 1.0, 0.0, 0.0, 0.0)
+    return q
+
+
+def gen_amr_flux():
+    g = np.load(os.path.join(OUT, "amr_ref.npz"))
+    out = {}
+    for name, (nb, nc, ng, per, passes) in AMR_CASES.items():
+        q = amr_flux_input(g[name + "_after"])
+        for sname, (sid, kw) in AMR_FLUX_SCHEMES.items():
+            rhs = O.ref_amr_flux_div(sid, nb, nc, ng, per, passes, P.scheme(**kw), q)
+            inner = rhs[:, ng:-ng, ng:-ng, ng:-ng]
+            assert np.all(np.isfinite(inner)), (name, sname)
+            out[name + "_" + sname] = inner.copy()
+    np.savez_compressed(os.path.join(OUT, "amr_flux_ref.npz"), **out)
+
+
 def read_dropin_records(path):
     """Parses the calls tests/cpp/gbns_record_stub.c recorded."""
     import struct
@@ -286,6 +316,7 @@ if __name__ == "__main__":
     gen_tgv()
     gen_channel()
     gen_amr()
+    gen_amr_flux()
     gen_dropin()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):

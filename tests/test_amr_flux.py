@@ -1,0 +1,88 @@
+"""flux_div on refined (AMR) block layouts, on the CPU.
+
+Each block of a layout refined through cartesian_grid_t::refine_blocks takes
+1/dx from its own bounding box (flux_div_basic.h:55, grid/grid_geometry.h:
+85-89).  tests/golden/amr_flux_ref.npz holds the reference's own flux_div
+(overwrite mode) on the exchanged arrays of tests/golden/amr_ref.npz for two
+scheme compositions (tests/golden/gen_golden.py).  Here:
+
+* the oracle's per-block-box flux_div reproduces it bit for bit;
+* where the reference harness is built, a third composition too;
+* gbns_flux_div_blocks rejects malformed layouts before any CUDA call.
+
+The GPU side is tests/test_gpu_amr_flux.py."""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from spade_gb300 import _abi, _native
+from oracle import oracle as O
+import problems as P
+from test_amr_exchange import CASES, golden
+from golden.gen_golden import AMR_CASES, AMR_FLUX_SCHEMES, amr_flux_input
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLD = os.path.join(ROOT, "tests", "golden", "amr_flux_ref.npz")
+
+
+def layout(case):
+    """(grid descriptor of the refined layout, boxes, the flux input state, ng)"""
+    g = golden(case)
+    ng = int(g["ng"])
+    q = amr_flux_input(g["after"])
+    grid = _abi.grid_desc((q.shape[0], 1, 1), tuple(int(n) for n in g["ncell"]), ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+    return grid, g["boxes"], q, ng
+
+
+@pytest.mark.parametrize("scheme", sorted(AMR_FLUX_SCHEMES))
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_flux_div_blocks_equals_reference(case, scheme):
+    grid, boxes, q, ng = layout(case)
+    s = P.scheme(**AMR_FLUX_SCHEMES[scheme][1])
+    r = np.zeros_like(q)
+    O.flux_div_blocks(grid, s, boxes, q, r, increment=False)
+    want = np.load(GOLD)[case + "_" + scheme]
+    assert np.array_equal(r[:, ng:-ng, ng:-ng, ng:-ng], want)
+    assert len(np.unique(boxes[:, 1] - boxes[:, 0])) >= 2          # blocks of more than one spacing
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference harness not built")
+@pytest.mark.parametrize("case", ["two_levels_walls_y", "anisotropic_blocks"])
+def test_oracle_flux_div_blocks_equals_reference_live(case):
+    """A composition the goldens do not hold: hybrid cent_keep<2>/fweno_t
+    with the Ducros blend."""
+    nb, nc, ng, per, passes = AMR_CASES[case]
+    grid, boxes, q, ng = layout(case)
+    s = P.scheme(conv=_abi.CONV_HYBRID, order=2, hybrid_flux=_abi.HYBRID_FULL_FLUX,
+                 hybrid_sensor=_abi.SENSOR_DUCROS, hybrid_param=0.5)
+    want = O.ref_amr_flux_div(O.REF_HYB_CK2_FULL, nb, nc, ng, per, passes, s, q)
+    r = np.zeros_like(q)
+    O.flux_div_blocks(grid, s, boxes, q, r, increment=False)
+    inner = (slice(None), slice(ng, -ng), slice(ng, -ng), slice(ng, -ng))
+    assert np.all(np.isfinite(want[inner]))
+    assert np.array_equal(r[inner], want[inner])
+
+
+def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
+    lib = _native.lib()
+    s = P.scheme(conv=_abi.CONV_CENT_KEEP, visc=1)
+    boxes = np.array([[0.0, 0.5, 0.0, 0.5, 0.0, 0.5], [0.5, 1.0, 0.0, 0.5, 0.0, 0.5]])
+    pq, pr = ctypes.c_void_p(16), ctypes.c_void_p(32)
+
+    def call(grid, b, scheme=s):
+        bp = b.ctypes.data_as(ctypes.c_void_p) if b is not None else None
+        return lib.gbns_flux_div_blocks(grid, scheme, bp, pq, pr, 0, None)
+
+    g = _abi.grid_desc((2, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1))
+    assert call(_abi.grid_desc((1, 2, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1)), boxes) == _abi.ERR_INVALID
+    assert call(_abi.grid_desc((2, 1, 1), (4, 4, 4), 2, (0, 1, 0, 1, 0, 1), _abi.COORDS_TANH_Y, (2.0, 0, 0, 0)),
+                boxes) == _abi.ERR_UNSUPPORTED
+    assert call(g, None) == _abi.ERR_INVALID
+    bad = boxes.copy()
+    bad[1, 3] = bad[1, 2]
+    assert call(g, bad) == _abi.ERR_INVALID and "block 1" in _native.last_error()
+    assert call(_abi.grid_desc((2, 1, 1), (4, 4, 4), 1, (0, 1, 0, 1, 0, 1)), boxes,
+                P.scheme(conv=_abi.CONV_FWENO)) == _abi.ERR_INVALID
+    assert "ghost layers" in _native.last_error()

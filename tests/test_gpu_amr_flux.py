@@ -1,0 +1,82 @@
+"""flux_div on refined (AMR) block layouts on the GPU (gbns_flux_div_blocks):
+the reference's own results from tests/golden/amr_flux_ref.npz, bit for bit,
+for three layouts refined through cartesian_grid_t::refine_blocks and two
+scheme compositions, in every tile variant; increment mode against the
+oracle; FP32-flux within its normwise bound; and the whole refined-layout
+path on the device (the reference's exchange plan run by
+gbns_exchange_plan_*, then flux_div) against the reference."""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from spade_gb300 import _abi, _native
+from spade_gb300 import grid as _grid
+from oracle import oracle as O
+import problems as P
+from test_amr_exchange import CASES, amr_fill, golden
+from test_amr_flux import GOLD, layout
+from golden.gen_golden import AMR_FLUX_SCHEMES
+
+pytestmark = pytest.mark.gpu
+
+
+def _st():
+    return int(torch.cuda.current_stream().cuda_stream)
+
+
+def _flux(grid, s, boxes, qd, rhs0, increment):
+    rd = torch.from_numpy(rhs0.copy()).cuda()
+    b = np.ascontiguousarray(boxes)
+    _native.check(_native.lib().gbns_flux_div_blocks(grid, s, b.ctypes.data_as(ctypes.c_void_p), qd.data_ptr(),
+                                                     rd.data_ptr(), int(increment), _st()))
+    torch.cuda.synchronize()
+    return rd.cpu().numpy()
+
+
+@pytest.mark.parametrize("scheme", sorted(AMR_FLUX_SCHEMES))
+@pytest.mark.parametrize("case", CASES)
+def test_flux_div_blocks_equals_reference_every_variant(case, scheme):
+    grid, boxes, q, ng = layout(case)
+    want = np.load(GOLD)[case + "_" + scheme]
+    qd = torch.from_numpy(q).cuda()
+    s = P.scheme(**AMR_FLUX_SCHEMES[scheme][1])
+    nvar = _native.lib().gbns_flux_variant_count(s)
+    assert nvar >= 2
+    for v in range(nvar):
+        s.tile_variant = v
+        r = _flux(grid, s, boxes, qd, np.zeros_like(q), False)
+        assert np.array_equal(r[:, ng:-ng, ng:-ng, ng:-ng], want), v
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_flux_div_blocks_increment_and_fp32_flux(case):
+    grid, boxes, q, ng = layout(case)
+    qd = torch.from_numpy(q).cuda()
+    s = P.scheme(**AMR_FLUX_SCHEMES["fweno_diss_visc"][1])
+    r0 = np.random.Generator(np.random.PCG64(5)).standard_normal(q.shape)
+    want = r0.copy()
+    O.flux_div_blocks(grid, s, boxes, q, want, increment=True)
+    assert np.array_equal(_flux(grid, s, boxes, qd, r0, True), want)
+    ref = np.load(GOLD)[case + "_fweno_diss_visc"]
+    s32 = P.scheme(precision=_abi.PREC_FP32_FLUX, **AMR_FLUX_SCHEMES["fweno_diss_visc"][1])
+    r = _flux(grid, s32, boxes, qd, np.zeros_like(q), False)[:, ng:-ng, ng:-ng, ng:-ng]
+    err = (np.abs(r - ref).reshape(-1, 5).max(axis=0) / np.abs(ref).reshape(-1, 5).max(axis=0)).max()
+    assert err < 2e-4, err
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_refined_layout_exchange_then_flux_on_the_device(case):
+    g = golden(case)
+    grid, boxes, _, ng = layout(case)
+    qd = torch.from_numpy(amr_fill(g["boxes"], g["ncell"], ng)).cuda()
+    plan = _grid.exchange_plan_t(g["ncell"], ng, qd.shape[0], g["plan"])
+    plan.exchange(qd)
+    plan.close()
+    hole = qd[..., 1] == 0.0                                  # wall ghosts the exchange leaves unset
+    qd[hole] = torch.tensor([3.0, 1.0, 0.0, 0.0, 0.0], dtype=torch.float64, device="cuda")
+    s = P.scheme(**AMR_FLUX_SCHEMES["ck2_visc"][1])
+    r = _flux(grid, s, boxes, qd, np.zeros(tuple(qd.shape)), False)
+    assert np.array_equal(r[:, ng:-ng, ng:-ng, ng:-ng], np.load(GOLD)[case + "_ck2_visc"])
