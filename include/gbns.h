@@ -372,6 +372,22 @@ int gbns_exchange_plan_waves(int nx, int ny, int nz, int ng, int nblocks, const 
                              int* waves);
 int gbns_exchange_plan_destroy(gbns_exchange_plan* plan);
 
+/* One SSPRK3 step on a refined (AMR) layout: integrator_t::advance with
+ * ssprk3_t and the conservative-variable state transform
+ * (time-integration/advance.h:234-280), with the layout's exchange as the
+ * boundary condition, as the reference's drivers pair them.  grid and
+ * block_bounds as for gbns_flux_div_blocks; plan the layout's exchange
+ * (created for grid->ncell, grid->ng and grid->nblk[0] blocks).  Each stage
+ * is one flux launch with the stage update fused (as gbns_ssprk3_step), then
+ * the exchange, on a stage array that starts as a copy of the stage's input
+ * (so the exchange sees the ghost values of the reference's in-place update:
+ * ghost donors read before they are written, ghosts it never writes).
+ * prims must hold exchanged ghosts on entry and does on exit.  work: 3 arrays
+ * of prims' size.  Asynchronous on `stream` (the per-block table is copied
+ * from pageable memory: not for stream capture). */
+int gbns_ssprk3_step_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                            gbns_exchange_plan* plan, double* prims, double* work, double dt, void* stream);
+
 /* dst = src on interior cells, dst's ghost layers filled from src's interior
  * donors (gbns_fill_ghosts of src, written into dst).  Asynchronous. */
 int gbns_copy_fill_ghosts(const gbns_grid_desc* grid, const gbns_bc_desc* bc, double* dst,

@@ -73,6 +73,8 @@ def ref():
                                                ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         lib.spade_ref_amr_flux_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        lib.spade_ref_amr_ssprk3.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_longlong, ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -253,3 +255,24 @@ def ref_amr_flux_div(ref_scheme, nb, nc, ng, periodic, passes, scheme, prims, bo
                                         ctypes.byref(nblk)), "spade_ref_amr_flux_div")
     assert nblk.value == q.shape[0]
     return rhs
+
+
+def _amr_ints(nb, nc, ng, periodic, passes):
+    ints = [nb[0], nb[1], nb[2], nc[0], nc[1], nc[2], ng] + [int(bool(p)) for p in periodic] + [len(passes)]
+    for ps in passes:
+        ints += [len(ps)] + list(ps)
+    return np.array(ints, dtype=np.int32)
+
+
+def ref_amr_ssprk3(ref_scheme, nb, nc, ng, periodic, passes, scheme, prims, dt, nsteps,
+                   bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    """nsteps of the reference's SSPRK3 (integrator_t, ssprk3_t, state
+    transform) on the refined layout of ref_amr_exchange, with the layout's
+    exchange as the boundary condition (oracle/ref_harness.cc
+    spade_ref_amr_ssprk3).  `prims` (full array) is updated in place."""
+    ints = _amr_ints(nb, nc, ng, periodic, passes)
+    grid = _abi.grid_desc(nb, nc, ng, bounds)
+    _, reals = _ref_problem(grid, scheme)
+    assert prims.dtype == np.float64 and prims.flags.c_contiguous
+    _check(ref().spade_ref_amr_ssprk3(int(ref_scheme), ints.ctypes.data, reals.ctypes.data, float(dt), int(nsteps),
+                                      prims.size, _ptr(prims)), "spade_ref_amr_ssprk3")

@@ -213,7 +213,39 @@ namespace
         }
         return sum/double(count);
     }
+    // Runs `body(grid, group, periodic)` on a single-rank compute environment
+    // with the refined identity-coordinate grid of spade_ref_amr_exchange's
+    // `ints`: an amr_blocks_t grid built unrefined, then refined in place pass
+    // by pass (grid/cartesian_grid.h:331-367).
+    template <typename body_t>
+    void with_amr_grid(const problem_t& pb, const int* ints, const body_t& body)
+    {
+        int argc = 0;
+        char** argv = nullptr;
+        spade::parallel::compute_env_t env(&argc, &argv, {0});
+        env.exec([&](spade::parallel::pool_t& group)
+        {
+            spade::ctrs::array<bool, 3> per(ints[7] != 0, ints[8] != 0, ints[9] != 0);
+            spade::bound_box_t<real_t, 3> bbx;
+            for (int d = 0; d < 3; ++d) { bbx.min(d) = pb.bounds[2*d]; bbx.max(d) = pb.bounds[2*d + 1]; }
+            spade::coords::identity<real_t> coords;
+            spade::ctrs::array<int, 3> num_blocks(pb.nb[0], pb.nb[1], pb.nb[2]), cells(pb.nc[0], pb.nc[1], pb.nc[2]);
+            spade::amr::amr_blocks_t blocks(num_blocks, bbx);
+            spade::grid::cartesian_grid_t grid(cells, blocks, coords, group);
+            const int npass = ints[10];
+            int pos = 11;
+            for (int pss = 0; pss < npass; ++pss)
+            {
+                const int cnt = ints[pos++];
+                std::vector<std::size_t> list;
+                for (int i = 0; i < cnt; ++i) list.push_back(std::size_t(ints[pos++]));
+                grid.refine_blocks(list, per);
+            }
+            body(grid, group, per);
+        });
+    }
 }
+
 
 extern "C"
 {
@@ -526,28 +558,9 @@ extern "C"
         try
         {
             const problem_t pb = make_problem_amr(ints, reals);
-            int argc = 0;
-            char** argv = nullptr;
-            spade::parallel::compute_env_t env(&argc, &argv, {0});
             int rc = 0;
-            env.exec([&](spade::parallel::pool_t& group)
+            with_amr_grid(pb, ints, [&](auto& grid, auto&, auto&)
             {
-                spade::ctrs::array<bool, 3> per(ints[7] != 0, ints[8] != 0, ints[9] != 0);
-                spade::bound_box_t<real_t, 3> bbx;
-                for (int d = 0; d < 3; ++d) { bbx.min(d) = pb.bounds[2*d]; bbx.max(d) = pb.bounds[2*d + 1]; }
-                spade::coords::identity<real_t> coords;
-                spade::ctrs::array<int, 3> num_blocks(pb.nb[0], pb.nb[1], pb.nb[2]), cells(pb.nc[0], pb.nc[1], pb.nc[2]);
-                spade::amr::amr_blocks_t blocks(num_blocks, bbx);
-                spade::grid::cartesian_grid_t grid(cells, blocks, coords, group);
-                const int npass = ints[10];
-                int pos = 11;
-                for (int pss = 0; pss < npass; ++pss)
-                {
-                    const int cnt = ints[pos++];
-                    std::vector<std::size_t> list;
-                    for (int i = 0; i < cnt; ++i) list.push_back(std::size_t(ints[pos++]));
-                    grid.refine_blocks(list, per);
-                }
                 spade::ctrs::array<int, 3> nexch(pb.ng, pb.ng, pb.ng);
                 spade::grid::grid_array q(grid, prim_t(0.0), nexch, spade::device::cpu);
                 spade::grid::grid_array r(grid, flux_t(0.0), nexch, spade::device::cpu);
@@ -563,5 +576,51 @@ extern "C"
             return rc;
         }
         catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_amr_flux_div: %s\n", e.what()); return -1; }
+    }
+
+    // nsteps of SSPRK3 on a refined layout (the grid of spade_ref_amr_flux_div)
+    // through integrator_t with the conservative-variable state transform; the
+    // boundary condition is the layout's exchange alone (make_exchange with the
+    // periodic flags; ghost cells it does not write keep their values).
+    // `prims` (cap doubles) holds the initial state on entry and the final
+    // state on exit; the exchange runs once before the first step.
+    int spade_ref_amr_ssprk3(int scheme, const int* ints, const double* reals, double dt, int nsteps, long long cap,
+                             double* prims)
+    {
+        try
+        {
+            const problem_t pb = make_problem_amr(ints, reals);
+            int rc = 0;
+            with_amr_grid(pb, ints, [&](auto& grid, auto& group, auto& per)
+            {
+                spade::ctrs::array<int, 3> nexch(pb.ng, pb.ng, pb.ng);
+                spade::grid::grid_array q  (grid, prim_t(0.0), nexch, spade::device::cpu);
+                spade::grid::grid_array rhs(grid, flux_t(0.0), nexch, spade::device::cpu);
+                if ((long long)q.data.size() > cap) { rc = -2; return; }
+                copy_in(q, prims);
+                auto handle = spade::grid::make_exchange(q, per);
+                handle.exchange(q, group);
+                gas_t air(pb.gamma, pb.rgas);
+                with_flux(pb, scheme, [&](const auto& flx)
+                {
+                    auto bc = [&](auto& sol, const auto&) { handle.exchange(sol, group); };
+                    auto calc_rhs = [&](auto& rhs_in, const auto& sol, const auto&)
+                    {
+                        rhs_in = real_t(0.0);
+                        spade::pde_algs::flux_div(sol, rhs_in, flx);
+                    };
+                    cons_t transform_state;
+                    spade::fluid_state::state_transform_t trans(transform_state, air);
+                    spade::time_integration::time_axis_t axis(real_t(0.0), dt);
+                    spade::time_integration::ssprk3_t alg;
+                    spade::time_integration::integrator_data_t data(q, rhs, alg);
+                    spade::time_integration::integrator_t time_int(axis, alg, data, calc_rhs, bc, trans);
+                    for (int n = 0; n < nsteps; ++n) time_int.advance();
+                    copy_out(time_int.solution(), prims);
+                });
+            });
+            return rc;
+        }
+        catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_amr_ssprk3: %s\n", e.what()); return -1; }
     }
 }

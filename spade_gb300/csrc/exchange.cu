@@ -371,3 +371,13 @@ extern "C"
         return GBNS_OK;
     }
 }
+
+namespace gbns
+{
+    int exchange_plan_shape(const gbns_exchange_plan* P, int* nx, int* ny, int* nz, int* ng, int* nblocks)
+    {
+        if (!P) return set_error(GBNS_ERR_INVALID, "exchange plan is NULL");
+        *nx = P->nx; *ny = P->ny; *nz = P->nz; *ng = P->G.ng; *nblocks = P->nblocks;
+        return GBNS_OK;
+    }
+}

@@ -148,6 +148,9 @@ namespace gbns
     // Stream-ordered device memory from the library's own pool (released
     // with cudaFreeAsync on the same stream).
     int pool_alloc(void** p, size_t bytes, cudaStream_t st);
+    // The cells per block, ghost layers and block count an exchange plan was
+    // created for (exchange.cu).
+    int exchange_plan_shape(const gbns_exchange_plan* P, int* nx, int* ny, int* nz, int* ng, int* nblocks);
     // gbns_flux_div_rk over the blocks blk0 .. blk1 - 1 (host.cu)
     int flux_div_rk_range(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
                           double* rhs, int write_rhs, int nres, const double* const* earlier,

@@ -384,22 +384,23 @@ extern "C"
                                scheme->tile_variant);
     }
 
-    int gbns_flux_div_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
-                             const double* prims, double* rhs, int increment, void* stream)
+    // The checks and the per-block 1/dx table of a refined layout, and the
+    // table in stream-ordered device memory (the caller frees *dinv on st).
+    static int blocks_setup(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                            gbns::GeomK& G, gbns::SchemeK& S, cudaStream_t st, double** dinv)
     {
         using namespace gbns;
+        *dinv = nullptr;
         if (!grid) return set_error(GBNS_ERR_INVALID, "grid descriptor is NULL");
         const int nblk = grid->nblk[0];
         if (nblk < 1 || nblk > 65535 || grid->nblk[1] != 1 || grid->nblk[2] != 1)
             return set_error(GBNS_ERR_INVALID, "a refined layout's blocks are given as nblk = (1..65535, 1, 1)");
         if (grid->coords != GBNS_COORDS_IDENTITY)
-            return set_error(GBNS_ERR_UNSUPPORTED, "flux_div on refined layouts takes identity coordinates");
+            return set_error(GBNS_ERR_UNSUPPORTED, "refined layouts take identity coordinates");
         if (!block_bounds) return set_error(GBNS_ERR_INVALID, "block_bounds is NULL");
         // the descriptor checks of one block, then the whole layout
         gbns_grid_desc one = *grid;
         one.nblk[0] = 1;
-        GeomK G;
-        SchemeK S;
         int rc = make_geom(&one, G);
         if (rc) return rc;
         G.nb[0] = nblk;
@@ -407,8 +408,6 @@ extern "C"
         if (double(nblk)*double(G.bstride) > 9.0e18) return set_error(GBNS_ERR_INVALID, "grid too large");
         rc = make_scheme(scheme, S);
         if (rc) return rc;
-        if (!prims || !rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
-        if (prims == rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
         if (scheme_halo(scheme) > G.ng)
             return set_error(GBNS_ERR_INVALID, "scheme stencil needs " + std::to_string(scheme_halo(scheme)) +
                              " ghost layers, grid has " + std::to_string(G.ng));
@@ -423,15 +422,89 @@ extern "C"
                 const double dx = (mx - mn)/G.n[d];
                 inv[3*lb + d] = 1.0/dx;
             }
-        const cudaStream_t st = static_cast<cudaStream_t>(stream);
-        void* dinv = nullptr;
-        rc = pool_alloc(&dinv, inv.size()*sizeof(double), st);
+        void* p = nullptr;
+        rc = pool_alloc(&p, inv.size()*sizeof(double), st);
         if (rc) return rc;
-        rc = check_cuda(cudaMemcpyAsync(dinv, inv.data(), inv.size()*sizeof(double), cudaMemcpyHostToDevice, st),
+        rc = check_cuda(cudaMemcpyAsync(p, inv.data(), inv.size()*sizeof(double), cudaMemcpyHostToDevice, st),
                         "per-block spacing to the device");
-        if (!rc)
-            rc = launch_flux_div(grid, G, nullptr, S, scheme, prims, rhs, increment, st, scheme->tile_variant, nullptr,
-                                 0, nblk, static_cast<const double*>(dinv));
+        if (rc) { cudaFreeAsync(p, st); return rc; }
+        *dinv = static_cast<double*>(p);
+        return GBNS_OK;
+    }
+
+    int gbns_flux_div_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                             const double* prims, double* rhs, int increment, void* stream)
+    {
+        using namespace gbns;
+        if (!prims || !rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
+        if (prims == rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        GeomK G;
+        SchemeK S;
+        double* dinv = nullptr;
+        int rc = blocks_setup(grid, scheme, block_bounds, G, S, st, &dinv);
+        if (rc) return rc;
+        rc = launch_flux_div(grid, G, nullptr, S, scheme, prims, rhs, increment, st, scheme->tile_variant, nullptr,
+                             0, G.nblk, dinv);
+        const int frc = check_cuda(cudaFreeAsync(dinv, st), "per-block spacing (pool free)");
+        return rc ? rc : frc;
+    }
+
+    int gbns_ssprk3_step_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                                gbns_exchange_plan* plan, double* prims, double* work, double dt, void* stream)
+    {
+        using namespace gbns;
+        if (!prims || !work) return set_error(GBNS_ERR_INVALID, "prims/work pointer is NULL");
+        int px = 0, py = 0, pz = 0, pg = 0, pn = 0;
+        int rc = exchange_plan_shape(plan, &px, &py, &pz, &pg, &pn);
+        if (rc) return rc;
+        if (!grid) return set_error(GBNS_ERR_INVALID, "grid descriptor is NULL");
+        if (px != grid->ncell[0] || py != grid->ncell[1] || pz != grid->ncell[2] || pg != grid->ng || pn != grid->nblk[0])
+            return set_error(GBNS_ERR_INVALID, "the exchange plan was created for another block layout");
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        GeomK G;
+        SchemeK S;
+        double* dinv = nullptr;
+        rc = blocks_setup(grid, scheme, block_bounds, G, S, st, &dinv);
+        if (rc) return rc;
+        const size_t n = size_t(G.bstride)*G.nblk;
+        double* R0 = work;
+        double* R1 = work + n;
+        double* B = work + 2*n;      // the state between stages
+        // ratio_diff_t of consecutive ssprk3_t rows (explicit.h:80-88, advance.h:80-95)
+        const double c[3][3] = {{(1.0/1.0)*dt, 0.0, 0.0}, {(-3.0/4.0)*dt, (1.0/4.0)*dt, 0.0},
+                                {(-1.0/12.0)*dt, (-1.0/12.0)*dt, (2.0/3.0)*dt}};
+        auto stage = [&](int k, const double* in, double* res, double* out) -> int
+        {
+            RkFuse f;
+            std::memset(&f, 0, sizeof(f));
+            f.nres = k + 1;
+            f.write_rhs = res ? 1 : 0;
+            f.res[0] = R0;
+            f.res[1] = R1;
+            for (int j = 0; j <= k; ++j) f.coeff[j] = c[k][j];
+            f.q_out = out;
+            return launch_flux_div(grid, G, nullptr, S, scheme, in, res ? res : out, 0, st, scheme->tile_variant, &f,
+                                   0, G.nblk, dinv);
+        };
+        // Each stage's output array starts as a copy of its input, so before
+        // the exchange it holds the ghost values the in-place update would:
+        // the plan can read ghost donors before it writes them (two levels
+        // with walls), and the ghosts it never writes keep their values.
+        auto copy = [&](double* dst, const double* src) -> int
+        {
+            return check_cuda(cudaMemcpyAsync(dst, src, n*sizeof(double), cudaMemcpyDeviceToDevice, st), "state copy");
+        };
+        rc = copy(B, prims);
+        if (!rc) rc = stage(0, prims, R0, B);
+        if (!rc) rc = gbns_exchange_plan_run(plan, B, stream);
+        if (!rc) rc = copy(prims, B);
+        if (!rc) rc = stage(1, B, R1, prims);
+        if (!rc) rc = gbns_exchange_plan_run(plan, prims, stream);
+        if (!rc) rc = copy(B, prims);
+        if (!rc) rc = stage(2, prims, nullptr, B);
+        if (!rc) rc = gbns_exchange_plan_run(plan, B, stream);
+        if (!rc) rc = copy(prims, B);
         const int frc = check_cuda(cudaFreeAsync(dinv, st), "per-block spacing (pool free)");
         return rc ? rc : frc;
     }

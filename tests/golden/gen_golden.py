@@ -7,6 +7,7 @@ reference sources exist).  Run from the repository root:
 Fixtures hold inputs (or the 1-D tables and seeds that rebuild them
 bit-exactly, tests/problems.py) and the reference's outputs.
 """
+import hashlib
 import math
 import os
 import sys
@@ -236,6 +237,9 @@ AMR_FLUX_SCHEMES = {
 }
 
 
+AMR_SSPRK3_DT, AMR_SSPRK3_STEPS = 1e-4, 3
+
+
 def amr_flux_input(after):
     q = after.copy()
     hole = q[..., 1] == 0.0
@@ -253,6 +257,13 @@ def gen_amr_flux():
             inner = rhs[:, ng:-ng, ng:-ng, ng:-ng]
             assert np.all(np.isfinite(inner)), (name, sname)
             out[name + "_" + sname] = inner.copy()
+            # AMR_SSPRK3_STEPS of the reference's SSPRK3 with the exchange as
+            # boundary condition: the SHA-256 of the final interior's bytes
+            a = q.copy()
+            O.ref_amr_ssprk3(sid, nb, nc, ng, per, passes, P.scheme(**kw), a, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS)
+            inner = np.ascontiguousarray(a[:, ng:-ng, ng:-ng, ng:-ng])
+            assert np.all(np.isfinite(inner)), (name, sname)
+            out[name + "_ssprk3_" + sname] = np.frombuffer(hashlib.sha256(inner.tobytes()).digest(), dtype=np.uint8)
     np.savez_compressed(os.path.join(OUT, "amr_flux_ref.npz"), **out)
 
 

@@ -8,10 +8,15 @@ scheme compositions (tests/golden/gen_golden.py).  Here:
 
 * the oracle's per-block-box flux_div reproduces it bit for bit;
 * where the reference harness is built, a third composition too;
+* three SSPRK3 steps composed from the oracle's exchange, flux_div and stage
+  update reproduce the reference's integrator_t run with the exchange as
+  boundary condition (the golden holds the SHA-256 of its final interior;
+  live, where the harness is built, the whole array);
 * gbns_flux_div_blocks rejects malformed layouts before any CUDA call.
 
 The GPU side is tests/test_gpu_amr_flux.py."""
 import ctypes
+import hashlib
 import os
 
 import numpy as np
@@ -21,7 +26,7 @@ from spade_gb300 import _abi, _native
 from oracle import oracle as O
 import problems as P
 from test_amr_exchange import CASES, golden
-from golden.gen_golden import AMR_CASES, AMR_FLUX_SCHEMES, amr_flux_input
+from golden.gen_golden import AMR_CASES, AMR_FLUX_SCHEMES, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS, amr_flux_input
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLD = os.path.join(ROOT, "tests", "golden", "amr_flux_ref.npz")
@@ -65,6 +70,45 @@ def test_oracle_flux_div_blocks_equals_reference_live(case):
     assert np.array_equal(r[inner], want[inner])
 
 
+def oracle_amr_ssprk3(case, s, q, dt, nsteps):
+    """nsteps of SSPRK3 on a refined layout from the oracle's pieces, after
+    one exchange (as the reference's driver refreshes the ghosts first): per
+    stage the residual (flux_div_blocks), the stage update (rk_stage, the
+    ratio_diff coefficients of ssprk3_t) and the exchange, in place."""
+    g = golden(case)
+    grid, boxes, _, ng = layout(case)
+    nc = tuple(int(n) for n in g["ncell"])
+    O.exchange_patches(nc, ng, q.shape[0], g["plan"], q)
+    coeffs = ([dt], [(-3.0 / 4.0) * dt, (1.0 / 4.0) * dt], [(-1.0 / 12.0) * dt, (-1.0 / 12.0) * dt, (2.0 / 3.0) * dt])
+    for _ in range(nsteps):
+        R = [np.zeros_like(q) for _ in range(3)]
+        for k, c in enumerate(coeffs):
+            O.flux_div_blocks(grid, s, boxes, q, R[k], increment=True)
+            O.rk_stage(grid, s.gas, q, R[:k + 1], c)
+            O.exchange_patches(nc, ng, q.shape[0], g["plan"], q)
+    return q
+
+
+def interior_digest(q, ng):
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(q[:, ng:-ng, ng:-ng, ng:-ng]).tobytes()).digest(),
+                         dtype=np.uint8)
+
+
+@pytest.mark.parametrize("scheme", sorted(AMR_FLUX_SCHEMES))
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_amr_ssprk3_equals_reference(case, scheme):
+    _, _, q, ng = layout(case)
+    s = P.scheme(**AMR_FLUX_SCHEMES[scheme][1])
+    a = oracle_amr_ssprk3(case, s, q.copy(), AMR_SSPRK3_DT, AMR_SSPRK3_STEPS)
+    assert np.array_equal(interior_digest(a, ng), np.load(GOLD)[case + "_ssprk3_" + scheme])
+    assert not np.array_equal(a, q)
+    if O.ref_available():
+        nb, nc, ng_, per, passes = AMR_CASES[case]
+        want = q.copy()
+        O.ref_amr_ssprk3(AMR_FLUX_SCHEMES[scheme][0], nb, nc, ng_, per, passes, s, want, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS)
+        assert np.array_equal(a, want)                    # ghost cells included
+
+
 def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
     lib = _native.lib()
     s = P.scheme(conv=_abi.CONV_CENT_KEEP, visc=1)
@@ -86,3 +130,6 @@ def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
     assert call(_abi.grid_desc((2, 1, 1), (4, 4, 4), 1, (0, 1, 0, 1, 0, 1)), boxes,
                 P.scheme(conv=_abi.CONV_FWENO)) == _abi.ERR_INVALID
     assert "ghost layers" in _native.last_error()
+    # the fused step: a missing exchange plan
+    assert lib.gbns_ssprk3_step_blocks(g, s, boxes.ctypes.data_as(ctypes.c_void_p), None, pq, pr,
+                                       ctypes.c_double(1e-4), None) == _abi.ERR_INVALID

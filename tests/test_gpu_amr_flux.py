@@ -2,9 +2,12 @@
 the reference's own results from tests/golden/amr_flux_ref.npz, bit for bit,
 for three layouts refined through cartesian_grid_t::refine_blocks and two
 scheme compositions, in every tile variant; increment mode against the
-oracle; FP32-flux within its normwise bound; and the whole refined-layout
+oracle; FP32-flux within its normwise bound; the whole refined-layout
 path on the device (the reference's exchange plan run by
-gbns_exchange_plan_*, then flux_div) against the reference."""
+gbns_exchange_plan_*, then flux_div) against the reference; and three fused
+SSPRK3 steps (gbns_ssprk3_step_blocks) against the reference's integrator
+run (the SHA-256 of its final interior) and the oracle's steps (the whole
+array, ghost cells included)."""
 import ctypes
 
 import numpy as np
@@ -17,8 +20,8 @@ from spade_gb300 import grid as _grid
 from oracle import oracle as O
 import problems as P
 from test_amr_exchange import CASES, amr_fill, golden
-from test_amr_flux import GOLD, layout
-from golden.gen_golden import AMR_FLUX_SCHEMES
+from test_amr_flux import GOLD, layout, oracle_amr_ssprk3, interior_digest
+from golden.gen_golden import AMR_FLUX_SCHEMES, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS
 
 pytestmark = pytest.mark.gpu
 
@@ -80,3 +83,26 @@ def test_refined_layout_exchange_then_flux_on_the_device(case):
     s = P.scheme(**AMR_FLUX_SCHEMES["ck2_visc"][1])
     r = _flux(grid, s, boxes, qd, np.zeros(tuple(qd.shape)), False)
     assert np.array_equal(r[:, ng:-ng, ng:-ng, ng:-ng], np.load(GOLD)[case + "_ck2_visc"])
+
+
+
+@pytest.mark.parametrize("scheme", sorted(AMR_FLUX_SCHEMES))
+@pytest.mark.parametrize("case", CASES)
+def test_ssprk3_step_blocks_equals_reference(case, scheme):
+    g = golden(case)
+    grid, boxes, q, ng = layout(case)
+    s = P.scheme(**AMR_FLUX_SCHEMES[scheme][1])
+    qd = torch.from_numpy(q.copy()).cuda()
+    work = torch.zeros(3 * q.size, dtype=torch.float64, device="cuda")
+    plan = _grid.exchange_plan_t(g["ncell"], ng, q.shape[0], g["plan"])
+    b = np.ascontiguousarray(boxes)
+    plan.exchange(qd)                                          # the ghosts on entry, as the reference's driver
+    for _ in range(AMR_SSPRK3_STEPS):
+        _native.check(_native.lib().gbns_ssprk3_step_blocks(grid, s, b.ctypes.data_as(ctypes.c_void_p), plan.handle,
+                                                            qd.data_ptr(), work.data_ptr(),
+                                                            ctypes.c_double(AMR_SSPRK3_DT), _st()))
+    torch.cuda.synchronize()
+    plan.close()
+    r = qd.cpu().numpy()
+    assert np.array_equal(interior_digest(r, ng), np.load(GOLD)[case + "_ssprk3_" + scheme])
+    assert np.array_equal(r, oracle_amr_ssprk3(case, s, q.copy(), AMR_SSPRK3_DT, AMR_SSPRK3_STEPS))
