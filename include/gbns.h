@@ -193,6 +193,10 @@ int gbns_flux_div(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
  * `stream`.  Stretched coordinates: GBNS_ERR_UNSUPPORTED. */
 int gbns_flux_div_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
                          const double* prims, double* rhs, int increment, void* stream);
+/* gbns_flux_div_blocks for prims and rhs in host memory, staged through the
+ * device buffers of gbns_flux_div_host (synchronises `stream`). */
+int gbns_flux_div_blocks_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                              const double* host_prims, double* host_rhs, int increment, void* stream);
 
 /* gbns_flux_div for prims and rhs in host memory (a grid_array on
  * device::cpu): both arrays are staged through device buffers the library

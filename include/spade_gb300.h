@@ -486,6 +486,55 @@ namespace spade::gb300
         return g;
     }
 
+    namespace detail
+    {
+        template <typename blocks_t> struct is_refined_blocks : std::false_type {};
+        template <typename val_t, typename desig_t>
+        struct is_refined_blocks<amr::amr_blocks_t<val_t, desig_t>> : std::true_type {};
+    }
+
+    // A grid_array on a refined (AMR) grid -> gbns_grid_desc with
+    // nblk = (blocks, 1, 1) in global block order and each block's bounding
+    // box (6 doubles: min, max per direction) for gbns_flux_div_blocks; the
+    // reference's flux_div takes 1/dx from that box (flux_div_basic.h:55,
+    // grid/grid_geometry.h:85-89).
+    template <typename arr_t>
+    gbns_grid_desc lower_refined_grid(const arr_t& arr, std::vector<double>& boxes)
+    {
+        const auto& grid = arr.get_grid();
+        using coord_t = typename utils::remove_all<decltype(grid.get_coord_sys())>::type;
+        static_assert(std::is_same_v<typename arr_t::value_type, double>, "the GB300 path works on double arrays");
+        if (grid.get_num_local_blocks() != grid.get_num_global_blocks())
+            throw except::sp_exception("gb300 flux_div: the grid must hold every block on this device");
+        const std::size_t nblk = grid.get_num_global_blocks();
+        gbns_grid_desc g{};
+        const auto bnd = grid.get_bounds();
+        g.nblk[0] = int(nblk);
+        g.nblk[1] = g.nblk[2] = 1;
+        for (int d = 0; d < 3; ++d)
+        {
+            g.ncell[d] = grid.get_num_cells(d);
+            g.bounds[2*d] = bnd.min(d);
+            g.bounds[2*d + 1] = bnd.max(d);
+        }
+        const int ng = arr.get_num_exchange(0);
+        if (arr.get_num_exchange(1) != ng || arr.get_num_exchange(2) != ng)
+            throw except::sp_exception("gb300 flux_div: equal ghost depth in every direction required");
+        g.ng = ng;
+        detail::lower_coords<coord_t>::apply(g, grid.get_coord_sys());
+        boxes.assign(6*nblk, 0.0);
+        for (std::size_t lb = 0; lb < nblk; ++lb)
+        {
+            const auto b = grid.get_bounding_box(utils::tag[partition::global](lb));
+            for (int d = 0; d < 3; ++d)
+            {
+                boxes[6*lb + 2*d] = b.min(d);
+                boxes[6*lb + 2*d + 1] = b.max(d);
+            }
+        }
+        return g;
+    }
+
     template <typename traits_t>
     concept selects_gb300 = requires { typename detail::fdiv_tag_of<traits_t>; } &&
                             std::same_as<detail::fdiv_tag_of<traits_t>, pde_algs::tgb300_t>;
@@ -517,10 +566,41 @@ namespace spade::pde_algs
         using namespace sym::literals;
         const auto& incr = algs::get_trait(traits, "pde_increment"_sym, increment);
         using incr_mode_t = typename utils::remove_all<decltype(incr)>::type;
-        const gbns_grid_desc g = gb300::lower_grid(prims);
         const gbns_scheme_desc s = gb300::lower_scheme(flux_func, gb300::precision_of<alg_traits_t>());
         const double* q = prims.image().base;
         double* r = rhs.image().base;
+        using blocks_t = typename utils::remove_all<decltype(prims.get_grid().get_blocks())>::type;
+        if constexpr (gb300::detail::is_refined_blocks<blocks_t>::value)
+        {
+            // refined layout: every block's own spacing (gbns_flux_div_blocks)
+            std::vector<double> boxes;
+            const gbns_grid_desc g = gb300::lower_refined_grid(prims, boxes);
+            int rc = GBNS_OK;
+#ifdef GBNS_DROPIN_HOOK
+            rc = GBNS_ERR_UNSUPPORTED;
+#else
+            constexpr bool on_gpu = device::is_gpu<typename sol_arr_t::device_type>;
+            static_assert(on_gpu == device::is_gpu<typename rhs_arr_t::device_type>,
+                          "the gb300 flux_div takes prims and rhs on the same device kind");
+            if constexpr (on_gpu)
+            {
+                rc = gbns_flux_div_blocks(&g, &s, boxes.data(), q, r, incr_mode_t::increment_mode ? 1 : 0, nullptr);
+                if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+            }
+            else
+                rc = gbns_flux_div_blocks_host(&g, &s, boxes.data(), q, r, incr_mode_t::increment_mode ? 1 : 0, nullptr);
+#endif
+            if (rc != GBNS_OK)
+            {
+                char msg[512] = "refined layouts are not routed to the drop-in hook";
+#ifndef GBNS_DROPIN_HOOK
+                gbns_last_error(msg, sizeof(msg));
+#endif
+                throw except::sp_exception(std::string("gb300 flux_div failed: ") + msg);
+            }
+            return;
+        }
+        const gbns_grid_desc g = gb300::lower_grid(prims);
 #ifdef GBNS_DROPIN_HOOK
         const int rc = GBNS_DROPIN_HOOK(&g, &s, q, r, incr_mode_t::increment_mode ? 1 : 0);
 #else

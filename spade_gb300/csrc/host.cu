@@ -509,20 +509,20 @@ extern "C"
         return rc ? rc : frc;
     }
 
-    int gbns_flux_div_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
-                           const double* host_prims, double* host_rhs, int increment, void* stream)
+    // Runs fn(ctx, q, r) on device copies of host prims and rhs (count
+    // doubles each) and copies rhs back: one pair of staging arrays per
+    // device, grown on demand; the lock covers the whole call so concurrent
+    // host-path calls never share them.  Synchronises `stream`.
+    typedef int (*staged_fn)(void* ctx, const double* q, double* r);
+    static int host_staged(size_t count, const double* host_prims, double* host_rhs, void* stream, staged_fn fn,
+                           void* ctx)
     {
         using namespace gbns;
         if (!host_prims || !host_rhs) return set_error(GBNS_ERR_INVALID, "prims/rhs pointer is NULL");
         if (host_prims == host_rhs) return set_error(GBNS_ERR_INVALID, "prims and rhs must not alias");
-        size_t count = 0;
-        int rc = gbns_array_size(grid, &count);
-        if (rc) return rc;
         int dev = 0;
-        rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+        int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
         if (rc) return rc;
-        // one pair of staging arrays per device, grown on demand; the lock
-        // covers the whole call so concurrent host-path calls never share them
         struct Staging { double* q = nullptr; double* r = nullptr; size_t count = 0; };
         static std::mutex mu;
         static Staging staging[64];
@@ -554,10 +554,48 @@ extern "C"
         rc = check_cuda(cudaMemcpyAsync(sg.q, host_prims, bytes, cudaMemcpyHostToDevice, st), "prims to device");
         // rhs goes down in both modes: overwrite leaves its ghost layers as they were
         if (!rc) rc = check_cuda(cudaMemcpyAsync(sg.r, host_rhs, bytes, cudaMemcpyHostToDevice, st), "rhs to device");
-        if (!rc) rc = gbns_flux_div(grid, scheme, sg.q, sg.r, increment, stream);
+        if (!rc) rc = fn(ctx, sg.q, sg.r);
         if (!rc) rc = check_cuda(cudaMemcpyAsync(host_rhs, sg.r, bytes, cudaMemcpyDeviceToHost, st), "rhs to host");
         if (!rc) rc = check_cuda(cudaStreamSynchronize(st), "host-path sync");
         return rc;
+    }
+
+    int gbns_flux_div_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                           const double* host_prims, double* host_rhs, int increment, void* stream)
+    {
+        size_t count = 0;
+        const int rc = gbns_array_size(grid, &count);
+        if (rc) return rc;
+        struct Ctx { const gbns_grid_desc* g; const gbns_scheme_desc* s; int incr; void* st; } c{grid, scheme, increment, stream};
+        return host_staged(count, host_prims, host_rhs, stream, [](void* p, const double* q, double* r) -> int
+        {
+            const Ctx& c = *static_cast<const Ctx*>(p);
+            return gbns_flux_div(c.g, c.s, q, r, c.incr, c.st);
+        }, &c);
+    }
+
+    int gbns_flux_div_blocks_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,
+                                  const double* block_bounds, const double* host_prims, double* host_rhs,
+                                  int increment, void* stream)
+    {
+        using namespace gbns;
+        if (!grid) return set_error(GBNS_ERR_INVALID, "grid descriptor is NULL");
+        const int nblk = grid->nblk[0];
+        if (nblk < 1 || nblk > 65535 || grid->nblk[1] != 1 || grid->nblk[2] != 1)
+            return set_error(GBNS_ERR_INVALID, "a refined layout's blocks are given as nblk = (1..65535, 1, 1)");
+        gbns_grid_desc one = *grid;
+        one.nblk[0] = 1;
+        size_t per_block = 0;
+        const int rc = gbns_array_size(&one, &per_block);
+        if (rc) return rc;
+        struct Ctx { const gbns_grid_desc* g; const gbns_scheme_desc* s; const double* b; int incr; void* st; }
+            c{grid, scheme, block_bounds, increment, stream};
+        return host_staged(per_block*size_t(nblk), host_prims, host_rhs, stream,
+                           [](void* p, const double* q, double* r) -> int
+        {
+            const Ctx& c = *static_cast<const Ctx*>(p);
+            return gbns_flux_div_blocks(c.g, c.s, c.b, q, r, c.incr, c.st);
+        }, &c);
     }
 
     int gbns_flux_div_variant(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme,

@@ -43,3 +43,29 @@ int gbns_last_error(char* buf, size_t len)
     if (buf && len) snprintf(buf, len, "recording stand-in");
     return 0;
 }
+
+/* gbns_flux_div_blocks_host calls (refined layouts) go to the file named by
+ * GBNS_RECORD_BLOCKS as the record above with, after the increment flag,
+ *   u64 nblocks, 6*nblocks doubles of block bounds,
+ * then count and the two arrays. */
+int gbns_flux_div_blocks_host(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
+                              const double* host_prims, double* host_rhs, int increment, void* stream)
+{
+    (void)stream;
+    const char* path = getenv("GBNS_RECORD_BLOCKS");
+    if (!path) return GBNS_ERR_INVALID;
+    FILE* f = fopen(path, "ab");
+    if (!f) return GBNS_ERR_INVALID;
+    const unsigned long long gs = sizeof(*grid), ss = sizeof(*scheme);
+    const unsigned long long nb = (unsigned long long)grid->nblk[0];
+    const unsigned long long n = array_doubles(grid);
+    const int incr = increment;
+    fwrite(&gs, 8, 1, f); fwrite(grid, 1, gs, f);
+    fwrite(&ss, 8, 1, f); fwrite(scheme, 1, ss, f);
+    fwrite(&incr, 4, 1, f);
+    fwrite(&nb, 8, 1, f); fwrite(block_bounds, 8, 6*nb, f);
+    fwrite(&n, 8, 1, f);
+    fwrite(host_prims, 8, n, f); fwrite(host_rhs, 8, n, f);
+    fclose(f);
+    return GBNS_OK;
+}

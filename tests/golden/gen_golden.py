@@ -318,6 +318,87 @@ def gen_dropin():
     np.savez_compressed(os.path.join(OUT, "dropin_ref.npz"), **out)
 
 
+def dropin_noise_state(n):
+    """The seeded state of tests/cpp/dropin_amr_record.cc over n doubles
+    (splitmix64 noise per index; the same operations in the same order)."""
+    i = np.arange(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        k = i + np.uint64(0x9E3779B97F4A7C15)
+        k = (k ^ (k >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        k = (k ^ (k >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        k = k ^ (k >> np.uint64(31))
+    nz = (k >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0) - 0.5
+    q = np.empty(n)
+    q[0::5] = 1.0e5 * (1.0 + 0.02 * nz[0::5])
+    q[1::5] = 300.0 * (1.0 + 0.02 * nz[1::5])
+    q[2::5] = 30.0 * nz[2::5]
+    q[3::5] = 30.0 * nz[3::5]
+    q[4::5] = 30.0 * nz[4::5]
+    return q
+
+
+def read_dropin_blocks_records(path):
+    """Parses the gbns_flux_div_blocks_host calls the stand-in recorded."""
+    import struct
+    d = open(path, "rb").read()
+    pos, out = 0, []
+    while pos < len(d):
+        gs = struct.unpack_from("<Q", d, pos)[0]; pos += 8
+        gb = d[pos:pos + gs]; pos += gs
+        ss = struct.unpack_from("<Q", d, pos)[0]; pos += 8
+        sb = d[pos:pos + ss]; pos += ss
+        incr = struct.unpack_from("<i", d, pos)[0]; pos += 4
+        nb = struct.unpack_from("<Q", d, pos)[0]; pos += 8
+        boxes = np.frombuffer(d, dtype=np.float64, count=6 * nb, offset=pos).reshape(nb, 6).copy(); pos += 48 * nb
+        n = struct.unpack_from("<Q", d, pos)[0]; pos += 8
+        q = np.frombuffer(d, dtype=np.float64, count=n, offset=pos).copy(); pos += 8 * n
+        r = np.frombuffer(d, dtype=np.float64, count=n, offset=pos).copy(); pos += 8 * n
+        out.append((gb, sb, incr, boxes, q, r))
+    return out
+
+
+def gen_dropin_amr():
+    """The C++ drop-in on a refined grid (tests/cpp/dropin_amr_record.cc),
+    linked with the recording stand-in: the lowered gbns_flux_div_blocks_host
+    calls (descriptors, boxes) and the reference's own flux_div interiors.
+    The state is rebuilt by the tests from the seeded noise and the
+    reference's exchange plan of the same layout (AMR_CASES
+    one_level_periodic); checked here against the recorded arrays."""
+    import subprocess
+    import tempfile
+    from __graft_entry__ import ref_src
+    src = ref_src()
+    with tempfile.TemporaryDirectory() as d:
+        stub = os.path.join(d, "stub.o")
+        exe = os.path.join(d, "dropin_amr_record")
+        subprocess.run(["gcc", "-O1", "-c", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "gbns_record_stub.c"), "-o", stub], check=True)
+        subprocess.run(["g++", "-std=c++20", "-O1", "-I" + src, "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(ROOT, "oracle", "mpi_stub"), "-I/usr/local/cuda/include",
+                        os.path.join(ROOT, "tests", "cpp", "dropin_amr_record.cc"), stub, "-o", exe], check=True)
+        rec, res = os.path.join(d, "calls.bin"), os.path.join(d, "ref.bin")
+        subprocess.run([exe, res], check=True, env=dict(os.environ, GBNS_RECORD_BLOCKS=rec))
+        calls = read_dropin_blocks_records(rec)
+        refs = np.fromfile(res)
+    assert len(calls) == 2
+    amr = np.load(os.path.join(OUT, "amr_ref.npz"))
+    nb, nc, ng, per, passes = AMR_CASES["one_level_periodic"]
+    q = dropin_noise_state(calls[0][4].size).reshape(-1, nc[2] + 2 * ng, nc[1] + 2 * ng, nc[0] + 2 * ng, 5)
+    O.exchange_patches(nc, ng, q.shape[0], amr["one_level_periodic_plan"], q)
+    refs = refs.reshape(2, *q.shape)
+    out = {}
+    for k, (gb, sb, incr, boxes, qr, r) in enumerate(calls):
+        assert np.array_equal(qr, q.ravel())                   # the state is rebuilt exactly
+        assert np.array_equal(boxes, amr["one_level_periodic_boxes"])
+        assert np.all(r == (0.0 if k == 0 else 0.25))
+        out["grid%d" % k] = np.frombuffer(gb, dtype=np.uint8)
+        out["scheme%d" % k] = np.frombuffer(sb, dtype=np.uint8)
+        out["incr%d" % k] = np.int32(incr)
+        out["rhs_fill%d" % k] = np.float64(0.0 if k == 0 else 0.25)
+        out["ref%d" % k] = refs[k][:, ng:-ng, ng:-ng, ng:-ng].copy()
+    np.savez_compressed(os.path.join(OUT, "dropin_amr_ref.npz"), **out)
+
+
 if __name__ == "__main__":
     if not O.ref_available():
         sys.exit("reference harness not built: make -C oracle ref")
@@ -329,6 +410,7 @@ if __name__ == "__main__":
     gen_amr()
     gen_amr_flux()
     gen_dropin()
+    gen_dropin_amr()
     for f in sorted(os.listdir(OUT)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(OUT, f)))

@@ -143,3 +143,68 @@ def test_recorded_dropin_calls_reproduce_the_reference_on_the_oracle():
         r = g["rhs_in%d" % k].reshape(shape).copy()
         O.flux_div(grid, s, q, r, increment=bool(g["incr%d" % k]))
         assert np.array_equal(r.ravel(), g["ref"][k]), k
+
+
+def refined_dropin_call(k):
+    """Call k of tests/golden/dropin_amr_ref.npz (the drop-in on a refined
+    grid, recorded by tests/cpp/dropin_amr_record.cc): its descriptors, block
+    boxes, the rebuilt state (seeded noise, then the reference's exchange plan
+    of the same layout), the rhs the call started from, its increment flag,
+    ghost depth and the reference's interior result."""
+    import numpy as np
+    from spade_gb300 import _abi
+    from oracle import oracle as O
+    from golden.gen_golden import AMR_CASES, dropin_noise_state
+    g = np.load(os.path.join(ROOT, "tests", "golden", "dropin_amr_ref.npz"))
+    amr = np.load(os.path.join(ROOT, "tests", "golden", "amr_ref.npz"))
+    grid = _abi.GridDesc.from_buffer_copy(g["grid%d" % k].tobytes())
+    s = _abi.SchemeDesc.from_buffer_copy(g["scheme%d" % k].tobytes())
+    nb, nc, ng, per, passes = AMR_CASES["one_level_periodic"]
+    assert tuple(grid.ncell) == tuple(nc) and grid.ng == ng and tuple(grid.nblk)[1:] == (1, 1)
+    shape = (grid.nblk[0], nc[2] + 2 * ng, nc[1] + 2 * ng, nc[0] + 2 * ng, 5)
+    q = dropin_noise_state(int(np.prod(shape))).reshape(shape)
+    O.exchange_patches(nc, ng, shape[0], amr["one_level_periodic_plan"], q)
+    r = np.full(shape, float(g["rhs_fill%d" % k]))
+    return grid, s, amr["one_level_periodic_boxes"], q, r, int(g["incr%d" % k]), ng, g["ref%d" % k]
+
+
+def test_refined_dropin_calls_reproduce_the_reference_on_the_oracle():
+    """The drop-in at a SPADE call site on a refined (amr_blocks_t) grid lowers
+    to gbns_flux_div_blocks_host with nblk = (15, 1, 1) and the grid's own
+    block boxes; run by the oracle, both recorded calls (overwrite and
+    increment) give the reference's CPU flux_div bit for bit."""
+    import numpy as np
+    from oracle import oracle as O
+    for k in range(2):
+        grid, s, boxes, q, r, incr, ng, want = refined_dropin_call(k)
+        assert grid.nblk[0] == 15
+        O.flux_div_blocks(grid, s, boxes, q, r, increment=bool(incr))
+        assert np.array_equal(r[:, ng:-ng, ng:-ng, ng:-ng], want), k
+
+
+@pytest.mark.skipif(not REF_SRC, reason="reference sources not present")
+def test_refined_dropin_records_match_the_golden():
+    """tests/cpp/dropin_amr_record.cc built here against the reference's
+    headers and the recording stand-in makes exactly the recorded calls:
+    the same descriptors, block boxes and arrays, and the reference's result."""
+    import numpy as np
+    from golden.gen_golden import read_dropin_blocks_records
+    g = np.load(os.path.join(ROOT, "tests", "golden", "dropin_amr_ref.npz"))
+    with tempfile.TemporaryDirectory() as d:
+        stub, exe = os.path.join(d, "stub.o"), os.path.join(d, "rec")
+        subprocess.run(["gcc", "-O1", "-c", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "gbns_record_stub.c"), "-o", stub], check=True)
+        subprocess.run(["g++", "-std=c++20", "-O1", "-I" + REF_SRC, "-I" + os.path.join(ROOT, "include"),
+                        "-I" + os.path.join(ROOT, "oracle", "mpi_stub"), "-I" + CUDA_INC,
+                        os.path.join(ROOT, "tests", "cpp", "dropin_amr_record.cc"), stub, "-o", exe], check=True)
+        rec, res = os.path.join(d, "calls.bin"), os.path.join(d, "ref.bin")
+        subprocess.run([exe, res], check=True, env=dict(os.environ, GBNS_RECORD_BLOCKS=rec))
+        calls = read_dropin_blocks_records(rec)
+        refs = np.fromfile(res)
+    assert len(calls) == 2
+    for k, (gb, sb, incr, boxes, q, r) in enumerate(calls):
+        grid, s, boxes_g, q_g, r_g, incr_g, ng, want = refined_dropin_call(k)
+        assert gb == g["grid%d" % k].tobytes() and sb == g["scheme%d" % k].tobytes() and incr == incr_g
+        assert np.array_equal(boxes, boxes_g) and np.array_equal(q, q_g.ravel()) and np.array_equal(r, r_g.ravel())
+        ref = refs.reshape(2, *q_g.shape)[k]
+        assert np.array_equal(ref[:, ng:-ng, ng:-ng, ng:-ng], want)

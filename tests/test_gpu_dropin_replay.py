@@ -15,7 +15,9 @@ through the real library on the GPU:
   reference's result;
 * the benchmarked channel scheme (gb300::weno5_t, pressure_diss_lr,
   visc_lr(gb300::sutherland_t)) on a gb300::tanh_stretch_1D grid, which the
-  reference cannot run: bit-identical to the oracle."""
+  reference cannot run: bit-identical to the oracle;
+* on a refined (amr_blocks_t) grid (tests/cpp/dropin_amr_record.cc,
+  gbns_flux_div_blocks_host): bit-identical to the reference's result."""
 import os
 
 import numpy as np
@@ -56,3 +58,15 @@ def test_dropin_channel_scheme_on_the_gpu_equals_the_oracle():
     _native.check(_native.lib().gbns_flux_div_host(grid, s, q.ctypes.data, r.ctypes.data, incr, None))
     assert np.isfinite(r).all()
     assert np.array_equal(r, want)
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_refined_dropin_calls_on_the_gpu_equal_the_reference(k):
+    """The drop-in's calls on a refined grid (tests/cpp/dropin_amr_record.cc,
+    gbns_flux_div_blocks_host with the grid's own block boxes) through the
+    real library: the reference's CPU flux_div bit for bit."""
+    from test_cpp_dropin import refined_dropin_call
+    grid, s, boxes, q, r, incr, ng, want = refined_dropin_call(k)
+    b = np.ascontiguousarray(boxes)
+    _native.check(_native.lib().gbns_flux_div_blocks_host(grid, s, b.ctypes.data, q.ctypes.data, r.ctypes.data, incr, None))
+    assert np.array_equal(r[:, ng:-ng, ng:-ng, ng:-ng], want)
