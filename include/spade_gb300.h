@@ -1021,4 +1021,60 @@ namespace spade::gb300
         arr_t& solution() { return q; }
         double time() const { return t; }
     };
+
+    // integrator_t with ssprk3_t on a refined (amr_blocks_t) grid, its exchange
+    // as the boundary condition (the reference's drivers: integrator_t whose bc
+    // runs handle.exchange, time-integration/advance.h:234-280): one
+    // gbns_ssprk3_step_blocks per advance() with the grid's own block boxes and
+    // the plan lowered from the reference's exchange handle
+    // (exchange_plan_t).  device::gpu arrays; q must hold exchanged ghosts
+    // (plan.exchange(q)) before the first step, as the reference's driver
+    // refreshes them.
+    template <typename arr_t, typename flux_func_t>
+    struct ssprk3_refined_integrator_t
+    {
+        arr_t& q;
+        const exchange_plan_t& plan;
+        std::vector<double> boxes;
+        gbns_grid_desc grid;
+        gbns_scheme_desc scheme;
+        double dt;
+        double t;
+        double* work = nullptr;
+
+        ssprk3_refined_integrator_t(arr_t& q_in, const flux_func_t& flux, const exchange_plan_t& plan_in, double dt_in,
+                                    double t0 = 0.0, int precision = GBNS_PREC_FP64)
+            : q{q_in}, plan{plan_in}, grid{lower_refined_grid(q_in, boxes)}, scheme{lower_scheme(flux, precision)},
+              dt{dt_in}, t{t0}
+        {
+#ifndef GBNS_DROPIN_HOOK
+            static_assert(device::is_gpu<typename arr_t::device_type>, "the gb300 integrator runs on device::gpu arrays");
+            const size_t n = size_t(5)*size_t(grid.nblk[0])*size_t(grid.ncell[0] + 2*grid.ng)*
+                             size_t(grid.ncell[1] + 2*grid.ng)*size_t(grid.ncell[2] + 2*grid.ng);
+            if (cudaMalloc(&work, 3*n*sizeof(double)) != cudaSuccess)
+                throw except::sp_exception("gb300 integrator: cannot allocate its scratch arrays");
+#endif
+        }
+        ssprk3_refined_integrator_t(const ssprk3_refined_integrator_t&) = delete;
+        ssprk3_refined_integrator_t& operator=(const ssprk3_refined_integrator_t&) = delete;
+        ~ssprk3_refined_integrator_t()
+        {
+#ifndef GBNS_DROPIN_HOOK
+            if (work) cudaFree(work);
+#endif
+        }
+
+        void advance()
+        {
+#ifndef GBNS_DROPIN_HOOK
+            int rc = gbns_ssprk3_step_blocks(&grid, &scheme, boxes.data(), plan.plan, q.image().base, work, dt, nullptr);
+            if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
+            detail::check_call(rc, "gb300 ssprk3 step failed: ");
+#endif
+            t += dt;
+        }
+
+        arr_t& solution() { return q; }
+        double time() const { return t; }
+    };
 }
