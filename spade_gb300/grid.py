@@ -233,6 +233,41 @@ class exchange_plan_t:
             pass
 
 
+class refined_layout_t:
+    """A refined (AMR) block layout as the GB300 kernels take it: nblocks
+    blocks of the same ncell cells and ng ghost layers, in the caller's
+    global block order, each with its bounding box (boxes: (nblocks, 6),
+    min and max along x, y, z), identity coordinates.  The block tree stays
+    the caller's (the reference's amr_blocks_t refined with
+    cartesian_grid_t::refine_blocks); every block takes 1/dx from its own box
+    as the reference's flux_div does (flux_div_basic.h:55,
+    grid/grid_geometry.h:85-89).  Arrays on it are float64 tensors of shape
+    (nblocks, nz+2ng, ny+2ng, nx+2ng, 5)."""
+
+    def __init__(self, ncell, ng, boxes):
+        self.ncell = tuple(int(n) for n in ncell)
+        self.ng = int(ng)
+        self.boxes = np.ascontiguousarray(boxes, dtype=np.float64)
+        if self.boxes.ndim != 2 or self.boxes.shape[1] != 6:
+            raise ValueError("boxes must be (nblocks, 6)")
+        self.nblocks = int(self.boxes.shape[0])
+        self._desc = _abi.grid_desc((self.nblocks, 1, 1), self.ncell, self.ng, (0.0, 1.0, 0.0, 1.0, 0.0, 1.0))
+
+    def desc(self):
+        return self._desc
+
+    def shape(self):
+        ng = self.ng
+        return (self.nblocks, self.ncell[2] + 2 * ng, self.ncell[1] + 2 * ng, self.ncell[0] + 2 * ng, 5)
+
+    def check(self, t):
+        if tuple(t.shape) != self.shape() or t.dtype != torch.float64 or not t.is_contiguous():
+            raise ValueError("expected a contiguous float64 array of shape %s" % (self.shape(),))
+
+    def boxes_ptr(self):
+        return ctypes.c_void_p(self.boxes.ctypes.data)
+
+
 def make_exchange(q, periodic):
     h = arr_exchange_t(periodic)
     q.periodic = h.periodic

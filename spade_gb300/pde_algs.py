@@ -4,7 +4,7 @@ boundary_flux, lowered onto libgbns.so."""
 import ctypes
 
 from . import _abi, _native, convective, viscous, omni
-from .grid import _stream
+from .grid import _stream, refined_layout_t
 
 
 class _trait:
@@ -91,6 +91,41 @@ def lower(flux_func, precision=_abi.PREC_FP64):
     return s
 
 
+def _traits(traits):
+    inc, prec = True, _abi.PREC_FP64
+    for t in traits or ():
+        lab = getattr(t, "trait_label", None)
+        if lab == "pde_increment":
+            inc = t.increment_mode
+        elif lab == "flux_precision":
+            prec = t.precision
+        elif lab != "flux_div":
+            raise ValueError("unknown trait %r" % (t,))
+    return inc, prec
+
+
+def flux_div_refined(layout, prims, rhs, flux_func, traits=None, stream=None):
+    """rhs (+)= div F(prims) on a refined layout (grid.refined_layout_t):
+    pde_algs::flux_div on an amr_blocks_t grid, every block with its own
+    spacing (gbns_flux_div_blocks; gbns_flux_div_blocks_host for CPU
+    tensors, which returns with rhs updated).  prims must hold the ghost
+    values of the layout's exchange (grid.exchange_plan_t)."""
+    if not isinstance(layout, refined_layout_t):
+        raise TypeError("layout must be a grid.refined_layout_t")
+    inc, prec = _traits(traits)
+    layout.check(prims)
+    layout.check(rhs)
+    scheme = flux_func if isinstance(flux_func, _abi.SchemeDesc) else lower(flux_func, prec)
+    args = (layout.desc(), scheme, layout.boxes_ptr(), ctypes.c_void_p(prims.data_ptr()), ctypes.c_void_p(rhs.data_ptr()),
+            int(inc))
+    if prims.device.type == "cpu" and rhs.device.type == "cpu":
+        _native.check(_native.lib().gbns_flux_div_blocks_host(*args, None))
+    elif prims.is_cuda and rhs.is_cuda:
+        _native.check(_native.lib().gbns_flux_div_blocks(*args, _stream(stream)))
+    else:
+        raise ValueError("prims and rhs must both be on the CPU or both on the GPU")
+
+
 def flux_div(prims, rhs, flux_func, traits=None, stream=None, variant=0):
     """rhs (+)= div F(prims): pde_algs::flux_div(prims, rhs, flux_func[, traits]).
     Default increment mode like the reference; pass
@@ -98,19 +133,7 @@ def flux_div(prims, rhs, flux_func, traits=None, stream=None, variant=0):
     current torch stream for device arrays; arrays on the CPU are staged
     through the GPU (gbns_flux_div_host) and the call returns with rhs
     updated."""
-    traits = traits or ()
-    inc = True
-    prec = _abi.PREC_FP64
-    for t in traits:
-        lab = getattr(t, "trait_label", None)
-        if lab == "pde_increment":
-            inc = t.increment_mode
-        elif lab == "flux_precision":
-            prec = t.precision
-        elif lab == "flux_div":
-            pass
-        else:
-            raise ValueError("unknown trait %r" % (t,))
+    inc, prec = _traits(traits)
     if prims.shape != rhs.shape or prims.grid is not rhs.grid and prims.shape != rhs.shape:
         raise ValueError("prims and rhs must live on the same grid")
     scheme = flux_func if isinstance(flux_func, _abi.SchemeDesc) else lower(flux_func, prec)

@@ -14,7 +14,7 @@ from fractions import Fraction as F
 import torch
 
 from . import _native
-from .grid import grid_array, _stream
+from .grid import grid_array, _stream, refined_layout_t
 
 
 class rk_t:
@@ -167,3 +167,28 @@ class ssprk3_stepper:
         _native.check(_native.lib().gbns_ssprk3_step_host(self.q.desc(), self.scheme, self.bc, host_q.data_ptr(),
                                                           self.q.ptr(), self.work.data_ptr(), ctypes.c_double(self.dt),
                                                           int(ngroups), st, cs))
+
+
+class ssprk3_refined_stepper:
+    """integrator_t with ssprk3_t on a refined layout (grid.refined_layout_t),
+    the layout's exchange (grid.exchange_plan_t) as the boundary condition:
+    one gbns_ssprk3_step_blocks per step, the stage updates fused into the
+    flux launches.  q: a CUDA float64 tensor of the layout's shape holding
+    exchanged ghosts (plan.exchange(q) before the first step, as the
+    reference's driver refreshes them)."""
+
+    def __init__(self, layout, q, scheme_desc, plan, dt):
+        if not isinstance(layout, refined_layout_t):
+            raise TypeError("layout must be a grid.refined_layout_t")
+        layout.check(q)
+        if not q.is_cuda:
+            raise ValueError("the refined-layout step runs on CUDA tensors")
+        self.layout, self.q, self.scheme, self.plan, self.dt = layout, q, scheme_desc, plan, float(dt)
+        self.work = torch.zeros(3 * q.numel(), dtype=torch.float64, device=q.device)
+
+    def step(self, nsteps=1, stream=None):
+        for _ in range(nsteps):
+            _native.check(_native.lib().gbns_ssprk3_step_blocks(
+                self.layout.desc(), self.scheme, self.layout.boxes_ptr(), self.plan.handle,
+                ctypes.c_void_p(self.q.data_ptr()), ctypes.c_void_p(self.work.data_ptr()), ctypes.c_double(self.dt),
+                _stream(stream)))

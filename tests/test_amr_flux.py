@@ -133,3 +133,18 @@ def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
     # the fused step: a missing exchange plan
     assert lib.gbns_ssprk3_step_blocks(g, s, boxes.ctypes.data_as(ctypes.c_void_p), None, pq, pr,
                                        ctypes.c_double(1e-4), None) == _abi.ERR_INVALID
+
+
+def test_refined_layout_python_checks():
+    """grid.refined_layout_t: descriptor and array shape of a layout; arrays of
+    another shape are refused before any library call."""
+    import torch
+    from spade_gb300 import grid as G, pde_algs
+    _, boxes, q, ng = layout("anisotropic_blocks")
+    lay = G.refined_layout_t((8, 4, 4), ng, boxes)
+    assert tuple(lay.desc().nblk) == (q.shape[0], 1, 1) and lay.shape() == q.shape
+    bad = torch.zeros((q.shape[0] - 1,) + q.shape[1:], dtype=torch.float64)
+    with pytest.raises(ValueError):
+        pde_algs.flux_div_refined(lay, bad, bad.clone(), P.scheme())
+    with pytest.raises(ValueError):
+        G.refined_layout_t((8, 4, 4), ng, boxes[:, :4])

@@ -106,3 +106,30 @@ def test_ssprk3_step_blocks_equals_reference(case, scheme):
     r = qd.cpu().numpy()
     assert np.array_equal(interior_digest(r, ng), np.load(GOLD)[case + "_ssprk3_" + scheme])
     assert np.array_equal(r, oracle_amr_ssprk3(case, s, q.copy(), AMR_SSPRK3_DT, AMR_SSPRK3_STEPS))
+
+
+def test_python_api_on_refined_layouts():
+    """The Python mirror: pde_algs.flux_div_refined on CUDA and CPU tensors
+    (gbns_flux_div_blocks / _host) and time_integration.ssprk3_refined_stepper
+    give the reference's results."""
+    from spade_gb300 import pde_algs, time_integration
+    case = "two_levels_walls_y"
+    g = golden(case)
+    _, boxes, q, ng = layout(case)
+    lay = _grid.refined_layout_t(g["ncell"], ng, boxes)
+    s = P.scheme(**AMR_FLUX_SCHEMES["ck2_visc"][1])
+    want = np.load(GOLD)[case + "_ck2_visc"]
+    for dev in ("cuda", "cpu"):
+        qt = torch.from_numpy(q.copy()).to(dev)
+        rt = torch.zeros_like(qt)
+        pde_algs.flux_div_refined(lay, qt, rt, s, traits=(pde_algs.overwrite,))
+        torch.cuda.synchronize()
+        assert np.array_equal(rt.cpu().numpy()[:, ng:-ng, ng:-ng, ng:-ng], want), dev
+    plan = _grid.exchange_plan_t(g["ncell"], ng, q.shape[0], g["plan"])
+    qd = torch.from_numpy(q.copy()).cuda()
+    plan.exchange(qd)
+    st = time_integration.ssprk3_refined_stepper(lay, qd, s, plan, AMR_SSPRK3_DT)
+    st.step(AMR_SSPRK3_STEPS)
+    torch.cuda.synchronize()
+    plan.close()
+    assert np.array_equal(interior_digest(qd.cpu().numpy(), ng), np.load(GOLD)[case + "_ssprk3_ck2_visc"])
