@@ -379,7 +379,8 @@ int gbns_exchange_plan_destroy(gbns_exchange_plan* plan);
 /* One SSPRK3 step on a refined (AMR) layout: integrator_t::advance with
  * ssprk3_t and the conservative-variable state transform
  * (time-integration/advance.h:234-280), with the layout's exchange as the
- * boundary condition, as the reference's drivers pair them.  grid and
+ * boundary condition (then, with bc, the wall fill of gbns_wall_fill_blocks;
+ * bc may be NULL), as the reference's drivers pair them.  grid and
  * block_bounds as for gbns_flux_div_blocks; plan the layout's exchange
  * (created for grid->ncell, grid->ng and grid->nblk[0] blocks).  Each stage
  * is one flux launch with the stage update fused (as gbns_ssprk3_step), then
@@ -390,7 +391,17 @@ int gbns_exchange_plan_destroy(gbns_exchange_plan* plan);
  * of prims' size.  Asynchronous on `stream` (the per-block table is copied
  * from pageable memory: not for stream capture). */
 int gbns_ssprk3_step_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
-                            gbns_exchange_plan* plan, double* prims, double* work, double dt, void* stream);
+                            gbns_exchange_plan* plan, const gbns_bc_desc* bc, double* prims, double* work, double dt,
+                            void* stream);
+/* The wall faces of a refined layout: for every face whose bc kind is a wall
+ * (GBNS_BC_ISOTHERMAL_NOSLIP, GBNS_BC_SLIP_ADIABATIC), in face order, the blocks
+ * whose box touches that domain face (block_bounds against grid->bounds) get
+ * their ghost slab (ng layers, the full padded extent across) mirrored from
+ * their own cells with the wall kernel: the reference's algs::boundary_fill
+ * (grid/boundary_fill.h:31-133) after its exchange.  Other faces are left
+ * alone.  Asynchronous on `stream`. */
+int gbns_wall_fill_blocks(const gbns_grid_desc* grid, const double* block_bounds, const gbns_bc_desc* bc,
+                          double* prims, void* stream);
 
 /* dst = src on interior cells, dst's ghost layers filled from src's interior
  * donors (gbns_fill_ghosts of src, written into dst).  Asynchronous. */

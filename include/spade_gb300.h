@@ -1067,7 +1067,8 @@ namespace spade::gb300
         void advance()
         {
 #ifndef GBNS_DROPIN_HOOK
-            int rc = gbns_ssprk3_step_blocks(&grid, &scheme, boxes.data(), plan.plan, q.image().base, work, dt, nullptr);
+            int rc = gbns_ssprk3_step_blocks(&grid, &scheme, boxes.data(), plan.plan, nullptr, q.image().base, work, dt,
+                                             nullptr);
             if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
             detail::check_call(rc, "gb300 ssprk3 step failed: ");
 #endif

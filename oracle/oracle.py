@@ -74,7 +74,8 @@ def ref():
         lib.spade_ref_amr_flux_div.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         lib.spade_ref_amr_ssprk3.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_int,
-                                             ctypes.c_longlong, ctypes.c_void_p]
+                                             ctypes.c_longlong, ctypes.c_void_p, ctypes.c_int]
+        lib.spade_ref_amr_fill.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_void_p]
         _ref = lib
     return _ref
 
@@ -265,14 +266,64 @@ def _amr_ints(nb, nc, ng, periodic, passes):
 
 
 def ref_amr_ssprk3(ref_scheme, nb, nc, ng, periodic, passes, scheme, prims, dt, nsteps,
-                   bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+                   bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), t_wall=None):
     """nsteps of the reference's SSPRK3 (integrator_t, ssprk3_t, state
     transform) on the refined layout of ref_amr_exchange, with the layout's
     exchange as the boundary condition (oracle/ref_harness.cc
-    spade_ref_amr_ssprk3).  `prims` (full array) is updated in place."""
+    spade_ref_amr_ssprk3).  `prims` (full array) is updated in place.  With
+    t_wall, the y faces are isothermal walls filled after each exchange."""
     ints = _amr_ints(nb, nc, ng, periodic, passes)
     grid = _abi.grid_desc(nb, nc, ng, bounds)
     _, reals = _ref_problem(grid, scheme)
+    if t_wall is not None:
+        reals[13] = float(t_wall)
     assert prims.dtype == np.float64 and prims.flags.c_contiguous
     _check(ref().spade_ref_amr_ssprk3(int(ref_scheme), ints.ctypes.data, reals.ctypes.data, float(dt), int(nsteps),
-                                      prims.size, _ptr(prims)), "spade_ref_amr_ssprk3")
+                                      prims.size, _ptr(prims), int(t_wall is not None)), "spade_ref_amr_ssprk3")
+
+
+
+def ref_amr_fill(nb, nc, ng, periodic, passes, prims, t_wall=None, bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0)):
+    """The reference's boundary condition on a refined layout: its exchange,
+    then with t_wall the isothermal-wall boundary_fill of the y faces
+    (oracle/ref_harness.cc spade_ref_amr_fill); prims updated in place."""
+    ints = _amr_ints(nb, nc, ng, periodic, passes)
+    grid = _abi.grid_desc(nb, nc, ng, bounds)
+    sch = _abi.SchemeDesc()
+    sch.gas.gamma, sch.gas.R = 1.4, 287.0
+    _, reals = _ref_problem(grid, sch)
+    reals[13] = 0.0 if t_wall is None else float(t_wall)
+    assert prims.dtype == np.float64 and prims.flags.c_contiguous
+    _check(ref().spade_ref_amr_fill(ints.ctypes.data, reals.ctypes.data, int(t_wall is not None), prims.size, _ptr(prims)),
+           "spade_ref_amr_fill")
+
+
+def wall_fill_blocks(ncell, ng, boxes, bounds, bc, prims):
+    """The wall faces of a refined layout, in place (numpy restatement of
+    algs::boundary_fill, grid/boundary_fill.h:31-133, as it runs after the
+    exchange): for each face f = 0..5 whose bc kind is a wall, every block
+    whose box touches domain face f (boxes[:, f] == bounds[f]) has its ghost
+    slab (ng layers, the full padded extent across) set from the mirrored
+    cells of the same block: isothermal no-slip T -> 2 T_w - T with the
+    velocity negated, slip the normal component negated."""
+    boxes = np.asarray(boxes)
+    for f in range(6):
+        kind = bc.kind[f]
+        if kind not in (_abi.BC_ISOTHERMAL_NOSLIP, _abi.BC_SLIP_ADIABATIC):
+            continue
+        d, hi = f // 2, f % 2
+        ax = 3 - d                                     # array axis of direction d: (lb, k, j, i, v)
+        for lb in np.nonzero(boxes[:, f] == bounds[f])[0]:
+            blk = prims[lb]
+            for layer in range(ng):
+                c = ncell[d] + layer if hi else layer - ng
+                img = 2 * ncell[d] - (c + 1) if hi else -1 - c
+                src = np.take(blk, img + ng, axis=ax - 1).copy()
+                if kind == _abi.BC_ISOTHERMAL_NOSLIP:
+                    src[..., 1] = 2.0 * bc.t_wall[f] - src[..., 1]
+                    src[..., 2:] = -src[..., 2:]
+                else:
+                    src[..., 2 + d] = -src[..., 2 + d]
+                idx = [slice(None)] * 4
+                idx[ax - 1] = c + ng
+                blk[tuple(idx)] = src

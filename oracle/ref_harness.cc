@@ -580,12 +580,44 @@ extern "C"
 
     // nsteps of SSPRK3 on a refined layout (the grid of spade_ref_amr_flux_div)
     // through integrator_t with the conservative-variable state transform; the
-    // boundary condition is the layout's exchange alone (make_exchange with the
-    // periodic flags; ghost cells it does not write keep their values).
+    // boundary condition is the layout's exchange (make_exchange with the
+    // periodic flags; ghost cells it does not write keep their values), then
+    // with wall_y the y walls' boundary_fill as in spade_ref_amr_fill.
     // `prims` (cap doubles) holds the initial state on entry and the final
     // state on exit; the exchange runs once before the first step.
+    // The boundary condition of a refined layout: the exchange, then (wall_y)
+    // the reference's boundary_fill of the y faces with the isothermal wall
+    // kernel at reals[13] (grid/boundary_fill.h:31-133), as apply_bc pairs them.
+    // `prims` (cap doubles) is filled in place.
+    int spade_ref_amr_fill(const int* ints, const double* reals, int wall_y, long long cap, double* prims)
+    {
+        try
+        {
+            const problem_t pb = make_problem_amr(ints, reals);
+            int rc = 0;
+            with_amr_grid(pb, ints, [&](auto& grid, auto& group, auto& per)
+            {
+                spade::ctrs::array<int, 3> nexch(pb.ng, pb.ng, pb.ng);
+                spade::grid::grid_array q(grid, prim_t(0.0), nexch, spade::device::cpu);
+                if ((long long)q.data.size() > cap) { rc = -2; return; }
+                copy_in(q, prims);
+                auto handle = spade::grid::make_exchange(q, per);
+                handle.exchange(q, group);
+                if (wall_y)
+                {
+                    isothermal_wall_t wall{pb.t_wall};
+                    spade::algs::boundary_fill(q, spade::boundary::ymin, wall);
+                    spade::algs::boundary_fill(q, spade::boundary::ymax, wall);
+                }
+                copy_out(q, prims);
+            });
+            return rc;
+        }
+        catch (const std::exception& e) { std::fprintf(stderr, "spade_ref_amr_fill: %s\n", e.what()); return -1; }
+    }
+
     int spade_ref_amr_ssprk3(int scheme, const int* ints, const double* reals, double dt, int nsteps, long long cap,
-                             double* prims)
+                             double* prims, int wall_y)
     {
         try
         {
@@ -599,11 +631,21 @@ extern "C"
                 if ((long long)q.data.size() > cap) { rc = -2; return; }
                 copy_in(q, prims);
                 auto handle = spade::grid::make_exchange(q, per);
-                handle.exchange(q, group);
+                isothermal_wall_t wall{pb.t_wall};
+                auto fill = [&](auto& sol)
+                {
+                    handle.exchange(sol, group);
+                    if (wall_y)
+                    {
+                        spade::algs::boundary_fill(sol, spade::boundary::ymin, wall);
+                        spade::algs::boundary_fill(sol, spade::boundary::ymax, wall);
+                    }
+                };
+                fill(q);
                 gas_t air(pb.gamma, pb.rgas);
                 with_flux(pb, scheme, [&](const auto& flx)
                 {
-                    auto bc = [&](auto& sol, const auto&) { handle.exchange(sol, group); };
+                    auto bc = [&](auto& sol, const auto&) { fill(sol); };
                     auto calc_rhs = [&](auto& rhs_in, const auto& sol, const auto&)
                     {
                         rhs_in = real_t(0.0);

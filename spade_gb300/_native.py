@@ -57,7 +57,9 @@ def lib():
     L.gbns_flux_div_host.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, ctypes.c_int, vp]
     L.gbns_flux_div_blocks.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, vp, ctypes.c_int, vp]
     L.gbns_flux_div_blocks_host.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, vp, ctypes.c_int, vp]
-    L.gbns_ssprk3_step_blocks.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, vp, vp, ctypes.c_double, vp]
+    L.gbns_ssprk3_step_blocks.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, P(_abi.BcDesc), vp, vp,
+                                          ctypes.c_double, vp]
+    L.gbns_wall_fill_blocks.argtypes = [P(_abi.GridDesc), vp, P(_abi.BcDesc), vp, vp]
     L.gbns_boundary_flux.argtypes = [P(_abi.GridDesc), P(_abi.SchemeDesc), vp, vp, P(ctypes.c_int), vp]
     L.gbns_selftest_wait_timeout.argtypes = [P(ctypes.c_int), vp]
     L.gbns_selftest_dmul_int.argtypes = [ctypes.c_uint64, ctypes.c_uint64, P(ctypes.c_uint64), vp]

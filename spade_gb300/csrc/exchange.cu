@@ -381,3 +381,104 @@ namespace gbns
         return GBNS_OK;
     }
 }
+
+namespace gbns
+{
+    namespace
+    {
+        // The wall fill of one domain face on a refined layout, for the blocks
+        // listed (their boxes touch that face): every ghost cell of the face's
+        // slab (ng layers, the full padded extent across) takes the mirrored
+        // cell of its own block (boundary_fill.h:107-124): isothermal no-slip
+        // T -> 2 T_w - T and the velocity negated, slip the normal component
+        // negated.  The mirrored cells are interior along the face normal, so
+        // no cell read is written by the launch.
+        __global__ void wall_fill_blocks_kernel(double* q, PlanGeom G, int n0, int n1, int n2,
+                                                const int* __restrict__ blocks, int nlist, int face, int kind,
+                                                double t_wall)
+        {
+            const int d = face/2, hi = face % 2;
+            const int n[3] = {n0, n1, n2};
+            const long long per = (long long)G.ng*(d == 0 ? (long long)G.nj*G.nk : (d == 1 ? (long long)G.ni*G.nk
+                                                                                           : (long long)G.ni*G.nj));
+            const long long total = per*nlist;
+            for (long long t = blockIdx.x*(long long)blockDim.x + threadIdx.x; t < total;
+                 t += (long long)gridDim.x*blockDim.x)
+            {
+                const int lb = blocks[t/per];
+                long long r = t % per;
+                int p[3];
+                if (d == 0) { p[0] = int(r % G.ng); r /= G.ng; p[1] = int(r % G.nj); p[2] = int(r / G.nj); }
+                else if (d == 1) { p[0] = int(r % G.ni); r /= G.ni; p[1] = int(r % G.ng); p[2] = int(r / G.ng); }
+                else { p[0] = int(r % G.ni); r /= G.ni; p[1] = int(r % G.nj); p[2] = int(r / G.nj); }
+                const int c = hi ? n[d] + p[d] : p[d] - G.ng;          // ghost cell, interior-relative
+                const int img = hi ? 2*n[d] - (c + 1) : -1 - c;        // its mirror (interior along d)
+                int src[3] = {p[0], p[1], p[2]}, dst[3] = {p[0], p[1], p[2]};
+                src[d] = img + G.ng;
+                dst[d] = c + G.ng;
+                const double* s = q + (long long)lb*G.bstride + ((long long)(src[2]*G.nj + src[1])*G.ni + src[0])*5;
+                double v[5];
+                #pragma unroll
+                for (int k = 0; k < 5; ++k) v[k] = s[k];
+                if (kind == GBNS_BC_ISOTHERMAL_NOSLIP)
+                {
+                    v[1] = 2.0*t_wall - v[1];
+                    v[2] = -v[2]; v[3] = -v[3]; v[4] = -v[4];
+                }
+                else v[2 + d] = -v[2 + d];
+                double* o = q + (long long)lb*G.bstride + ((long long)(dst[2]*G.nj + dst[1])*G.ni + dst[0])*5;
+                #pragma unroll
+                for (int k = 0; k < 5; ++k) o[k] = v[k];
+            }
+        }
+    }
+
+    int wall_lists(const gbns_grid_desc* g, const double* boxes, const gbns_bc_desc* bc, WallLists& W)
+    {
+        W.idx.clear();
+        for (int f = 0; f < 7; ++f) W.off[f] = 0;
+        for (int f = 0; f < 6; ++f)
+        {
+            W.off[f] = int(W.idx.size());
+            const int kind = bc->kind[f];
+            if (kind != GBNS_BC_ISOTHERMAL_NOSLIP && kind != GBNS_BC_SLIP_ADIABATIC) continue;
+            const int d = f/2;
+            if (g->ncell[d] < g->ng)
+                return set_error(GBNS_ERR_UNSUPPORTED, "wall fill needs at least ng cells per block across a wall");
+            for (int lb = 0; lb < g->nblk[0]; ++lb)
+            {
+                const double v = boxes[6*lb + f], wall = g->bounds[f];
+                if (v == wall) W.idx.push_back(lb);
+            }
+        }
+        W.off[6] = int(W.idx.size());
+        return GBNS_OK;
+    }
+
+    int launch_wall_fill(const gbns_grid_desc* g, const gbns_bc_desc* bc, const WallLists& W, const int* d_idx,
+                         double* prims, cudaStream_t st)
+    {
+        PlanGeom G;
+        G.ni = g->ncell[0] + 2*g->ng;
+        G.nj = g->ncell[1] + 2*g->ng;
+        G.nk = g->ncell[2] + 2*g->ng;
+        G.ng = g->ng;
+        G.bstride = 5ll*G.ni*G.nj*G.nk;
+        for (int f = 0; f < 6; ++f)
+        {
+            const int nlist = W.off[f + 1] - W.off[f];
+            if (nlist == 0) continue;
+            const int d = f/2;
+            const long long per = (long long)G.ng*(d == 0 ? (long long)G.nj*G.nk : (d == 1 ? (long long)G.ni*G.nk
+                                                                                           : (long long)G.ni*G.nj));
+            long long nb = (per*nlist + 255)/256;
+            const long long cap = (long long)sm_count()*8;
+            if (nb > cap) nb = cap;
+            wall_fill_blocks_kernel<<<unsigned(nb), 256, 0, st>>>(prims, G, g->ncell[0], g->ncell[1], g->ncell[2],
+                                                                   d_idx + W.off[f], nlist, f, bc->kind[f], bc->t_wall[f]);
+            const int rc = check_cuda(cudaGetLastError(), "wall fill launch");
+            if (rc) return rc;
+        }
+        return GBNS_OK;
+    }
+}

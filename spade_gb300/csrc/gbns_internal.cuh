@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <string>
+#include <vector>
 
 #include "gbns.h"
 #include "fp64_int.cuh"
@@ -151,6 +152,20 @@ namespace gbns
     // The cells per block, ghost layers and block count an exchange plan was
     // created for (exchange.cu).
     int exchange_plan_shape(const gbns_exchange_plan* P, int* nx, int* ny, int* nz, int* ng, int* nblocks);
+    // Wall faces of a refined layout (grid nblk = (N, 1, 1), 6 box doubles per
+    // block): per face f the blocks whose box touches domain face f
+    // (grid->bounds[f]), idx[off[f] .. off[f+1]); faces that are not walls
+    // have none (exchange.cu).
+    struct WallLists
+    {
+        std::vector<int> idx;
+        int off[7];
+    };
+    int wall_lists(const gbns_grid_desc* g, const double* boxes, const gbns_bc_desc* bc, WallLists& W);
+    // One launch per wall face in face order (boundary_fill's order), d_idx
+    // the lists in device memory.
+    int launch_wall_fill(const gbns_grid_desc* g, const gbns_bc_desc* bc, const WallLists& W, const int* d_idx,
+                         double* prims, cudaStream_t st);
     // gbns_flux_div_rk over the blocks blk0 .. blk1 - 1 (host.cu)
     int flux_div_rk_range(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* prims,
                           double* rhs, int write_rhs, int nres, const double* const* earlier,

@@ -450,8 +450,55 @@ extern "C"
         return rc ? rc : frc;
     }
 
+    // The wall lists of a refined layout in stream-ordered device memory
+    // (*d_idx stays NULL when no block touches a wall face; the caller frees
+    // it on st).
+    static int upload_walls(const gbns_grid_desc* grid, const double* boxes, const gbns_bc_desc* bc,
+                            gbns::WallLists& W, int** d_idx, cudaStream_t st)
+    {
+        using namespace gbns;
+        *d_idx = nullptr;
+        for (int f = 0; f < 7; ++f) W.off[f] = 0;
+        W.idx.clear();
+        if (!bc) return GBNS_OK;
+        int rc = wall_lists(grid, boxes, bc, W);
+        if (rc || W.idx.empty()) return rc;
+        void* p = nullptr;
+        rc = pool_alloc(&p, W.idx.size()*sizeof(int), st);
+        if (rc) return rc;
+        rc = check_cuda(cudaMemcpyAsync(p, W.idx.data(), W.idx.size()*sizeof(int), cudaMemcpyHostToDevice, st),
+                        "wall lists to the device");
+        if (rc) { cudaFreeAsync(p, st); return rc; }
+        *d_idx = static_cast<int*>(p);
+        return GBNS_OK;
+    }
+
+    int gbns_wall_fill_blocks(const gbns_grid_desc* grid, const double* block_bounds, const gbns_bc_desc* bc,
+                              double* prims, void* stream)
+    {
+        using namespace gbns;
+        if (!grid || !block_bounds || !bc || !prims) return set_error(GBNS_ERR_INVALID, "NULL argument");
+        const int nblk = grid->nblk[0];
+        if (nblk < 1 || nblk > 65535 || grid->nblk[1] != 1 || grid->nblk[2] != 1)
+            return set_error(GBNS_ERR_INVALID, "a refined layout's blocks are given as nblk = (1..65535, 1, 1)");
+        gbns_grid_desc one = *grid;
+        one.nblk[0] = 1;
+        size_t per_block = 0;
+        int rc = gbns_array_size(&one, &per_block);
+        if (rc) return rc;
+        const cudaStream_t st = static_cast<cudaStream_t>(stream);
+        WallLists W;
+        int* d_idx = nullptr;
+        rc = upload_walls(grid, block_bounds, bc, W, &d_idx, st);
+        if (rc || !d_idx) return rc;
+        rc = launch_wall_fill(grid, bc, W, d_idx, prims, st);
+        const int frc = check_cuda(cudaFreeAsync(d_idx, st), "wall lists (pool free)");
+        return rc ? rc : frc;
+    }
+
     int gbns_ssprk3_step_blocks(const gbns_grid_desc* grid, const gbns_scheme_desc* scheme, const double* block_bounds,
-                                gbns_exchange_plan* plan, double* prims, double* work, double dt, void* stream)
+                                gbns_exchange_plan* plan, const gbns_bc_desc* bc, double* prims, double* work, double dt,
+                                void* stream)
     {
         using namespace gbns;
         if (!prims || !work) return set_error(GBNS_ERR_INVALID, "prims/work pointer is NULL");
@@ -467,6 +514,17 @@ extern "C"
         double* dinv = nullptr;
         rc = blocks_setup(grid, scheme, block_bounds, G, S, st, &dinv);
         if (rc) return rc;
+        WallLists W;
+        int* d_walls = nullptr;
+        rc = upload_walls(grid, block_bounds, bc, W, &d_walls, st);
+        if (rc) { cudaFreeAsync(dinv, st); return rc; }
+        // the boundary condition: the exchange, then the walls (apply_bc's order)
+        auto fill = [&](double* a) -> int
+        {
+            int r = gbns_exchange_plan_run(plan, a, stream);
+            if (!r && d_walls) r = launch_wall_fill(grid, bc, W, d_walls, a, st);
+            return r;
+        };
         const size_t n = size_t(G.bstride)*G.nblk;
         double* R0 = work;
         double* R1 = work + n;
@@ -497,15 +555,16 @@ extern "C"
         };
         rc = copy(B, prims);
         if (!rc) rc = stage(0, prims, R0, B);
-        if (!rc) rc = gbns_exchange_plan_run(plan, B, stream);
+        if (!rc) rc = fill(B);
         if (!rc) rc = copy(prims, B);
         if (!rc) rc = stage(1, B, R1, prims);
-        if (!rc) rc = gbns_exchange_plan_run(plan, prims, stream);
+        if (!rc) rc = fill(prims);
         if (!rc) rc = copy(B, prims);
         if (!rc) rc = stage(2, prims, nullptr, B);
-        if (!rc) rc = gbns_exchange_plan_run(plan, B, stream);
+        if (!rc) rc = fill(B);
         if (!rc) rc = copy(prims, B);
-        const int frc = check_cuda(cudaFreeAsync(dinv, st), "per-block spacing (pool free)");
+        int frc = check_cuda(cudaFreeAsync(dinv, st), "per-block spacing (pool free)");
+        if (d_walls && !frc) frc = check_cuda(cudaFreeAsync(d_walls, st), "wall lists (pool free)");
         return rc ? rc : frc;
     }
 

@@ -175,20 +175,22 @@ class ssprk3_refined_stepper:
     one gbns_ssprk3_step_blocks per step, the stage updates fused into the
     flux launches.  q: a CUDA float64 tensor of the layout's shape holding
     exchanged ghosts (plan.exchange(q) before the first step, as the
-    reference's driver refreshes them)."""
+    reference's driver refreshes them); bc (a gbns_bc_desc, optional): the
+    wall faces filled after each exchange (gbns_wall_fill_blocks)."""
 
-    def __init__(self, layout, q, scheme_desc, plan, dt):
+    def __init__(self, layout, q, scheme_desc, plan, dt, bc=None):
         if not isinstance(layout, refined_layout_t):
             raise TypeError("layout must be a grid.refined_layout_t")
         layout.check(q)
         if not q.is_cuda:
             raise ValueError("the refined-layout step runs on CUDA tensors")
         self.layout, self.q, self.scheme, self.plan, self.dt = layout, q, scheme_desc, plan, float(dt)
+        self.bc = bc
         self.work = torch.zeros(3 * q.numel(), dtype=torch.float64, device=q.device)
 
     def step(self, nsteps=1, stream=None):
         for _ in range(nsteps):
             _native.check(_native.lib().gbns_ssprk3_step_blocks(
-                self.layout.desc(), self.scheme, self.layout.boxes_ptr(), self.plan.handle,
+                self.layout.desc(), self.scheme, self.layout.boxes_ptr(), self.plan.handle, self.bc,
                 ctypes.c_void_p(self.q.data_ptr()), ctypes.c_void_p(self.work.data_ptr()), ctypes.c_double(self.dt),
                 _stream(stream)))

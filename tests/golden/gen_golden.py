@@ -238,6 +238,7 @@ AMR_FLUX_SCHEMES = {
 
 
 AMR_SSPRK3_DT, AMR_SSPRK3_STEPS = 1e-4, 3
+AMR_T_WALL = 1.25
 
 
 def amr_flux_input(after):
@@ -264,6 +265,16 @@ def gen_amr_flux():
             inner = np.ascontiguousarray(a[:, ng:-ng, ng:-ng, ng:-ng])
             assert np.all(np.isfinite(inner)), (name, sname)
             out[name + "_ssprk3_" + sname] = np.frombuffer(hashlib.sha256(inner.tobytes()).digest(), dtype=np.uint8)
+            if not all(per):
+                # the same with the non-periodic y faces as isothermal walls at
+                # AMR_T_WALL, filled after each exchange (boundary_fill)
+                a = q.copy()
+                O.ref_amr_ssprk3(sid, nb, nc, ng, per, passes, P.scheme(**kw), a, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS,
+                                 t_wall=AMR_T_WALL)
+                inner = np.ascontiguousarray(a[:, ng:-ng, ng:-ng, ng:-ng])
+                assert np.all(np.isfinite(inner)), (name, sname)
+                out[name + "_ssprk3_walls_" + sname] = np.frombuffer(hashlib.sha256(inner.tobytes()).digest(),
+                                                                     dtype=np.uint8)
     np.savez_compressed(os.path.join(OUT, "amr_flux_ref.npz"), **out)
 
 

@@ -11,7 +11,8 @@ scheme compositions (tests/golden/gen_golden.py).  Here:
 * three SSPRK3 steps composed from the oracle's exchange, flux_div and stage
   update reproduce the reference's integrator_t run with the exchange as
   boundary condition (the golden holds the SHA-256 of its final interior;
-  live, where the harness is built, the whole array);
+  live, where the harness is built, the whole array), also with y walls
+  filled after each exchange (the reference's boundary_fill);
 * gbns_flux_div_blocks rejects malformed layouts before any CUDA call.
 
 The GPU side is tests/test_gpu_amr_flux.py."""
@@ -26,7 +27,7 @@ from spade_gb300 import _abi, _native
 from oracle import oracle as O
 import problems as P
 from test_amr_exchange import CASES, golden
-from golden.gen_golden import AMR_CASES, AMR_FLUX_SCHEMES, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS, amr_flux_input
+from golden.gen_golden import AMR_CASES, AMR_FLUX_SCHEMES, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS, AMR_T_WALL, amr_flux_input
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLD = os.path.join(ROOT, "tests", "golden", "amr_flux_ref.npz")
@@ -70,22 +71,34 @@ def test_oracle_flux_div_blocks_equals_reference_live(case):
     assert np.array_equal(r[inner], want[inner])
 
 
-def oracle_amr_ssprk3(case, s, q, dt, nsteps):
+DOMAIN = (0.0, 1.0, 0.0, 1.0, 0.0, 1.0)
+
+
+def oracle_amr_fill(case, q, bc=None):
+    """The boundary condition of a refined layout: the exchange, then with bc
+    the wall faces (oracle.wall_fill_blocks), in place."""
+    g = golden(case)
+    nc = tuple(int(n) for n in g["ncell"])
+    ng = int(g["ng"])
+    O.exchange_patches(nc, ng, q.shape[0], g["plan"], q)
+    if bc is not None:
+        O.wall_fill_blocks(nc, ng, g["boxes"], DOMAIN, bc, q)
+
+
+def oracle_amr_ssprk3(case, s, q, dt, nsteps, bc=None):
     """nsteps of SSPRK3 on a refined layout from the oracle's pieces, after
     one exchange (as the reference's driver refreshes the ghosts first): per
     stage the residual (flux_div_blocks), the stage update (rk_stage, the
     ratio_diff coefficients of ssprk3_t) and the exchange, in place."""
-    g = golden(case)
     grid, boxes, _, ng = layout(case)
-    nc = tuple(int(n) for n in g["ncell"])
-    O.exchange_patches(nc, ng, q.shape[0], g["plan"], q)
+    oracle_amr_fill(case, q, bc)
     coeffs = ([dt], [(-3.0 / 4.0) * dt, (1.0 / 4.0) * dt], [(-1.0 / 12.0) * dt, (-1.0 / 12.0) * dt, (2.0 / 3.0) * dt])
     for _ in range(nsteps):
         R = [np.zeros_like(q) for _ in range(3)]
         for k, c in enumerate(coeffs):
             O.flux_div_blocks(grid, s, boxes, q, R[k], increment=True)
             O.rk_stage(grid, s.gas, q, R[:k + 1], c)
-            O.exchange_patches(nc, ng, q.shape[0], g["plan"], q)
+            oracle_amr_fill(case, q, bc)
     return q
 
 
@@ -107,6 +120,29 @@ def test_oracle_amr_ssprk3_equals_reference(case, scheme):
         want = q.copy()
         O.ref_amr_ssprk3(AMR_FLUX_SCHEMES[scheme][0], nb, nc, ng_, per, passes, s, want, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS)
         assert np.array_equal(a, want)                    # ghost cells included
+
+
+@pytest.mark.parametrize("scheme", sorted(AMR_FLUX_SCHEMES))
+def test_oracle_amr_ssprk3_with_walls_equals_reference(scheme):
+    """Two levels with y walls, the walls filled after each exchange (the
+    reference's boundary_fill with the isothermal wall kernel)."""
+    case = "two_levels_walls_y"
+    _, _, q, ng = layout(case)
+    s = P.scheme(**AMR_FLUX_SCHEMES[scheme][1])
+    bc = P.channel_bc(AMR_T_WALL)
+    a = oracle_amr_ssprk3(case, s, q.copy(), AMR_SSPRK3_DT, AMR_SSPRK3_STEPS, bc)
+    assert np.array_equal(interior_digest(a, ng), np.load(GOLD)[case + "_ssprk3_walls_" + scheme])
+    if O.ref_available():
+        nb, nc, ng_, per, passes = AMR_CASES[case]
+        want = q.copy()
+        O.ref_amr_fill(nb, nc, ng_, per, passes, want, t_wall=AMR_T_WALL)
+        got = q.copy()
+        oracle_amr_fill(case, got, bc)
+        assert np.array_equal(got, want)                  # the boundary condition alone, ghosts included
+        want = q.copy()
+        O.ref_amr_ssprk3(AMR_FLUX_SCHEMES[scheme][0], nb, nc, ng_, per, passes, s, want, AMR_SSPRK3_DT,
+                         AMR_SSPRK3_STEPS, t_wall=AMR_T_WALL)
+        assert np.array_equal(a, want)
 
 
 def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
@@ -131,7 +167,7 @@ def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
                 P.scheme(conv=_abi.CONV_FWENO)) == _abi.ERR_INVALID
     assert "ghost layers" in _native.last_error()
     # the fused step: a missing exchange plan
-    assert lib.gbns_ssprk3_step_blocks(g, s, boxes.ctypes.data_as(ctypes.c_void_p), None, pq, pr,
+    assert lib.gbns_ssprk3_step_blocks(g, s, boxes.ctypes.data_as(ctypes.c_void_p), None, None, pq, pr,
                                        ctypes.c_double(1e-4), None) == _abi.ERR_INVALID
 
 

@@ -20,8 +20,8 @@ from spade_gb300 import grid as _grid
 from oracle import oracle as O
 import problems as P
 from test_amr_exchange import CASES, amr_fill, golden
-from test_amr_flux import GOLD, layout, oracle_amr_ssprk3, interior_digest
-from golden.gen_golden import AMR_FLUX_SCHEMES, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS
+from test_amr_flux import GOLD, DOMAIN, layout, oracle_amr_fill, oracle_amr_ssprk3, interior_digest
+from golden.gen_golden import AMR_FLUX_SCHEMES, AMR_SSPRK3_DT, AMR_SSPRK3_STEPS, AMR_T_WALL
 
 pytestmark = pytest.mark.gpu
 
@@ -98,7 +98,7 @@ def test_ssprk3_step_blocks_equals_reference(case, scheme):
     b = np.ascontiguousarray(boxes)
     plan.exchange(qd)                                          # the ghosts on entry, as the reference's driver
     for _ in range(AMR_SSPRK3_STEPS):
-        _native.check(_native.lib().gbns_ssprk3_step_blocks(grid, s, b.ctypes.data_as(ctypes.c_void_p), plan.handle,
+        _native.check(_native.lib().gbns_ssprk3_step_blocks(grid, s, b.ctypes.data_as(ctypes.c_void_p), plan.handle, None,
                                                             qd.data_ptr(), work.data_ptr(),
                                                             ctypes.c_double(AMR_SSPRK3_DT), _st()))
     torch.cuda.synchronize()
@@ -133,3 +133,35 @@ def test_python_api_on_refined_layouts():
     torch.cuda.synchronize()
     plan.close()
     assert np.array_equal(interior_digest(qd.cpu().numpy(), ng), np.load(GOLD)[case + "_ssprk3_ck2_visc"])
+
+
+
+@pytest.mark.parametrize("scheme", sorted(AMR_FLUX_SCHEMES))
+def test_wall_fill_and_walled_steps_equal_reference(scheme):
+    """Two levels with y walls: the exchange then gbns_wall_fill_blocks equals
+    the oracle's boundary condition (ghosts included); three fused steps with
+    the walls filled after each exchange give the reference's run."""
+    case = "two_levels_walls_y"
+    g = golden(case)
+    grid, boxes, q, ng = layout(case)
+    bc = P.channel_bc(AMR_T_WALL)
+    b = np.ascontiguousarray(boxes)
+    plan = _grid.exchange_plan_t(g["ncell"], ng, q.shape[0], g["plan"])
+    qd = torch.from_numpy(q.copy()).cuda()
+    plan.exchange(qd)
+    _native.check(_native.lib().gbns_wall_fill_blocks(grid, b.ctypes.data_as(ctypes.c_void_p), bc, qd.data_ptr(), _st()))
+    torch.cuda.synchronize()
+    want = q.copy()
+    oracle_amr_fill(case, want, bc)
+    assert np.array_equal(qd.cpu().numpy(), want)
+    s = P.scheme(**AMR_FLUX_SCHEMES[scheme][1])
+    work = torch.zeros(3 * q.size, dtype=torch.float64, device="cuda")
+    for _ in range(AMR_SSPRK3_STEPS):
+        _native.check(_native.lib().gbns_ssprk3_step_blocks(grid, s, b.ctypes.data_as(ctypes.c_void_p), plan.handle, bc,
+                                                            qd.data_ptr(), work.data_ptr(),
+                                                            ctypes.c_double(AMR_SSPRK3_DT), _st()))
+    torch.cuda.synchronize()
+    plan.close()
+    r = qd.cpu().numpy()
+    assert np.array_equal(interior_digest(r, ng), np.load(GOLD)[case + "_ssprk3_walls_" + scheme])
+    assert np.array_equal(r, oracle_amr_ssprk3(case, s, q.copy(), AMR_SSPRK3_DT, AMR_SSPRK3_STEPS, bc))
