@@ -1038,6 +1038,8 @@ namespace spade::gb300
         std::vector<double> boxes;
         gbns_grid_desc grid;
         gbns_scheme_desc scheme;
+        gbns_bc_desc bc{};
+        bool walls_on = false;
         double dt;
         double t;
         double* work = nullptr;
@@ -1046,6 +1048,23 @@ namespace spade::gb300
                                     double t0 = 0.0, int precision = GBNS_PREC_FP64)
             : q{q_in}, plan{plan_in}, grid{lower_refined_grid(q_in, boxes)}, scheme{lower_scheme(flux, precision)},
               dt{dt_in}, t{t0}
+        {
+            allocate();
+        }
+
+        // with walls: after each exchange the wall faces are filled as the
+        // reference's boundary_fill(q, faces, wall) does (gbns_wall_fill_blocks)
+        template <typename wall_t>
+        ssprk3_refined_integrator_t(arr_t& q_in, const flux_func_t& flux, const exchange_plan_t& plan_in,
+                                    const ctrs::array<bool, 3>& periodic, const bound_box_t<bool, 3>& walls,
+                                    const wall_t& wall, double dt_in, double t0 = 0.0, int precision = GBNS_PREC_FP64)
+            : q{q_in}, plan{plan_in}, grid{lower_refined_grid(q_in, boxes)}, scheme{lower_scheme(flux, precision)},
+              bc{lower_bc(periodic, walls, wall)}, walls_on{true}, dt{dt_in}, t{t0}
+        {
+            allocate();
+        }
+
+        void allocate()
         {
 #ifndef GBNS_DROPIN_HOOK
             static_assert(device::is_gpu<typename arr_t::device_type>, "the gb300 integrator runs on device::gpu arrays");
@@ -1067,8 +1086,8 @@ namespace spade::gb300
         void advance()
         {
 #ifndef GBNS_DROPIN_HOOK
-            int rc = gbns_ssprk3_step_blocks(&grid, &scheme, boxes.data(), plan.plan, nullptr, q.image().base, work, dt,
-                                             nullptr);
+            int rc = gbns_ssprk3_step_blocks(&grid, &scheme, boxes.data(), plan.plan, walls_on ? &bc : nullptr,
+                                             q.image().base, work, dt, nullptr);
             if (rc == GBNS_OK && cudaDeviceSynchronize() != cudaSuccess) rc = GBNS_ERR_CUDA;
             detail::check_call(rc, "gb300 ssprk3 step failed: ");
 #endif

@@ -48,4 +48,6 @@ void run_on_gpu_arrays(spade::parallel::pool_t& group)
     spade::pde_algs::flux_div(aq, arhs, flux, spade::algs::make_traits(spade::pde_algs::gb300));
     spade::gb300::ssprk3_refined_integrator_t astep(aq, flux, plan, 1.0e-4);
     astep.advance();
+    spade::gb300::ssprk3_refined_integrator_t wstep(aq, flux, plan, periodic, walls, wall, 1.0e-4);
+    wstep.advance();
 }
