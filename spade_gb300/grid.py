@@ -267,6 +267,18 @@ class refined_layout_t:
     def boxes_ptr(self):
         return ctypes.c_void_p(self.boxes.ctypes.data)
 
+    def fill_walls(self, q, bc, bounds=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), stream=None):
+        """The wall faces of bc (a gbns_bc_desc) on the CUDA tensor q, after its
+        exchange: the blocks whose box touches a wall face of the domain
+        `bounds` mirror their ghost slab through the wall kernel
+        (algs::boundary_fill, gbns_wall_fill_blocks)."""
+        self.check(q)
+        if not q.is_cuda:
+            raise ValueError("the wall fill runs on CUDA tensors")
+        g = _abi.grid_desc((self.nblocks, 1, 1), self.ncell, self.ng, bounds)
+        _native.check(_native.lib().gbns_wall_fill_blocks(g, self.boxes_ptr(), bc, ctypes.c_void_p(q.data_ptr()),
+                                                          _stream(stream)))
+
 
 def make_exchange(q, periodic):
     h = arr_exchange_t(periodic)

@@ -131,8 +131,17 @@ def test_python_api_on_refined_layouts():
     st = time_integration.ssprk3_refined_stepper(lay, qd, s, plan, AMR_SSPRK3_DT)
     st.step(AMR_SSPRK3_STEPS)
     torch.cuda.synchronize()
-    plan.close()
     assert np.array_equal(interior_digest(qd.cpu().numpy(), ng), np.load(GOLD)[case + "_ssprk3_ck2_visc"])
+    # with the y walls: the layout's wall fill, then the walled stepper
+    bc = P.channel_bc(AMR_T_WALL)
+    qd = torch.from_numpy(q.copy()).cuda()
+    plan.exchange(qd)
+    lay.fill_walls(qd, bc)
+    st = time_integration.ssprk3_refined_stepper(lay, qd, s, plan, AMR_SSPRK3_DT, bc=bc)
+    st.step(AMR_SSPRK3_STEPS)
+    torch.cuda.synchronize()
+    plan.close()
+    assert np.array_equal(interior_digest(qd.cpu().numpy(), ng), np.load(GOLD)[case + "_ssprk3_walls_ck2_visc"])
 
 
 
