@@ -166,6 +166,11 @@ def test_flux_div_blocks_rejects_bad_layouts_before_cuda():
     assert call(_abi.grid_desc((2, 1, 1), (4, 4, 4), 1, (0, 1, 0, 1, 0, 1)), boxes,
                 P.scheme(conv=_abi.CONV_FWENO)) == _abi.ERR_INVALID
     assert "ghost layers" in _native.last_error()
+    # the wall fill: no boundary descriptor; a wall across blocks thinner than the ghost depth
+    assert lib.gbns_wall_fill_blocks(g, boxes.ctypes.data_as(ctypes.c_void_p), None, pq, None) == _abi.ERR_INVALID
+    thin = _abi.grid_desc((2, 1, 1), (4, 1, 4), 2, (0, 1, 0, 1, 0, 1))
+    assert lib.gbns_wall_fill_blocks(thin, boxes.ctypes.data_as(ctypes.c_void_p), P.channel_bc(300.0), pq,
+                                     None) == _abi.ERR_UNSUPPORTED
     # the fused step: a missing exchange plan
     assert lib.gbns_ssprk3_step_blocks(g, s, boxes.ctypes.data_as(ctypes.c_void_p), None, None, pq, pr,
                                        ctypes.c_double(1e-4), None) == _abi.ERR_INVALID
